@@ -1,0 +1,288 @@
+"""Benchmark: batched explicit-target ALS rank reduction (ALS reductions/s).
+
+Workload (the ALS microbenchmark configuration): 64 independent reductions
+of random CP vectors with D=30 modes of n=12 basis functions, target rank
+3200 (rank 20 x 160 Hamiltonian terms), reduced to rank 20 by 10 ALS sweeps;
+factor entries N(0,1)/sqrt(12), target weights log-uniform in [1e-6, 1],
+starting guess = the first 20 target terms.  Seeded synthetic data.
+
+One step = one batched reduction of all 64 vectors (the starting guesses are
+restored from a pristine copy at the start of every step).  The FP64 target
+(595 MB) is larger than L2 (129 MB), so no explicit L2 flush is needed.
+
+--impl reference times the reference algorithm's CPU implementation (the C
+restatement in oracle/, OpenMP over vectors, all host threads) on a bounded
+sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NVEC, D, N, RG, RF, NALS = 64, 30, 12, 3200, 20, 10
+CONFIG = {"workload": "ALS microbenchmark: 64 x (D=30, n=12, rank 3200 -> 20, 10 sweeps)",
+          "batch": NVEC, "ndof": D, "nbas": N, "rank_in": RG, "rank_out": RF, "sweeps": NALS,
+          "l2": "inputs larger than L2 (595 MB FP64 target per step)"}
+METRIC = "ALS reductions/s"
+UNIT = "reductions/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons in the background."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+        self._thread = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                           "--format=csv,noheader,nounits", "-lms", "100"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self._proc = None
+            return self
+
+        def reader():
+            for line in self._proc.stdout:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 7:
+                    self.samples.append(parts)
+        self._thread = threading.Thread(target=reader, daemon=True)
+        self._thread.start()
+        return self
+
+    def stop(self):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+        if self._thread is not None:
+            self._thread.join(timeout=5)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        smax = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_sample_rate(batch, nvec_sample: int, threads: int):
+    """Oracle (C restatement of the reference algorithm) on nvec_sample vectors."""
+    import oracle
+    coefs, bases, rfs, rgs = [], [], [], []
+    for v in range(nvec_sample):
+        c, b = batch.vector(v)
+        coefs.append(np.ascontiguousarray(c))
+        bases.append(np.ascontiguousarray(b))
+        rfs.append(int(batch.rF[v]))
+        rgs.append(int(batch.rG[v]))
+    t0 = time.perf_counter()
+    oracle.als_batched(coefs, bases, batch.nbas, rfs, rgs, NALS, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return nvec_sample / dt, dt
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from mlcp_gb300 import workloads
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    sample = min(NVEC, threads)
+    batch = workloads.als_batch(NVEC, D, N, RF, RG)
+    for _ in range(args.warmup):
+        cpu_sample_rate(batch, sample, threads)
+    times = []
+    for _ in range(args.steps):
+        _, dt = cpu_sample_rate(batch, sample, threads)
+        times.append(dt)
+    total = sum(times)
+    value = sample * args.steps / total
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": dict(CONFIG), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{sample} of the {NVEC} vectors per step, full 10 sweeps each"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    from mlcp_gb300 import _lib, als, workloads
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    L = _lib.load()
+    batch = workloads.als_batch(NVEC, D, N, RF, RG, seed=workloads.ALS_SEED + rank)
+    coef0 = torch.from_numpy(batch.coef).to(dev)
+    base0 = torch.from_numpy(batch.base).to(dev)
+    coef = coef0.clone()
+    base = base0.clone()
+    status = torch.zeros(NVEC, dtype=torch.int32, device=dev)
+    # F rows of every vector (restored from the pristine copy each step)
+    f_rows = torch.cat([torch.arange(int(t), int(t) + RF) for t in batch.term_off]).to(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        base.index_copy_(0, f_rows, base0.index_select(0, f_rows))
+        coef.index_copy_(0, f_rows, coef0.index_select(0, f_rows))
+        als.reduce_batched(coef, base, batch.nbas, batch.rF, batch.rG, batch.term_off, NALS, status=status,
+                           stream=stream)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    assert not status.any().item(), "non-positive-definite normal equations in warm-up"
+
+    # device-resident timing
+    clocks = ClockSampler(local).start() if rank == 0 else None
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop() if clocks else None
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = NVEC * ws * args.steps / (ms / 1e3)
+
+    # dominant-kernel timing (cluster ALS kernel) on the launching stream
+    L.mlcp_gb300_set_kernel_timing(1)
+    kms = []
+    for _ in range(args.steps):
+        step()
+        kms.append(L.mlcp_gb300_last_kernel_ms())
+    L.mlcp_gb300_set_kernel_timing(0)
+    kernel_ms = float(np.mean(kms))
+    alg_bytes = NALS * batch.g_bytes(4)  # FP32 target slice streamed once per mode visit
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
+
+    # end to end through the host-buffer C entry point (pinned host memory)
+    hcoef = torch.from_numpy(batch.coef.copy()).pin_memory()
+    hbase = torch.from_numpy(batch.base.copy()).pin_memory()
+    hc, hb = hcoef.numpy(), hbase.numpy()
+    f_idx = np.concatenate([np.arange(int(t), int(t) + RF) for t in batch.term_off])
+
+    def e2e_step():
+        hb[f_idx] = batch.base[f_idx]
+        hc[f_idx] = batch.coef[f_idx]
+        als.reduce_batched_host(hc, hb, batch.nbas, batch.rF, batch.rG, batch.term_off, NALS)
+    for _ in range(2):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = time.perf_counter() - t0
+    h2d = int(batch.coef.nbytes + batch.base.nbytes)
+    d2h = int(NVEC * RF * (batch.nD + 1) * 8)
+    e2e_value = NVEC * ws * args.steps / e2e_s
+
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "als_cluster_kernel_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("bytes_per_launch")
+
+    # CPU baseline: the oracle on a bounded sample (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        sample = min(NVEC, threads)
+        rate, dt = cpu_sample_rate(batch, sample, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{sample} of the {NVEC} vectors (full 10 sweeps each) in {dt:.1f} s"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
+                "config": dict(CONFIG, parallelism=f"replicas x{ws}"),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "gpu_launches": 2 * args.steps,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                             "kernel": "als_cluster_kernel", "kernel_ms": kernel_ms,
+                             "algorithmic_bytes": alg_bytes},
+                "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

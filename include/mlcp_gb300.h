@@ -1,0 +1,107 @@
+/*
+ * mlcp_gb300 — GB300-native replacement for MLCP's GPU power-iteration path.
+ *
+ * C ABI.  The first three entry points carry exactly the signatures of the
+ * reference's extern "C" layer (src/intertwining.cu:31, :98, :180), which
+ * MLCP's Fortran host binds through an implicit interface (gfortran name
+ * mangling: lower case plus a trailing underscore; every argument passed by
+ * reference, src/GPUIterate.f90:78, :162, :273).  prec_typ is double, as in
+ * the shipped build (Makefile:17, src/global.h:9-13).  Fortran LOGICAL
+ * arguments are read as one byte (`const bool &`), as the reference does.
+ *
+ * Unlike the reference, no entry point calls exit() or cudaDeviceReset():
+ * errors are recorded and can be read with mlcp_gb300_last_error(); the CUDA
+ * context, a device workspace and the uploaded operator list persist across
+ * calls.
+ *
+ * CP-vector layout for all calls (src/cpvector.cu:407-414): term r, mode d,
+ * index i at base[r*nD + off_d + i], off_d = sum_{e<d} nbas[e]; coef[r] per
+ * term.  Operator lists follow src/hoplist.h:2-7 (1-based opid and mptr,
+ * packed upper-triangular symmetric matrices).
+ */
+#ifndef MLCP_GB300_H
+#define MLCP_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define MLCP_API __attribute__((visibility("default")))
+#else
+#define MLCP_API
+#endif
+
+#ifdef __cplusplus
+#define MLCP_REF(T) const T&
+extern "C" {
+#else
+#include <stdbool.h>
+#define MLCP_REF(T) const T*
+#endif
+
+/* Replaces src/intertwining.cu:31 (intwdevicemem_): prints the device memory
+ * this implementation needs for one power cycle of the given shape. */
+MLCP_API void intwdevicemem_(MLCP_REF(int) rk, MLCP_REF(int) ndof, MLCP_REF(int) nbloc, MLCP_REF(int) TxD,
+                    MLCP_REF(int) nops, MLCP_REF(int) msize, MLCP_REF(int) ncpu, MLCP_REF(bool) update,
+                    const int *nbas);
+
+/* Replaces src/intertwining.cu:98 (intertwinecpp_): one intertwined power
+ * cycle on a block of nbloc vectors of rank rk — npow ALS-fitted applications
+ * of (H - Eshift) (sign flipped when ishift < 0; no shift when ishift == 0),
+ * ALS-guided Gram-Schmidt, and, when update is true, the block Rayleigh-Ritz
+ * problem (eigenvalues to eigv, ascending) followed by ALS-fitted vector
+ * updates.  base/coef/eigv are overwritten in place.  ncpu is accepted and
+ * ignored: the whole block is processed by batched kernels. */
+MLCP_API void intertwinecpp_(double *base, double *coef, int *nbas, MLCP_REF(int) rk, MLCP_REF(int) ndof,
+                    MLCP_REF(int) nbloc, int *opid, int *mptr, double *Hcoef, double *mat, MLCP_REF(int) TxD,
+                    MLCP_REF(int) nops, MLCP_REF(int) msize, double *eigv, MLCP_REF(int) npow,
+                    MLCP_REF(int) ncpu, MLCP_REF(int) nals, MLCP_REF(bool) update, MLCP_REF(int) ishift,
+                    MLCP_REF(double) Eshift);
+
+/* Replaces src/intertwining.cu:180 (alscpp_): nals ALS sweeps reducing the
+ * rank-rG target G (terms rF..rF+rG-1 of coef/base) to the rank-rF vector F
+ * (terms 0..rF-1, also the starting guess).  Overwrites terms 0..rF-1. */
+MLCP_API void alscpp_(double *coef, double *base, int *nbas, MLCP_REF(int) ndof, MLCP_REF(int) rF, MLCP_REF(int) rG,
+             MLCP_REF(int) nals);
+
+/* ---- Extensions (no counterpart in the reference's C layer) ---------- */
+
+/* Message describing the last failure on the calling thread ("" if none). */
+MLCP_API const char *mlcp_gb300_last_error(void);
+
+/* Status of the last entry-point call on the calling thread (0 = success). */
+MLCP_API int mlcp_gb300_last_status(void);
+
+/* Batched explicit-G ALS on device-resident data: nvec independent
+ * reductions with per-vector ranks.  Vector v occupies terms
+ * [term_off[v], term_off[v] + rF[v] + rG[v]) of d_coef/d_base: its rF[v]
+ * F terms (starting guess, overwritten) followed by its rG[v] target terms.
+ * Host arrays: nbas[ndof], rF, rG, term_off [nvec].  stream: a cudaStream_t
+ * (NULL = the library's own stream).  Returns 0 or an error code; per-vector
+ * numerical flags go to d_status[nvec] when non-NULL (bit 0: a normal-equation
+ * matrix was not positive definite).  Limits: rF <= 64, nbas[d] <= 64. */
+MLCP_API int mlcp_als_batched(int nvec, int ndof, const int *nbas, const int *rF, const int *rG, const long long *term_off,
+                     double *d_coef, double *d_base, int nals, int *d_status, void *stream);
+
+/* Same computation on host buffers: copies the batch to the device, reduces,
+ * and copies the F terms back (pinned host memory gives asynchronous copies). */
+MLCP_API int mlcp_als_batched_host(int nvec, int ndof, const int *nbas, const int *rF, const int *rG,
+                          const long long *term_off, double *h_coef, double *h_base, int nals, void *stream);
+
+/* Kernel timing (extension).  When enabled, the library records CUDA events
+ * around its dominant kernel of each call on the call's stream;
+ * mlcp_gb300_last_kernel_ms() synchronises on the end event and returns the
+ * elapsed milliseconds of the most recent such kernel (negative if none). */
+MLCP_API void mlcp_gb300_set_kernel_timing(int enable);
+MLCP_API double mlcp_gb300_last_kernel_ms(void);
+
+/* Full CP inner products out[v] = <X_v, Y_v> for nvec pairs of CP vectors in
+ * the reference layout on the device (FP64 arithmetic), used for residuals
+ * ||F - G|| = sqrt(<F,F> + <G,G> - 2<F,G>). */
+MLCP_API int mlcp_cp_dot_batched(int nvec, int ndof, const int *nbas, const long long *x_off, const int *rx,
+                        const long long *y_off, const int *ry, const double *d_coef, const double *d_base,
+                        double *d_out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

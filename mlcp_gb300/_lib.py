@@ -1,0 +1,79 @@
+"""Loader for the C-ABI library ``libmlcp_gb300.so`` (built in-tree).
+
+The product path has no CPU fallback: if the library cannot be built or
+loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+_lock = threading.Lock()
+_lib = None
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+_LL = ctypes.POINTER(ctypes.c_longlong)
+_V = ctypes.c_void_p
+
+
+class MlcpError(RuntimeError):
+    """Raised when an entry point of libmlcp_gb300 reports a failure."""
+
+
+def lib_path() -> str:
+    from . import build as _build
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = lib_path()
+        if build_if_missing:
+            from . import build as _build
+            path = _build.build()
+        if not os.path.exists(path):
+            raise MlcpError(f"libmlcp_gb300.so not found at {path}; run mlcp_gb300.build.build()")
+        L = ctypes.CDLL(path)
+        L.mlcp_gb300_last_error.restype = ctypes.c_char_p
+        L.mlcp_gb300_last_error.argtypes = []
+        L.mlcp_gb300_last_status.restype = ctypes.c_int
+        L.mlcp_als_batched.restype = ctypes.c_int
+        L.mlcp_als_batched.argtypes = [ctypes.c_int, ctypes.c_int, _I, _I, _I, _LL, _V, _V, ctypes.c_int, _V, _V]
+        L.mlcp_als_batched_host.restype = ctypes.c_int
+        L.mlcp_als_batched_host.argtypes = [ctypes.c_int, ctypes.c_int, _I, _I, _I, _LL, _D, _D, ctypes.c_int, _V]
+        L.mlcp_cp_dot_batched.restype = ctypes.c_int
+        L.mlcp_cp_dot_batched.argtypes = [ctypes.c_int, ctypes.c_int, _I, _LL, _I, _LL, _I, _V, _V, _V, _V]
+        L.mlcp_gb300_set_kernel_timing.restype = None
+        L.mlcp_gb300_set_kernel_timing.argtypes = [ctypes.c_int]
+        L.mlcp_gb300_last_kernel_ms.restype = ctypes.c_double
+        L.mlcp_gb300_last_kernel_ms.argtypes = []
+        L.alscpp_.restype = None
+        L.alscpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I]
+        if hasattr(L, "intertwinecpp_"):
+            L.intertwinecpp_.restype = None
+            L.intertwinecpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I, _I, _D, _D, _I, _I, _I, _D, _I, _I, _I,
+                                         ctypes.POINTER(ctypes.c_bool), _I, _D]
+        if hasattr(L, "intwdevicemem_"):
+            L.intwdevicemem_.restype = None
+            L.intwdevicemem_.argtypes = [_I, _I, _I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_bool), _I]
+        _lib = L
+        return L
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        msg = load().mlcp_gb300_last_error().decode(errors="replace")
+        raise MlcpError(f"libmlcp_gb300 error {rc}: {msg}")
+
+
+def last_status() -> int:
+    return load().mlcp_gb300_last_status()
+
+
+def last_error() -> str:
+    return load().mlcp_gb300_last_error().decode(errors="replace")

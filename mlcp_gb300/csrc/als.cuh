@@ -1,0 +1,50 @@
+// Batched explicit-target ALS: parameter block shared by host and device.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace mlcp {
+
+// All arrays are device pointers unless marked otherwise.
+struct AlsParams {
+  int nvec;          // vectors in the batch
+  int ndof;          // modes D
+  int nD;            // sum of basis sizes (reference layout row length)
+  int nDp;           // sum of 4-padded basis sizes (FP32 copies)
+  int npmax;         // max 4-padded basis size
+  int nals;          // sweeps
+  int rows_cta_max;  // max target terms owned by one CTA
+  long long total_rows;     // sum of rG
+  long long total_f_terms;  // sum of rF
+  const int* nbas;   // [D]
+  const int* off;    // [D+1] offsets in the reference layout
+  const int* offp;   // [D+1] offsets of the 4-padded layout
+  const int* rF;     // [nvec]
+  const int* rG;     // [nvec]
+  const long long* term_off;   // [nvec] first term (F) of each vector in base/coef
+  const long long* g_row_off;  // [nvec] prefix sum of rG
+  const long long* f_row_off;  // [nvec] prefix sum of rF
+  const long long* gm_off;     // [nvec] start of each vector in gm
+  const long long* sq_off;     // [nvec] prefix sum of rF*rF*D (Gram storage)
+  double* base;      // reference-layout factors, F terms overwritten in place
+  double* coef;      // reference-layout weights, F weights overwritten
+  float* gm;         // FP32 mode-major target factors
+  float* gc;         // FP32 target weights [total_rows]
+  float* f32;        // FP32 copy of F [total_f_terms][nDp]
+  double* gram;      // FP64 per-mode F Grams [total_f_terms * rF * D] (rF*rF*D per vector)
+  double* suf;       // FP64 suffix products, same shape as gram
+  int* status;       // [nvec] bit 0: non-positive Cholesky pivot
+};
+
+constexpr int kAlsThreads = 256;
+
+// Shared memory of the cluster kernel for a CTA owning rows_cta target terms.
+size_t als_smem_bytes(int rows_cta, int rF, int npmax);
+
+// Enqueue the preparation kernel and the persistent cluster kernel
+// (grid = nvec clusters of `cluster` CTAs).  Returns a Status.
+// When t0/t1 are non-null they are recorded around the cluster kernel.
+int als_launch(const AlsParams& p, int cluster, size_t smem, cudaStream_t st, cudaEvent_t t0 = nullptr,
+               cudaEvent_t t1 = nullptr);
+
+}  // namespace mlcp

@@ -1,0 +1,549 @@
+// C entry points (drop-in for the reference's src/intertwining.cu) and the
+// host-side planners of the batched ALS.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/mlcp_gb300.h"
+#include "als.cuh"
+#include "common.cuh"
+#include "context.cuh"
+
+namespace mlcp {
+
+// ---------------------------------------------------------------------------
+// Errors
+// ---------------------------------------------------------------------------
+
+static thread_local std::string t_error;
+static thread_local int t_status = 0;
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  t_error = buf;
+}
+const char* last_error() { return t_error.c_str(); }
+
+static int finish(int status) {
+  t_status = status;
+  if (status == kOk) t_error.clear();
+  return status;
+}
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+
+static std::mutex g_ctx_mu;
+static std::map<int, Context*> g_ctx;
+
+Context* get_context(int* status) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_error("cudaGetDevice failed: %s", cudaGetErrorString(e));
+    *status = kCudaError;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  auto it = g_ctx.find(dev);
+  if (it != g_ctx.end()) {
+    *status = kOk;
+    return it->second;
+  }
+  Context* c = new Context();
+  c->device = dev;
+  cudaDeviceProp prop;
+  e = cudaGetDeviceProperties(&prop, dev);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->t0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->t1);
+  if (e != cudaSuccess) {
+    set_error("context creation failed: %s", cudaGetErrorString(e));
+    delete c;
+    *status = kCudaError;
+    return nullptr;
+  }
+  c->num_sms = prop.multiProcessorCount;
+  c->smem_optin = prop.sharedMemPerBlockOptin;
+  g_ctx[dev] = c;
+  *status = kOk;
+  return c;
+}
+
+int ensure_workspace(Context* ctx, size_t bytes, void** out) {
+  if (bytes > ctx->ws_bytes) {
+    if (ctx->ws) {
+      MLCP_CUDA_TRY(cudaDeviceSynchronize());
+      MLCP_CUDA_TRY(cudaFree(ctx->ws));
+      ctx->ws = nullptr;
+      ctx->ws_bytes = 0;
+    }
+    size_t want = std::max(bytes, ctx->ws_bytes + ctx->ws_bytes / 2);
+    MLCP_CUDA_TRY(cudaMalloc(&ctx->ws, want));
+    ctx->ws_bytes = want;
+  }
+  *out = ctx->ws;
+  return kOk;
+}
+
+int ensure_stage(Context* ctx, size_t bytes, void** out) {
+  MLCP_CUDA_TRY(cudaEventSynchronize(ctx->staged));
+  if (bytes > ctx->stage_bytes) {
+    if (ctx->stage) MLCP_CUDA_TRY(cudaFreeHost(ctx->stage));
+    size_t want = std::max(bytes, size_t(1) << 16);
+    MLCP_CUDA_TRY(cudaMallocHost(&ctx->stage, want));
+    ctx->stage_bytes = want;
+  }
+  *out = ctx->stage;
+  return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// Batched explicit-G ALS planner
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr int kMaxRank = 64;
+constexpr int kMaxBasis = 64;
+
+struct AlsPlan {
+  int D, nD, nDp, npmax, cluster, rows_cta_max, rFmax;
+  std::vector<int> off, offp;
+  std::vector<long long> g_row_off, f_row_off, gm_off, sq_off;
+  long long total_rows, total_f, gm_floats, sq_doubles;
+  size_t smem;
+};
+
+int plan_als(Context* ctx, int nvec, int ndof, const int* nbas, const int* rF, const int* rG, AlsPlan* P) {
+  if (nvec < 1 || ndof < 1) {
+    set_error("mlcp_als_batched: nvec (%d) and ndof (%d) must be positive", nvec, ndof);
+    return kBadArgument;
+  }
+  P->D = ndof;
+  P->off.assign(ndof + 1, 0);
+  P->offp.assign(ndof + 1, 0);
+  P->npmax = 4;
+  for (int d = 0; d < ndof; ++d) {
+    if (nbas[d] < 1 || nbas[d] > kMaxBasis) {
+      set_error("mlcp_als_batched: nbas[%d] = %d outside [1, %d]", d, nbas[d], kMaxBasis);
+      return nbas[d] < 1 ? kBadArgument : kTooLarge;
+    }
+    P->off[d + 1] = P->off[d] + nbas[d];
+    P->offp[d + 1] = P->offp[d] + round_up(nbas[d], 4);
+    P->npmax = std::max(P->npmax, round_up(nbas[d], 4));
+  }
+  P->nD = P->off[ndof];
+  P->nDp = P->offp[ndof];
+  P->g_row_off.resize(nvec);
+  P->f_row_off.resize(nvec);
+  P->gm_off.resize(nvec);
+  P->sq_off.resize(nvec);
+  long long gr = 0, fr = 0, gmo = 0, sq = 0;
+  int rGmax = 0;
+  P->rFmax = 0;
+  for (int v = 0; v < nvec; ++v) {
+    if (rF[v] < 1 || rG[v] < 1) {
+      set_error("mlcp_als_batched: vector %d has rF=%d rG=%d (both must be positive)", v, rF[v], rG[v]);
+      return kBadArgument;
+    }
+    if (rF[v] > kMaxRank) {
+      set_error("mlcp_als_batched: vector %d has rF=%d > %d", v, rF[v], kMaxRank);
+      return kTooLarge;
+    }
+    P->g_row_off[v] = gr;
+    P->f_row_off[v] = fr;
+    P->gm_off[v] = gmo;
+    P->sq_off[v] = sq;
+    gr += rG[v];
+    fr += rF[v];
+    gmo += (long long)rG[v] * P->nDp;
+    sq += (long long)rF[v] * rF[v] * ndof;
+    rGmax = std::max(rGmax, rG[v]);
+    P->rFmax = std::max(P->rFmax, rF[v]);
+  }
+  P->total_rows = gr;
+  P->total_f = fr;
+  P->gm_floats = gmo;
+  P->sq_doubles = sq;
+  // cluster size: enough CTAs to cover the SMs, enough to fit the running
+  // products of a term range in shared memory
+  int cl = 1;
+  while (cl < 16 && cl * 2 * nvec <= ctx->num_sms) cl *= 2;
+  for (;;) {
+    const int rows = (rGmax + cl - 1) / cl;
+    const size_t smem = als_smem_bytes(rows, P->rFmax, P->npmax);
+    if (smem <= ctx->smem_optin) {
+      P->cluster = cl;
+      P->rows_cta_max = rows;
+      P->smem = smem;
+      break;
+    }
+    if (cl >= 16) {
+      set_error("mlcp_als_batched: rank-%d target with rank-%d F needs %zu bytes of shared memory per CTA "
+                "even with 16-CTA clusters (limit %zu)", rGmax, P->rFmax, smem, ctx->smem_optin);
+      return kTooLarge;
+    }
+    cl *= 2;
+  }
+  return kOk;
+}
+
+}  // namespace
+
+// Runs the batched ALS on device data; everything is enqueued on `st`.
+int als_batched_device(Context* ctx, int nvec, int ndof, const int* nbas, const int* rF, const int* rG,
+                       const long long* term_off, double* d_coef, double* d_base, int nals, int* d_status,
+                       cudaStream_t st) {
+  if (nals == 0) return kOk;  // reference returns before touching the data (src/als.cu:1026)
+  if (nals < 0) {
+    set_error("mlcp_als_batched: nals = %d is negative", nals);
+    return kBadArgument;
+  }
+  AlsPlan P;
+  int rc = plan_als(ctx, nvec, ndof, nbas, rF, rG, &P);
+  if (rc) return rc;
+
+  // metadata block: ints then long longs (uploaded in one copy)
+  const size_t n_int = (size_t)(ndof) + 2 * (ndof + 1) + 2 * nvec;
+  const size_t n_ll = (size_t)6 * nvec;
+  const size_t meta_bytes = align256(n_int * sizeof(int)) + n_ll * sizeof(long long);
+  // workspace layout
+  size_t bytes = 0;
+  auto reserve = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
+  const size_t o_meta = reserve(meta_bytes);
+  const size_t o_gm = reserve(sizeof(float) * P.gm_floats);
+  const size_t o_gc = reserve(sizeof(float) * P.total_rows);
+  const size_t o_f32 = reserve(sizeof(float) * P.total_f * P.nDp);
+  const size_t o_gram = reserve(sizeof(double) * P.sq_doubles);
+  const size_t o_suf = reserve(sizeof(double) * P.sq_doubles);
+  const size_t o_status = reserve(sizeof(int) * nvec);
+  void* ws = nullptr;
+  rc = ensure_workspace(ctx, bytes, &ws);
+  if (rc) return rc;
+  char* w = static_cast<char*>(ws);
+
+  void* stage = nullptr;
+  rc = ensure_stage(ctx, meta_bytes, &stage);
+  if (rc) return rc;
+  int* hi = static_cast<int*>(stage);
+  long long* hl = reinterpret_cast<long long*>(static_cast<char*>(stage) + align256(n_int * sizeof(int)));
+  int* p_nbas = hi;
+  int* p_off = p_nbas + ndof;
+  int* p_offp = p_off + (ndof + 1);
+  int* p_rF = p_offp + (ndof + 1);
+  int* p_rG = p_rF + nvec;
+  std::memcpy(p_nbas, nbas, sizeof(int) * ndof);
+  std::memcpy(p_off, P.off.data(), sizeof(int) * (ndof + 1));
+  std::memcpy(p_offp, P.offp.data(), sizeof(int) * (ndof + 1));
+  std::memcpy(p_rF, rF, sizeof(int) * nvec);
+  std::memcpy(p_rG, rG, sizeof(int) * nvec);
+  long long* p_term = hl;
+  long long* p_gro = p_term + nvec;
+  long long* p_fro = p_gro + nvec;
+  long long* p_gmo = p_fro + nvec;
+  long long* p_sqo = p_gmo + nvec;
+  std::memcpy(p_term, term_off, sizeof(long long) * nvec);
+  std::memcpy(p_gro, P.g_row_off.data(), sizeof(long long) * nvec);
+  std::memcpy(p_fro, P.f_row_off.data(), sizeof(long long) * nvec);
+  std::memcpy(p_gmo, P.gm_off.data(), sizeof(long long) * nvec);
+  std::memcpy(p_sqo, P.sq_off.data(), sizeof(long long) * nvec);
+  MLCP_CUDA_TRY(cudaMemcpyAsync(w + o_meta, stage, meta_bytes, cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaEventRecord(ctx->staged, st));
+
+  const char* dm = w + o_meta;
+  const int* d_int = reinterpret_cast<const int*>(dm);
+  const long long* d_ll = reinterpret_cast<const long long*>(dm + align256(n_int * sizeof(int)));
+  AlsParams prm;
+  prm.nvec = nvec;
+  prm.ndof = ndof;
+  prm.nD = P.nD;
+  prm.nDp = P.nDp;
+  prm.npmax = P.npmax;
+  prm.nals = nals;
+  prm.rows_cta_max = P.rows_cta_max;
+  prm.total_rows = P.total_rows;
+  prm.total_f_terms = P.total_f;
+  prm.nbas = d_int;
+  prm.off = d_int + ndof;
+  prm.offp = prm.off + (ndof + 1);
+  prm.rF = prm.offp + (ndof + 1);
+  prm.rG = prm.rF + nvec;
+  prm.term_off = d_ll;
+  prm.g_row_off = d_ll + nvec;
+  prm.f_row_off = d_ll + 2 * nvec;
+  prm.gm_off = d_ll + 3 * nvec;
+  prm.sq_off = d_ll + 4 * nvec;
+  prm.base = d_base;
+  prm.coef = d_coef;
+  prm.gm = reinterpret_cast<float*>(w + o_gm);
+  prm.gc = reinterpret_cast<float*>(w + o_gc);
+  prm.f32 = reinterpret_cast<float*>(w + o_f32);
+  prm.gram = reinterpret_cast<double*>(w + o_gram);
+  prm.suf = reinterpret_cast<double*>(w + o_suf);
+  prm.status = d_status ? d_status : reinterpret_cast<int*>(w + o_status);
+  MLCP_CUDA_TRY(cudaMemsetAsync(prm.status, 0, sizeof(int) * nvec, st));
+
+  ctx->timed = ctx->timing;
+  return als_launch(prm, P.cluster, P.smem, st, ctx->timing ? ctx->t0 : nullptr, ctx->timing ? ctx->t1 : nullptr);
+}
+
+// ---------------------------------------------------------------------------
+// Full CP inner products (FP64), deterministic two-stage reduction
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct DotParams {
+  int nvec, ndof, nD, chunks;
+  const int* nbas;
+  const long long* x_off;
+  const int* rx;
+  const long long* y_off;
+  const int* ry;
+  const double* coef;
+  const double* base;
+  double* partial;  // [nvec][chunks]
+};
+
+__global__ void cp_dot_kernel(DotParams p) {
+  const int v = blockIdx.y, chunk = blockIdx.x;
+  const int rx = p.rx[v], ry = p.ry[v];
+  const long long npairs = (long long)rx * ry;
+  const long long per = (npairs + p.chunks - 1) / p.chunks;
+  const long long e0 = chunk * per, e1 = min(npairs, e0 + per);
+  double acc = 0.0;
+  for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const int i = (int)(e / ry), j = (int)(e % ry);
+    const double* a = p.base + (p.x_off[v] + i) * (long long)p.nD;
+    const double* b = p.base + (p.y_off[v] + j) * (long long)p.nD;
+    double prod = p.coef[p.x_off[v] + i] * p.coef[p.y_off[v] + j];
+    int s = 0;
+    for (int d = 0; d < p.ndof; ++d) {
+      const int n = p.nbas[d];
+      double t = 0.0;
+      for (int q = 0; q < n; ++q) t += a[s + q] * b[s + q];
+      prod *= t;
+      s += n;
+    }
+    acc += prod;
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) p.partial[(long long)v * p.chunks + chunk] = red[0];
+}
+
+__global__ void cp_dot_finish(const double* partial, int chunks, int nvec, double* out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nvec) return;
+  double s = 0.0;
+  for (int c = 0; c < chunks; ++c) s += partial[(long long)v * chunks + c];
+  out[v] = s;
+}
+
+}  // namespace
+
+int cp_dot_device(Context* ctx, int nvec, int ndof, const int* nbas, const long long* x_off, const int* rx,
+                  const long long* y_off, const int* ry, const double* d_coef, const double* d_base, double* d_out,
+                  cudaStream_t st) {
+  if (nvec < 1 || ndof < 1) {
+    set_error("mlcp_cp_dot_batched: nvec and ndof must be positive");
+    return kBadArgument;
+  }
+  int nD = 0;
+  for (int d = 0; d < ndof; ++d) nD += nbas[d];
+  const int chunks = std::max(1, (2 * ctx->num_sms + nvec - 1) / nvec);
+  const size_t n_int = (size_t)ndof + 2 * nvec;
+  const size_t meta = align256(n_int * sizeof(int)) + 2 * nvec * sizeof(long long);
+  void* ws = nullptr;
+  int rc = ensure_workspace(ctx, align256(meta) + sizeof(double) * (size_t)nvec * chunks, &ws);
+  if (rc) return rc;
+  void* stage = nullptr;
+  rc = ensure_stage(ctx, meta, &stage);
+  if (rc) return rc;
+  int* hi = static_cast<int*>(stage);
+  std::memcpy(hi, nbas, sizeof(int) * ndof);
+  std::memcpy(hi + ndof, rx, sizeof(int) * nvec);
+  std::memcpy(hi + ndof + nvec, ry, sizeof(int) * nvec);
+  long long* hl = reinterpret_cast<long long*>(static_cast<char*>(stage) + align256(n_int * sizeof(int)));
+  std::memcpy(hl, x_off, sizeof(long long) * nvec);
+  std::memcpy(hl + nvec, y_off, sizeof(long long) * nvec);
+  char* w = static_cast<char*>(ws);
+  MLCP_CUDA_TRY(cudaMemcpyAsync(w, stage, meta, cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaEventRecord(ctx->staged, st));
+  DotParams p;
+  p.nvec = nvec;
+  p.ndof = ndof;
+  p.nD = nD;
+  p.chunks = chunks;
+  p.nbas = reinterpret_cast<const int*>(w);
+  p.rx = p.nbas + ndof;
+  p.ry = p.rx + nvec;
+  p.x_off = reinterpret_cast<const long long*>(w + align256(n_int * sizeof(int)));
+  p.y_off = p.x_off + nvec;
+  p.coef = d_coef;
+  p.base = d_base;
+  p.partial = reinterpret_cast<double*>(w + align256(meta));
+  cp_dot_kernel<<<dim3(chunks, nvec), 256, 0, st>>>(p);
+  MLCP_CUDA_TRY(cudaGetLastError());
+  cp_dot_finish<<<(nvec + 127) / 128, 128, 0, st>>>(p.partial, chunks, nvec, d_out);
+  MLCP_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+}  // namespace mlcp
+
+// ---------------------------------------------------------------------------
+// extern "C" layer
+// ---------------------------------------------------------------------------
+
+using namespace mlcp;
+
+extern "C" const char* mlcp_gb300_last_error(void) { return last_error(); }
+
+extern "C" void mlcp_gb300_set_kernel_timing(int enable) {
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (!ctx) return;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->timing = enable != 0;
+}
+
+extern "C" double mlcp_gb300_last_kernel_ms(void) {
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (!ctx) return -1.0;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!ctx->timed) return -1.0;
+  if (cudaEventSynchronize(ctx->t1) != cudaSuccess) return -1.0;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, ctx->t0, ctx->t1) != cudaSuccess) return -1.0;
+  return ms;
+}
+extern "C" int mlcp_gb300_last_status(void) { return t_status; }
+
+static cudaStream_t pick_stream(Context* ctx, void* stream) {
+  return stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+}
+
+extern "C" int mlcp_als_batched(int nvec, int ndof, const int* nbas, const int* rF, const int* rG,
+                                const long long* term_off, double* d_coef, double* d_base, int nals, int* d_status,
+                                void* stream) {
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (!ctx) return finish(rc);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  rc = als_batched_device(ctx, nvec, ndof, nbas, rF, rG, term_off, d_coef, d_base, nals, d_status,
+                          pick_stream(ctx, stream));
+  return finish(rc);
+}
+
+extern "C" int mlcp_als_batched_host(int nvec, int ndof, const int* nbas, const int* rF, const int* rG,
+                                     const long long* term_off, double* h_coef, double* h_base, int nals,
+                                     void* stream) {
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (!ctx) return finish(rc);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (nals == 0) return finish(kOk);
+  if (nvec < 1 || ndof < 1) {
+    set_error("mlcp_als_batched_host: nvec and ndof must be positive");
+    return finish(kBadArgument);
+  }
+  cudaStream_t st = pick_stream(ctx, stream);
+  int nD = 0;
+  for (int d = 0; d < ndof; ++d) nD += nbas[d];
+  long long nterms = 0;
+  for (int v = 0; v < nvec; ++v) nterms = std::max(nterms, term_off[v] + rF[v] + rG[v]);
+  // device copies of the caller's buffers live in their own allocation so the
+  // ALS workspace can grow independently
+  const size_t need = sizeof(double) * (size_t)nterms * (nD + 1);
+  if (need > ctx->io_bytes) {
+    if (ctx->io) {
+      cudaError_t e0 = cudaStreamSynchronize(st);
+      if (e0 == cudaSuccess) e0 = cudaFree(ctx->io);
+      if (e0 != cudaSuccess) {
+        set_error("releasing the I/O buffer failed: %s", cudaGetErrorString(e0));
+        return finish(kCudaError);
+      }
+    }
+    ctx->io = nullptr;
+    ctx->io_bytes = 0;
+    cudaError_t e = cudaMalloc(&ctx->io, need);
+    if (e != cudaSuccess) {
+      set_error("cudaMalloc(%zu) failed: %s", need, cudaGetErrorString(e));
+      return finish(kCudaError);
+    }
+    ctx->io_bytes = need;
+  }
+  double* d_buf = static_cast<double*>(ctx->io);
+  double* d_base = d_buf;
+  double* d_coef = d_buf + (size_t)nterms * nD;
+  auto cpy = [&](void* dst, const void* src, size_t b, cudaMemcpyKind k) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, b, k, st);
+    if (e != cudaSuccess) set_error("cudaMemcpyAsync failed: %s", cudaGetErrorString(e));
+    return e == cudaSuccess ? kOk : kCudaError;
+  };
+  if ((rc = cpy(d_base, h_base, sizeof(double) * (size_t)nterms * nD, cudaMemcpyHostToDevice))) return finish(rc);
+  if ((rc = cpy(d_coef, h_coef, sizeof(double) * (size_t)nterms, cudaMemcpyHostToDevice))) return finish(rc);
+  rc = als_batched_device(ctx, nvec, ndof, nbas, rF, rG, term_off, d_coef, d_base, nals, nullptr, st);
+  if (rc) return finish(rc);
+  for (int v = 0; v < nvec; ++v) {
+    const size_t t0 = (size_t)term_off[v];
+    if ((rc = cpy(h_base + t0 * nD, d_base + t0 * nD, sizeof(double) * (size_t)rF[v] * nD, cudaMemcpyDeviceToHost)))
+      return finish(rc);
+    if ((rc = cpy(h_coef + t0, d_coef + t0, sizeof(double) * (size_t)rF[v], cudaMemcpyDeviceToHost)))
+      return finish(rc);
+  }
+  if (!stream) {
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      set_error("ALS failed: %s", cudaGetErrorString(e));
+      return finish(kCudaError);
+    }
+  }
+  return finish(kOk);
+}
+
+extern "C" int mlcp_cp_dot_batched(int nvec, int ndof, const int* nbas, const long long* x_off, const int* rx,
+                                   const long long* y_off, const int* ry, const double* d_coef,
+                                   const double* d_base, double* d_out, void* stream) {
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (!ctx) return finish(rc);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  rc = cp_dot_device(ctx, nvec, ndof, nbas, x_off, rx, y_off, ry, d_coef, d_base, d_out, pick_stream(ctx, stream));
+  return finish(rc);
+}
+
+// Reference src/intertwining.cu:180.  Same argument meaning; the whole
+// reduction runs in one cluster launch and the context is kept.
+extern "C" void alscpp_(double* coef, double* base, int* nbas, const int& ndof, const int& rF, const int& rG,
+                        const int& nals) {
+  if (nals == 0) {
+    finish(kOk);
+    return;
+  }
+  // The reference walks the target in blocks of rF terms (nbloc = (rF+rG)/rF,
+  // src/intertwining.cu:189, src/als.cu:1003), so only the first
+  // (rG/rF)*rF target terms take part; callers pad G to a multiple of rF.
+  const int rGe = (rG / rF) * rF;
+  const long long term_off = 0;
+  const int rc = mlcp_als_batched_host(1, ndof, nbas, &rF, &rGe, &term_off, coef, base, nals, nullptr);
+  if (rc != kOk) fprintf(stderr, "alscpp_: %s\n", mlcp_gb300_last_error());
+}

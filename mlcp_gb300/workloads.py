@@ -1,0 +1,67 @@
+"""Seeded synthetic inputs with the shapes and value distributions of the
+benchmark configurations (no dataset is involved anywhere in this path).
+
+ALS microbenchmark (explicit-target reduction): D modes of n basis
+functions, a target of rank rG with factor entries N(0,1)/sqrt(n) and weights
+log-uniform in [1e-6, 1], reduced to rank rF; the starting guess is the first
+rF target terms.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+ALS_SEED = 20261203
+
+
+@dataclass
+class AlsBatch:
+    nbas: np.ndarray      # int32 [D]
+    rF: np.ndarray        # int32 [nvec]
+    rG: np.ndarray        # int32 [nvec]
+    term_off: np.ndarray  # int64 [nvec]
+    coef: np.ndarray      # float64 [nterms]
+    base: np.ndarray      # float64 [nterms, nD]
+
+    @property
+    def nvec(self) -> int:
+        return int(self.rF.size)
+
+    @property
+    def nD(self) -> int:
+        return int(self.nbas.sum())
+
+    def vector(self, v: int):
+        """(coef, base) of vector v: F terms then G terms (copies)."""
+        t0 = int(self.term_off[v])
+        t1 = t0 + int(self.rF[v] + self.rG[v])
+        return self.coef[t0:t1].copy(), self.base[t0:t1].copy()
+
+    def g_bytes(self, itemsize: int = 4) -> int:
+        return int(self.rG.sum()) * self.nD * itemsize
+
+
+def als_batch(nvec: int, D: int, n, rF, rG, seed: int = ALS_SEED) -> AlsBatch:
+    """Batch of independent reductions.  ``n`` may be an int or a per-mode
+    list; ``rF``/``rG`` may be ints or per-vector lists (ragged batches)."""
+    rng = np.random.default_rng(seed)
+    nbas = np.full(D, n, dtype=np.int32) if np.isscalar(n) else np.asarray(n, dtype=np.int32)
+    rFa = np.full(nvec, rF, dtype=np.int32) if np.isscalar(rF) else np.asarray(rF, dtype=np.int32)
+    rGa = np.full(nvec, rG, dtype=np.int32) if np.isscalar(rG) else np.asarray(rG, dtype=np.int32)
+    nD = int(nbas.sum())
+    sizes = (rFa + rGa).astype(np.int64)
+    term_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    nterms = int(sizes.sum())
+    base = np.empty((nterms, nD))
+    coef = np.empty(nterms)
+    scale = np.repeat(1.0 / np.sqrt(nbas.astype(np.float64)), nbas)
+    for v in range(nvec):
+        t0, f, g = int(term_off[v]), int(rFa[v]), int(rGa[v])
+        G = rng.standard_normal((g, nD)) * scale
+        cg = np.exp(rng.uniform(np.log(1e-6), 0.0, g))
+        base[t0 + f:t0 + f + g] = G
+        coef[t0 + f:t0 + f + g] = cg
+        base[t0:t0 + f] = G[:f]
+        coef[t0:t0 + f] = cg[:f]
+    return AlsBatch(nbas=nbas, rF=rFa, rG=rGa, term_off=term_off, coef=coef, base=base)

@@ -1,0 +1,182 @@
+"""CPU oracle for the MLCP power-iteration hot path (test infrastructure).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this package, and only as the checker.  The product
+library under ``mlcp_gb300/`` never calls it.
+
+The C code in ``mlcp_oracle.c`` restates the reference's CUDA algorithm
+(src/intertwining.cu, src/als.cu, src/intertw_mvp.cu, src/intertw_lcv.cu)
+in FP64.  Parity is unpinned: the reference holds no golden vectors for this
+path and cannot be run here; mathematical known answers stand in.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_LIB_PATH = os.path.join(_BUILD, "libmlcp_oracle.so")
+_lib: Optional[ctypes.CDLL] = None
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (FP contraction off: identical bits on x86 and Arm)."""
+    src = os.path.join(_HERE, "mlcp_oracle.c")
+    if not force and os.path.exists(_LIB_PATH) and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(src):
+        return _LIB_PATH
+    os.makedirs(_BUILD, exist_ok=True)
+    tmp = _LIB_PATH + f".tmp{os.getpid()}"
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC", "-o", tmp, src, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, _LIB_PATH)
+    return _LIB_PATH
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        L = _lib
+        L.orc_alscpp.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_intertwine.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        L.orc_pow_als_block.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+        L.orc_gram_schmidt.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_gen_eig.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D,
+                                  ctypes.c_int, ctypes.c_int, _D, _D, ctypes.c_int]
+        L.orc_vector_updates.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D,
+                                         ctypes.c_int, ctypes.c_int]
+        L.orc_cp_dot.restype = ctypes.c_double
+        L.orc_cp_dot.argtypes = [_D, _D, ctypes.c_int, _D, _D, ctypes.c_int, _I, ctypes.c_int]
+        L.orc_als_batched.argtypes = [ctypes.c_int, ctypes.POINTER(_D), ctypes.POINTER(_D), _I, ctypes.c_int,
+                                      _I, _I, ctypes.c_int, ctypes.c_int]
+        L.orc_sygv.restype = ctypes.c_int
+        L.orc_sygv.argtypes = [ctypes.c_int, _D, _D, _D, _D]
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_D)
+
+
+def _ip(a: np.ndarray):
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_I)
+
+
+def als(coef: np.ndarray, base: np.ndarray, nbas, rF: int, rG: int, nals: int):
+    """Reference alscpp_ semantics.  ``base`` is (rF+rG, nD) row = term; returns
+    the reduced (coef[rF], base[rF, nD]) as new arrays.  As in the reference,
+    the target is processed in blocks of rF terms, so rG must be a multiple of
+    rF (callers pad with zero-weight terms, src/GPUIterate.f90:249-268)."""
+    if rG % rF != 0:
+        raise ValueError(f"rG={rG} is not a multiple of rF={rF}; pad the target (see pad_target)")
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    lib().orc_alscpp(_dp(coef), _dp(base), _ip(nb), len(nb), rF, rG, nals)
+    return coef[:rF].copy(), base[:rF].copy()
+
+
+def pad_target(coef: np.ndarray, base: np.ndarray, rF: int, rG: int, seed: int = 0):
+    """Pad the target to a multiple of rF with random-factor, zero-weight
+    terms, as the reference's GPU_ALS_AB does (src/GPUIterate.f90:249-268)."""
+    rGa = (rG + rF - 1) // rF * rF
+    if rGa == rG:
+        return coef.copy(), base.copy(), rG
+    rng = np.random.default_rng(seed)
+    extra = rGa - rG
+    c = np.concatenate([coef[:rF + rG], np.zeros(extra)])
+    b = np.vstack([base[:rF + rG], rng.uniform(0.0, 1.0, size=(extra, base.shape[1]))])
+    return c, b, rGa
+
+
+def als_batched(coefs, bases, nbas, rFs, rGs, nals: int, nthreads: int = 0):
+    """Independent explicit-G reductions, OpenMP over vectors; in place."""
+    n = len(coefs)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    cp = (_D * n)(*[_dp(c) for c in coefs])
+    bp = (_D * n)(*[_dp(b) for b in bases])
+    rf = np.ascontiguousarray(rFs, dtype=np.int32)
+    rg = np.ascontiguousarray(rGs, dtype=np.int32)
+    lib().orc_als_batched(n, cp, bp, _ip(nb), len(nb), _ip(rf), _ip(rg), nals, nthreads)
+
+
+def intertwine(base, coef, nbas, rk, nbloc, hl, eigv, npow, nals, update=True, ishift=1, Eshift=0.0, ncpu=0):
+    """Reference intertwinecpp_ semantics on copies; returns (base, coef, eigv)."""
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    eig = np.ascontiguousarray(eigv, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    lib().orc_intertwine(_dp(base), _dp(coef), _ip(nb), rk, len(nb), nbloc, _ip(hl.opid), _ip(hl.mptr),
+                         _dp(hl.coef), _dp(hl.mat), hl.opid.size, hl.mptr.size, hl.mat.size, _dp(eig),
+                         npow, ncpu, nals, int(bool(update)), ishift, float(Eshift))
+    return base, coef, eig
+
+
+def pow_als_block(base, coef, nbas, rk, nbloc, hl, npow, ishift=1, Eshift=0.0, nthreads=0):
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    lib().orc_pow_als_block(_dp(base), _dp(coef), _ip(nb), rk, len(nb), nbloc, _ip(hl.opid), _ip(hl.mptr),
+                            _dp(hl.coef), _dp(hl.mat), hl.nterms, npow, ishift, float(Eshift), nthreads)
+    return base, coef
+
+
+def gram_schmidt(base, coef, nbas, rk, nbloc, nals):
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    lib().orc_gram_schmidt(_dp(base), _dp(coef), _ip(nb), rk, len(nb), nbloc, nals)
+    return base, coef
+
+
+def gen_eig(base, coef, nbas, rk, nbloc, hl, nals, nthreads=0):
+    base = np.ascontiguousarray(base, dtype=np.float64)
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    eig = np.zeros(nbloc)
+    U = np.zeros(nbloc * nbloc)
+    lib().orc_gen_eig(_dp(base), _dp(coef), _ip(nb), rk, len(nb), nbloc, _ip(hl.opid), _ip(hl.mptr),
+                      _dp(hl.coef), _dp(hl.mat), hl.nterms, nals, _dp(eig), _dp(U), nthreads)
+    return eig, U.reshape(nbloc, nbloc).T.copy()  # U[:, i] = eigenvector i
+
+
+def vector_updates(base, coef, nbas, rk, nbloc, U, nals, nthreads=0):
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    Ucm = np.ascontiguousarray(np.asarray(U, dtype=np.float64).T)  # column-major
+    lib().orc_vector_updates(_dp(base), _dp(coef), _ip(nb), rk, len(nb), nbloc, _dp(Ucm), nals, nthreads)
+    return base, coef
+
+
+def cp_dot(vb, vc, wb, wc, nbas) -> float:
+    vb = np.ascontiguousarray(vb, dtype=np.float64)
+    vc = np.ascontiguousarray(vc, dtype=np.float64)
+    wb = np.ascontiguousarray(wb, dtype=np.float64)
+    wc = np.ascontiguousarray(wc, dtype=np.float64)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    return lib().orc_cp_dot(_dp(vb), _dp(vc), vc.size, _dp(wb), _dp(wc), wc.size, _ip(nb), len(nb))
+
+
+def sygv(A: np.ndarray, B: np.ndarray):
+    """A x = w B x; returns (w ascending, X with columns = eigenvectors)."""
+    n = A.shape[0]
+    Acm = np.ascontiguousarray(np.asarray(A, dtype=np.float64).T)
+    Bcm = np.ascontiguousarray(np.asarray(B, dtype=np.float64).T)
+    w = np.zeros(n)
+    X = np.zeros(n * n)
+    info = lib().orc_sygv(n, _dp(Acm), _dp(Bcm), _dp(w), _dp(X))
+    return w, X.reshape(n, n).T.copy(), info

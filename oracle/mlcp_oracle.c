@@ -1,0 +1,691 @@
+/*
+ * CPU oracle for the MLCP GPU power-iteration hot path (TEST INFRASTRUCTURE).
+ *
+ * Only tests/, the smoke entry and bench.py's CPU-baseline leg call this code,
+ * as the checker.  It restates the reference's CUDA algorithm in FP64 C; each
+ * function names the reference file:line it follows.  Parity is unpinned
+ * (the reference has no golden data for this path); see mlcp_oracle.h.
+ *
+ * Built with -ffp-contract=off so that x86 and Arm hosts give identical bits.
+ */
+#include "mlcp_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------ */
+/* CP-vector views                                                      */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+  int nrk;           /* number of terms */
+  int ndof;          /* number of modes */
+  int nD;            /* sum of basis sizes */
+  const int *nbas;   /* basis size per mode */
+  const int *off;    /* mode offsets, off[ndof] == nD */
+  double *coef;      /* nrk weights */
+  double *base;      /* nrk * nD factors */
+} cpv;
+
+/* Reference src/cpvector.cu:291 (PointCPvecRtermsonGPU): a window of R terms. */
+static cpv cp_window(const cpv *v, int iR, int R) {
+  cpv w = *v;
+  w.nrk = R;
+  w.coef = v->coef + iR;
+  w.base = v->base + (size_t)iR * v->nD;
+  return w;
+}
+
+static int *make_offsets(const int *nbas, int ndof) {
+  int *off = (int *)malloc(sizeof(int) * (ndof + 1));
+  off[0] = 0;
+  for (int d = 0; d < ndof; ++d) off[d + 1] = off[d] + nbas[d];
+  return off;
+}
+
+/* ------------------------------------------------------------------ */
+/* Inner-product building blocks (reference src/modvecvec.cu)          */
+/* ------------------------------------------------------------------ */
+
+/* constpstot (src/modvecvec.cu:724): PS(i1,i2) = [cv][cw] prod_{d != idof}
+ * <v_i1^d, w_i2^d>, column-major with leading dimension v->nrk. */
+static void pstot(const cpv *v, const cpv *w, double *PS, int idof, int multv, int multw) {
+  for (int i2 = 0; i2 < w->nrk; ++i2) {
+    for (int i1 = 0; i1 < v->nrk; ++i1) {
+      const double *a = v->base + (size_t)i1 * v->nD;
+      const double *b = w->base + (size_t)i2 * w->nD;
+      double normND = 1.0;
+      if (multv) normND *= v->coef[i1];
+      if (multw) normND *= w->coef[i2];
+      int s = 0;
+      for (int d = 0; d < v->ndof; ++d) {
+        int n = v->nbas[d];
+        if (d != idof) {
+          double norm1D = 0.0;
+          for (int k = 0; k < n; ++k) norm1D += a[s + k] * b[s + k];
+          normND *= norm1D;
+        }
+        s += n;
+      }
+      PS[i1 + (size_t)i2 * v->nrk] = normND;
+    }
+  }
+}
+
+/* constpsk with reset (src/modvecvec.cu:360): PS(i1,i2) = <v_i1^k, w_i2^k>. */
+static void psk(const cpv *v, const cpv *w, double *PS, int k) {
+  int n = v->nbas[k], o = v->off[k];
+  for (int i2 = 0; i2 < w->nrk; ++i2)
+    for (int i1 = 0; i1 < v->nrk; ++i1) {
+      const double *a = v->base + (size_t)i1 * v->nD + o;
+      const double *b = w->base + (size_t)i2 * w->nD + o;
+      double t = 0.0;
+      for (int j = 0; j < n; ++j) t += a[j] * b[j];
+      PS[i1 + (size_t)i2 * v->nrk] = t;
+    }
+}
+
+/* Sum of all entries in row-then-array order: sumoverrow (src/modvecvec.cu:1154)
+ * followed by sumarray (:1193). */
+static double sum_all(const double *M, int nr, int nc) {
+  double total = 0.0;
+  for (int r = 0; r < nr; ++r) {
+    double row = 0.0;
+    for (int c = 0; c < nc; ++c) row += M[r + (size_t)c * nr];
+    total += row;
+  }
+  return total;
+}
+
+/* constbjk (src/als.cu:332 and :361): bjk(i1,i2) += fac * sum_j w.coef[j]
+ * w_j^k(i2) PS(j,i1); bjk is column-major rk x n_k, PS has leading dim w->nrk. */
+static void bjk_accumulate(const cpv *w, const double *PS, double *bjk, int rkv, int k, const double *fac) {
+  int n = w->nbas[k], o = w->off[k];
+  for (int i2 = 0; i2 < n; ++i2)
+    for (int i1 = 0; i1 < rkv; ++i1) {
+      double t = 0.0;
+      if (!fac) t = bjk[i1 + (size_t)i2 * rkv];
+      for (int j = 0; j < w->nrk; ++j)
+        t += w->coef[j] * w->base[(size_t)j * w->nD + o + i2] * PS[j + (size_t)i1 * w->nrk];
+      if (fac) t = fac[0] * t + bjk[i1 + (size_t)i2 * rkv];
+      bjk[i1 + (size_t)i2 * rkv] = t;
+    }
+}
+
+/* normonebase (src/modvecvec.cu:225): max-scaled 2-norm of mode idof of each
+ * term; the factor is divided by it and the weight replaced by it. */
+static void normonebase(cpv *v, int idof) {
+  int n = v->nbas[idof], o = v->off[idof];
+  for (int r = 0; r < v->nrk; ++r) {
+    double *x = v->base + (size_t)r * v->nD + o;
+    double largest = 0.0;
+    for (int k = 0; k < n; ++k) largest = (largest > fabs(x[k])) ? largest : fabs(x[k]);
+    double norm1D = 0.0;
+    for (int k = 0; k < n; ++k) {
+      double t = x[k] / largest;
+      norm1D += t * t;
+    }
+    norm1D = largest * sqrt(fabs(norm1D));
+    for (int k = 0; k < n; ++k) x[k] /= norm1D;
+    v->coef[r] = norm1D;
+  }
+}
+
+/* Coefficient renormalisation used after sweeps: constpstot(F,F,-1,T,T),
+ * sumoverrow, sumarray, normalizecoef (src/intertw_mvp.cu:491-494). */
+static void normalize_coefs(cpv *F, double *BB) {
+  pstot(F, F, BB, -1, 1, 1);
+  double s = sum_all(BB, F->nrk, F->nrk);
+  double q = sqrt(fabs(s));
+  for (int r = 0; r < F->nrk; ++r) F->coef[r] /= q;
+}
+
+/* setpenalty (src/als.cu:248): 1e-10 times the largest weight (FP64 build). */
+static double penalty(const double *coef, int n) {
+  double p = coef[0];
+  for (int i = 1; i < n; ++i) p = (coef[i] > p) ? coef[i] : p;
+  return p * 1.0e-10;
+}
+
+/* ------------------------------------------------------------------ */
+/* Dense solves                                                        */
+/* ------------------------------------------------------------------ */
+
+/* solve_linsys (src/linalg.cu:73): LU with partial pivoting of the n x n
+ * column-major A (dgetrf), then forward/back substitution for nrhs columns
+ * of B (dgetrs, no transpose).  A and B are overwritten. */
+static void lu_solve(double *A, double *B, int n, int nrhs, int *ipiv) {
+  for (int j = 0; j < n; ++j) {
+    int p = j;
+    double amax = fabs(A[j + (size_t)j * n]);
+    for (int i = j + 1; i < n; ++i) {
+      double a = fabs(A[i + (size_t)j * n]);
+      if (a > amax) { amax = a; p = i; }
+    }
+    ipiv[j] = p;
+    if (p != j)
+      for (int c = 0; c < n; ++c) {
+        double t = A[j + (size_t)c * n]; A[j + (size_t)c * n] = A[p + (size_t)c * n]; A[p + (size_t)c * n] = t;
+      }
+    double piv = A[j + (size_t)j * n];
+    if (piv != 0.0)
+      for (int i = j + 1; i < n; ++i) A[i + (size_t)j * n] /= piv;
+    for (int c = j + 1; c < n; ++c) {
+      double u = A[j + (size_t)c * n];
+      for (int i = j + 1; i < n; ++i) A[i + (size_t)c * n] -= A[i + (size_t)j * n] * u;
+    }
+  }
+  for (int c = 0; c < nrhs; ++c) {
+    double *b = B + (size_t)c * n;
+    for (int j = 0; j < n; ++j)
+      if (ipiv[j] != j) { double t = b[j]; b[j] = b[ipiv[j]]; b[ipiv[j]] = t; }
+    for (int j = 0; j < n; ++j)
+      for (int i = j + 1; i < n; ++i) b[i] -= A[i + (size_t)j * n] * b[j];
+    for (int j = n - 1; j >= 0; --j) {
+      b[j] /= A[j + (size_t)j * n];
+      for (int i = 0; i < j; ++i) b[i] -= A[i + (size_t)j * n] * b[j];
+    }
+  }
+}
+
+/* Cyclic Jacobi eigen-decomposition of the symmetric n x n column-major C
+ * (overwritten); eigenvalues to w, eigenvectors (columns) to V. */
+static void jacobi_eig(double *C, int n, double *w, double *V) {
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) V[i + (size_t)j * n] = (i == j) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, diag = 0.0;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        double c = C[i + (size_t)j * n];
+        if (i != j) off += c * c; else diag += c * c;
+      }
+    if (off <= 1e-30 * diag || off == 0.0) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        double apq = C[p + (size_t)q * n];
+        if (apq == 0.0) continue;
+        double app = C[p + (size_t)p * n], aqq = C[q + (size_t)q * n];
+        double theta = (aqq - app) / (2.0 * apq);
+        double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) { /* columns p,q */
+          double ckp = C[k + (size_t)p * n], ckq = C[k + (size_t)q * n];
+          C[k + (size_t)p * n] = c * ckp - s * ckq;
+          C[k + (size_t)q * n] = s * ckp + c * ckq;
+        }
+        for (int k = 0; k < n; ++k) { /* rows p,q */
+          double cpk = C[p + (size_t)k * n], cqk = C[q + (size_t)k * n];
+          C[p + (size_t)k * n] = c * cpk - s * cqk;
+          C[q + (size_t)k * n] = s * cpk + c * cqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          double vkp = V[k + (size_t)p * n], vkq = V[k + (size_t)q * n];
+          V[k + (size_t)p * n] = c * vkp - s * vkq;
+          V[k + (size_t)q * n] = s * vkp + c * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < n; ++i) w[i] = C[i + (size_t)i * n];
+}
+
+/* solve_geneigval (src/linalg.cu:22, cusolverDnDsygvd itype=1, jobz=V,
+ * uplo=L): B = L L^T, C = L^-1 A L^-T, C = Y diag(w) Y^T, X = L^-T Y. */
+int orc_sygv(int n, const double *A, const double *B, double *w, double *X) {
+  double *L = (double *)calloc((size_t)n * n, sizeof(double));
+  double *C = (double *)calloc((size_t)n * n, sizeof(double));
+  double *Y = (double *)calloc((size_t)n * n, sizeof(double));
+  double *wt = (double *)malloc(sizeof(double) * n);
+  int info = 0;
+  for (int j = 0; j < n; ++j) { /* Cholesky of the lower triangle of B */
+    double s = B[j + (size_t)j * n];
+    for (int k = 0; k < j; ++k) s -= L[j + (size_t)k * n] * L[j + (size_t)k * n];
+    if (!(s > 0.0)) { info = j + 1; s = fabs(s) + 1e-300; }
+    double ljj = sqrt(s);
+    L[j + (size_t)j * n] = ljj;
+    for (int i = j + 1; i < n; ++i) {
+      double t = B[i + (size_t)j * n];
+      for (int k = 0; k < j; ++k) t -= L[i + (size_t)k * n] * L[j + (size_t)k * n];
+      L[i + (size_t)j * n] = t / ljj;
+    }
+  }
+  /* symmetric A from its lower triangle */
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) C[i + (size_t)j * n] = (i >= j) ? A[i + (size_t)j * n] : A[j + (size_t)i * n];
+  /* C <- L^-1 C (forward substitution on each column) */
+  for (int c = 0; c < n; ++c)
+    for (int i = 0; i < n; ++i) {
+      double t = C[i + (size_t)c * n];
+      for (int k = 0; k < i; ++k) t -= L[i + (size_t)k * n] * C[k + (size_t)c * n];
+      C[i + (size_t)c * n] = t / L[i + (size_t)i * n];
+    }
+  /* C <- C L^-T (forward substitution on each row) */
+  for (int r = 0; r < n; ++r)
+    for (int j = 0; j < n; ++j) {
+      double t = C[r + (size_t)j * n];
+      for (int k = 0; k < j; ++k) t -= C[r + (size_t)k * n] * L[j + (size_t)k * n];
+      C[r + (size_t)j * n] = t / L[j + (size_t)j * n];
+    }
+  for (int j = 0; j < n; ++j) /* symmetrise rounding */
+    for (int i = j + 1; i < n; ++i) {
+      double a = 0.5 * (C[i + (size_t)j * n] + C[j + (size_t)i * n]);
+      C[i + (size_t)j * n] = a; C[j + (size_t)i * n] = a;
+    }
+  jacobi_eig(C, n, wt, Y);
+  /* X = L^-T Y (back substitution on each column) */
+  double *Xt = (double *)malloc(sizeof(double) * (size_t)n * n);
+  for (int c = 0; c < n; ++c)
+    for (int i = n - 1; i >= 0; --i) {
+      double t = Y[i + (size_t)c * n];
+      for (int k = i + 1; k < n; ++k) t -= L[k + (size_t)i * n] * Xt[k + (size_t)c * n];
+      Xt[i + (size_t)c * n] = t / L[i + (size_t)i * n];
+    }
+  /* ascending order (stable selection), then sign normalisation */
+  int *idx = (int *)malloc(sizeof(int) * n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  for (int i = 0; i < n; ++i) {
+    int m = i;
+    for (int j = i + 1; j < n; ++j)
+      if (wt[idx[j]] < wt[idx[m]]) m = j;
+    int t = idx[i]; idx[i] = idx[m]; idx[m] = t;
+  }
+  for (int c = 0; c < n; ++c) {
+    int src = idx[c];
+    w[c] = wt[src];
+    int imax = 0;
+    double amax = -1.0;
+    for (int i = 0; i < n; ++i) {
+      double a = fabs(Xt[i + (size_t)src * n]);
+      if (a > amax) { amax = a; imax = i; }
+    }
+    double sg = (Xt[imax + (size_t)src * n] < 0.0) ? -1.0 : 1.0;
+    for (int i = 0; i < n; ++i) X[i + (size_t)c * n] = sg * Xt[i + (size_t)src * n];
+  }
+  free(idx); free(Xt); free(L); free(C); free(Y); free(wt);
+  return info;
+}
+
+/* ------------------------------------------------------------------ */
+/* Explicit-G ALS (reference src/als.cu:976-1078)                      */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+  int rk, nmax;
+  double *BB, *BBk, *bjk, *tmp;
+  int *ipiv;
+} work_t;
+
+static void work_init(work_t *w, int rk, int nmax, int nblocmax) {
+  w->rk = rk; w->nmax = nmax;
+  int m = rk > nblocmax ? rk : nblocmax;
+  w->BB = (double *)malloc(sizeof(double) * (size_t)rk * rk);
+  w->BBk = (double *)malloc(sizeof(double) * (size_t)rk * rk);
+  w->bjk = (double *)malloc(sizeof(double) * (size_t)rk * nmax);
+  w->tmp = (double *)malloc(sizeof(double) * (size_t)m);
+  w->ipiv = (int *)malloc(sizeof(int) * rk);
+}
+static void work_free(work_t *w) { free(w->BB); free(w->BBk); free(w->bjk); free(w->tmp); free(w->ipiv); }
+
+static void add_penalty(double *BB, int rk, double pen) {
+  for (int i = 0; i < rk; ++i) BB[i + (size_t)i * rk] += pen;
+}
+
+/* replacevwithsolns (src/als.cu:310): F^idof(r,:) = X(r,:). */
+static void replace_with_solution(cpv *F, const double *X, int idof) {
+  int n = F->nbas[idof], o = F->off[idof];
+  for (int r = 0; r < F->nrk; ++r)
+    for (int i = 0; i < n; ++i) F->base[(size_t)r * F->nD + o + i] = X[r + (size_t)i * F->nrk];
+}
+
+/* ITERATE_ALS (src/als.cu:1021) with als_build_linear_system (:976). */
+static void iterate_als(cpv *Q, int rk, int nbloc, int nals, work_t *W) {
+  if (nals == 0) return;
+  cpv F = cp_window(Q, 0, rk);
+  double pen = penalty(F.coef, rk);
+  for (int it = 0; it < nals; ++it)
+    for (int j = 0; j < Q->ndof; ++j) {
+      int n = Q->nbas[j];
+      memset(W->bjk, 0, sizeof(double) * (size_t)rk * n);
+      for (int k = 1; k < nbloc; ++k) {
+        cpv G = cp_window(Q, k * rk, rk);
+        pstot(&G, &F, W->BB, j, 0, 0);
+        bjk_accumulate(&G, W->BB, W->bjk, rk, j, NULL);
+      }
+      pstot(&F, &F, W->BB, j, 0, 0);
+      add_penalty(W->BB, rk, pen);
+      lu_solve(W->BB, W->bjk, rk, n, W->ipiv);
+      replace_with_solution(&F, W->bjk, j);
+      normonebase(&F, j);
+    }
+}
+
+static int max_nbas(const int *nbas, int ndof) {
+  int m = 0;
+  for (int d = 0; d < ndof; ++d) m = nbas[d] > m ? nbas[d] : m;
+  return m;
+}
+
+void orc_alscpp(double *coef, double *base, const int *nbas, int ndof, int rF, int rG, int nals) {
+  int *off = make_offsets(nbas, ndof);
+  cpv Q = {rF + rG, ndof, off[ndof], nbas, off, coef, base};
+  work_t W;
+  work_init(&W, rF, max_nbas(nbas, ndof), 1);
+  iterate_als(&Q, rF, (rF + rG) / rF, nals, &W);
+  work_free(&W);
+  free(off);
+}
+
+void orc_als_batched(int nvec, double *const *coef, double *const *base, const int *nbas, int ndof,
+                     const int *rF, const int *rG, int nals, int nthreads) {
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+  for (int v = 0; v < nvec; ++v) orc_alscpp(coef[v], base[v], nbas, ndof, rF[v], rG[v], nals);
+  (void)nthreads;
+}
+
+/* ------------------------------------------------------------------ */
+/* Hamiltonian term application (reference src/intertw_mvp.cu:39)       */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+  int T, ndof;
+  const int *opid, *mptr;
+  const double *coef, *mat;
+} hoplist;
+
+/* mvp_kernel (src/intertw_mvp.cu:39): G^d_r = alpha_d h_{t,d} v^d_r with the
+ * packed upper-triangular operator h[ir + ic(ic+1)/2], alpha_0 = Hcoef[t]. */
+static void apply_term(const hoplist *H, int t, const cpv *v, cpv *G) {
+  for (int d = 0; d < v->ndof; ++d) {
+    int n = v->nbas[d], o = v->off[d];
+    int hsft = H->mptr[H->opid[t * v->ndof + d] - 1] - 1;
+    double alpha = (d == 0) ? H->coef[t] : 1.0;
+    for (int r = 0; r < v->nrk; ++r) {
+      const double *x = v->base + (size_t)r * v->nD + o;
+      double *y = G->base + (size_t)r * v->nD + o;
+      for (int ib = 0; ib < n; ++ib) {
+        double t2 = 0.0;
+        for (int i = 0; i < n; ++i) {
+          int ir = i < ib ? i : ib, ic = i < ib ? ib : i;
+          t2 += x[i] * H->mat[hsft + ir + ic * (ic + 1) / 2];
+        }
+        y[ib] = t2 * alpha;
+      }
+    }
+  }
+}
+
+/* mvp_build_linear_system (src/intertw_mvp.cu:380). */
+static void mvp_build(const hoplist *H, const cpv *Fo, cpv *F, cpv *G, work_t *W, int idof, int ishift,
+                      double Eshift, int recalcB) {
+  int rk = F->nrk, n = F->nbas[idof], o = F->off[idof];
+  memset(W->bjk, 0, sizeof(double) * (size_t)rk * n);
+  memcpy(G->coef, Fo->coef, sizeof(double) * rk);
+  for (int t = 0; t < H->T; ++t) {
+    apply_term(H, t, Fo, G);
+    pstot(G, F, W->BB, idof, 0, 0);
+    bjk_accumulate(G, W->BB, W->bjk, rk, idof, NULL);
+  }
+  memcpy(G->base, Fo->base, sizeof(double) * (size_t)rk * F->nD);
+  pstot(G, F, W->BB, idof, 0, 0);
+  if (ishift != 0) {
+    for (int r = 0; r < rk; ++r)
+      for (int i = 0; i < n; ++i) G->base[(size_t)r * F->nD + o + i] *= -Eshift;
+    bjk_accumulate(G, W->BB, W->bjk, rk, idof, NULL);
+    if (ishift < 0)
+      for (int i = 0; i < rk * n; ++i) W->bjk[i] *= -1.0;
+  }
+  if (recalcB) {
+    memcpy(G->base, F->base, sizeof(double) * (size_t)rk * F->nD);
+    pstot(G, F, W->BB, idof, 0, 0);
+  }
+}
+
+/* POW_ALS (src/intertw_mvp.cu:452): F <- ALS fit of (H - E)F, mode by mode. */
+static void pow_als(const hoplist *H, cpv *F, cpv *G, work_t *W, int npow, int ishift, double Eshift) {
+  if (npow == 0) return;
+  double pen = penalty(F->coef, F->nrk);
+  for (int it = 0; it < npow; ++it) {
+    for (int j = 0; j < F->ndof; ++j) {
+      int n = F->nbas[j];
+      mvp_build(H, F, F, G, W, j, ishift, Eshift, 0);
+      add_penalty(W->BB, F->nrk, pen);
+      lu_solve(W->BB, W->bjk, F->nrk, n, W->ipiv);
+      replace_with_solution(F, W->bjk, j);
+      normonebase(F, j);
+    }
+    normalize_coefs(F, W->BB);
+  }
+}
+
+/* PRODHV_ALS (src/intertw_mvp.cu:501): F <- ALS fit of H Fo, starting at Fo. */
+static void prodhv_als(const hoplist *H, const cpv *Fo, cpv *F, cpv *G, work_t *W, int nals) {
+  if (nals == 0) return;
+  memcpy(F->coef, Fo->coef, sizeof(double) * F->nrk);
+  memcpy(F->base, Fo->base, sizeof(double) * (size_t)F->nrk * F->nD);
+  double pen = penalty(Fo->coef, F->nrk);
+  for (int it = 0; it < nals; ++it)
+    for (int j = 0; j < F->ndof; ++j) {
+      int n = F->nbas[j];
+      mvp_build(H, Fo, F, G, W, j, 0, 0.0, 1);
+      add_penalty(W->BB, F->nrk, pen);
+      lu_solve(W->BB, W->bjk, F->nrk, n, W->ipiv);
+      replace_with_solution(F, W->bjk, j);
+      normonebase(F, j);
+    }
+}
+
+static cpv cp_alloc(int rk, const int *nbas, const int *off, int ndof) {
+  cpv v = {rk, ndof, off[ndof], nbas, off, NULL, NULL};
+  v.coef = (double *)calloc(rk, sizeof(double));
+  v.base = (double *)calloc((size_t)rk * off[ndof], sizeof(double));
+  return v;
+}
+static void cp_free(cpv *v) { free(v->coef); free(v->base); }
+
+/* MatrixVectorProducts (src/intertw_mvp.cu:553): POW_ALS on every vector. */
+void orc_pow_als_block(double *base, double *coef, const int *nbas, int rk, int ndof, int nbloc,
+                       const int *opid, const int *mptr, const double *Hcoef, const double *mat,
+                       int T, int npow, int ishift, double Eshift, int nthreads) {
+  int *off = make_offsets(nbas, ndof);
+  cpv Q = {rk * nbloc, ndof, off[ndof], nbas, off, coef, base};
+  hoplist H = {T, ndof, opid, mptr, Hcoef, mat};
+  int nmax = max_nbas(nbas, ndof);
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+  for (int i = 0; i < nbloc; ++i) {
+    work_t W;
+    work_init(&W, rk, nmax, nbloc);
+    cpv F = cp_window(&Q, i * rk, rk);
+    cpv G = cp_alloc(rk, nbas, off, ndof);
+    pow_als(&H, &F, &G, &W, npow, ishift, Eshift);
+    cp_free(&G);
+    work_free(&W);
+  }
+  (void)nthreads;
+  free(off);
+}
+
+/* ------------------------------------------------------------------ */
+/* Gram-Schmidt and vector updates (reference src/intertw_lcv.cu)       */
+/* ------------------------------------------------------------------ */
+
+/* lcv_build_linear_system (src/intertw_lcv.cu:77). gcoef[k] is the weight
+ * of vector k; with gs != 0 the weights of k < iv are recomputed as
+ * -<Q_k, F> (gramsumoverrow + sumarray, :51 and :117). */
+static void lcv_build(const cpv *Q, cpv *F, work_t *W, double *gcoef, int idof, int iv, int gs) {
+  int rk = F->nrk, n = F->nbas[idof];
+  memset(W->bjk, 0, sizeof(double) * (size_t)rk * n);
+  for (int k = 0; k < iv; ++k) {
+    cpv G = cp_window(Q, k * rk, rk);
+    pstot(&G, F, W->BB, idof, 0, 0);
+    if (gs) {
+      psk(&G, F, W->BBk, idof);
+      double total = 0.0;
+      for (int row = 0; row < rk; ++row) {
+        double u = 0.0;
+        for (int col = 0; col < rk; ++col)
+          u -= F->coef[col] * W->BB[row + (size_t)col * rk] * W->BBk[row + (size_t)col * rk];
+        u *= G.coef[row];
+        total += u;
+      }
+      gcoef[k] = total;
+    }
+    bjk_accumulate(&G, W->BB, W->bjk, rk, idof, &gcoef[k]);
+  }
+  pstot(F, F, W->BB, idof, 0, 0);
+  if (gs) bjk_accumulate(F, W->BB, W->bjk, rk, idof, &gcoef[iv]);
+}
+
+/* GramSchmidt (src/intertw_lcv.cu:131). */
+void orc_gram_schmidt(double *base, double *coef, const int *nbas, int rk, int ndof, int nbloc, int nals) {
+  if (nals == 0) return;
+  int *off = make_offsets(nbas, ndof);
+  cpv Q = {rk * nbloc, ndof, off[ndof], nbas, off, coef, base};
+  work_t W;
+  work_init(&W, rk, max_nbas(nbas, ndof), nbloc);
+  double *gcoef = (double *)malloc(sizeof(double) * nbloc);
+  for (int i = 0; i < nbloc; ++i) gcoef[i] = 1.0;
+  cpv F = cp_window(&Q, 0, rk);
+  normalize_coefs(&F, W.BB);
+  for (int iv = 1; iv < nbloc; ++iv) {
+    F = cp_window(&Q, iv * rk, rk);
+    double pen = penalty(F.coef, rk);
+    for (int it = 0; it < nals; ++it)
+      for (int j = 0; j < ndof; ++j) {
+        int n = nbas[j];
+        lcv_build(&Q, &F, &W, gcoef, j, iv, 1);
+        add_penalty(W.BB, rk, pen);
+        lu_solve(W.BB, W.bjk, rk, n, W.ipiv);
+        replace_with_solution(&F, W.bjk, j);
+        normonebase(&F, j);
+        normalize_coefs(&F, W.BB);
+      }
+  }
+  free(gcoef);
+  work_free(&W);
+  free(off);
+}
+
+/* GenEigvalProblem (src/intertw_mvp.cu:589): QHQ(i,j) = <Q_j, H Q_i> with H Q_i
+ * from PRODHV_ALS, S(i,j) = <Q_j, Q_i>, j <= i; then the generalised problem. */
+void orc_gen_eig(const double *base, const double *coef, const int *nbas, int rk, int ndof, int nbloc,
+                 const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T,
+                 int nals, double *eigv, double *U, int nthreads) {
+  int *off = make_offsets(nbas, ndof);
+  cpv Q = {rk * nbloc, ndof, off[ndof], nbas, off, (double *)coef, (double *)base};
+  hoplist H = {T, ndof, opid, mptr, Hcoef, mat};
+  int nmax = max_nbas(nbas, ndof);
+  double *QHQ = (double *)calloc((size_t)nbloc * nbloc, sizeof(double));
+  double *S = (double *)calloc((size_t)nbloc * nbloc, sizeof(double));
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+  for (int i = 0; i < nbloc; ++i) {
+    work_t W;
+    work_init(&W, rk, nmax, nbloc);
+    cpv Fo = cp_window(&Q, i * rk, rk);
+    cpv F = cp_alloc(rk, nbas, off, ndof);
+    cpv G = cp_alloc(rk, nbas, off, ndof);
+    prodhv_als(&H, &Fo, &F, &G, &W, nals);
+    if (nals == 0) { /* PRODHV_ALS returns early: F keeps its prior (zero) contents */ }
+    for (int j = 0; j <= i; ++j) {
+      cpv Gj = cp_window(&Q, j * rk, rk);
+      pstot(&Gj, &F, W.BB, -1, 1, 1);
+      QHQ[i + (size_t)j * nbloc] = sum_all(W.BB, rk, rk);
+      pstot(&Gj, &Fo, W.BB, -1, 1, 1);
+      S[i + (size_t)j * nbloc] = sum_all(W.BB, rk, rk);
+    }
+    cp_free(&F); cp_free(&G);
+    work_free(&W);
+  }
+  (void)nthreads;
+  orc_sygv(nbloc, QHQ, S, eigv, U);
+  free(QHQ); free(S); free(off);
+}
+
+/* VectorUpdates (src/intertw_lcv.cu:270) with UPDATES_ALS (:209): the new
+ * vector i is the ALS fit of sum_l U(l,i) Q_l, starting from Q_i. */
+void orc_vector_updates(double *base, double *coef, const int *nbas, int rk, int ndof, int nbloc,
+                        const double *U, int nals, int nthreads) {
+  int *off = make_offsets(nbas, ndof);
+  int nD = off[ndof];
+  cpv Q = {rk * nbloc, ndof, nD, nbas, off, coef, base};
+  int nmax = max_nbas(nbas, ndof);
+  double *newbase = (double *)malloc(sizeof(double) * (size_t)rk * nbloc * nD);
+  double *newcoef = (double *)malloc(sizeof(double) * (size_t)rk * nbloc);
+  memcpy(newbase, base, sizeof(double) * (size_t)rk * nbloc * nD);
+  memcpy(newcoef, coef, sizeof(double) * (size_t)rk * nbloc);
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+  for (int i = 0; i < nbloc; ++i) {
+    if (nals == 0) continue;
+    work_t W;
+    work_init(&W, rk, nmax, nbloc);
+    cpv F = {rk, ndof, nD, nbas, off, newcoef + (size_t)i * rk, newbase + (size_t)i * rk * nD};
+    double pen = penalty(F.coef, rk);
+    double *gcoef = (double *)malloc(sizeof(double) * nbloc);
+    memcpy(gcoef, U + (size_t)i * nbloc, sizeof(double) * nbloc);
+    for (int it = 0; it < nals; ++it)
+      for (int j = 0; j < ndof; ++j) {
+        int n = nbas[j];
+        lcv_build(&Q, &F, &W, gcoef, j, nbloc, 0);
+        add_penalty(W.BB, rk, pen);
+        lu_solve(W.BB, W.bjk, rk, n, W.ipiv);
+        replace_with_solution(&F, W.bjk, j);
+        normonebase(&F, j);
+      }
+    normalize_coefs(&F, W.BB);
+    free(gcoef);
+    work_free(&W);
+  }
+  (void)nthreads;
+  memcpy(base, newbase, sizeof(double) * (size_t)rk * nbloc * nD);
+  memcpy(coef, newcoef, sizeof(double) * (size_t)rk * nbloc);
+  free(newbase); free(newcoef); free(off);
+}
+
+/* intertwinecpp_ (src/intertwining.cu:98): MVP -> GS -> (GEP -> updates). */
+void orc_intertwine(double *base, double *coef, const int *nbas, int rk, int ndof, int nbloc,
+                    const int *opid, const int *mptr, const double *Hcoef, const double *mat,
+                    int TxD, int nops, int msize, double *eigv, int npow, int ncpu, int nals,
+                    int update, int ishift, double Eshift) {
+  (void)nops; (void)msize;
+  int T = TxD / ndof;
+  orc_pow_als_block(base, coef, nbas, rk, ndof, nbloc, opid, mptr, Hcoef, mat, T, npow, ishift, Eshift, ncpu);
+  orc_gram_schmidt(base, coef, nbas, rk, ndof, nbloc, nals);
+  if (update) {
+    double *U = (double *)malloc(sizeof(double) * (size_t)nbloc * nbloc);
+    orc_gen_eig(base, coef, nbas, rk, ndof, nbloc, opid, mptr, Hcoef, mat, T, nals, eigv, U, ncpu);
+    orc_vector_updates(base, coef, nbas, rk, ndof, nbloc, U, nals, ncpu);
+    free(U);
+  }
+}
+
+double orc_cp_dot(const double *vb, const double *vc, int rv, const double *wb, const double *wc, int rw,
+                  const int *nbas, int ndof) {
+  int *off = make_offsets(nbas, ndof);
+  cpv v = {rv, ndof, off[ndof], nbas, off, (double *)vc, (double *)vb};
+  cpv w = {rw, ndof, off[ndof], nbas, off, (double *)wc, (double *)wb};
+  double total = 0.0;
+  double *col = (double *)malloc(sizeof(double) * rv);
+  for (int j = 0; j < rw; ++j) {
+    cpv wj = cp_window(&w, j, 1);
+    pstot(&v, &wj, col, -1, 1, 1);
+    for (int i = 0; i < rv; ++i) total += col[i];
+  }
+  free(col);
+  free(off);
+  return total;
+}

@@ -1,0 +1,78 @@
+/*
+ * CPU oracle for the MLCP GPU power-iteration hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: tests/, the
+ * smoke entry and the CPU-baseline leg of bench.py call it to produce the
+ * expected answer.  The product library (libmlcp_gb300.so) never links it.
+ *
+ * It restates, in plain FP64 C, the algorithm of the reference's CUDA path
+ * (src/intertwining.cu, src/als.cu, src/intertw_mvp.cu, src/intertw_lcv.cu,
+ * src/modvecvec.cu, src/linalg.cu) with the same loop structure, the same
+ * penalty rule and the same normalisations.  Dense solves follow the
+ * published LAPACK algorithms the reference calls through cuSOLVER
+ * (dgetrf/dgetrs with partial pivoting; dsygvd is replaced by a Cholesky
+ * reduction followed by cyclic Jacobi, which yields the same eigenpairs).
+ *
+ * Parity unpinned: the reference ships no tests, golden vectors or
+ * fixtures for this path, its Fortran host cannot be compiled without a
+ * Fortran compiler, and its CUDA library cannot be built for the Arm GPU
+ * host from here.  Known-answer tests derived from mathematics (exactly
+ * representable reductions, analytically solvable Hamiltonians, a Lanczos
+ * reference on the full direct-product basis) stand in.
+ *
+ * Layout (reference src/cpvector.cu:407-414): a CP vector of rank R over D
+ * modes with basis sizes nbas[d] stores term r, mode d, index i at
+ * base[r*nD + off_d + i] with off_d = sum_{e<d} nbas[e], nD = off_D, and one
+ * weight coef[r] per term.
+ */
+#ifndef MLCP_ORACLE_H
+#define MLCP_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Reference src/intertwining.cu:180 (alscpp_) -> src/als.cu:1021 (ITERATE_ALS).
+ * F = first rF terms of (coef, base), G = next rG terms (rG a multiple of rF).
+ * Overwrites the first rF terms with the reduced vector. */
+void orc_alscpp(double *coef, double *base, const int *nbas, int ndof, int rF, int rG, int nals);
+
+/* Reference src/intertwining.cu:98 (intertwinecpp_): one intertwined power
+ * cycle on a block of nbloc vectors of rank rk.  Overwrites base/coef (and
+ * eigv when update != 0).  Eigenvectors of the block Rayleigh-Ritz problem
+ * are sign-normalised so that their largest-magnitude component is positive. */
+void orc_intertwine(double *base, double *coef, const int *nbas, int rk, int ndof, int nbloc,
+                    const int *opid, const int *mptr, const double *Hcoef, const double *mat,
+                    int TxD, int nops, int msize, double *eigv, int npow, int ncpu, int nals,
+                    int update, int ishift, double Eshift);
+
+/* Stages of one cycle, exposed so tests can check each one alone. */
+void orc_pow_als_block(double *base, double *coef, const int *nbas, int rk, int ndof, int nbloc,
+                       const int *opid, const int *mptr, const double *Hcoef, const double *mat,
+                       int T, int npow, int ishift, double Eshift, int nthreads);
+void orc_gram_schmidt(double *base, double *coef, const int *nbas, int rk, int ndof, int nbloc, int nals);
+/* Fills eigv[nbloc] and U[nbloc*nbloc] (column-major, column i = eigenvector i). */
+void orc_gen_eig(const double *base, const double *coef, const int *nbas, int rk, int ndof, int nbloc,
+                 const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T,
+                 int nals, double *eigv, double *U, int nthreads);
+void orc_vector_updates(double *base, double *coef, const int *nbas, int rk, int ndof, int nbloc,
+                        const double *U, int nals, int nthreads);
+
+/* Full inner product <v,w> of two CP vectors (reference src/modvecvec.cu:724
+ * constpstot with idof=-1 and both weights, summed). */
+double orc_cp_dot(const double *vb, const double *vc, int rv, const double *wb, const double *wc, int rw,
+                  const int *nbas, int ndof);
+
+/* Batched explicit-G ALS: nvec independent reductions, OpenMP over vectors. */
+void orc_als_batched(int nvec, double *const *coef, double *const *base, const int *nbas, int ndof,
+                     const int *rF, const int *rG, int nals, int nthreads);
+
+/* Generalised symmetric eigenproblem A x = lambda B x (lower triangles of
+ * column-major A, B used).  Eigenvalues ascending; X column-major with
+ * X^T B X = I and the largest-magnitude entry of each column positive. */
+int orc_sygv(int n, const double *A, const double *B, double *w, double *X);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
