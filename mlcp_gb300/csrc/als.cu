@@ -43,8 +43,10 @@ namespace mlcp {
 __global__ void als_prep_kernel(AlsParams p) {
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  // target factors: total_g_rows * ndof element runs
-  for (long long e = tid; e < p.total_rows * p.ndof; e += stride) {
+  // target factors: one element run per (target term, mode); with a shared
+  // target only vector 0's terms are converted (gm_off is 0 for every vector)
+  const long long grows = p.shared_target ? (long long)p.rG[0] : p.total_rows;
+  for (long long e = tid; e < grows * p.ndof; e += stride) {
     const long long row = e / p.ndof;
     const int d = (int)(e % p.ndof);
     // locate vector: binary search over row offsets
@@ -53,15 +55,17 @@ __global__ void als_prep_kernel(AlsParams p) {
       int mid = (lo + hi + 1) >> 1;
       if (p.g_row_off[mid] <= row) lo = mid; else hi = mid - 1;
     }
-    const int v = lo;
+    const int v = p.shared_target ? 0 : lo;
     const int j = (int)(row - p.g_row_off[v]);
     const int rG = p.rG[v];
     const int n = p.nbas[d], np = round_up(n, 4);
-    const double* src = p.base + (p.term_off[v] + p.rF[v] + j) * (long long)p.nD + p.off[d];
+    const double* src = p.g_base + (p.g_term_off[v] + j) * (long long)p.nD + p.off[d];
     float* dst = p.gm + p.gm_off[v] + (long long)p.offp[d] * rG + (long long)j * np;
     for (int i = 0; i < np; ++i) dst[i] = (i < n) ? (float)src[i] : 0.f;
-    if (d == 0) p.gc[p.g_row_off[v] + j] = (float)p.coef[p.term_off[v] + p.rF[v] + j];
+    if (d == 0 && !p.shared_target) p.gc[p.g_row_off[v] + j] = (float)p.g_coef[p.g_term_off[v] + j];
   }
+  if (p.shared_target)
+    for (long long e = tid; e < p.total_rows; e += stride) p.gc[e] = (float)p.shared_w[e];
   // FP32 copy of F
   for (long long e = tid; e < p.total_f_terms * p.ndof; e += stride) {
     const long long frow = e / p.ndof;
@@ -87,14 +91,15 @@ __global__ void als_prep_kernel(AlsParams p) {
 namespace {
 
 constexpr int kThreads = kAlsThreads;
-constexpr int kTileRows = kThreads;  // one target term per thread in the row phase
+constexpr int kTileRows = 256;  // target terms staged per tile (multiple of 4)
 
 struct Smem {
   float* ps;      // [rows_cta][rFp] running products
   float* fold;    // [rFp][npmax] FP32 old factor of the mode being solved
   float* fnew;    // [rFp][npmax] FP32 new factor of the mode just solved
   float* wt;      // [kTileRows][rFp] weights c_j * PS(j,i) of the tile
-  float* gt;      // [kTileRows][npmax] target factors of the tile
+  float* gt;      // [kTileRows][npmax] target factors of mode k for the tile
+  float* gp;      // [kTileRows][npmax] target factors of the previous mode for the tile
   float* bpart;   // [rFp][npmax] partial right-hand side of this CTA
   float* red;     // [kThreads][16] reduction scratch
   double* BB;     // [rF][rF]
@@ -167,6 +172,7 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
     s.fnew = (float*)take(sizeof(float) * rFp * npmax);
     s.wt = (float*)take(sizeof(float) * kTileRows * rFp);
     s.gt = (float*)take(sizeof(float) * kTileRows * npmax);
+    s.gp = (float*)take(sizeof(float) * kTileRows * npmax);
     s.bpart = (float*)take(sizeof(float) * rFp * npmax);
     s.red = (float*)take(sizeof(float) * kThreads * 16);
     s.BB = (double*)take(sizeof(double) * rF * rF);
@@ -252,45 +258,106 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
 
     for (int tile0 = 0; tile0 < nrows; tile0 += kTileRows) {
       const int tr = min(kTileRows, nrows - tile0);
-      // -- per-term update: fold in the new factor of kprev, divide out mode k --
-      {
-        float* wrow = s.wt + tid * rFp;
-        float* grow = s.gt + tid * npmax;
-        if (tid < tr) {
-          const int r = tile0 + tid;
-          const int j = row0 + r;
-          float gk[NP], gp[NP];
-          load_row<NP>(gk, gmk + (long long)j * npk, npk);
+      // -- stage the tile's factors of modes k and kprev (coalesced float4) --
+      for (int e = tid; e < kTileRows * (npk / 4); e += kThreads) {
+        const int r = e / (npk / 4), q = (e % (npk / 4)) * 4;
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (r < tr) x = *reinterpret_cast<const float4*>(gmk + (long long)(row0 + tile0 + r) * npk + q);
+        *reinterpret_cast<float4*>(s.gt + r * npmax + q) = x;
+      }
+      if (kprev >= 0) {
+        for (int e = tid; e < kTileRows * (npp / 4); e += kThreads) {
+          const int r = e / (npp / 4), q = (e % (npp / 4)) * 4;
+          float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (r < tr) x = *reinterpret_cast<const float4*>(gmp + (long long)(row0 + tile0 + r) * npp + q);
+          *reinterpret_cast<float4*>(s.gp + r * npmax + q) = x;
+        }
+      }
+      __syncthreads();
+      // -- running products: fold in the new factor of kprev, divide out mode k.
+      //    Register blocks of 4 terms x 4 F terms. --
+      for (int blk = tid; blk < (kTileRows / 4) * nib; blk += kThreads) {
+        const int rb = blk / nib, ibk = blk % nib;
+        float po[16], pn[16];
 #pragma unroll
-          for (int q = 0; q < NP; q += 4)
-            if (q < npk) *reinterpret_cast<float4*>(grow + q) = make_float4(gk[q], gk[q + 1], gk[q + 2], gk[q + 3]);
-          if (kprev >= 0) load_row<NP>(gp, gmp + (long long)j * npp, npp);
-          const float cj = gc[j];
-          float* psr = s.ps + r * rFp;
-          for (int i = 0; i < rF; ++i) {
-            float tot = psr[i];
-            if (kprev >= 0) tot *= dot_reg<NP>(gp, s.fnew + i * npmax, npp);
-            const float po = dot_reg<NP>(gk, s.fold + i * npmax, npk);
-            float psk;
-            if (po != 0.f && fabsf(tot) >= FLT_MIN && isfinite(tot)) {
-              psk = __fdiv_rn(tot, po);
-            } else {
-              // unsafe division: rebuild prod_{d != k} <G_j^d, F_i^d> directly
-              psk = 1.f;
-              for (int d = 0; d < D; ++d) {
-                if (d == k) continue;
-                const int npd = round_up(p.nbas[d], 4);
-                psk *= dot_global(gm + (long long)p.offp[d] * rG + (long long)j * npd,
-                                  f32 + (long long)i * p.nDp + p.offp[d], npd);
-              }
+        for (int q = 0; q < 16; ++q) { po[q] = 0.f; pn[q] = 1.f; }
+        for (int q = 0; q < npk; q += 4) {
+          float4 g[4], f[4];
+#pragma unroll
+          for (int a = 0; a < 4; ++a) g[a] = *reinterpret_cast<const float4*>(s.gt + (rb * 4 + a) * npmax + q);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) f[c] = *reinterpret_cast<const float4*>(s.fold + (ibk * 4 + c) * npmax + q);
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              float v = po[a * 4 + c];
+              v = fmaf(g[a].x, f[c].x, v);
+              v = fmaf(g[a].y, f[c].y, v);
+              v = fmaf(g[a].z, f[c].z, v);
+              v = fmaf(g[a].w, f[c].w, v);
+              po[a * 4 + c] = v;
             }
-            psr[i] = psk;  // holds prod_{d != k} until mode k is solved
-            wrow[i] = cj * psk;
+        }
+        if (kprev >= 0) {
+#pragma unroll
+          for (int q = 0; q < 16; ++q) pn[q] = 0.f;
+          for (int q = 0; q < npp; q += 4) {
+            float4 g[4], f[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) g[a] = *reinterpret_cast<const float4*>(s.gp + (rb * 4 + a) * npmax + q);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) f[c] = *reinterpret_cast<const float4*>(s.fnew + (ibk * 4 + c) * npmax + q);
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+              for (int c = 0; c < 4; ++c) {
+                float v = pn[a * 4 + c];
+                v = fmaf(g[a].x, f[c].x, v);
+                v = fmaf(g[a].y, f[c].y, v);
+                v = fmaf(g[a].z, f[c].z, v);
+                v = fmaf(g[a].w, f[c].w, v);
+                pn[a * 4 + c] = v;
+              }
           }
-          for (int i = rF; i < rFp; ++i) wrow[i] = 0.f;
-        } else {
-          for (int i = 0; i < rFp; ++i) wrow[i] = 0.f;
-          for (int q = 0; q < npk; ++q) grow[q] = 0.f;
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const int r = tile0 + rb * 4 + a;
+          if (rb * 4 + a >= tr) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) s.wt[(rb * 4 + a) * rFp + ibk * 4 + c] = 0.f;
+            continue;
+          }
+          const int j = row0 + r;
+          const float cj = gc[j];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int i = ibk * 4 + c;
+            float psk = 0.f;
+            if (i < rF) {
+              const float tot = s.ps[r * rFp + i] * pn[a * 4 + c];
+              const float d = po[a * 4 + c];
+              if (d != 0.f && fabsf(tot) >= FLT_MIN && fabsf(tot) <= FLT_MAX) {
+                // quotient from the reciprocal plus one Newton correction
+                const float rc = __frcp_rn(d);
+                float qt = tot * rc;
+                qt = fmaf(fmaf(-d, qt, tot), rc, qt);
+                psk = qt;
+              } else {
+                // unsafe division: rebuild prod_{d' != k} <G_j^d', F_i^d'> directly
+                psk = 1.f;
+                for (int dd = 0; dd < D; ++dd) {
+                  if (dd == k) continue;
+                  const int npd = round_up(p.nbas[dd], 4);
+                  psk *= dot_global(gm + (long long)p.offp[dd] * rG + (long long)j * npd,
+                                    f32 + (long long)i * p.nDp + p.offp[dd], npd);
+                }
+              }
+              s.ps[r * rFp + i] = psk;  // holds prod_{d != k} until mode k is solved
+            }
+            s.wt[(rb * 4 + a) * rFp + i] = cj * psk;
+          }
         }
       }
       __syncthreads();
@@ -408,6 +475,7 @@ size_t als_smem_bytes(int rows_cta, int rF, int npmax) {
   take(sizeof(float) * rFp * npmax);
   take(sizeof(float) * rFp * npmax);
   take(sizeof(float) * kTileRows * rFp);
+  take(sizeof(float) * kTileRows * npmax);
   take(sizeof(float) * kTileRows * npmax);
   take(sizeof(float) * rFp * npmax);
   take(sizeof(float) * kThreads * 16);

@@ -37,6 +37,7 @@ static int finish(int status) {
   if (status == kOk) t_error.clear();
   return status;
 }
+int finish_status(int status) { return finish(status); }
 
 // ---------------------------------------------------------------------------
 // Context
@@ -201,10 +202,14 @@ int plan_als(Context* ctx, int nvec, int ndof, const int* nbas, const int* rF, c
 
 }  // namespace
 
-// Runs the batched ALS on device data; everything is enqueued on `st`.
-int als_batched_device(Context* ctx, int nvec, int ndof, const int* nbas, const int* rF, const int* rG,
-                       const long long* term_off, double* d_coef, double* d_base, int nals, int* d_status,
-                       cudaStream_t st) {
+// Runs one batched reduction; everything is enqueued on `st`.
+int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
+  const int nvec = job.nvec, ndof = job.ndof, nals = job.nals;
+  const int *nbas = job.nbas, *rF = job.rF, *rG = job.rG;
+  const long long* term_off = job.term_off;
+  double* d_coef = job.d_coef;
+  double* d_base = job.d_base;
+  int* d_status = job.d_status;
   if (nals == 0) return kOk;  // reference returns before touching the data (src/als.cu:1026)
   if (nals < 0) {
     set_error("mlcp_als_batched: nals = %d is negative", nals);
@@ -216,13 +221,13 @@ int als_batched_device(Context* ctx, int nvec, int ndof, const int* nbas, const 
 
   // metadata block: ints then long longs (uploaded in one copy)
   const size_t n_int = (size_t)(ndof) + 2 * (ndof + 1) + 2 * nvec;
-  const size_t n_ll = (size_t)6 * nvec;
+  const size_t n_ll = (size_t)7 * nvec;
   const size_t meta_bytes = align256(n_int * sizeof(int)) + n_ll * sizeof(long long);
   // workspace layout
   size_t bytes = 0;
   auto reserve = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
   const size_t o_meta = reserve(meta_bytes);
-  const size_t o_gm = reserve(sizeof(float) * P.gm_floats);
+  const size_t o_gm = reserve(sizeof(float) * (job.shared_w ? (long long)rG[0] * P.nDp : P.gm_floats));
   const size_t o_gc = reserve(sizeof(float) * P.total_rows);
   const size_t o_f32 = reserve(sizeof(float) * P.total_f * P.nDp);
   const size_t o_gram = reserve(sizeof(double) * P.sq_doubles);
@@ -258,6 +263,13 @@ int als_batched_device(Context* ctx, int nvec, int ndof, const int* nbas, const 
   std::memcpy(p_fro, P.f_row_off.data(), sizeof(long long) * nvec);
   std::memcpy(p_gmo, P.gm_off.data(), sizeof(long long) * nvec);
   std::memcpy(p_sqo, P.sq_off.data(), sizeof(long long) * nvec);
+  long long* p_gto = p_sqo + nvec;
+  for (int v = 0; v < nvec; ++v)
+    p_gto[v] = job.shared_w ? 0 : (job.g_term_off ? job.g_term_off[v] : term_off[v] + rF[v]);
+  if (job.shared_w) {
+    // every vector reads vector 0's converted target
+    for (int v = 0; v < nvec; ++v) p_gmo[v] = 0;
+  }
   MLCP_CUDA_TRY(cudaMemcpyAsync(w + o_meta, stage, meta_bytes, cudaMemcpyHostToDevice, st));
   MLCP_CUDA_TRY(cudaEventRecord(ctx->staged, st));
 
@@ -286,6 +298,11 @@ int als_batched_device(Context* ctx, int nvec, int ndof, const int* nbas, const 
   prm.sq_off = d_ll + 4 * nvec;
   prm.base = d_base;
   prm.coef = d_coef;
+  prm.g_base = job.g_base ? job.g_base : d_base;
+  prm.g_coef = job.g_coef ? job.g_coef : d_coef;
+  prm.g_term_off = d_ll + 6 * nvec;
+  prm.shared_target = job.shared_w ? 1 : 0;
+  prm.shared_w = job.shared_w;
   prm.gm = reinterpret_cast<float*>(w + o_gm);
   prm.gc = reinterpret_cast<float*>(w + o_gc);
   prm.f32 = reinterpret_cast<float*>(w + o_f32);
@@ -448,8 +465,10 @@ extern "C" int mlcp_als_batched(int nvec, int ndof, const int* nbas, const int* 
   Context* ctx = get_context(&rc);
   if (!ctx) return finish(rc);
   std::lock_guard<std::mutex> lk(ctx->mu);
-  rc = als_batched_device(ctx, nvec, ndof, nbas, rF, rG, term_off, d_coef, d_base, nals, d_status,
-                          pick_stream(ctx, stream));
+  AlsJob job;
+  job.nvec = nvec; job.ndof = ndof; job.nals = nals; job.nbas = nbas; job.rF = rF; job.rG = rG;
+  job.term_off = term_off; job.d_base = d_base; job.d_coef = d_coef; job.d_status = d_status;
+  rc = als_run(ctx, job, pick_stream(ctx, stream));
   return finish(rc);
 }
 
@@ -501,7 +520,10 @@ extern "C" int mlcp_als_batched_host(int nvec, int ndof, const int* nbas, const 
   };
   if ((rc = cpy(d_base, h_base, sizeof(double) * (size_t)nterms * nD, cudaMemcpyHostToDevice))) return finish(rc);
   if ((rc = cpy(d_coef, h_coef, sizeof(double) * (size_t)nterms, cudaMemcpyHostToDevice))) return finish(rc);
-  rc = als_batched_device(ctx, nvec, ndof, nbas, rF, rG, term_off, d_coef, d_base, nals, nullptr, st);
+  AlsJob job;
+  job.nvec = nvec; job.ndof = ndof; job.nals = nals; job.nbas = nbas; job.rF = rF; job.rG = rG;
+  job.term_off = term_off; job.d_base = d_base; job.d_coef = d_coef;
+  rc = als_run(ctx, job, st);
   if (rc) return finish(rc);
   for (int v = 0; v < nvec; ++v) {
     const size_t t0 = (size_t)term_off[v];

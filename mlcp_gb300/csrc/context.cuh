@@ -22,6 +22,10 @@ struct Context {
   void* stage = nullptr;
   size_t stage_bytes = 0;
   cudaEvent_t staged = nullptr;
+  // power-cycle workspace (separate from the ALS workspace, which the cycle
+  // also uses for its vector updates)
+  void* cyc = nullptr;
+  size_t cyc_bytes = 0;
   // device copies of caller host buffers (host-buffer entry points)
   void* io = nullptr;
   size_t io_bytes = 0;

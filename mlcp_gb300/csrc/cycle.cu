@@ -1,0 +1,447 @@
+// One intertwined power cycle on a block of CP vectors: the drop-in
+// intertwinecpp_ (reference src/intertwining.cu:98-176) and intwdevicemem_
+// (:31-94).
+//
+// Reference flow per call: upload the HopList, per-vector POW_ALS with a
+// host round trip per vector, free and re-upload the HopList, upload the
+// block, Gram-Schmidt, (update: GenEigvalProblem with cuSOLVER sygvd,
+// VectorUpdates with a host round trip per vector), cudaDeviceReset.
+//
+// Here: the block goes to the device once and comes back once; the operator
+// list is preprocessed once per distinct content (hash) and stays resident;
+// each phase is one launch over the whole block:
+//   opals (POW_ALS, all vectors)  ->  gs (Gram-Schmidt)  ->
+//   opals (PRODHV_ALS, all vectors) -> gep (inner products, Rayleigh-Ritz) ->
+//   batched ALS with a shared target (vector updates) -> weight normalisation.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "../../include/mlcp_gb300.h"
+#include "als.cuh"
+#include "common.cuh"
+#include "context.cuh"
+#include "intertwine.cuh"
+
+namespace mlcp {
+
+int als_run(Context* ctx, const AlsJob& job, cudaStream_t st);
+int finish_status(int status);
+
+namespace {
+
+constexpr int kMaxRankCycle = 64;
+constexpr int kMaxBasisCycle = 64;
+
+uint64_t fnv1a(uint64_t h, const void* data, size_t bytes) {
+  const unsigned char* p = static_cast<const unsigned char*>(data);
+  for (size_t i = 0; i < bytes; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+// Device-resident operator table of one HopList (per device, per rank).
+struct HopCache {
+  uint64_t key = 0;
+  int R = 0;
+  void* dev = nullptr;
+  size_t bytes = 0;
+  OpTable tab{};
+};
+
+std::mutex g_hop_mu;
+std::map<int, HopCache> g_hop;  // per device
+
+struct Layout {
+  int D, nD, nDp, npmax;
+  std::vector<int> off, offp;
+};
+
+int make_layout(int ndof, const int* nbas, Layout* L) {
+  L->D = ndof;
+  L->off.assign(ndof + 1, 0);
+  L->offp.assign(ndof + 1, 0);
+  L->npmax = 4;
+  for (int d = 0; d < ndof; ++d) {
+    if (nbas[d] < 1 || nbas[d] > kMaxBasisCycle) {
+      set_error("intertwinecpp_: nbas[%d] = %d outside [1, %d]", d, nbas[d], kMaxBasisCycle);
+      return nbas[d] < 1 ? kBadArgument : kTooLarge;
+    }
+    L->off[d + 1] = L->off[d] + nbas[d];
+    L->offp[d + 1] = L->offp[d] + round_up(nbas[d], 4);
+    L->npmax = std::max(L->npmax, round_up(nbas[d], 4));
+  }
+  L->nD = L->off[ndof];
+  L->nDp = L->offp[ndof];
+  return kOk;
+}
+
+// Build (or reuse) the device operator table for this HopList.
+int get_optable(Context* ctx, const Layout& Ly, const int* nbas, int R, int T, const int* opid, const int* mptr,
+                const double* Hcoef, const double* mat, int nops, int msize, cudaStream_t st, OpTable* out) {
+  const int D = Ly.D;
+  uint64_t key = 1469598103934665603ull;
+  const int hdr[5] = {D, T, nops, msize, R};
+  key = fnv1a(key, hdr, sizeof(hdr));
+  key = fnv1a(key, nbas, sizeof(int) * D);
+  key = fnv1a(key, opid, sizeof(int) * (size_t)T * D);
+  key = fnv1a(key, mptr, sizeof(int) * nops);
+  key = fnv1a(key, Hcoef, sizeof(double) * T);
+  key = fnv1a(key, mat, sizeof(double) * msize);
+  std::lock_guard<std::mutex> lk(g_hop_mu);
+  HopCache& hc = g_hop[ctx->device];
+  if (hc.dev && hc.key == key) {
+    *out = hc.tab;
+    return kOk;
+  }
+  // validate every reference before touching the matrices
+  for (long long e = 0; e < (long long)T * D; ++e) {
+    const int o = opid[e];
+    if (o < 1 || o > nops) {
+      set_error("intertwinecpp_: opid[%lld] = %d outside [1, %d]", e, o, nops);
+      return kBadArgument;
+    }
+    const int d = (int)(e % D), n = nbas[d];
+    const long long start = (long long)mptr[o - 1] - 1;
+    if (start < 0 || start + (long long)n * (n + 1) / 2 > msize) {
+      set_error("intertwinecpp_: operator %d (mode %d) at mptr %d exceeds msize %d", o, d, mptr[o - 1], msize);
+      return kBadArgument;
+    }
+  }
+  // distinct operators per mode; local index 0 is always the identity
+  std::vector<std::vector<long long>> starts(D);  // -1 marks the identity slot
+  std::vector<int> uid((size_t)T * D);
+  for (int d = 0; d < D; ++d) starts[d].push_back(-1);
+  for (int t = 0; t < T; ++t)
+    for (int d = 0; d < D; ++d) {
+      const int n = nbas[d];
+      const long long st0 = (long long)mptr[opid[(size_t)t * D + d] - 1] - 1;
+      bool ident = true;
+      for (int c = 0; c < n && ident; ++c)
+        for (int r = 0; r <= c && ident; ++r) ident = (mat[st0 + r + (long long)c * (c + 1) / 2] == (r == c ? 1.0 : 0.0));
+      int u = 0;
+      if (!ident) {
+        auto it = std::find(starts[d].begin(), starts[d].end(), st0);
+        if (it == starts[d].end()) {
+          starts[d].push_back(st0);
+          u = (int)starts[d].size() - 1;
+        } else {
+          u = (int)(it - starts[d].begin());
+        }
+      }
+      uid[(size_t)t * D + d] = u;
+    }
+  std::vector<int> uoff(D + 1, 0);
+  int umax = 0;
+  for (int d = 0; d < D; ++d) {
+    uoff[d + 1] = uoff[d] + (int)starts[d].size();
+    umax = std::max(umax, (int)starts[d].size());
+  }
+  const int utot = uoff[D];
+  const int npm = Ly.npmax;
+  std::vector<float> hmat((size_t)utot * npm * npm, 0.f);
+  std::vector<unsigned char> ident(utot, 0);
+  for (int d = 0; d < D; ++d) {
+    const int n = nbas[d];
+    for (int u = 0; u < (int)starts[d].size(); ++u) {
+      float* h = &hmat[(size_t)(uoff[d] + u) * npm * npm];
+      if (starts[d][u] < 0) {
+        ident[uoff[d] + u] = 1;
+        for (int i = 0; i < n; ++i) h[i * npm + i] = 1.f;
+        continue;
+      }
+      const double* pk = mat + starts[d][u];
+      for (int c = 0; c < n; ++c)
+        for (int r = 0; r <= c; ++r) {
+          const float v = (float)pk[r + (size_t)c * (c + 1) / 2];
+          h[r * npm + c] = v;
+          h[c * npm + r] = v;
+        }
+    }
+  }
+  // per mode j: terms grouped by their operator at j (stable)
+  std::vector<int> order((size_t)D * T), gstart((size_t)D * (umax + 1), 0);
+  for (int j = 0; j < D; ++j) {
+    const int nu = (int)starts[j].size();
+    std::vector<int> cnt(nu + 1, 0);
+    for (int t = 0; t < T; ++t) cnt[uid[(size_t)t * D + j] + 1]++;
+    for (int u = 0; u < nu; ++u) cnt[u + 1] += cnt[u];
+    for (int u = 0; u <= umax; ++u) gstart[(size_t)j * (umax + 1) + u] = cnt[std::min(u, nu)];
+    std::vector<int> pos(cnt.begin(), cnt.end() - 1);
+    for (int t = 0; t < T; ++t) order[(size_t)j * T + pos[uid[(size_t)t * D + j]]++] = t;
+  }
+  // one device allocation for the whole table
+  size_t bytes = 0;
+  auto reserve = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
+  const size_t o_nbas = reserve(sizeof(int) * D), o_off = reserve(sizeof(int) * (D + 1)),
+               o_offp = reserve(sizeof(int) * (D + 1)), o_uoff = reserve(sizeof(int) * (D + 1)),
+               o_uid = reserve(sizeof(int) * uid.size()), o_ident = reserve(utot),
+               o_h = reserve(sizeof(float) * hmat.size()), o_alpha = reserve(sizeof(double) * T),
+               o_order = reserve(sizeof(int) * order.size()), o_gs = reserve(sizeof(int) * gstart.size());
+  std::vector<char> host(bytes);
+  std::memcpy(&host[o_nbas], nbas, sizeof(int) * D);
+  std::memcpy(&host[o_off], Ly.off.data(), sizeof(int) * (D + 1));
+  std::memcpy(&host[o_offp], Ly.offp.data(), sizeof(int) * (D + 1));
+  std::memcpy(&host[o_uoff], uoff.data(), sizeof(int) * (D + 1));
+  std::memcpy(&host[o_uid], uid.data(), sizeof(int) * uid.size());
+  std::memcpy(&host[o_ident], ident.data(), utot);
+  std::memcpy(&host[o_h], hmat.data(), sizeof(float) * hmat.size());
+  std::memcpy(&host[o_alpha], Hcoef, sizeof(double) * T);
+  std::memcpy(&host[o_order], order.data(), sizeof(int) * order.size());
+  std::memcpy(&host[o_gs], gstart.data(), sizeof(int) * gstart.size());
+  if (hc.dev) {
+    MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+    MLCP_CUDA_TRY(cudaFree(hc.dev));
+    hc.dev = nullptr;
+  }
+  MLCP_CUDA_TRY(cudaMalloc(&hc.dev, bytes));
+  MLCP_CUDA_TRY(cudaMemcpy(hc.dev, host.data(), bytes, cudaMemcpyHostToDevice));
+  char* b = static_cast<char*>(hc.dev);
+  OpTable& t = hc.tab;
+  t.D = D; t.T = T; t.R = R; t.nDp = Ly.nDp; t.npmax = npm; t.umax = umax; t.utot = utot;
+  t.nbas = (const int*)(b + o_nbas); t.off = (const int*)(b + o_off); t.offp = (const int*)(b + o_offp);
+  t.uoff = (const int*)(b + o_uoff); t.uid = (const int*)(b + o_uid);
+  t.ident = (const unsigned char*)(b + o_ident); t.hmat = (const float*)(b + o_h);
+  t.alpha = (const double*)(b + o_alpha); t.order = (const int*)(b + o_order); t.gstart = (const int*)(b + o_gs);
+  hc.key = key;
+  hc.R = R;
+  hc.bytes = bytes;
+  *out = t;
+  return kOk;
+}
+
+__global__ void update_weights_kernel(int B, int R, const double* qcoef, const double* U, double* w) {
+  // w[v][k*R + r] = c(k,r) * U(k, v)
+  const long long n = (long long)B * B * R;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int v = (int)(e / ((long long)B * R));
+    const int kr = (int)(e % ((long long)B * R));
+    const int k = kr / R;
+    w[e] = qcoef[kr] * U[k + (size_t)v * B];
+  }
+}
+
+struct CycleBuffers {
+  double *q, *qc, *hq, *hqc, *qn, *qnc;
+  float *mscr, *wscr, *zscr, *q32, *pscr;
+  double *g64, *gcoef, *A, *S, *U, *eigv, *gwork, *wts;
+  int *meta, *status;
+};
+
+size_t plan_cycle(const Layout& Ly, const OpTable& t, int R, int B, CycleBuffers* cb, char* base) {
+  size_t bytes = 0;
+  auto take = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return base ? base + o : nullptr; };
+  const size_t vec = (size_t)B * R;
+  cb->q = (double*)take(sizeof(double) * vec * Ly.nD);
+  cb->qc = (double*)take(sizeof(double) * vec);
+  cb->hq = (double*)take(sizeof(double) * vec * Ly.nD);
+  cb->hqc = (double*)take(sizeof(double) * vec);
+  cb->qn = (double*)take(sizeof(double) * vec * Ly.nD);
+  cb->qnc = (double*)take(sizeof(double) * vec);
+  cb->mscr = (float*)take(sizeof(float) * (size_t)B * t.utot * R * R);
+  cb->wscr = (float*)take(sizeof(float) * (size_t)B * t.umax * R * R);
+  cb->zscr = (float*)take(sizeof(float) * (size_t)B * t.umax * R * t.npmax);
+  cb->g64 = (double*)take(sizeof(double) * (size_t)B * Ly.D * R * R);
+  cb->q32 = (float*)take(sizeof(float) * vec * Ly.nDp);
+  cb->pscr = (float*)take(sizeof(float) * (size_t)B * (Ly.D + 1) * R * R);
+  cb->gcoef = (double*)take(sizeof(double) * B);
+  cb->A = (double*)take(sizeof(double) * (size_t)B * B);
+  cb->S = (double*)take(sizeof(double) * (size_t)B * B);
+  cb->U = (double*)take(sizeof(double) * (size_t)B * B);
+  cb->eigv = (double*)take(sizeof(double) * B);
+  cb->gwork = (double*)take(sizeof(double) * gep_work_doubles(B));
+  cb->wts = (double*)take(sizeof(double) * (size_t)B * B * R);
+  cb->meta = (int*)take(sizeof(int) * 3 * (Ly.D + 1));
+  cb->status = (int*)take(sizeof(int) * (B + 4));
+  return bytes;
+}
+
+}  // namespace
+
+// Full cycle; host buffers in, host buffers out.  Returns a Status.
+int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, int rk, int ndof, int nbloc,
+                     const int* opid, const int* mptr, const double* Hcoef, const double* mat, int TxD, int nops,
+                     int msize, double* eigv, int npow, int nals, bool update, int ishift, double Eshift) {
+  if (rk < 1 || rk > kMaxRankCycle) {
+    set_error("intertwinecpp_: rk = %d outside [1, %d]", rk, kMaxRankCycle);
+    return rk < 1 ? kBadArgument : kTooLarge;
+  }
+  if (ndof < 1 || nbloc < 1 || TxD < ndof || TxD % ndof != 0 || nops < 1 || msize < 1) {
+    set_error("intertwinecpp_: bad sizes (ndof=%d nbloc=%d TxD=%d nops=%d msize=%d)", ndof, nbloc, TxD, nops, msize);
+    return kBadArgument;
+  }
+  if (npow < 0 || nals < 0) {
+    set_error("intertwinecpp_: npow (%d) and nals (%d) must be non-negative", npow, nals);
+    return kBadArgument;
+  }
+  if (update && nbloc > 160) {
+    set_error("intertwinecpp_: block size %d exceeds the 160 vectors of the on-chip Rayleigh-Ritz solver", nbloc);
+    return kTooLarge;
+  }
+  Layout Ly;
+  int rc = make_layout(ndof, nbas, &Ly);
+  if (rc) return rc;
+  const int T = TxD / ndof, R = rk, B = nbloc;
+  cudaStream_t st = ctx->stream;
+  OpTable tab;
+  rc = get_optable(ctx, Ly, nbas, R, T, opid, mptr, Hcoef, mat, nops, msize, st, &tab);
+  if (rc) return rc;
+  {
+    size_t smem = opals_smem_bytes(tab);
+    if (smem > ctx->smem_optin) {
+      set_error("intertwinecpp_: rank %d with %d padded basis functions needs %zu bytes of shared memory", R,
+                Ly.nDp, smem);
+      return kTooLarge;
+    }
+  }
+  CycleBuffers cb;
+  const size_t bytes = plan_cycle(Ly, tab, R, B, &cb, nullptr);
+  if (bytes > ctx->cyc_bytes) {
+    if (ctx->cyc) {
+      MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+      MLCP_CUDA_TRY(cudaFree(ctx->cyc));
+      ctx->cyc = nullptr;
+      ctx->cyc_bytes = 0;
+    }
+    MLCP_CUDA_TRY(cudaMalloc(&ctx->cyc, bytes));
+    ctx->cyc_bytes = bytes;
+  }
+  plan_cycle(Ly, tab, R, B, &cb, static_cast<char*>(ctx->cyc));
+  const size_t nvals = (size_t)B * R * Ly.nD;
+  MLCP_CUDA_TRY(cudaMemcpyAsync(cb.q, base, sizeof(double) * nvals, cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qc, coef, sizeof(double) * B * R, cudaMemcpyHostToDevice, st));
+  {
+    std::vector<int> meta(3 * (ndof + 1), 0);
+    std::memcpy(meta.data(), nbas, sizeof(int) * ndof);
+    std::memcpy(meta.data() + (ndof + 1), Ly.off.data(), sizeof(int) * (ndof + 1));
+    std::memcpy(meta.data() + 2 * (ndof + 1), Ly.offp.data(), sizeof(int) * (ndof + 1));
+    MLCP_CUDA_TRY(cudaMemcpyAsync(cb.meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, st));
+    MLCP_CUDA_TRY(cudaStreamSynchronize(st));  // meta lives on the host stack
+  }
+  const int* d_nbas = cb.meta;
+  const int* d_off = cb.meta + (ndof + 1);
+  const int* d_offp = cb.meta + 2 * (ndof + 1);
+  MLCP_CUDA_TRY(cudaMemsetAsync(cb.status, 0, sizeof(int) * (B + 4), st));
+
+  // --- matrix-vector products: POW_ALS on every vector ---
+  if (npow > 0) {
+    OpAlsParams p;
+    p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 0; p.nsweeps = npow; p.ishift = ishift; p.eshift = Eshift;
+    p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.q; p.f_coef = cb.qc;
+    p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
+    if ((rc = opals_launch(p, st))) return rc;
+  }
+  // --- Gram-Schmidt ---
+  if (nals > 0) {
+    GsParams g;
+    g.D = ndof; g.R = R; g.nbloc = B; g.nD = Ly.nD; g.nDp = Ly.nDp; g.npmax = Ly.npmax; g.nals = nals;
+    g.nbas = d_nbas; g.off = d_off; g.offp = d_offp; g.base = cb.q; g.coef = cb.qc; g.q32 = cb.q32;
+    g.pscr = cb.pscr; g.g64 = cb.g64; g.gcoef = cb.gcoef; g.status = cb.status + B;
+    if ((rc = gs_launch(g, st))) return rc;
+  }
+  if (update) {
+    // --- <Q|H|Q>, <Q|Q>, generalised eigenproblem ---
+    if (nals > 0) {
+      OpAlsParams p;
+      p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 1; p.nsweeps = nals; p.ishift = 0; p.eshift = 0.0;
+      p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.hq; p.f_coef = cb.hqc;
+      p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
+      if ((rc = opals_launch(p, st))) return rc;
+    } else {
+      MLCP_CUDA_TRY(cudaMemsetAsync(cb.hq, 0, sizeof(double) * nvals, st));
+      MLCP_CUDA_TRY(cudaMemsetAsync(cb.hqc, 0, sizeof(double) * B * R, st));
+    }
+    GepParams gp;
+    gp.D = ndof; gp.R = R; gp.nbloc = B; gp.nD = Ly.nD; gp.nbas = d_nbas;
+    gp.q_base = cb.q; gp.q_coef = cb.qc; gp.hq_base = cb.hq; gp.hq_coef = cb.hqc;
+    gp.A = cb.A; gp.S = cb.S; gp.eigv = cb.eigv; gp.U = cb.U; gp.work = cb.gwork; gp.status = cb.status + B + 1;
+    if ((rc = gep_launch(gp, st))) return rc;
+    // --- vector updates: new Q_i fits sum_k U(k,i) Q_k, starting from Q_i ---
+    if (nals > 0) {
+      MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qn, cb.q, sizeof(double) * nvals, cudaMemcpyDeviceToDevice, st));
+      MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qnc, cb.qc, sizeof(double) * B * R, cudaMemcpyDeviceToDevice, st));
+      update_weights_kernel<<<std::min(ctx->num_sms * 8, (B * B * R + 255) / 256), 256, 0, st>>>(B, R, cb.qc, cb.U,
+                                                                                                  cb.wts);
+      MLCP_CUDA_TRY(cudaGetLastError());
+      std::vector<int> rF(B, R), rG(B, B * R);
+      std::vector<long long> toff(B), gtoff(B, 0);
+      for (int v = 0; v < B; ++v) toff[v] = (long long)v * R;
+      AlsJob job;
+      job.nvec = B; job.ndof = ndof; job.nals = nals; job.nbas = nbas; job.rF = rF.data(); job.rG = rG.data();
+      job.term_off = toff.data(); job.d_base = cb.qn; job.d_coef = cb.qnc;
+      job.g_base = cb.q; job.g_coef = cb.qc; job.g_term_off = gtoff.data(); job.shared_w = cb.wts;
+      job.d_status = cb.status;
+      if ((rc = als_run(ctx, job, st))) return rc;
+      if ((rc = normalize_coefs_launch(B, R, ndof, Ly.nD, d_nbas, cb.qn, cb.qnc, st))) return rc;
+      std::swap(cb.q, cb.qn);
+      std::swap(cb.qc, cb.qnc);
+    }
+    MLCP_CUDA_TRY(cudaMemcpyAsync(eigv, cb.eigv, sizeof(double) * B, cudaMemcpyDeviceToHost, st));
+  }
+  MLCP_CUDA_TRY(cudaMemcpyAsync(base, cb.q, sizeof(double) * nvals, cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(coef, cb.qc, sizeof(double) * B * R, cudaMemcpyDeviceToHost, st));
+  std::vector<int> status(B + 4);
+  MLCP_CUDA_TRY(cudaMemcpyAsync(status.data(), cb.status, sizeof(int) * (B + 4), cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int i = 0; i < B + 2; ++i)
+    if (status[i]) {
+      set_error("intertwinecpp_: a normal-equation or overlap matrix was not positive definite (flag %d at %d)",
+                status[i], i);
+      return kNumerical;
+    }
+  return kOk;
+}
+
+// Device bytes one cycle of this shape needs (workspace + operator table).
+size_t cycle_bytes_estimate(int rk, int ndof, int nbloc, const int* nbas, int T, int msize) {
+  Layout Ly;
+  if (make_layout(ndof, nbas, &Ly) != kOk) return 0;
+  OpTable t{};
+  t.D = ndof; t.T = T; t.R = rk; t.nDp = Ly.nDp; t.npmax = Ly.npmax;
+  // upper bound on distinct operators per mode: all terms distinct
+  t.umax = std::min(T + 1, msize);
+  t.utot = t.umax * ndof;
+  CycleBuffers cb;
+  return plan_cycle(Ly, t, rk, nbloc, &cb, nullptr);
+}
+
+}  // namespace mlcp
+
+using namespace mlcp;
+
+extern "C" void intertwinecpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof,
+                               const int& nbloc, int* opid, int* mptr, double* Hcoef, double* mat, const int& TxD,
+                               const int& nops, const int& msize, double* eigv, const int& npow, const int& ncpu,
+                               const int& nals, const bool& update, const int& ishift, const double& Eshift) {
+  (void)ncpu;
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (ctx) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    rc = intertwine_cycle(ctx, base, coef, nbas, rk, ndof, nbloc, opid, mptr, Hcoef, mat, TxD, nops, msize, eigv,
+                          npow, nals, update, ishift, Eshift);
+  }
+  finish_status(rc);
+  if (rc != kOk) fprintf(stderr, "intertwinecpp_: %s\n", last_error());
+}
+
+extern "C" void intwdevicemem_(const int& rk, const int& ndof, const int& nbloc, const int& TxD, const int& nops,
+                               const int& msize, const int& ncpu, const bool& update, const int* nbas) {
+  (void)nops; (void)ncpu; (void)update;
+  const int T = ndof > 0 ? TxD / ndof : 0;
+  const double MB = 1.0 / (1 << 20);
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const size_t cyc = cycle_bytes_estimate(rk, ndof, nbloc, nbas, T, msize);
+  const size_t hl = sizeof(double) * ((size_t)T + msize) + sizeof(int) * ((size_t)T * ndof + nops);
+  printf(" *** Device memory (mlcp_gb300) *** \n");
+  printf(" Free / total device memory : %10.2f / %10.2f MB\n", free_b * MB, total_b * MB);
+  printf(" Hamiltonian storage        : %10.2f MB (kept resident between cycles)\n", hl * MB);
+  printf(" Power-cycle workspace      : %10.2f MB (upper bound)\n", cyc * MB);
+  printf(" (double precision normal equations, single precision contractions)\n\n");
+}

@@ -1,0 +1,91 @@
+// Intertwined power cycle (reference src/intertwining.cu:98, intertw_mvp.cu,
+// intertw_lcv.cu): parameter blocks shared by host and device.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace mlcp {
+
+// Operator list prepared once per distinct HopList (cached on the device).
+// Per mode d the distinct operators used by any term get local indices
+// u = 0..nops_mode[d]-1; u = 0 is always the identity.
+struct OpTable {
+  int D, T, R;              // modes, terms, vector rank
+  int nDp;                  // sum of 4-padded basis sizes
+  int npmax;                // max padded basis size
+  int umax;                 // max operators in one mode
+  int utot;                 // total operators over modes
+  const int* nbas;          // [D]
+  const int* off;           // [D+1] reference layout offsets
+  const int* offp;          // [D+1] padded offsets
+  const int* uoff;          // [D+1] first global operator slot of each mode
+  const int* uid;           // [T*D] local operator index of term t at mode d
+  const unsigned char* ident;  // [utot] 1 if the operator is the identity
+  const float* hmat;        // [utot][npmax][npmax] dense FP32 operators
+  const double* alpha;      // [T] term coefficients
+  const int* order;         // [D][T] terms grouped by their operator at mode j
+  const int* gstart;        // [D][umax+1] group starts in order[j]
+};
+
+// Per-vector sweep of ALS-fitted operator applications.
+struct OpAlsParams {
+  OpTable ops;
+  int nvec;
+  int nD;
+  int mode;           // 0: POW_ALS (F fits (H - E)F in place), 1: PRODHV_ALS (F fits H Fo)
+  int nsweeps;
+  int ishift;
+  double eshift;
+  const double* fo_base;  // Fo vectors (reference layout, rank R each, vector v at v*R terms)
+  const double* fo_coef;
+  double* f_base;         // F output (may alias fo for POW)
+  double* f_coef;
+  float* mscr;            // [nvec][utot][R][R] operator Grams M = Fo^T h F
+  float* wscr;            // [nvec][umax][R][R] grouped term products W
+  float* zscr;            // [nvec][umax][R][npmax] h Fo_j
+  double* g64;            // [nvec][D][R][R] FP64 Grams of F
+  int* status;            // [nvec]
+};
+
+int opals_launch(const OpAlsParams& p, cudaStream_t st);
+size_t opals_smem_bytes(const OpTable& t);
+
+// ALS-guided Gram-Schmidt over a block (reference src/intertw_lcv.cu:131).
+struct GsParams {
+  int D, R, nbloc, nD, nDp, npmax, nals;
+  const int* nbas;
+  const int* off;
+  const int* offp;
+  double* base;   // block, in place
+  double* coef;
+  float* q32;     // [nbloc][R][nDp] FP32 copy of the block (kept in step)
+  float* pscr;    // [nbloc][D][R][R] P(k,d) = Q_k,d F_d^T
+  double* g64;    // [D][R][R]
+  double* gcoef;  // [nbloc]
+  int* status;
+};
+int gs_launch(const GsParams& p, cudaStream_t st);
+
+// Block Rayleigh-Ritz inner products: QHQ(i,j) = <Q_j, HQ_i>, S(i,j) = <Q_j, Q_i>, j <= i.
+struct GepParams {
+  int D, R, nbloc, nD;
+  const int* nbas;
+  const double* q_base;
+  const double* q_coef;
+  const double* hq_base;
+  const double* hq_coef;
+  double* A;  // [nbloc][nbloc] column-major (lower triangle filled)
+  double* S;
+  double* eigv;   // [nbloc]
+  double* U;      // [nbloc][nbloc] eigenvectors (column-major)
+  double* work;   // scratch, see gep_work_doubles
+  int* status;
+};
+int gep_launch(const GepParams& p, cudaStream_t st);
+size_t gep_work_doubles(int nbloc);
+
+// Divide the weights of each rank-R vector by its norm (FP64).
+int normalize_coefs_launch(int nvec, int R, int D, int nD, const int* nbas, const double* base, double* coef,
+                           cudaStream_t st);
+
+}  // namespace mlcp

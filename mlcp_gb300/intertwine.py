@@ -1,0 +1,58 @@
+"""Host-side interface to one intertwined power cycle.
+
+Mirrors the reference's IntertwineCPP/intertwinecpp_ operator
+(src/GPUIterate.f90:89-187, src/intertwining.cu:98): for a block of nbloc
+CP vectors of rank rk and a Hamiltonian operator list, run npow ALS-fitted
+applications of (H - Eshift), the ALS-guided Gram-Schmidt, and (update=True)
+the block Rayleigh-Ritz problem and ALS-fitted vector updates.  The call
+goes through the C ABI with the reference's by-reference argument passing.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int)
+
+
+def intertwine(base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int, hl, eigv: np.ndarray, npow: int,
+               nals: int, update: bool = True, ishift: int = 1, Eshift: float = 0.0, ncpu: int = 1):
+    """Run one cycle on copies of (base, coef, eigv) and return the new
+    (base, coef, eigv).  base is (nbloc*rk, nD) with row = term."""
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    eig = np.ascontiguousarray(eigv, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32).copy()
+    opid = np.ascontiguousarray(hl.opid, dtype=np.int32).copy()
+    mptr = np.ascontiguousarray(hl.mptr, dtype=np.int32).copy()
+    hcoef = np.ascontiguousarray(hl.coef, dtype=np.float64).copy()
+    mat = np.ascontiguousarray(hl.mat, dtype=np.float64).copy()
+    ints = [ctypes.c_int(x) for x in (rk, nb.size, nbloc, opid.size, mptr.size, mat.size, npow, ncpu, nals,
+                                      ishift)]
+    upd = ctypes.c_bool(bool(update))
+    esh = ctypes.c_double(float(Eshift))
+    L = _lib.load()
+    L.intertwinecpp_(base.ctypes.data_as(_D), coef.ctypes.data_as(_D), nb.ctypes.data_as(_I),
+                     ctypes.byref(ints[0]), ctypes.byref(ints[1]), ctypes.byref(ints[2]),
+                     opid.ctypes.data_as(_I), mptr.ctypes.data_as(_I), hcoef.ctypes.data_as(_D),
+                     mat.ctypes.data_as(_D), ctypes.byref(ints[3]), ctypes.byref(ints[4]), ctypes.byref(ints[5]),
+                     eig.ctypes.data_as(_D), ctypes.byref(ints[6]), ctypes.byref(ints[7]), ctypes.byref(ints[8]),
+                     ctypes.byref(upd), ctypes.byref(ints[9]), ctypes.byref(esh))
+    if L.mlcp_gb300_last_status() != 0:
+        raise _lib.MlcpError(_lib.last_error())
+    return base, coef, eig
+
+
+def block_shift(eigv, emax: float) -> float:
+    """Reference GetBlockShift (src/BlockPower.f90:20-45): half way between an
+    estimate of the first eigenvalue above the block and the spectrum's top."""
+    eigv = np.asarray(eigv, dtype=np.float64)
+    if eigv.size > 1:
+        a = 2 * eigv[-1] - eigv[-2]
+    else:
+        a = 2 * eigv[0]
+    return 0.5 * (a + emax)

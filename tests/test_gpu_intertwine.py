@@ -1,0 +1,93 @@
+"""GPU intertwined power cycle (intertwinecpp_ through the C ABI) against the
+FP64 oracle.
+
+Tolerances (FP32 contractions, FP64 normal equations and Rayleigh-Ritz):
+eigenvalues agree to 1e-6 relative; each output vector agrees with the
+oracle's as a function, |<a,b>| / (|a| |b|) >= 1 - 1e-6 (sign-insensitive:
+the eigenvector sign convention is fixed identically on both sides, but a
+vector's factors may carry compensating signs).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from mlcp_gb300 import hoplist as H
+from mlcp_gb300 import intertwine as IT
+
+EIG_RTOL = 1e-6
+COS_TOL = 1e-6
+
+
+def cos_sim(ab, ac, bb, bc, nbas):
+    aa = oracle.cp_dot(ab, ac, ab, ac, nbas)
+    bbv = oracle.cp_dot(bb, bc, bb, bc, nbas)
+    x = oracle.cp_dot(ab, ac, bb, bc, nbas)
+    return abs(x) / np.sqrt(aa * bbv)
+
+
+def start_block(nbas, rk, nbloc, seed):
+    rng = np.random.default_rng(seed)
+    Q = rng.uniform(-0.5, 0.5, size=(rk * nbloc, int(np.sum(nbas))))
+    qc = np.ones(rk * nbloc)
+    return Q, qc
+
+
+def compare_blocks(gb, gc, ob, oc, nbas, rk, nbloc, tol=COS_TOL):
+    worst = 1.0
+    for i in range(nbloc):
+        s = slice(i * rk, (i + 1) * rk)
+        worst = min(worst, cos_sim(gb[s], gc[s], ob[s], oc[s], nbas))
+    assert 1 - worst <= tol, worst
+
+
+CASES = [
+    # (hoplist factory, rk, nbloc, npow, nals, update, ishift, Eshift)
+    (lambda: H.random_hoplist([4, 5, 3], 6, seed=3), 3, 4, 3, 4, True, 1, 2.0),
+    (lambda: H.coupled_oscillators(3, 6), 5, 4, 4, 4, True, 1, 4.0),
+    (lambda: H.henon_heiles(D=4, n=6), 6, 5, 3, 3, True, 1, 6.0),
+    (lambda: H.random_hoplist([6, 4, 5, 3], 9, seed=8, coupling=3), 4, 3, 2, 3, False, -1, 1.5),
+    (lambda: H.random_hoplist([5, 7], 4, seed=2), 3, 3, 3, 0, False, 0, 0.0),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_cycle_matches_oracle(case, cuda_device):
+    make, rk, nbloc, npow, nals, update, ishift, esh = CASES[case]
+    hl = make()
+    Q, qc = start_block(hl.nbas, rk, nbloc, seed=case)
+    eig0 = np.arange(nbloc, dtype=float)
+    gb, gc, ge = IT.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, eig0, npow, nals, update, ishift, esh)
+    ob, oc, oe = oracle.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, eig0, npow, nals, update, ishift, esh)
+    if update:
+        np.testing.assert_allclose(ge, oe, rtol=EIG_RTOL, atol=1e-12)
+    else:
+        np.testing.assert_array_equal(ge, eig0)
+    compare_blocks(gb, gc, ob, oc, hl.nbas, rk, nbloc)
+
+
+@pytest.mark.gpu
+def test_cycles_converge_to_exact_spectrum(cuda_device):
+    """Known answer: repeated GPU cycles reproduce the lowest eigenvalues of a
+    small Henon-Heiles Hamiltonian from dense diagonalisation."""
+    hl = H.henon_heiles(D=3, n=6, lam=0.111803)
+    ex = np.linalg.eigvalsh(H.dense_hamiltonian(hl))
+    rk, nbloc = 8, 4
+    Q, qc = start_block(hl.nbas, rk, nbloc, seed=1)
+    est = ex[:nbloc] + 0.3
+    eig = np.zeros(nbloc)
+    for _ in range(20):
+        esh = IT.block_shift(est, ex[-1])
+        Q, qc, eig = IT.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, eig, 5, 5, True, 1, esh)
+        est = eig
+    np.testing.assert_allclose(eig, ex[:nbloc], rtol=1e-5)
+
+
+@pytest.mark.gpu
+def test_cycle_rejects_bad_operator_index(cuda_device):
+    hl = H.random_hoplist([4, 3], 3, seed=1)
+    bad = H.HopList(nbas=hl.nbas, opid=hl.opid.copy(), mptr=hl.mptr, coef=hl.coef, mat=hl.mat)
+    bad.opid[2] = hl.mptr.size + 5
+    Q, qc = start_block(hl.nbas, 2, 2, seed=0)
+    with pytest.raises(Exception, match="opid"):
+        IT.intertwine(Q, qc, hl.nbas, 2, 2, bad, np.zeros(2), 2, 2, True, 1, 1.0)
