@@ -147,6 +147,50 @@ def run_reference(args):
     return 0
 
 
+# Power cycle (intertwinecpp_): Henon-Heiles with the config-1 shape at its
+# 6-mode level (10 HO functions per mode, lambda = 0.111803), rank 16, a
+# block of 40 vectors, npow = nals = 10, update on.
+CYC_D, CYC_N, CYC_R, CYC_B, CYC_NPOW, CYC_NALS = 6, 10, 16, 40, 10, 10
+
+
+def cycle_inputs(seed=20261203):
+    from mlcp_gb300 import hoplist as H
+    hl = H.henon_heiles(D=CYC_D, n=CYC_N, lam=0.111803)
+    rng = np.random.default_rng(seed)
+    Q = rng.uniform(-0.5, 0.5, size=(CYC_R * CYC_B, CYC_D * CYC_N))
+    qc = np.ones(CYC_R * CYC_B)
+    # shift from harmonic estimates: E ~ 3 + (number of quanta)
+    eig0 = 3.0 + np.sort(np.concatenate([[0], np.ones(6), 2 * np.ones(21), 3 * np.ones(56)]))[:CYC_B]
+    esh = 0.5 * (2 * eig0[-1] - eig0[-2] + (3.0 + 9 * CYC_D))
+    return hl, Q, qc, eig0, esh
+
+
+def run_cycle_bench(steps: int, cpu: bool):
+    """GPU power-cycle time through the C ABI (host buffers in and out, as
+    the Fortran host calls it), the oracle's time for one cycle on the host
+    cores, and the eigenvalue agreement of the two."""
+    from mlcp_gb300 import intertwine as IT
+    hl, Q, qc, eig0, esh = cycle_inputs()
+    IT.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        gb, gc, ge = IT.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
+    gpu_ms = 1e3 * (time.perf_counter() - t0) / steps
+    out = {"workload": f"Henon-Heiles D={CYC_D} n={CYC_N}, rank {CYC_R}, block {CYC_B}, npow={CYC_NPOW}, "
+                       f"nals={CYC_NALS}, update on", "gpu_ms_per_cycle": gpu_ms}
+    if cpu:
+        import oracle
+        oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
+        t0 = time.perf_counter()
+        ob, oc, oe = oracle.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
+        out["cpu_ms_per_cycle"] = 1e3 * (time.perf_counter() - t0)
+        out["cpu_cores"] = os.cpu_count()
+        out["cpu_kind"] = "port"
+        out["max_rel_eig_diff_vs_oracle"] = float(np.max(np.abs(ge - oe) / np.abs(oe)))
+        oracle.set_cycle_penalties()
+    return out
+
+
 def run_gpu(args):
     import torch
     from mlcp_gb300 import _lib, als, workloads
@@ -265,6 +309,8 @@ def run_gpu(args):
                              "kernel": "als_cluster_kernel", "kernel_ms": kernel_ms,
                              "algorithmic_bytes": alg_bytes},
                 "cpu_baseline": cpu, "clocks": clk}
+        if not args.no_cycle and ws == 1:
+            line["power_cycle"] = run_cycle_bench(max(1, min(args.steps, 5)), cpu=not args.no_cpu)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -278,6 +324,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--no-cycle", action="store_true", help="skip the power-cycle measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -92,22 +92,38 @@ namespace {
 
 constexpr int kThreads = kAlsThreads;
 constexpr int kTileRows = 256;  // target terms staged per tile (multiple of 4)
+constexpr int kWtStride = kTileRows + 1;  // odd stride: per-term weight rows on distinct banks
 
 struct Smem {
-  float* ps;      // [rows_cta][rFp] running products
+  float* ps;      // [rFp][rows_cta] running products (term index fastest: conflict-free)
   float* fold;    // [rFp][npmax] FP32 old factor of the mode being solved
   float* fnew;    // [rFp][npmax] FP32 new factor of the mode just solved
-  float* wt;      // [kTileRows][rFp] weights c_j * PS(j,i) of the tile
-  float* gt;      // [kTileRows][npmax] target factors of mode k for the tile
-  float* gp;      // [kTileRows][npmax] target factors of the previous mode for the tile
+  float* wt;      // [rFp][kWtStride] weights c_j * PS(j,i) of the tile
+  float* gt;      // [kTileRows][gstride] target factors of mode k for the tile
+  float* gp;      // [kTileRows][gstride] target factors of the previous mode for the tile
   float* bpart;   // [rFp][npmax] partial right-hand side of this CTA
   float* red;     // [kThreads][16] reduction scratch
   double* BB;     // [rF][rF]
   double* X;      // [rF][npmax] column-major rF x n (ld rF)
   double* L;      // [rF][rF] prefix of F Gram products
   double* misc;   // [4]
+  double* dinv;   // [rF] reciprocal pivots of the LDL^T factor
+  double* u;      // [rF] LDL^T scratch column
   int* flags;     // [4]
 };
+
+// Row stride of staged tiles: an odd number of float4 per row keeps the
+// float4 accesses of consecutive rows on distinct shared-memory banks.
+__host__ __device__ inline int tile_stride(int npmax) { return ((npmax / 4) % 2 == 1) ? npmax : npmax + 4; }
+
+// Quotient a / b from the approximate reciprocal plus one Newton correction
+// (within an ulp or two of the rounded quotient).
+__device__ __forceinline__ float div_nr(float a, float b) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  float q = a * r;
+  return fmaf(fmaf(-b, q, a), r, q);
+}
 
 // <g, f> over NP padded entries; g in registers, f in shared memory.
 template <int NP>
@@ -170,15 +186,17 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
     s.ps = (float*)take(sizeof(float) * (size_t)p.rows_cta_max * rFp);
     s.fold = (float*)take(sizeof(float) * rFp * npmax);
     s.fnew = (float*)take(sizeof(float) * rFp * npmax);
-    s.wt = (float*)take(sizeof(float) * kTileRows * rFp);
-    s.gt = (float*)take(sizeof(float) * kTileRows * npmax);
-    s.gp = (float*)take(sizeof(float) * kTileRows * npmax);
+    s.wt = (float*)take(sizeof(float) * kWtStride * rFp);
+    s.gt = (float*)take(sizeof(float) * kTileRows * tile_stride(npmax));
+    s.gp = (float*)take(sizeof(float) * kTileRows * tile_stride(npmax));
     s.bpart = (float*)take(sizeof(float) * rFp * npmax);
     s.red = (float*)take(sizeof(float) * kThreads * 16);
     s.BB = (double*)take(sizeof(double) * rF * rF);
     s.X = (double*)take(sizeof(double) * rF * npmax);
     s.L = (double*)take(sizeof(double) * rF * rF);
     s.misc = (double*)take(sizeof(double) * 4);
+    s.dinv = (double*)take(sizeof(double) * rF);
+    s.u = (double*)take(sizeof(double) * rF);
     s.flags = (int*)take(sizeof(int) * 4);
   }
 
@@ -191,7 +209,8 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
   double* suf = p.suf + p.sq_off[v];     // [D][rF][rF]
 
   // ---- prologue: running products over all modes, F Grams, penalty ----
-  for (int e = tid; e < nrows * rFp; e += kThreads) s.ps[e] = 1.f;
+  const int psld = p.rows_cta_max;
+  for (int e = tid; e < rFp * psld; e += kThreads) s.ps[e] = 1.f;
   __syncthreads();
   for (int d = 0; d < D; ++d) {
     const int np = round_up(p.nbas[d], 4);
@@ -204,7 +223,7 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
     for (int r = tid; r < nrows; r += kThreads) {
       float g[NP];
       load_row<NP>(g, gmd + (long long)(row0 + r) * np, np);
-      for (int i = 0; i < rF; ++i) s.ps[r * rFp + i] *= dot_reg<NP>(g, s.fold + i * npmax, np);
+      for (int i = 0; i < rF; ++i) s.ps[i * psld + r] *= dot_reg<NP>(g, s.fold + i * npmax, np);
     }
     __syncthreads();
   }
@@ -223,7 +242,7 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
   if (rank == 0 && tid == 0) {
     double pen = fcoef[0];
     for (int i = 1; i < rF; ++i) pen = fcoef[i] > pen ? fcoef[i] : pen;
-    s.misc[0] = pen * 1.0e-10;
+    s.misc[0] = pen * p.pen_factor;
   }
   __threadfence();
   cluster.sync();
@@ -256,6 +275,8 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
     const float* gmk = gm + (long long)p.offp[k] * rG;
     const float* gmp = (kprev >= 0) ? gm + (long long)p.offp[kprev] * rG : nullptr;
 
+    const int gsd = tile_stride(npmax);
+    constexpr int kRowSlots = kTileRows / 4;  // register block = rows {rb, rb+64, rb+128, rb+192}
     for (int tile0 = 0; tile0 < nrows; tile0 += kTileRows) {
       const int tr = min(kTileRows, nrows - tile0);
       // -- stage the tile's factors of modes k and kprev (coalesced float4) --
@@ -263,28 +284,30 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
         const int r = e / (npk / 4), q = (e % (npk / 4)) * 4;
         float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
         if (r < tr) x = *reinterpret_cast<const float4*>(gmk + (long long)(row0 + tile0 + r) * npk + q);
-        *reinterpret_cast<float4*>(s.gt + r * npmax + q) = x;
+        *reinterpret_cast<float4*>(s.gt + r * gsd + q) = x;
       }
       if (kprev >= 0) {
         for (int e = tid; e < kTileRows * (npp / 4); e += kThreads) {
           const int r = e / (npp / 4), q = (e % (npp / 4)) * 4;
           float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
           if (r < tr) x = *reinterpret_cast<const float4*>(gmp + (long long)(row0 + tile0 + r) * npp + q);
-          *reinterpret_cast<float4*>(s.gp + r * npmax + q) = x;
+          *reinterpret_cast<float4*>(s.gp + r * gsd + q) = x;
         }
       }
       __syncthreads();
       // -- running products: fold in the new factor of kprev, divide out mode k.
-      //    Register blocks of 4 terms x 4 F terms. --
-      for (int blk = tid; blk < (kTileRows / 4) * nib; blk += kThreads) {
-        const int rb = blk / nib, ibk = blk % nib;
+      //    Register blocks of 4 terms x 4 F terms; consecutive threads take
+      //    consecutive terms, so shared-memory accesses are conflict-free and
+      //    the F reads of a warp are broadcasts. --
+      for (int blk = tid; blk < kRowSlots * nib; blk += kThreads) {
+        const int rb = blk % kRowSlots, ibk = blk / kRowSlots;
         float po[16], pn[16];
 #pragma unroll
         for (int q = 0; q < 16; ++q) { po[q] = 0.f; pn[q] = 1.f; }
         for (int q = 0; q < npk; q += 4) {
           float4 g[4], f[4];
 #pragma unroll
-          for (int a = 0; a < 4; ++a) g[a] = *reinterpret_cast<const float4*>(s.gt + (rb * 4 + a) * npmax + q);
+          for (int a = 0; a < 4; ++a) g[a] = *reinterpret_cast<const float4*>(s.gt + (rb + a * kRowSlots) * gsd + q);
 #pragma unroll
           for (int c = 0; c < 4; ++c) f[c] = *reinterpret_cast<const float4*>(s.fold + (ibk * 4 + c) * npmax + q);
 #pragma unroll
@@ -305,7 +328,7 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
           for (int q = 0; q < npp; q += 4) {
             float4 g[4], f[4];
 #pragma unroll
-            for (int a = 0; a < 4; ++a) g[a] = *reinterpret_cast<const float4*>(s.gp + (rb * 4 + a) * npmax + q);
+            for (int a = 0; a < 4; ++a) g[a] = *reinterpret_cast<const float4*>(s.gp + (rb + a * kRowSlots) * gsd + q);
 #pragma unroll
             for (int c = 0; c < 4; ++c) f[c] = *reinterpret_cast<const float4*>(s.fnew + (ibk * 4 + c) * npmax + q);
 #pragma unroll
@@ -321,59 +344,66 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
               }
           }
         }
+        // elementwise update; the rare unsafe divisions are rebuilt after the
+        // loop so that the common path stays branch-light
+        unsigned rebuild = 0u;
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-          const int r = tile0 + rb * 4 + a;
-          if (rb * 4 + a >= tr) {
-#pragma unroll
-            for (int c = 0; c < 4; ++c) s.wt[(rb * 4 + a) * rFp + ibk * 4 + c] = 0.f;
-            continue;
-          }
-          const int j = row0 + r;
-          const float cj = gc[j];
+          const int rt = rb + a * kRowSlots;  // row within the tile
+          const bool live = rt < tr;
+          const float cj = live ? gc[row0 + tile0 + rt] : 0.f;
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
             const int i = ibk * 4 + c;
             float psk = 0.f;
-            if (i < rF) {
-              const float tot = s.ps[r * rFp + i] * pn[a * 4 + c];
+            if (live && i < rF) {
+              const float tot = s.ps[i * psld + tile0 + rt] * pn[a * 4 + c];
               const float d = po[a * 4 + c];
               if (d != 0.f && fabsf(tot) >= FLT_MIN && fabsf(tot) <= FLT_MAX) {
-                // quotient from the reciprocal plus one Newton correction
-                const float rc = __frcp_rn(d);
-                float qt = tot * rc;
-                qt = fmaf(fmaf(-d, qt, tot), rc, qt);
-                psk = qt;
+                psk = div_nr(tot, d);
+                s.ps[i * psld + tile0 + rt] = psk;  // holds prod_{d != k} until mode k is solved
               } else {
-                // unsafe division: rebuild prod_{d' != k} <G_j^d', F_i^d'> directly
-                psk = 1.f;
-                for (int dd = 0; dd < D; ++dd) {
-                  if (dd == k) continue;
-                  const int npd = round_up(p.nbas[dd], 4);
-                  psk *= dot_global(gm + (long long)p.offp[dd] * rG + (long long)j * npd,
-                                    f32 + (long long)i * p.nDp + p.offp[dd], npd);
-                }
+                rebuild |= 1u << (a * 4 + c);
               }
-              s.ps[r * rFp + i] = psk;  // holds prod_{d != k} until mode k is solved
             }
-            s.wt[(rb * 4 + a) * rFp + i] = cj * psk;
+            s.wt[i * kWtStride + rt] = cj * psk;
           }
+        }
+        while (rebuild) {
+          // unsafe division: rebuild prod_{d' != k} <G_j^d', F_i^d'> directly
+          const int bit = __ffs(rebuild) - 1;
+          rebuild &= rebuild - 1;
+          const int a = bit / 4, c = bit % 4;
+          const int rt = rb + a * kRowSlots, i = ibk * 4 + c;
+          const int j = row0 + tile0 + rt;
+          float psk = 1.f;
+          for (int dd = 0; dd < D; ++dd) {
+            if (dd == k) continue;
+            const int npd = round_up(p.nbas[dd], 4);
+            psk *= dot_global(gm + (long long)p.offp[dd] * rG + (long long)j * npd,
+                              f32 + (long long)i * p.nDp + p.offp[dd], npd);
+          }
+          s.ps[i * psld + tile0 + rt] = psk;
+          s.wt[i * kWtStride + rt] = gc[j] * psk;
         }
       }
       __syncthreads();
       // -- right-hand-side accumulation: acc(ib*4+a, nb*4+c) += w(r,i) g(r,n) --
       if (acc_active) {
         for (int rr = my_grp; rr < tr; rr += ngroups) {
-          float4 w = *reinterpret_cast<const float4*>(s.wt + rr * rFp + ib * 4);
-          float4 g = *reinterpret_cast<const float4*>(s.gt + rr * npmax + nb * 4);
-          acc[0] = fmaf(w.x, g.x, acc[0]);  acc[1] = fmaf(w.x, g.y, acc[1]);
-          acc[2] = fmaf(w.x, g.z, acc[2]);  acc[3] = fmaf(w.x, g.w, acc[3]);
-          acc[4] = fmaf(w.y, g.x, acc[4]);  acc[5] = fmaf(w.y, g.y, acc[5]);
-          acc[6] = fmaf(w.y, g.z, acc[6]);  acc[7] = fmaf(w.y, g.w, acc[7]);
-          acc[8] = fmaf(w.z, g.x, acc[8]);  acc[9] = fmaf(w.z, g.y, acc[9]);
-          acc[10] = fmaf(w.z, g.z, acc[10]); acc[11] = fmaf(w.z, g.w, acc[11]);
-          acc[12] = fmaf(w.w, g.x, acc[12]); acc[13] = fmaf(w.w, g.y, acc[13]);
-          acc[14] = fmaf(w.w, g.z, acc[14]); acc[15] = fmaf(w.w, g.w, acc[15]);
+          const float w0 = s.wt[(ib * 4 + 0) * kWtStride + rr];
+          const float w1 = s.wt[(ib * 4 + 1) * kWtStride + rr];
+          const float w2 = s.wt[(ib * 4 + 2) * kWtStride + rr];
+          const float w3 = s.wt[(ib * 4 + 3) * kWtStride + rr];
+          const float4 g = *reinterpret_cast<const float4*>(s.gt + rr * gsd + nb * 4);
+          acc[0] = fmaf(w0, g.x, acc[0]);  acc[1] = fmaf(w0, g.y, acc[1]);
+          acc[2] = fmaf(w0, g.z, acc[2]);  acc[3] = fmaf(w0, g.w, acc[3]);
+          acc[4] = fmaf(w1, g.x, acc[4]);  acc[5] = fmaf(w1, g.y, acc[5]);
+          acc[6] = fmaf(w1, g.z, acc[6]);  acc[7] = fmaf(w1, g.w, acc[7]);
+          acc[8] = fmaf(w2, g.x, acc[8]);  acc[9] = fmaf(w2, g.y, acc[9]);
+          acc[10] = fmaf(w2, g.z, acc[10]); acc[11] = fmaf(w2, g.w, acc[11]);
+          acc[12] = fmaf(w3, g.x, acc[12]); acc[13] = fmaf(w3, g.y, acc[13]);
+          acc[14] = fmaf(w3, g.z, acc[14]); acc[15] = fmaf(w3, g.w, acc[15]);
         }
       }
       __syncthreads();
@@ -425,19 +455,13 @@ __global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
         s.BB[e] = bb;
       }
       __syncthreads();
-      block_cholesky(s.BB, rF, rF, &s.flags[0]);
-      block_cholesky_solve(s.BB, rF, rF, s.X, nk, rF);
+      block_ldlt(s.BB, rF, rF, s.dinv, s.u, &s.flags[0]);
+      block_ldlt_solve(s.BB, rF, rF, s.dinv, s.X, nk, rF);
       // normalise each term's new factor (max-scaled 2-norm), write F
       for (int i = tid; i < rF; i += kThreads) {
-        double largest = 0.0;
-        for (int n = 0; n < nk; ++n) largest = fmax(largest, fabs(s.X[i + n * rF]));
-        double nrm = 0.0;
-        for (int n = 0; n < nk; ++n) {
-          const double q = s.X[i + n * rF] / largest;
-          nrm += q * q;
-        }
-        nrm = largest * sqrt(fabs(nrm));
-        for (int n = 0; n < nk; ++n) s.X[i + n * rF] /= nrm;
+        double nrm, inv;
+        scaled_norm(s.X + i, nk, rF, &nrm, &inv);
+        for (int n = 0; n < nk; ++n) s.X[i + n * rF] *= inv;
         fcoef[i] = nrm;
       }
       __syncthreads();
@@ -474,15 +498,17 @@ size_t als_smem_bytes(int rows_cta, int rF, int npmax) {
   take(sizeof(float) * (size_t)rows_cta * rFp);
   take(sizeof(float) * rFp * npmax);
   take(sizeof(float) * rFp * npmax);
-  take(sizeof(float) * kTileRows * rFp);
-  take(sizeof(float) * kTileRows * npmax);
-  take(sizeof(float) * kTileRows * npmax);
+  take(sizeof(float) * kWtStride * rFp);
+  take(sizeof(float) * kTileRows * tile_stride(npmax));
+  take(sizeof(float) * kTileRows * tile_stride(npmax));
   take(sizeof(float) * rFp * npmax);
   take(sizeof(float) * kThreads * 16);
   take(sizeof(double) * rF * rF);
   take(sizeof(double) * rF * npmax);
   take(sizeof(double) * rF * rF);
   take(sizeof(double) * 4);
+  take(sizeof(double) * rF);
+  take(sizeof(double) * rF);
   take(sizeof(int) * 4);
   return b;
 }

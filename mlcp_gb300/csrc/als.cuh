@@ -13,6 +13,7 @@ struct AlsParams {
   int nDp;           // sum of 4-padded basis sizes (FP32 copies)
   int npmax;         // max 4-padded basis size
   int nals;          // sweeps
+  double pen_factor; // penalty = pen_factor * max(F weights) (1e-10 FP64 rule, 1e-5 FP32 rule)
   int rows_cta_max;  // max target terms owned by one CTA
   long long total_rows;     // sum of rG
   long long total_f_terms;  // sum of rF
@@ -60,6 +61,7 @@ struct AlsJob {
   const double* g_coef = nullptr;
   const long long* g_term_off = nullptr; // host [nvec]; null: term_off + rF
   const double* shared_w = nullptr;      // device [nvec][rG]: shared target of vector 0
+  double pen_factor = 1.0e-10;           // reference FP64-build penalty rule
   int* d_status = nullptr;
 };
 

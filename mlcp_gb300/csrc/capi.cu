@@ -221,7 +221,7 @@ int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
 
   // metadata block: ints then long longs (uploaded in one copy)
   const size_t n_int = (size_t)(ndof) + 2 * (ndof + 1) + 2 * nvec;
-  const size_t n_ll = (size_t)7 * nvec;
+  const size_t n_ll = (size_t)6 * nvec;  // term, g_row, f_row, gm, sq, g_term offsets
   const size_t meta_bytes = align256(n_int * sizeof(int)) + n_ll * sizeof(long long);
   // workspace layout
   size_t bytes = 0;
@@ -283,6 +283,7 @@ int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
   prm.nDp = P.nDp;
   prm.npmax = P.npmax;
   prm.nals = nals;
+  prm.pen_factor = job.pen_factor;
   prm.rows_cta_max = P.rows_cta_max;
   prm.total_rows = P.total_rows;
   prm.total_f_terms = P.total_f;
@@ -300,7 +301,7 @@ int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
   prm.coef = d_coef;
   prm.g_base = job.g_base ? job.g_base : d_base;
   prm.g_coef = job.g_coef ? job.g_coef : d_coef;
-  prm.g_term_off = d_ll + 6 * nvec;
+  prm.g_term_off = d_ll + 5 * nvec;
   prm.shared_target = job.shared_w ? 1 : 0;
   prm.shared_w = job.shared_w;
   prm.gm = reinterpret_cast<float*>(w + o_gm);

@@ -34,6 +34,10 @@ int finish_status(int status);
 namespace {
 
 constexpr int kMaxRankCycle = 64;
+// Penalty factors (reference src/als.cu:248-267): the FP32-build rule for the
+// stages whose right-hand sides are FP32 contractions, the FP64-build rule for
+// the FP64 Gram-Schmidt (applied inside gs.cu).
+constexpr double kPenFP32 = 1.0e-5;
 constexpr int kMaxBasisCycle = 64;
 
 uint64_t fnv1a(uint64_t h, const void* data, size_t bytes) {
@@ -228,8 +232,8 @@ __global__ void update_weights_kernel(int B, int R, const double* qcoef, const d
 
 struct CycleBuffers {
   double *q, *qc, *hq, *hqc, *qn, *qnc;
-  float *mscr, *wscr, *zscr, *q32, *pscr;
-  double *g64, *gcoef, *A, *S, *U, *eigv, *gwork, *wts;
+  float *mscr, *wscr, *zscr;
+  double *pscr, *g64, *gcoef, *A, *S, *U, *eigv, *gwork, *wts;
   int *meta, *status;
 };
 
@@ -247,8 +251,7 @@ size_t plan_cycle(const Layout& Ly, const OpTable& t, int R, int B, CycleBuffers
   cb->wscr = (float*)take(sizeof(float) * (size_t)B * t.umax * R * R);
   cb->zscr = (float*)take(sizeof(float) * (size_t)B * t.umax * R * t.npmax);
   cb->g64 = (double*)take(sizeof(double) * (size_t)B * Ly.D * R * R);
-  cb->q32 = (float*)take(sizeof(float) * vec * Ly.nDp);
-  cb->pscr = (float*)take(sizeof(float) * (size_t)B * (Ly.D + 1) * R * R);
+  cb->pscr = (double*)take(sizeof(double) * (size_t)B * (Ly.D + 1) * R * R);
   cb->gcoef = (double*)take(sizeof(double) * B);
   cb->A = (double*)take(sizeof(double) * (size_t)B * B);
   cb->S = (double*)take(sizeof(double) * (size_t)B * B);
@@ -332,6 +335,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
   if (npow > 0) {
     OpAlsParams p;
     p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 0; p.nsweeps = npow; p.ishift = ishift; p.eshift = Eshift;
+    p.pen_factor = kPenFP32;
     p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.q; p.f_coef = cb.qc;
     p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
     if ((rc = opals_launch(p, st))) return rc;
@@ -340,7 +344,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
   if (nals > 0) {
     GsParams g;
     g.D = ndof; g.R = R; g.nbloc = B; g.nD = Ly.nD; g.nDp = Ly.nDp; g.npmax = Ly.npmax; g.nals = nals;
-    g.nbas = d_nbas; g.off = d_off; g.offp = d_offp; g.base = cb.q; g.coef = cb.qc; g.q32 = cb.q32;
+    g.nbas = d_nbas; g.off = d_off; g.offp = d_offp; g.base = cb.q; g.coef = cb.qc;
     g.pscr = cb.pscr; g.g64 = cb.g64; g.gcoef = cb.gcoef; g.status = cb.status + B;
     if ((rc = gs_launch(g, st))) return rc;
   }
@@ -349,6 +353,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
     if (nals > 0) {
       OpAlsParams p;
       p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 1; p.nsweeps = nals; p.ishift = 0; p.eshift = 0.0;
+      p.pen_factor = kPenFP32;
       p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.hq; p.f_coef = cb.hqc;
       p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
       if ((rc = opals_launch(p, st))) return rc;
@@ -376,6 +381,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
       job.term_off = toff.data(); job.d_base = cb.qn; job.d_coef = cb.qnc;
       job.g_base = cb.q; job.g_coef = cb.qc; job.g_term_off = gtoff.data(); job.shared_w = cb.wts;
       job.d_status = cb.status;
+      job.pen_factor = kPenFP32;
       if ((rc = als_run(ctx, job, st))) return rc;
       if ((rc = normalize_coefs_launch(B, R, ndof, Ly.nD, d_nbas, cb.qn, cb.qnc, st))) return rc;
       std::swap(cb.q, cb.qn);

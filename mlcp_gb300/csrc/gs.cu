@@ -5,11 +5,14 @@
 //   F - sum_{k<iv} <Q_k, F> Q_k,
 // where F is its current iterate and the coefficients <Q_k, F> are
 // recomputed at every mode step (gramsumoverrow + sumarray in the reference).
-// The pairwise per-mode overlaps P(k,d) = Q_{k,d} F_d^T (R x R, FP32) are kept
-// and only the mode just solved is refreshed, so a mode step costs
+// The pairwise per-mode overlaps P(k,d) = Q_{k,d} F_d^T (R x R) are kept and
+// only the mode just solved is refreshed, so a mode step costs
 // O(iv R^2 (D + 2n)) instead of rebuilding every product over all modes.
-// Normal equations, weights and norms run in FP64.  The loop over vectors is
-// inherently sequential; the whole orthogonalisation is one launch.
+// Everything here runs in FP64: once power iteration has made the block's
+// vectors nearly parallel, the target F - sum_k <Q_k,F> Q_k is a small
+// difference of large terms, and FP32 contractions lose it to cancellation.
+// The loop over vectors is inherently sequential; the whole orthogonalisation
+// is one launch.
 #include "common.cuh"
 #include "intertwine.cuh"
 
@@ -30,19 +33,12 @@ __global__ void __launch_bounds__(kGsThreads) gs_kernel(GsParams p) {
   double* BB = (double*)take(sizeof(double) * R * R);
   double* cf = (double*)take(sizeof(double) * R);
   double* red = (double*)take(sizeof(double) * nt);
+  double* dinv = (double*)take(sizeof(double) * R);
+  double* ucol = (double*)take(sizeof(double) * R);
   int* flags = (int*)take(sizeof(int) * 4);
 
-  float* psn = p.pscr + (size_t)B * D * R * R;  // [B][R][R] products over d != j
+  double* psn = p.pscr + (size_t)B * D * R * R;  // [B][R][R] products over d != j
 
-  // FP32 copy of the whole block
-  for (size_t e = tid; e < (size_t)B * R * nDp; e += nt) {
-    const size_t row = e / nDp;
-    const int q = (int)(e % nDp);
-    int d = 0;
-    while (d + 1 < D && p.offp[d + 1] <= q) ++d;
-    const int k = q - p.offp[d];
-    p.q32[e] = (k < p.nbas[d]) ? (float)p.base[row * nD + p.off[d] + k] : 0.f;
-  }
   for (int k = tid; k < B; k += nt) p.gcoef[k] = 1.0;
   if (tid == 0) flags[1] = 0;
   __syncthreads();
@@ -86,11 +82,10 @@ __global__ void __launch_bounds__(kGsThreads) gs_kernel(GsParams p) {
   for (int iv = 1; iv < B && p.nals > 0; ++iv) {
     double* fb = p.base + (size_t)iv * R * nD;
     double* fc = p.coef + (size_t)iv * R;
-    float* f32 = p.q32 + (size_t)iv * R * nDp;
     if (tid == 0) {
       double pen = fc[0];
       for (int i = 1; i < R; ++i) pen = fc[i] > pen ? fc[i] : pen;
-      red[0] = pen * 1.0e-10;
+      red[0] = pen * 1.0e-10;  // FP64-build rule: this stage is FP64 throughout
     }
     grams_of(iv);
     // overlaps with every earlier vector, every mode
@@ -98,10 +93,10 @@ __global__ void __launch_bounds__(kGsThreads) gs_kernel(GsParams p) {
       const int k = (int)(e / ((size_t)D * R * R));
       const int rem = (int)(e % ((size_t)D * R * R));
       const int d = rem / (R * R), r = (rem % (R * R)) / R, i = rem % R;
-      const float* a = p.q32 + ((size_t)k * R + r) * nDp + p.offp[d];
-      const float* b = f32 + (size_t)i * nDp + p.offp[d];
-      float acc = 0.f;
-      for (int q = 0; q < p.nbas[d]; ++q) acc = fmaf(a[q], b[q], acc);
+      const double* a = p.base + ((size_t)k * R + r) * nD + p.off[d];
+      const double* b = fb + (size_t)i * nD + p.off[d];
+      double acc = 0.0;
+      for (int q = 0; q < p.nbas[d]; ++q) acc = fma(a[q], b[q], acc);
       p.pscr[((size_t)k * D + d) * R * R + r * R + i] = acc;
     }
     __syncthreads();
@@ -114,7 +109,7 @@ __global__ void __launch_bounds__(kGsThreads) gs_kernel(GsParams p) {
         // products over d != j and the coefficients -<Q_k, F> (one warp per k)
         for (size_t e = tid; e < (size_t)iv * R * R; e += nt) {
           const int k = (int)(e / (R * R)), ee = (int)(e % (R * R));
-          float prod = 1.f;
+          double prod = 1.0;
           for (int d = 0; d < D; ++d)
             if (d != j) prod *= p.pscr[((size_t)k * D + d) * R * R + ee];
           psn[(size_t)k * R * R + ee] = prod;
@@ -125,8 +120,7 @@ __global__ void __launch_bounds__(kGsThreads) gs_kernel(GsParams p) {
           double part = 0.0;
           for (int ee = lane; ee < R * R; ee += 32) {
             const int r = ee / R, i = ee % R;
-            part -= qc[r] * fc[i] * (double)psn[(size_t)k * R * R + ee] *
-                    (double)p.pscr[((size_t)k * D + j) * R * R + ee];
+            part -= qc[r] * fc[i] * psn[(size_t)k * R * R + ee] * p.pscr[((size_t)k * D + j) * R * R + ee];
           }
           for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
           if (lane == 0) p.gcoef[k] = part;
@@ -138,11 +132,11 @@ __global__ void __launch_bounds__(kGsThreads) gs_kernel(GsParams p) {
           double acc = 0.0;
           for (int k = 0; k < iv; ++k) {
             const double* qc = p.coef + (size_t)k * R;
-            float inner = 0.f;
+            double inner = 0.0;
             for (int r = 0; r < R; ++r)
-              inner = fmaf((float)qc[r] * p.q32[((size_t)k * R + r) * nDp + p.offp[j] + m],
-                           psn[(size_t)k * R * R + r * R + i], inner);
-            acc += p.gcoef[k] * (double)inner;
+              inner = fma(qc[r] * p.base[((size_t)k * R + r) * nD + p.off[j] + m], psn[(size_t)k * R * R + r * R + i],
+                          inner);
+            acc += p.gcoef[k] * inner;
           }
           double self = 0.0;
           for (int r = 0; r < R; ++r) {
@@ -161,26 +155,19 @@ __global__ void __launch_bounds__(kGsThreads) gs_kernel(GsParams p) {
           BB[e] = bb;
         }
         __syncthreads();
-        block_cholesky(BB, R, R, &flags[0]);
+        block_ldlt(BB, R, R, dinv, ucol, &flags[0]);
         if (tid == 0 && flags[0]) flags[1] = 1;
-        block_cholesky_solve(BB, R, R, X, nj, R);
+        block_ldlt_solve(BB, R, R, dinv, X, nj, R);
         for (int i = tid; i < R; i += nt) {
-          double largest = 0.0;
-          for (int m = 0; m < nj; ++m) largest = fmax(largest, fabs(X[i + m * R]));
-          double nrm = 0.0;
-          for (int m = 0; m < nj; ++m) {
-            const double q = X[i + m * R] / largest;
-            nrm += q * q;
-          }
-          nrm = largest * sqrt(fabs(nrm));
-          for (int m = 0; m < nj; ++m) X[i + m * R] /= nrm;
+          double nrm, inv;
+          scaled_norm(X + i, nj, R, &nrm, &inv);
+          for (int m = 0; m < nj; ++m) X[i + m * R] *= inv;
           fc[i] = nrm;
         }
         __syncthreads();
         for (int e = tid; e < R * nj; e += nt) {
           const int i = e / nj, m = e % nj;
           fb[(size_t)i * nD + p.off[j] + m] = X[i + m * R];
-          f32[(size_t)i * nDp + p.offp[j] + m] = (float)X[i + m * R];
         }
         __syncthreads();
         // refresh Gram and overlaps of mode j
@@ -192,10 +179,10 @@ __global__ void __launch_bounds__(kGsThreads) gs_kernel(GsParams p) {
         }
         for (size_t e = tid; e < (size_t)iv * R * R; e += nt) {
           const int k = (int)(e / (R * R)), r = (int)(e % (R * R)) / R, i = (int)(e % R);
-          const float* a = p.q32 + ((size_t)k * R + r) * nDp + p.offp[j];
-          const float* b = f32 + (size_t)i * nDp + p.offp[j];
-          float acc = 0.f;
-          for (int q = 0; q < nj; ++q) acc = fmaf(a[q], b[q], acc);
+          const double* a = p.base + ((size_t)k * R + r) * nD + p.off[j];
+          const double* b = fb + (size_t)i * nD + p.off[j];
+          double acc = 0.0;
+          for (int q = 0; q < nj; ++q) acc = fma(a[q], b[q], acc);
           p.pscr[((size_t)k * D + j) * R * R + r * R + i] = acc;
         }
         __syncthreads();
@@ -213,6 +200,8 @@ int gs_launch(const GsParams& p, cudaStream_t st) {
   take(sizeof(double) * p.R * p.R);
   take(sizeof(double) * p.R);
   take(sizeof(double) * kGsThreads);
+  take(sizeof(double) * p.R);
+  take(sizeof(double) * p.R);
   take(sizeof(int) * 4);
   MLCP_CUDA_TRY(cudaFuncSetAttribute(gs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   gs_kernel<<<1, kGsThreads, smem, st>>>(p);

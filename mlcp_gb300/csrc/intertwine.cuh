@@ -36,6 +36,7 @@ struct OpAlsParams {
   int nsweeps;
   int ishift;
   double eshift;
+  double pen_factor;      // penalty = pen_factor * max(Fo weights)
   const double* fo_base;  // Fo vectors (reference layout, rank R each, vector v at v*R terms)
   const double* fo_coef;
   double* f_base;         // F output (may alias fo for POW)
@@ -58,8 +59,7 @@ struct GsParams {
   const int* offp;
   double* base;   // block, in place
   double* coef;
-  float* q32;     // [nbloc][R][nDp] FP32 copy of the block (kept in step)
-  float* pscr;    // [nbloc][D][R][R] P(k,d) = Q_k,d F_d^T
+  double* pscr;   // [nbloc][D+1][R][R] P(k,d) = Q_k,d F_d^T, then products over d != j
   double* g64;    // [D][R][R]
   double* gcoef;  // [nbloc]
   int* status;

@@ -13,7 +13,11 @@
 //   b(i,n) = sum_u sum_r c_r W_u(r,i) (h_u Fo_r^j)(n)
 // so a mode step costs O(T R^2 D) instead of O(T R (sum_d n_d^2 + R nD)).
 // The energy shift enters as an identity term with weight -E; for ishift < 0
-// b changes sign, as in the reference.  The R x R normal equations
+// b changes sign, as in the reference.  Because the right-hand sides carry
+// FP32 rounding, the penalty follows the reference's FP32-build rule
+// (1e-5 max c, src/als.cu:248-267): with the FP64 rule (1e-10) the rounding
+// noise in near-null directions of the normal equations is amplified by up
+// to 1e10 and the CP weights blow up over successive cycles.  The R x R normal equations
 // (prod_{d!=j} F_d F_d^T + pen I), their Cholesky solve, the F Grams and the
 // weight normalisation run in FP64; the operator Grams, term products and
 // right-hand sides run in FP32.
@@ -35,6 +39,8 @@ struct OpSmem {
   double* cf;     // [R] weights of F
   double* cfo;    // [R] weights of Fo
   double* red;    // [kThreads] reduction scratch
+  double* dinv;   // [R] reciprocal pivots
+  double* u;      // [R] LDL^T scratch column
   int* flags;     // [4]
 };
 
@@ -49,6 +55,8 @@ __device__ inline void carve(OpSmem& s, unsigned char* base, const OpTable& t, b
   s.cf = (double*)take(sizeof(double) * t.R);
   s.cfo = (double*)take(sizeof(double) * t.R);
   s.red = (double*)take(sizeof(double) * kThreads);
+  s.dinv = (double*)take(sizeof(double) * t.R);
+  s.u = (double*)take(sizeof(double) * t.R);
   s.flags = (int*)take(sizeof(int) * 4);
 }
 
@@ -134,7 +142,7 @@ __global__ void __launch_bounds__(kThreads) opals_kernel(OpAlsParams p) {
   if (threadIdx.x == 0) {
     double pen = s.cfo[0];
     for (int i = 1; i < R; ++i) pen = s.cfo[i] > pen ? s.cfo[i] : pen;
-    s.red[0] = pen * 1.0e-10;
+    s.red[0] = pen * p.pen_factor;
     s.flags[0] = 0;
     s.flags[1] = 0;
   }
@@ -212,19 +220,13 @@ __global__ void __launch_bounds__(kThreads) opals_kernel(OpAlsParams p) {
         s.BB[e] = bb;
       }
       __syncthreads();
-      block_cholesky(s.BB, R, R, &s.flags[2]);
+      block_ldlt(s.BB, R, R, s.dinv, s.u, &s.flags[2]);
       if (threadIdx.x == 0 && s.flags[2]) s.flags[1] = 1;
-      block_cholesky_solve(s.BB, R, R, s.X, nj, R);
+      block_ldlt_solve(s.BB, R, R, s.dinv, s.X, nj, R);
       for (int i = threadIdx.x; i < R; i += blockDim.x) {
-        double largest = 0.0;
-        for (int m = 0; m < nj; ++m) largest = fmax(largest, fabs(s.X[i + m * R]));
-        double nrm = 0.0;
-        for (int m = 0; m < nj; ++m) {
-          const double q = s.X[i + m * R] / largest;
-          nrm += q * q;
-        }
-        nrm = largest * sqrt(fabs(nrm));
-        for (int m = 0; m < nj; ++m) s.X[i + m * R] /= nrm;
+        double nrm, inv;
+        scaled_norm(s.X + i, nj, R, &nrm, &inv);
+        for (int m = 0; m < nj; ++m) s.X[i + m * R] *= inv;
         s.cf[i] = nrm;
         fc[i] = nrm;
       }
@@ -295,6 +297,8 @@ size_t opals_smem_bytes(const OpTable& t) {
   take(sizeof(double) * t.R);
   take(sizeof(double) * t.R);
   take(sizeof(double) * kThreads);
+  take(sizeof(double) * t.R);
+  take(sizeof(double) * t.R);
   take(sizeof(int) * 4);
   return b;
 }

@@ -60,6 +60,8 @@ def lib() -> ctypes.CDLL:
         L.orc_cp_dot.argtypes = [_D, _D, ctypes.c_int, _D, _D, ctypes.c_int, _I, ctypes.c_int]
         L.orc_als_batched.argtypes = [ctypes.c_int, ctypes.POINTER(_D), ctypes.POINTER(_D), _I, ctypes.c_int,
                                       _I, _I, ctypes.c_int, ctypes.c_int]
+        L.orc_set_penalty_factor.argtypes = [ctypes.c_double]
+        L.orc_set_cycle_penalties.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double]
         L.orc_sygv.restype = ctypes.c_int
         L.orc_sygv.argtypes = [ctypes.c_int, _D, _D, _D, _D]
     return _lib
@@ -169,6 +171,21 @@ def cp_dot(vb, vc, wb, wc, nbas) -> float:
     wc = np.ascontiguousarray(wc, dtype=np.float64)
     nb = np.ascontiguousarray(nbas, dtype=np.int32)
     return lib().orc_cp_dot(_dp(vb), _dp(vc), vc.size, _dp(wb), _dp(wc), wc.size, _ip(nb), len(nb))
+
+
+# Penalty factors of the reference's two builds (src/als.cu:248-267).
+PEN_FP64 = 1.0e-10
+PEN_FP32 = 1.0e-5
+
+
+def set_cycle_penalties(mvp: float = PEN_FP64, gs: float = PEN_FP64, upd: float = PEN_FP64) -> None:
+    """Penalty factors of the cycle's stages (power sweeps and H-applications,
+    Gram-Schmidt, vector updates).  Defaults restore the FP64 rule."""
+    lib().orc_set_cycle_penalties(mvp, gs, upd)
+
+
+def set_penalty_factor(f: float) -> None:
+    lib().orc_set_penalty_factor(f)
 
 
 def sygv(A: np.ndarray, B: np.ndarray):

@@ -144,11 +144,20 @@ static void normalize_coefs(cpv *F, double *BB) {
   for (int r = 0; r < F->nrk; ++r) F->coef[r] /= q;
 }
 
-/* setpenalty (src/als.cu:248): 1e-10 times the largest weight (FP64 build). */
-static double penalty(const double *coef, int n) {
+/* setpenalty (src/als.cu:248): the largest weight times 1e-10 in the FP64
+ * build or 1e-5 in the FP32 build.  The factor is selectable per stage of the
+ * cycle (orc_set_cycle_penalties); every stage defaults to the FP64 rule. */
+static double g_pen_als = 1.0e-10, g_pen_mvp = 1.0e-10, g_pen_gs = 1.0e-10, g_pen_upd = 1.0e-10;
+void orc_set_penalty_factor(double f) { g_pen_als = g_pen_mvp = g_pen_gs = g_pen_upd = f; }
+void orc_set_cycle_penalties(double mvp, double gs, double upd) {
+  g_pen_mvp = mvp;
+  g_pen_gs = gs;
+  g_pen_upd = upd;
+}
+static double penalty_f(const double *coef, int n, double factor) {
   double p = coef[0];
   for (int i = 1; i < n; ++i) p = (coef[i] > p) ? coef[i] : p;
-  return p * 1.0e-10;
+  return p * factor;
 }
 
 /* ------------------------------------------------------------------ */
@@ -345,7 +354,7 @@ static void replace_with_solution(cpv *F, const double *X, int idof) {
 static void iterate_als(cpv *Q, int rk, int nbloc, int nals, work_t *W) {
   if (nals == 0) return;
   cpv F = cp_window(Q, 0, rk);
-  double pen = penalty(F.coef, rk);
+  double pen = penalty_f(F.coef, rk, g_pen_als);
   for (int it = 0; it < nals; ++it)
     for (int j = 0; j < Q->ndof; ++j) {
       int n = Q->nbas[j];
@@ -450,7 +459,7 @@ static void mvp_build(const hoplist *H, const cpv *Fo, cpv *F, cpv *G, work_t *W
 /* POW_ALS (src/intertw_mvp.cu:452): F <- ALS fit of (H - E)F, mode by mode. */
 static void pow_als(const hoplist *H, cpv *F, cpv *G, work_t *W, int npow, int ishift, double Eshift) {
   if (npow == 0) return;
-  double pen = penalty(F->coef, F->nrk);
+  double pen = penalty_f(F->coef, F->nrk, g_pen_mvp);
   for (int it = 0; it < npow; ++it) {
     for (int j = 0; j < F->ndof; ++j) {
       int n = F->nbas[j];
@@ -469,7 +478,7 @@ static void prodhv_als(const hoplist *H, const cpv *Fo, cpv *F, cpv *G, work_t *
   if (nals == 0) return;
   memcpy(F->coef, Fo->coef, sizeof(double) * F->nrk);
   memcpy(F->base, Fo->base, sizeof(double) * (size_t)F->nrk * F->nD);
-  double pen = penalty(Fo->coef, F->nrk);
+  double pen = penalty_f(Fo->coef, F->nrk, g_pen_mvp);
   for (int it = 0; it < nals; ++it)
     for (int j = 0; j < F->ndof; ++j) {
       int n = F->nbas[j];
@@ -558,7 +567,7 @@ void orc_gram_schmidt(double *base, double *coef, const int *nbas, int rk, int n
   normalize_coefs(&F, W.BB);
   for (int iv = 1; iv < nbloc; ++iv) {
     F = cp_window(&Q, iv * rk, rk);
-    double pen = penalty(F.coef, rk);
+    double pen = penalty_f(F.coef, rk, g_pen_gs);
     for (int it = 0; it < nals; ++it)
       for (int j = 0; j < ndof; ++j) {
         int n = nbas[j];
@@ -634,7 +643,7 @@ void orc_vector_updates(double *base, double *coef, const int *nbas, int rk, int
     work_t W;
     work_init(&W, rk, nmax, nbloc);
     cpv F = {rk, ndof, nD, nbas, off, newcoef + (size_t)i * rk, newbase + (size_t)i * rk * nD};
-    double pen = penalty(F.coef, rk);
+    double pen = penalty_f(F.coef, rk, g_pen_upd);
     double *gcoef = (double *)malloc(sizeof(double) * nbloc);
     memcpy(gcoef, U + (size_t)i * nbloc, sizeof(double) * nbloc);
     for (int it = 0; it < nals; ++it)

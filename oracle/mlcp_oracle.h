@@ -67,6 +67,14 @@ double orc_cp_dot(const double *vb, const double *vc, int rv, const double *wb, 
 void orc_als_batched(int nvec, double *const *coef, double *const *base, const int *nbas, int ndof,
                      const int *rF, const int *rG, int nals, int nthreads);
 
+/* Penalty factor of the normal equations: 1e-10 (reference FP64 build,
+ * default) or 1e-5 (reference FP32 build, src/als.cu:248-267).
+ * orc_set_penalty_factor sets every stage; orc_set_cycle_penalties sets the
+ * power sweeps and H-applications, the Gram-Schmidt and the vector updates of
+ * the intertwined cycle separately. */
+void orc_set_penalty_factor(double f);
+void orc_set_cycle_penalties(double mvp, double gs, double upd);
+
 /* Generalised symmetric eigenproblem A x = lambda B x (lower triangles of
  * column-major A, B used).  Eigenvalues ascending; X column-major with
  * X^T B X = I and the largest-magnitude entry of each column positive. */
