@@ -87,6 +87,21 @@ MLCP_API int mlcp_als_batched(int nvec, int ndof, const int *nbas, const int *rF
 MLCP_API int mlcp_als_batched_host(int nvec, int ndof, const int *nbas, const int *rF, const int *rG,
                           const long long *term_off, double *h_coef, double *h_base, int nals, void *stream);
 
+/* Allocation-free explicit-G ALS (no counterpart in the reference): the
+ * alscpp_ reduction of one vector held in caller-provided DEVICE buffers
+ * (d_coef/d_base in the reference layout: rF F terms, then rG target terms;
+ * the F terms are overwritten).  For callers that cannot allocate device
+ * memory at call time (inside stream capture, under an allocator that owns the
+ * device, in latency-critical loops): all scratch comes from a fixed 32 MiB
+ * array inside the library, held by every GPU that loads it.  The first call
+ * on a device looks up that array's address and must come before any stream
+ * capture.  Calls share the array: calls whose work overlaps on the GPU race.
+ * Sizes whose scratch exceeds the array return an error.  Enqueued on stream
+ * (NULL: the legacy default stream); d_status (optional, device int) receives
+ * bit 0 when a normal-equation matrix was not positive definite. */
+MLCP_API int mlcp_als_noalloc(int ndof, const int *nbas, int rF, int rG, double *d_coef, double *d_base, int nals,
+                              int *d_status, void *stream);
+
 /* Kernel timing (extension).  When enabled, the library records CUDA events
  * around its dominant kernel of each call on the call's stream;
  * mlcp_gb300_last_kernel_ms() synchronises on the end event and returns the
