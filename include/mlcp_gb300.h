@@ -78,7 +78,9 @@ MLCP_API int mlcp_gb300_last_status(void);
  * Host arrays: nbas[ndof], rF, rG, term_off [nvec].  stream: a cudaStream_t
  * (NULL = the library's own stream).  Returns 0 or an error code; per-vector
  * numerical flags go to d_status[nvec] when non-NULL (bit 0: a normal-equation
- * matrix was not positive definite).  Limits: rF <= 64, nbas[d] <= 64. */
+ * matrix was not positive definite; bit 1: an internal pipeline wait timed out
+ * and the vector's result is not valid).  Limits: ndof >= 2, rF <= 64,
+ * nbas[d] <= 64. */
 MLCP_API int mlcp_als_batched(int nvec, int ndof, const int *nbas, const int *rF, const int *rG, const long long *term_off,
                      double *d_coef, double *d_base, int nals, int *d_status, void *stream);
 
@@ -98,7 +100,8 @@ MLCP_API int mlcp_als_batched_host(int nvec, int ndof, const int *nbas, const in
  * capture.  Calls share the array: calls whose work overlaps on the GPU race.
  * Sizes whose scratch exceeds the array return an error.  Enqueued on stream
  * (NULL: the legacy default stream); d_status (optional, device int) receives
- * bit 0 when a normal-equation matrix was not positive definite. */
+ * bit 0 when a normal-equation matrix was not positive definite and bit 1
+ * when an internal pipeline wait timed out (result not valid). */
 MLCP_API int mlcp_als_noalloc(int ndof, const int *nbas, int rF, int rG, double *d_coef, double *d_base, int nals,
                               int *d_status, void *stream);
 

@@ -7,538 +7,930 @@
 //     BB(i,i') = prod_{d!=k} <F_i^d, F_i'^d> + pen delta(i,i'),  pen = 1e-10 max cF
 //     X = BB^-1 b;  F_i^k = X(i,:) / ||X(i,:)||,  cF_i = ||X(i,:)||
 //
-// GB300 design (one persistent thread-block cluster per vector):
-//  * The target G is converted once to an FP32 mode-major copy, so the slice
-//    of mode k for a range of terms is one contiguous run of memory.
-//  * Each CTA of the cluster owns a contiguous range of target terms j and
-//    keeps, per term and per F term i, the running product
-//    PS(j,i) = prod_d <G_j^d, F_i^d> in shared memory.  A mode step divides
-//    the old mode-k factor out and, after the solve, multiplies the new one in,
-//    so each mode step streams only the mode-k slice of G (the reference
-//    rebuilds the full product over all modes at every step).  Entries whose
-//    division is unsafe (zero divisor, subnormal product) are rebuilt from
-//    the factors directly.
-//  * The products and contractions run in FP32 with FP32 accumulation; the
-//    per-step R x R normal equations, their regularisation, the F Gram
-//    products and the normalisation run in FP64 on the cluster's rank-0 CTA.
-//  * Partial right-hand sides are reduced through distributed shared memory
-//    and the new factor is broadcast back the same way; one cluster barrier
-//    pair per mode step, no host round trip, one launch for all sweeps.
+// GB300 design: one persistent thread-block cluster per vector, 16 warps per
+// CTA, each CTA owning a contiguous range of target terms j.
+//  * State.  Each CTA keeps in shared memory, for its terms j and every F term
+//    i, the running product P(j,i) = prod over all modes but one of
+//    <G_j^d, F_i^d> (FP32).  Mode step t solves mode k = t mod D; kp and kn
+//    are the modes before and after it.
+//  * Phase B (critical path, all 16 warps): P(j,i) holds the product without
+//    modes kp and k; multiply in <G_j^kp, Fnew_i^kp> with the factor solved in
+//    the previous step, and accumulate b(i,n) += cG_j P(j,i) G_j^k(n).  The
+//    partial b of the CTA goes to distributed shared memory.
+//  * One cluster barrier.  Every CTA then gathers the partial right-hand sides
+//    in the same order and runs the same R x R solve (warps 0-3), so each CTA
+//    holds the identical new factor and nothing is broadcast back.
+//  * Phase A (warps 4-15, concurrent with the solve): divide mode kn out of
+//    P, <G_j^kn, F_i^kn> with the current factor, so that the next phase B
+//    only has to multiply mode k back in.  Unsafe divisions (zero divisor,
+//    product outside the normal FP32 range) are rebuilt from the factors.
+//  * Target factors live in an FP32 mode-major copy, so the slice of one mode
+//    for a CTA's terms is one contiguous run; tiles of 128 terms stream into a
+//    ring of shared-memory stages with cp.async.bulk and mbarrier completion.
+//  * The R x R normal equations, the F Gram products and the normalisation run
+//    in double-word arithmetic (dword.cuh) on the FP32 pipes.
+// One launch covers all sweeps; the host is not involved between steps.
 
 #include <cooperative_groups.h>
 #include <cfloat>
+#include <cstdint>
 
 #include "common.cuh"
 #include "als.cuh"
+#include "dword.cuh"
 
 namespace cg = cooperative_groups;
 
 namespace mlcp {
 
 // ---------------------------------------------------------------------------
-// Preparation: FP32 mode-major target, FP32 copy of F, FP32 target weights.
+// Preparation: FP32 mode-major target copy, FP32 weights, unit-normalised
+// double-word copy of F.
 // ---------------------------------------------------------------------------
 
-// One thread per (vector, target term, mode) element run; grid-stride.
+// Vector owning row `row` of a prefix-sum table (binary search).
+__device__ inline int owner(const long long* row_off, int nvec, long long row) {
+  int lo = 0, hi = nvec - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (row_off[mid] <= row) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// One thread per (term, mode) element run; grid-stride.
 __global__ void als_prep_kernel(AlsParams p) {
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  // target factors: one element run per (target term, mode); with a shared
-  // target only vector 0's terms are converted (gm_off is 0 for every vector)
+  // target factors; with a shared target only vector 0's terms are converted
   const long long grows = p.shared_target ? (long long)p.rG[0] : p.total_rows;
   for (long long e = tid; e < grows * p.ndof; e += stride) {
     const long long row = e / p.ndof;
     const int d = (int)(e % p.ndof);
-    // locate vector: binary search over row offsets
-    int lo = 0, hi = p.nvec - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (p.g_row_off[mid] <= row) lo = mid; else hi = mid - 1;
-    }
-    const int v = p.shared_target ? 0 : lo;
+    const int v = p.shared_target ? 0 : owner(p.g_row_off, p.nvec, row);
     const int j = (int)(row - p.g_row_off[v]);
     const int rG = p.rG[v];
-    const int n = p.nbas[d], np = round_up(n, 4);
+    const int n = p.nbas[d], gs = als_gstride(n);
     const double* src = p.g_base + (p.g_term_off[v] + j) * (long long)p.nD + p.off[d];
-    float* dst = p.gm + p.gm_off[v] + (long long)p.offp[d] * rG + (long long)j * np;
-    for (int i = 0; i < np; ++i) dst[i] = (i < n) ? (float)src[i] : 0.f;
+    float* dst = p.gm + p.gm_off[v] + (long long)p.offg[d] * rG + (long long)j * gs;
+    for (int q = 0; q < gs; ++q) dst[q] = (q < n) ? (float)src[q] : 0.f;
     if (d == 0 && !p.shared_target) p.gc[p.g_row_off[v] + j] = (float)p.g_coef[p.g_term_off[v] + j];
   }
   if (p.shared_target)
     for (long long e = tid; e < p.total_rows; e += stride) p.gc[e] = (float)p.shared_w[e];
-  // FP32 copy of F
+  // F: each factor scaled to unit 2-norm (a zero factor stays zero), split
+  // into FP32 high and low parts.  Scaling F's factors only rescales the rows
+  // and columns of the normal equations and the rows of b; the normalised
+  // solution is unchanged, and the products stay inside the FP32 exponent
+  // range for any factor norms the FP64 reference handles.
   for (long long e = tid; e < p.total_f_terms * p.ndof; e += stride) {
     const long long frow = e / p.ndof;
     const int d = (int)(e % p.ndof);
-    int lo = 0, hi = p.nvec - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (p.f_row_off[mid] <= frow) lo = mid; else hi = mid - 1;
-    }
-    const int v = lo;
+    const int v = owner(p.f_row_off, p.nvec, frow);
     const int i = (int)(frow - p.f_row_off[v]);
     const int n = p.nbas[d], np = round_up(n, 4);
     const double* src = p.base + (p.term_off[v] + i) * (long long)p.nD + p.off[d];
-    float* dst = p.f32 + (p.f_row_off[v] + i) * (long long)p.nDp + p.offp[d];
-    for (int q = 0; q < np; ++q) dst[q] = (q < n) ? (float)src[q] : 0.f;
+    double ss = 0.0;
+    for (int q = 0; q < n; ++q) ss += src[q] * src[q];
+    const double sc = (ss > 0.0) ? 1.0 / sqrt(ss) : 1.0;
+    float* hi = p.f32 + frow * p.nDp + p.offp[d];
+    float* lo = p.f32lo + frow * p.nDp + p.offp[d];
+    for (int q = 0; q < np; ++q) {
+      const double x = (q < n) ? src[q] * sc : 0.0;
+      const float h = (float)x;
+      hi[q] = h;
+      lo[q] = (float)(x - (double)h);
+    }
   }
 }
+
+// ---------------------------------------------------------------------------
+// Bulk-copy ring primitives (cp.async.bulk + mbarrier, inline PTX)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+__device__ __forceinline__ uint32_t smem_addr(const void* ptr) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(ptr));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Global -> shared bulk copy completing on `bar` (addresses 16-byte aligned,
+// size a multiple of 16).
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+// Barrier among the solver warps only (named barrier 1).
+__device__ __forceinline__ void solver_sync() {
+  asm volatile("bar.sync 1, %0;" ::"r"(kAlsSolverWarps * 32) : "memory");
+}
+
+// Iterations of mbarrier.try_wait (each suspends the thread for a bounded
+// hardware interval) before a stage wait is declared failed.
+constexpr int kWaitLimit = 1 << 20;
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Shared-memory carve (host and device agree on it)
+// ---------------------------------------------------------------------------
+
+struct AlsSmem {
+  int rFp, ldP, stage_floats;
+  size_t bar, done, issued, fillno, flags, ring, P, cw, fa, fb, bred, bpart, BB, X, L, sk, dinv, u, nrm, misc, total;
+};
+
+__host__ __device__ inline size_t carve(size_t* cursor, size_t bytes, size_t align) {
+  const size_t o = (*cursor + align - 1) / align * align;
+  *cursor = o + bytes;
+  return o;
+}
+
+__host__ __device__ inline AlsSmem als_smem_layout(int rows_cta, int rF, int npmax, int gsmax, int stages) {
+  AlsSmem s;
+  s.rFp = round_up(rF, 4);
+  s.ldP = round_up(rows_cta > 0 ? rows_cta : 1, 32);
+  s.stage_floats = kAlsTileRows * 2 * gsmax;
+  size_t o = 0;
+  s.bar = carve(&o, 8 * (size_t)stages, 16);
+  s.done = carve(&o, 4 * (size_t)stages, 16);
+  s.issued = carve(&o, 4 * (size_t)stages, 16);
+  s.fillno = carve(&o, 4 * (size_t)stages, 16);
+  s.flags = carve(&o, 4 * 8, 16);
+  s.ring = carve(&o, sizeof(float) * (size_t)stages * s.stage_floats, 128);
+  s.P = carve(&o, sizeof(float) * (size_t)s.rFp * s.ldP, 16);
+  s.cw = carve(&o, sizeof(float) * (size_t)s.ldP, 16);
+  s.fa = carve(&o, sizeof(float) * (size_t)s.rFp * gsmax, 16);
+  s.fb = carve(&o, sizeof(float) * (size_t)s.rFp * gsmax, 16);
+  s.bred = carve(&o, sizeof(float) * kAlsWarps * 64, 16);
+  s.bpart = carve(&o, sizeof(float) * 2 * (size_t)s.rFp * npmax, 16);
+  s.BB = carve(&o, sizeof(dw) * (size_t)rF * rF, 16);
+  s.X = carve(&o, sizeof(dw) * (size_t)rF * npmax, 16);
+  s.L = carve(&o, sizeof(dw) * (size_t)rF * rF, 16);
+  s.sk = carve(&o, sizeof(dw) * (size_t)rF * rF, 16);
+  s.dinv = carve(&o, sizeof(dw) * (size_t)rF, 16);
+  s.u = carve(&o, sizeof(dw) * (size_t)rF, 16);
+  s.nrm = carve(&o, sizeof(dw) * (size_t)rF, 16);
+  s.misc = carve(&o, sizeof(dw) * 4, 16);
+  s.total = o;
+  return s;
+}
+
+namespace {
+
+// Per-thread view of one CTA's part of the reduction.
+struct Cta {
+  int tid, warp, lane, rank, CL, v, D, rF, rFp, nIq, rG, row0, nrows, ntiles, ldP, gsmax, npmax, nDp, stages,
+      stage_floats;
+  uint64_t* bar;
+  int* done;
+  int* issued;
+  unsigned* fillno;  // [stages] tile sequence number the stage was last armed with
+  int* flags;  // [0] pipeline abort, [1] non-positive pivot seen
+  float* ring;
+  float* P;    // [rFp][ldP] running products (term index fastest)
+  float* cw;   // [ldP] target weights of the CTA's terms
+  float* fa;   // [rFp][gsmax] factor divided out in phase A / multiplied in the prologue
+  float* fb;   // [rFp][gsmax] factor multiplied in by phase B (solved in the previous step)
+  float* bred; // [warps][64] per-warp partial right-hand sides
+  float* bpart;  // [2][rFp][npmax] CTA partial right-hand side (read by the cluster)
+  dw *BB, *X, *L, *sk, *dinv, *u, *nrm, *misc;
+  const float* gm;  // this vector's FP32 target copy
+  float* fcta;      // this CTA's FP32 factor copy [rF][nDp]
+  dw* gram;         // this CTA's Grams [D][rF][rF]
+  dw* suf;          // this CTA's suffix products [D][rF][rF]
+};
+
+// Tile source: one or two mode slabs of the CTA's target terms.
+struct TileSrc {
+  const float* a;
+  int gsa;
+  const float* b;
+  int gsb;
+};
+
+__device__ void issue_tile(const Cta& c, unsigned g, int T, const TileSrc& s) {
+  const int st = (int)(g % (unsigned)c.stages);
+  const int r0 = T * kAlsTileRows;
+  const int rows = min(kAlsTileRows, c.nrows - r0);
+  float* dst = c.ring + (size_t)st * c.stage_floats;
+  const uint32_t ba = (uint32_t)(rows * s.gsa * 4);
+  const uint32_t bb = s.b ? (uint32_t)(rows * s.gsb * 4) : 0u;
+  c.issued[st] += 1;
+  *(volatile unsigned*)&c.fillno[st] = g;
+  fence_async_shared();
+  mbar_expect_tx(&c.bar[st], ba + bb);
+  bulk_load(dst, s.a + (long long)(c.row0 + r0) * s.gsa, ba, &c.bar[st]);
+  if (s.b) bulk_load(dst + kAlsTileRows * s.gsa, s.b + (long long)(c.row0 + r0) * s.gsb, bb, &c.bar[st]);
+}
+
+// First tiles of a phase (one thread; the ring is idle).
+__device__ void start_phase(const Cta& c, unsigned seq, const TileSrc& s) {
+  for (int T = 0; T < c.ntiles && T < c.stages; ++T) issue_tile(c, seq + T, T, s);
+}
+
+// Wait until tile g has landed (every lane of the warp calls it).  The
+// stage's phase parity alone cannot tell fill g from fill g - 2*stages, and a
+// warp whose items skip tiles can reach fill g while the stage still holds
+// an older one; so the stage must first be armed with g (fillno), after which
+// every earlier fill of the stage has completed and the parity is unambiguous.
+__device__ bool wait_tile(const Cta& c, unsigned g) {
+  const int st = (int)(g % (unsigned)c.stages);
+  const uint32_t par = (g / (unsigned)c.stages) & 1u;
+  volatile int* abort_flag = c.flags;
+  volatile unsigned* armed = c.fillno + st;
+  for (int it = 0; it < kWaitLimit; ++it) {
+    if (*armed == g && mbar_try_wait(&c.bar[st], par)) return true;
+    if (*abort_flag) return false;
+  }
+  atomicExch(c.flags, 1);
+  return false;
+}
+
+// The warp is done with tile g (index T in its phase); the last of the
+// tile's `consumers` warps refills the stage with tile T + stages.
+__device__ void release_tile(const Cta& c, unsigned g, int T, int consumers, const TileSrc& s) {
+  __syncwarp();
+  if (c.lane == 0) {
+    const int st = (int)(g % (unsigned)c.stages);
+    __threadfence_block();
+    const int old = atomicAdd(&c.done[st], 1);
+    if (old == consumers - 1) {
+      c.done[st] = 0;
+      if (T + c.stages < c.ntiles && !*(volatile int*)c.flags) issue_tile(c, g + c.stages, T + c.stages, s);
+    }
+  }
+  __syncwarp();
+}
+
+// Quotient a / b from the approximate reciprocal plus one Newton correction.
+__device__ __forceinline__ float div_nr(float a, float b) {
+  const float r = f_rcp_approx(b);
+  const float q = a * r;
+  return fmaf(fmaf(-b, q, a), r, q);
+}
+
+// out[a][cc] = <G_row, F_{cc}> for the lane's four rows lane + 32a of a tile
+// (row stride gs) and four factors f + cc*fld, over np padded entries.  Phase
+// A, phase B and the prologue all use this routine, so a factor divided out
+// of P is bit-identical to the one multiplied in earlier.
+__device__ __forceinline__ void tile_dots(const float* tile, int gs, const float* f, int fld, int np, int lane,
+                                          float (&out)[4][4]) {
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) out[a][cc] = 0.f;
+  for (int q = 0; q < np; q += 4) {
+    float4 g[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) g[a] = *reinterpret_cast<const float4*>(tile + (lane + 32 * a) * gs + q);
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+      const float4 x = *reinterpret_cast<const float4*>(f + cc * fld + q);
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        float s = out[a][cc];
+        s = fmaf(g[a].x, x.x, s);
+        s = fmaf(g[a].y, x.y, s);
+        s = fmaf(g[a].z, x.z, s);
+        s = fmaf(g[a].w, x.w, s);
+        out[a][cc] = s;
+      }
+    }
+  }
+}
+
+// prod over modes d not in {ex1, ex2} of <G_j^d, F_i^d>, straight from the
+// FP32 copies in global memory (unsafe-division fallback; rare).
+__device__ float rebuild_product(const Cta& c, const AlsParams& p, int j, int i, int ex1, int ex2) {
+  float s = 1.f;
+  for (int d = 0; d < c.D; ++d) {
+    if (d == ex1 || d == ex2) continue;
+    const int n = p.nbas[d], gs = als_gstride(n);
+    const float* g = c.gm + (long long)p.offg[d] * c.rG + (long long)(c.row0 + j) * gs;
+    const float* f = c.fcta + (long long)i * c.nDp + p.offp[d];
+    float t = 0.f;
+    for (int q = 0; q < n; ++q) t = fmaf(g[q], f[q], t);
+    s *= t;
+  }
+  return s;
+}
+
+// Stage the current FP32 factor of mode d from this CTA's copy into dst
+// ([rFp][gsmax], zero rows beyond rF).  Threads [t0, t0 + nt) take part.
+__device__ void load_factor(const Cta& c, const AlsParams& p, int d, float* dst, int t0, int nt) {
+  const int np = round_up(p.nbas[d], 4);
+  for (int e = c.tid - t0; e < c.rFp * np; e += nt) {
+    const int i = e / np, q = e - i * np;
+    dst[i * c.gsmax + q] = (i < c.rF) ? c.fcta[(long long)i * c.nDp + p.offp[d] + q] : 0.f;
+  }
+}
+
+// Product pass over the tiles of mode d, items (tile, i-quad) dealt
+// round-robin to warps [w0, w0 + nw):
+//   divide = false: P(j,i) *= <G_j^d, F_i^d>            (prologue)
+//   divide = true:  P(j,i) /= <G_j^d, F_i^d>, rebuilding prod_{d' not in
+//                   {ex, d}} when the division is unsafe  (phase A)
+// fa holds F^d.  One thread of the group must call start_phase first.
+__device__ void product_pass(const Cta& c, const AlsParams& p, unsigned seq, int d, bool divide, int ex, int w0,
+                             int nw) {
+  const int n = p.nbas[d], np = round_up(n, 4), gs = als_gstride(n);
+  const TileSrc src{c.gm + (long long)p.offg[d] * c.rG, gs, nullptr, 0};
+  const int nitems = c.ntiles * c.nIq;
+  for (int it = c.warp - w0; it < nitems; it += nw) {
+    const int T = it / c.nIq, iq = it - T * c.nIq;
+    const unsigned g = seq + (unsigned)T;
+    if (wait_tile(c, g)) {
+      const float* tile = c.ring + (size_t)(g % (unsigned)c.stages) * c.stage_floats;
+      float po[4][4];
+      tile_dots(tile, gs, c.fa + iq * 4 * c.gsmax, c.gsmax, np, c.lane, po);
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const int j = T * kAlsTileRows + c.lane + 32 * a;
+        if (j >= c.nrows) continue;
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+          const int i = iq * 4 + cc;
+          if (i >= c.rF) continue;
+          float* st = c.P + (size_t)i * c.ldP + j;
+          if (!divide) {
+            *st *= po[a][cc];
+          } else {
+            const float pv = *st, dv = po[a][cc];
+            float qv = 0.f;
+            bool ok = dv != 0.f && fabsf(pv) >= FLT_MIN && fabsf(pv) <= FLT_MAX;
+            if (ok) {
+              qv = div_nr(pv, dv);
+              ok = fabsf(qv) <= FLT_MAX;
+            }
+            if (!ok) qv = rebuild_product(c, p, j, i, ex, d);
+            *st = qv;
+          }
+        }
+      }
+    }
+    release_tile(c, g, T, c.nIq, src);
+  }
+}
+
+// Phase B, first right-hand-side columns [0, MW) (round 0): P(j,i) *= <G_j^kp,
+// Fnew_i^kp>, then acc(i,m) += cG_j P(j,i) G_j^k(m) for the warp's i-quad.
+template <int MW>
+__device__ __forceinline__ void item_b0(const Cta& c, const float* tp, int gsp, int npp, const float* tk, int gsk,
+                                        int T, int iq, float (&acc)[4][MW]) {
+  float pn[4][4];
+  tile_dots(tp, gsp, c.fb + iq * 4 * c.gsmax, c.gsmax, npp, c.lane, pn);
+  float w[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int j = T * kAlsTileRows + c.lane + 32 * a;
+    const bool live = j < c.nrows;
+    const float cwj = live ? c.cw[j] : 0.f;
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+      float* st = c.P + (size_t)(iq * 4 + cc) * c.ldP + j;
+      const float pv = live ? *st * pn[a][cc] : 0.f;
+      if (live) *st = pv;
+      w[a][cc] = cwj * pv;
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    float4 g4[MW / 4];
+#pragma unroll
+    for (int m4 = 0; m4 < MW / 4; ++m4)
+      g4[m4] = *reinterpret_cast<const float4*>(tk + (c.lane + 32 * a) * gsk + 4 * m4);
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {
+      const float wv = w[a][cc];
+#pragma unroll
+      for (int m4 = 0; m4 < MW / 4; ++m4) {
+        acc[cc][4 * m4 + 0] = fmaf(wv, g4[m4].x, acc[cc][4 * m4 + 0]);
+        acc[cc][4 * m4 + 1] = fmaf(wv, g4[m4].y, acc[cc][4 * m4 + 1]);
+        acc[cc][4 * m4 + 2] = fmaf(wv, g4[m4].z, acc[cc][4 * m4 + 2]);
+        acc[cc][4 * m4 + 3] = fmaf(wv, g4[m4].w, acc[cc][4 * m4 + 3]);
+      }
+    }
+  }
+}
+
+// Phase B, later right-hand-side columns [m0, m0 + MW): P is already updated.
+template <int MW>
+__device__ __forceinline__ void item_bm(const Cta& c, const float* tk, int gsk, int m0, int T, int iq,
+                                        float (&acc)[4][MW]) {
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int j = T * kAlsTileRows + c.lane + 32 * a;
+    const bool live = j < c.nrows;
+    const float cwj = live ? c.cw[j] : 0.f;
+    float w[4];
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) w[cc] = live ? cwj * c.P[(size_t)(iq * 4 + cc) * c.ldP + j] : 0.f;
+    float4 g4[MW / 4];
+#pragma unroll
+    for (int m4 = 0; m4 < MW / 4; ++m4)
+      g4[m4] = *reinterpret_cast<const float4*>(tk + (c.lane + 32 * a) * gsk + m0 + 4 * m4);
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc)
+#pragma unroll
+      for (int m4 = 0; m4 < MW / 4; ++m4) {
+        acc[cc][4 * m4 + 0] = fmaf(w[cc], g4[m4].x, acc[cc][4 * m4 + 0]);
+        acc[cc][4 * m4 + 1] = fmaf(w[cc], g4[m4].y, acc[cc][4 * m4 + 1]);
+        acc[cc][4 * m4 + 2] = fmaf(w[cc], g4[m4].z, acc[cc][4 * m4 + 2]);
+        acc[cc][4 * m4 + 3] = fmaf(w[cc], g4[m4].w, acc[cc][4 * m4 + 3]);
+      }
+  }
+}
+
+// One round of phase B over all tiles (all 16 warps; warp -> i-quad iq =
+// warp mod nIq, tiles T = warp / nIq (mod warps per i-quad)), ending with the
+// CTA's partial right-hand side columns [16 round, 16 round + MW) in bout.
+template <int MW>
+__device__ void phase_b_round(const Cta& c, const AlsParams& p, unsigned seq, int round, int k, int kp, float* bout) {
+  const int nk = p.nbas[k], gsk = als_gstride(nk);
+  const int npp = round_up(p.nbas[kp], 4), gsp = als_gstride(p.nbas[kp]);
+  const float* slab_k = c.gm + (long long)p.offg[k] * c.rG;
+  const float* slab_p = c.gm + (long long)p.offg[kp] * c.rG;
+  const TileSrc src = (round == 0) ? TileSrc{slab_p, gsp, slab_k, gsk} : TileSrc{slab_k, gsk, nullptr, 0};
+  const int wpi = kAlsWarps / c.nIq;
+  const bool active = c.warp < wpi * c.nIq;
+  const int iq = c.warp % c.nIq, sub = c.warp / c.nIq;
+  if (c.tid == 0) start_phase(c, seq, src);
+  float acc[4][MW];
+#pragma unroll
+  for (int cc = 0; cc < 4; ++cc)
+#pragma unroll
+    for (int m = 0; m < MW; ++m) acc[cc][m] = 0.f;
+  if (active) {
+    for (int T = sub; T < c.ntiles; T += wpi) {
+      const unsigned g = seq + (unsigned)T;
+      if (wait_tile(c, g)) {
+        const float* tile = c.ring + (size_t)(g % (unsigned)c.stages) * c.stage_floats;
+        if (round == 0)
+          item_b0<MW>(c, tile, gsp, npp, tile + kAlsTileRows * gsp, gsk, T, iq, acc);
+        else
+          item_bm<MW>(c, tile, gsk, 16 * round, T, iq, acc);
+      }
+      release_tile(c, g, T, c.nIq, src);
+    }
+    // sum over the warp's lanes
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc)
+#pragma unroll
+      for (int m = 0; m < MW; ++m) {
+        float s = acc[cc][m];
+        s += __shfl_xor_sync(0xffffffffu, s, 16);
+        s += __shfl_xor_sync(0xffffffffu, s, 8);
+        s += __shfl_xor_sync(0xffffffffu, s, 4);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        if (c.lane == 0) c.bred[c.warp * 64 + cc * MW + m] = s;
+      }
+  }
+  __syncthreads();
+  // sum over the warps of each i-quad (fixed order)
+  for (int e = c.tid; e < c.nIq * 4 * MW; e += kAlsThreads) {
+    const int q4 = e / (4 * MW), r = e - q4 * 4 * MW, cc = r / MW, m = r - cc * MW;
+    float s = 0.f;
+    for (int sb = 0; sb < wpi; ++sb) s += c.bred[(q4 + sb * c.nIq) * 64 + cc * MW + m];
+    bout[(q4 * 4 + cc) * c.npmax + 16 * round + m] = s;
+  }
+  __syncthreads();
+}
+
+// All rounds of phase B for mode k (previous mode kp); returns tiles used.
+__device__ unsigned phase_b(const Cta& c, const AlsParams& p, unsigned seq, int k, int kp, float* bout) {
+  const int npk = round_up(p.nbas[k], 4);
+  unsigned used = 0;
+  for (int round = 0; 16 * round < npk; ++round) {
+    const int mw = min(16, npk - 16 * round);
+    switch (mw) {
+      case 4: phase_b_round<4>(c, p, seq + used, round, k, kp, bout); break;
+      case 8: phase_b_round<8>(c, p, seq + used, round, k, kp, bout); break;
+      case 12: phase_b_round<12>(c, p, seq + used, round, k, kp, bout); break;
+      default: phase_b_round<16>(c, p, seq + used, round, k, kp, bout); break;
+    }
+    used += (unsigned)c.ntiles;
+  }
+  return used;
+}
+
+// ---------------------------------------------------------------------------
+// Double-word dense kernels for one n x n system, run by the solver warps
+// (threads 0-127).  Matrices are column-major with leading dimension n.
+// ---------------------------------------------------------------------------
+
+constexpr int kSolverThreads = kAlsSolverWarps * 32;
+
+// In-place LDL^T of the symmetric A (lower triangle): afterwards A(i,j) =
+// L(i,j) for i > j and dinv[j] = 1/D(j).  The next pivot is formed first so
+// its reciprocal overlaps the rest of the trailing update.  Returns the
+// 1-based index of the first non-positive pivot (replaced by its magnitude
+// plus a tiny amount, as the FP64 Cholesky fallback of the reference would
+// fail there) or 0.  u is scratch of n entries.
+__device__ int dw_ldlt(dw* A, int n, dw* dinv, dw* u) {
+  const int t = threadIdx.x, lane = t & 31, wq = t >> 5;
+  int bad = 0;
+  dw d0 = A[0];
+  if (!(d0.hi > 0.f)) {
+    bad = 1;
+    d0 = dw_make(fabsf(d0.hi) + 1e-30f);
+  }
+  dw inv = dw_rcp(d0);
+  for (int j = 0; j < n; ++j) {
+    const int m = n - j - 1;
+    for (int r = t; r < m; r += kSolverThreads) {
+      const dw a = A[j + 1 + r + j * n];
+      u[j + 1 + r] = a;
+      A[j + 1 + r + j * n] = dw_mul(a, inv);
+    }
+    if (t == 0) dinv[j] = inv;
+    solver_sync();
+    if (m == 0) break;
+    dw next = dw_fms(A[j + 1 + j * n], u[j + 1], A[(j + 1) * (n + 1)]);
+    if (!(next.hi > 0.f)) {
+      if (!bad) bad = j + 2;
+      next = dw_make(fabsf(next.hi) + 1e-30f);
+    }
+    const dw inv_next = dw_rcp(next);
+    // trailing update: row i = j+1+ri (lane), columns j+1+cc <= i (warp-strided)
+    for (int ri = lane; ri < m; ri += 32) {
+      if (ri == 0) continue;  // (j+1, j+1) is `next`
+      const int i = j + 1 + ri;
+      const dw l = A[i + j * n];
+      for (int cc = wq; cc <= ri; cc += kAlsSolverWarps) {
+        const int col = j + 1 + cc;
+        A[i + col * n] = dw_fms(l, u[col], A[i + col * n]);
+      }
+    }
+    if (t == 0) A[(j + 1) * (n + 1)] = next;
+    inv = inv_next;
+    solver_sync();
+  }
+  return bad;
+}
+
+// Solve L D L^T X = B in place for nrhs columns (B column-major, ld n).
+__device__ void dw_ldlt_solve(const dw* A, int n, const dw* dinv, dw* B, int nrhs) {
+  const int t = threadIdx.x;
+  for (int j = 0; j < n - 1; ++j) {
+    const int m = n - j - 1;
+    for (int e = t; e < m * nrhs; e += kSolverThreads) {
+      const int col = e / m, i = j + 1 + (e - col * m);
+      B[i + col * n] = dw_fms(A[i + j * n], B[j + col * n], B[i + col * n]);
+    }
+    solver_sync();
+  }
+  for (int e = t; e < n * nrhs; e += kSolverThreads) {
+    const int col = e / n, i = e - col * n;
+    B[i + col * n] = dw_mul(B[i + col * n], dinv[i]);
+  }
+  solver_sync();
+  for (int j = n - 1; j > 0; --j) {
+    for (int e = t; e < j * nrhs; e += kSolverThreads) {
+      const int col = e / j, i = e - col * j;
+      B[i + col * n] = dw_fms(A[j + i * n], B[j + col * n], B[i + col * n]);
+    }
+    solver_sync();
+  }
+}
+
+// Max-scaled 2-norm of row i of X (n entries, stride ld), as the reference's
+// normonebase (src/modvecvec.cu:225-262); scales the row to unit norm.  A zero
+// row gives NaN, as in the reference.
+__device__ dw dw_normalise_row(dw* x, int n, int ld) {
+  dw largest = dw_make(0.f);
+  for (int q = 0; q < n; ++q) {
+    const dw a = dw_abs(x[q * ld]);
+    if (dw_gt(a, largest)) largest = a;
+  }
+  if (!(largest.hi > 0.f)) {
+    const float nan = __int_as_float(0x7fffffff);
+    for (int q = 0; q < n; ++q) x[q * ld] = dw_make(nan);
+    return dw_make(nan);
+  }
+  const dw il = dw_rcp(largest);
+  dw acc = dw_make(0.f);
+  for (int q = 0; q < n; ++q) {
+    const dw y = dw_mul(x[q * ld], il);
+    acc = dw_fma(y, y, acc);
+  }
+  const dw r = dw_mul(largest, dw_sqrt(acc));
+  const dw inv = dw_rcp(r);
+  for (int q = 0; q < n; ++q) x[q * ld] = dw_mul(x[q * ld], inv);
+  return r;
+}
+
+// Suffix products for the next sweep: suf[d] = prod_{d' > d} gram[d']
+// (elementwise), suf[D-1] = 1; and the prefix L reset to 1.
+__device__ void dw_suffix(const Cta& c) {
+  const int rr = c.rF * c.rF;
+  for (int e = c.tid; e < rr; e += kSolverThreads) {
+    dw a = dw_make(1.f);
+    c.suf[(size_t)(c.D - 1) * rr + e] = a;
+    for (int d = c.D - 1; d >= 1; --d) {
+      a = dw_mul(a, c.gram[(size_t)d * rr + e]);
+      c.suf[(size_t)(d - 1) * rr + e] = a;
+    }
+    c.L[e] = dw_make(1.f);
+  }
+}
+
+// Gram matrix of the unit-normalised new factor of mode k (rows of X), stored
+// for the suffix products of the next sweep and folded into the prefix L.
+__device__ void dw_new_gram(const Cta& c, int k, int nk) {
+  const int rF = c.rF, rr = rF * rF;
+  for (int e = c.tid; e < rr; e += kSolverThreads) {
+    const int i = e % rF, i2 = e / rF;
+    if (i > i2) continue;
+    dw s = dw_make(0.f);
+    for (int q = 0; q < nk; ++q) s = dw_fma(c.X[i + q * rF], c.X[i2 + q * rF], s);
+    c.gram[(size_t)k * rr + i + i2 * rF] = s;
+    c.gram[(size_t)k * rr + i2 + i * rF] = s;
+    if (k < c.D - 1) {
+      c.L[i + i2 * rF] = dw_mul(c.L[i + i2 * rF], s);
+      if (i != i2) c.L[i2 + i * rF] = dw_mul(c.L[i2 + i * rF], s);
+    }
+  }
+}
+
+// The R x R solve of step t (mode k; kn is the next step's mode), run
+// identically by every CTA of the cluster on the solver warps.
+__device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& cluster, int t, int k, int kn) {
+  const int rF = c.rF, nk = p.nbas[k], npk = round_up(nk, 4);
+  const int rr = rF * rF;
+  // gather the partial right-hand sides of the cluster in rank order
+  const size_t boff = (size_t)(t & 1) * c.rFp * c.npmax;
+  for (int e = c.tid; e < rF * nk; e += kSolverThreads) {
+    const int i = e % rF, n = e / rF;
+    dw s = dw_make(0.f);
+    for (int r = 0; r < c.CL; ++r) {
+      const float* peer = cluster.map_shared_rank(c.bpart + boff, r);
+      s = dw_add_f(s, peer[i * c.npmax + n]);
+    }
+    c.X[i + n * rF] = s;
+  }
+  // normal equations: prefix (this sweep) x suffix (previous sweep) + penalty
+  const dw pen = c.misc[0];
+  for (int e = c.tid; e < rr; e += kSolverThreads) {
+    dw b = dw_mul(c.L[e], c.sk[e]);
+    if (e % rF == e / rF) b = dw_add(b, pen);
+    c.BB[e] = b;
+  }
+  solver_sync();
+  const int bad = dw_ldlt(c.BB, rF, c.dinv, c.u);
+  dw_ldlt_solve(c.BB, rF, c.dinv, c.X, nk);
+  for (int i = c.tid; i < rF; i += kSolverThreads) c.nrm[i] = dw_normalise_row(c.X + i, nk, rF);
+  solver_sync();
+  // new factor: FP32 copy for phase B and for this CTA's rebuilds; the
+  // caller's FP64 arrays from cluster rank 0
+  for (int e = c.tid; e < c.rFp * npk; e += kSolverThreads) {
+    const int i = e / npk, q = e - i * npk;
+    const float x = (i < rF && q < nk) ? c.X[i + q * rF].hi : 0.f;
+    c.fb[i * c.gsmax + q] = x;
+    if (i < rF) c.fcta[(long long)i * c.nDp + p.offp[k] + q] = x;
+  }
+  if (c.rank == 0) {
+    double* fbase = p.base + p.term_off[c.v] * (long long)p.nD;
+    for (int e = c.tid; e < rF * nk; e += kSolverThreads) {
+      const int i = e / nk, q = e - i * nk;
+      fbase[(long long)i * p.nD + p.off[k] + q] = dw_to_double(c.X[i + q * rF]);
+    }
+    for (int i = c.tid; i < rF; i += kSolverThreads) p.coef[p.term_off[c.v] + i] = dw_to_double(c.nrm[i]);
+  }
+  dw_new_gram(c, k, nk);
+  solver_sync();
+  if (k == c.D - 1) {
+    dw_suffix(c);
+    solver_sync();
+  }
+  for (int e = c.tid; e < rr; e += kSolverThreads) c.sk[e] = c.suf[(size_t)kn * rr + e];
+  if (c.tid == 0 && bad) c.flags[1] = 1;
+}
+
+// Barrier among the phase-A warps only (named barrier 2).
+__device__ __forceinline__ void worker_sync() {
+  asm volatile("bar.sync 2, %0;" ::"r"(kAlsThreads - kSolverThreads) : "memory");
+}
+
+}  // namespace
 
 // ---------------------------------------------------------------------------
 // Persistent cluster kernel
 // ---------------------------------------------------------------------------
 
-namespace {
-
-constexpr int kThreads = kAlsThreads;
-constexpr int kTileRows = 256;  // target terms staged per tile (multiple of 4)
-constexpr int kWtStride = kTileRows + 1;  // odd stride: per-term weight rows on distinct banks
-
-struct Smem {
-  float* ps;      // [rFp][rows_cta] running products (term index fastest: conflict-free)
-  float* fold;    // [rFp][npmax] FP32 old factor of the mode being solved
-  float* fnew;    // [rFp][npmax] FP32 new factor of the mode just solved
-  float* wt;      // [rFp][kWtStride] weights c_j * PS(j,i) of the tile
-  float* gt;      // [kTileRows][gstride] target factors of mode k for the tile
-  float* gp;      // [kTileRows][gstride] target factors of the previous mode for the tile
-  float* bpart;   // [rFp][npmax] partial right-hand side of this CTA
-  float* red;     // [kThreads][16] reduction scratch
-  double* BB;     // [rF][rF]
-  double* X;      // [rF][npmax] column-major rF x n (ld rF)
-  double* L;      // [rF][rF] prefix of F Gram products
-  double* misc;   // [4]
-  double* dinv;   // [rF] reciprocal pivots of the LDL^T factor
-  double* u;      // [rF] LDL^T scratch column
-  int* flags;     // [4]
-};
-
-// Row stride of staged tiles: an odd number of float4 per row keeps the
-// float4 accesses of consecutive rows on distinct shared-memory banks.
-__host__ __device__ inline int tile_stride(int npmax) { return ((npmax / 4) % 2 == 1) ? npmax : npmax + 4; }
-
-// Quotient a / b from the approximate reciprocal plus one Newton correction
-// (within an ulp or two of the rounded quotient).
-__device__ __forceinline__ float div_nr(float a, float b) {
-  float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
-  float q = a * r;
-  return fmaf(fmaf(-b, q, a), r, q);
-}
-
-// <g, f> over NP padded entries; g in registers, f in shared memory.
-template <int NP>
-__device__ __forceinline__ float dot_reg(const float (&g)[NP], const float* f, int np) {
-  float s = 0.f;
-#pragma unroll
-  for (int q = 0; q < NP; q += 4) {
-    if (q < np) {
-      float4 y = *reinterpret_cast<const float4*>(f + q);
-      s = fmaf(g[q], y.x, s);
-      s = fmaf(g[q + 1], y.y, s);
-      s = fmaf(g[q + 2], y.z, s);
-      s = fmaf(g[q + 3], y.w, s);
-    }
-  }
-  return s;
-}
-
-template <int NP>
-__device__ __forceinline__ void load_row(float (&g)[NP], const float* src, int np) {
-#pragma unroll
-  for (int q = 0; q < NP; q += 4) {
-    float4 x = (q < np) ? *reinterpret_cast<const float4*>(src + q) : make_float4(0.f, 0.f, 0.f, 0.f);
-    g[q] = x.x; g[q + 1] = x.y; g[q + 2] = x.z; g[q + 3] = x.w;
-  }
-}
-
-// Plain dot product of two padded FP32 runs in global memory (rebuild path).
-__device__ inline float dot_global(const float* a, const float* b, int np) {
-  float s = 0.f;
-  for (int q = 0; q < np; ++q) s = fmaf(a[q], b[q], s);
-  return s;
-}
-
-}  // namespace
-
-template <int NP>
-__global__ void __launch_bounds__(kThreads, 1) als_cluster_kernel(AlsParams p) {
+__global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p) {
   cg::cluster_group cluster = cg::this_cluster();
-  const int CL = (int)cluster.num_blocks();
-  const int rank = (int)cluster.block_rank();
-  const int v = blockIdx.x / CL;
-  if (v >= p.nvec) return;  // whole cluster exits together (same v)
+  extern __shared__ __align__(128) unsigned char smem_raw[];
 
-  const int tid = threadIdx.x;
-  const int D = p.ndof;
-  const int rF = p.rF[v], rG = p.rG[v];
-  const int rFp = round_up(rF, 4);
-  const int npmax = p.npmax;
-  const int rows_per = (rG + CL - 1) / CL;
-  const int row0 = min(rG, rank * rows_per);
-  const int row1 = min(rG, row0 + rows_per);
-  const int nrows = row1 - row0;
-
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  Smem s;
+  Cta c;
+  c.tid = threadIdx.x;
+  c.warp = c.tid >> 5;
+  c.lane = c.tid & 31;
+  c.CL = p.cluster;
+  c.rank = (int)cluster.block_rank();
+  c.v = blockIdx.x / c.CL;
+  c.D = p.ndof;
+  c.rF = p.rF[c.v];
+  c.rFp = round_up(c.rF, 4);
+  c.nIq = c.rFp / 4;
+  c.rG = p.rG[c.v];
   {
-    unsigned char* ptr = smem_raw;
-    auto take = [&](size_t bytes) { unsigned char* r = ptr; ptr += round_up((int)bytes, 16); return r; };
-    s.ps = (float*)take(sizeof(float) * (size_t)p.rows_cta_max * rFp);
-    s.fold = (float*)take(sizeof(float) * rFp * npmax);
-    s.fnew = (float*)take(sizeof(float) * rFp * npmax);
-    s.wt = (float*)take(sizeof(float) * kWtStride * rFp);
-    s.gt = (float*)take(sizeof(float) * kTileRows * tile_stride(npmax));
-    s.gp = (float*)take(sizeof(float) * kTileRows * tile_stride(npmax));
-    s.bpart = (float*)take(sizeof(float) * rFp * npmax);
-    s.red = (float*)take(sizeof(float) * kThreads * 16);
-    s.BB = (double*)take(sizeof(double) * rF * rF);
-    s.X = (double*)take(sizeof(double) * rF * npmax);
-    s.L = (double*)take(sizeof(double) * rF * rF);
-    s.misc = (double*)take(sizeof(double) * 4);
-    s.dinv = (double*)take(sizeof(double) * rF);
-    s.u = (double*)take(sizeof(double) * rF);
-    s.flags = (int*)take(sizeof(int) * 4);
+    const int rows_per = (c.rG + c.CL - 1) / c.CL;
+    c.row0 = min(c.rG, c.rank * rows_per);
+    c.nrows = min(c.rG, c.row0 + rows_per) - c.row0;
   }
+  c.ntiles = (c.nrows + kAlsTileRows - 1) / kAlsTileRows;
+  const AlsSmem lay = als_smem_layout(p.rows_cta_max, p.rf_max, p.npmax, p.gsmax, p.stages);
+  c.ldP = lay.ldP;
+  c.gsmax = p.gsmax;
+  c.npmax = p.npmax;
+  c.nDp = p.nDp;
+  c.stages = p.stages;
+  c.stage_floats = lay.stage_floats;
+  c.bar = reinterpret_cast<uint64_t*>(smem_raw + lay.bar);
+  c.done = reinterpret_cast<int*>(smem_raw + lay.done);
+  c.issued = reinterpret_cast<int*>(smem_raw + lay.issued);
+  c.fillno = reinterpret_cast<unsigned*>(smem_raw + lay.fillno);
+  c.flags = reinterpret_cast<int*>(smem_raw + lay.flags);
+  c.ring = reinterpret_cast<float*>(smem_raw + lay.ring);
+  c.P = reinterpret_cast<float*>(smem_raw + lay.P);
+  c.cw = reinterpret_cast<float*>(smem_raw + lay.cw);
+  c.fa = reinterpret_cast<float*>(smem_raw + lay.fa);
+  c.fb = reinterpret_cast<float*>(smem_raw + lay.fb);
+  c.bred = reinterpret_cast<float*>(smem_raw + lay.bred);
+  c.bpart = reinterpret_cast<float*>(smem_raw + lay.bpart);
+  c.BB = reinterpret_cast<dw*>(smem_raw + lay.BB);
+  c.X = reinterpret_cast<dw*>(smem_raw + lay.X);
+  c.L = reinterpret_cast<dw*>(smem_raw + lay.L);
+  c.sk = reinterpret_cast<dw*>(smem_raw + lay.sk);
+  c.dinv = reinterpret_cast<dw*>(smem_raw + lay.dinv);
+  c.u = reinterpret_cast<dw*>(smem_raw + lay.u);
+  c.nrm = reinterpret_cast<dw*>(smem_raw + lay.nrm);
+  c.misc = reinterpret_cast<dw*>(smem_raw + lay.misc);
+  c.gm = p.gm + p.gm_off[c.v];
+  c.fcta = p.fcta + (p.f_row_off[c.v] * c.CL + (long long)c.rank * c.rF) * p.nDp;
+  {
+    const long long sq = p.sq_off[c.v] * c.CL + (long long)c.rank * c.rF * c.rF * c.D;
+    c.gram = p.gram + sq;
+    c.suf = p.suf + sq;
+  }
+  const int D = c.D, rF = c.rF, rr = rF * rF;
 
-  const float* gm = p.gm + p.gm_off[v];
-  const float* gc = p.gc + p.g_row_off[v];
-  float* f32 = p.f32 + p.f_row_off[v] * p.nDp;
-  double* fbase = p.base + p.term_off[v] * (long long)p.nD;
-  double* fcoef = p.coef + p.term_off[v];
-  double* gram = p.gram + p.sq_off[v];   // [D][rF][rF]
-  double* suf = p.suf + p.sq_off[v];     // [D][rF][rF]
-
-  // ---- prologue: running products over all modes, F Grams, penalty ----
-  const int psld = p.rows_cta_max;
-  for (int e = tid; e < rFp * psld; e += kThreads) s.ps[e] = 1.f;
+  // ---- prologue ----
+  for (int e = c.tid; e < c.stages * c.stage_floats; e += kAlsThreads) c.ring[e] = 0.f;  // stale reads stay finite
+  for (int e = c.tid; e < lay.rFp * c.ldP; e += kAlsThreads) c.P[e] = (e / c.ldP < rF) ? 1.f : 0.f;
+  for (int j = c.tid; j < c.ldP; j += kAlsThreads) c.cw[j] = (j < c.nrows) ? p.gc[p.g_row_off[c.v] + c.row0 + j] : 0.f;
+  for (int e = c.tid; e < 2 * lay.rFp * c.npmax; e += kAlsThreads) c.bpart[e] = 0.f;
+  if (c.tid < c.stages) {
+    c.done[c.tid] = 0;
+    c.issued[c.tid] = 0;
+    c.fillno[c.tid] = 0xffffffffu;
+  }
+  if (c.tid < 8) c.flags[c.tid] = 0;
+  if (c.tid == 0) {
+    for (int s = 0; s < c.stages; ++s) mbar_init(&c.bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  const float* f32v = p.f32 + p.f_row_off[c.v] * p.nDp;
+  const float* f32lo_v = p.f32lo + p.f_row_off[c.v] * p.nDp;
+  for (int e = c.tid; e < rF * p.nDp; e += kAlsThreads) c.fcta[e] = f32v[e];
   __syncthreads();
-  for (int d = 0; d < D; ++d) {
-    const int np = round_up(p.nbas[d], 4);
-    for (int e = tid; e < rFp * np; e += kThreads) {
-      const int i = e / np, q = e % np;
-      s.fold[i * npmax + q] = (i < rF) ? f32[(long long)i * p.nDp + p.offp[d] + q] : 0.f;
-    }
+
+  // running products without modes 0 and D-1 (the state phase B of step 0 expects)
+  unsigned seq = 0;
+  for (int d = 1; d <= D - 2; ++d) {
+    load_factor(c, p, d, c.fa, 0, kAlsThreads);
     __syncthreads();
-    const float* gmd = gm + (long long)p.offp[d] * rG;
-    for (int r = tid; r < nrows; r += kThreads) {
-      float g[NP];
-      load_row<NP>(g, gmd + (long long)(row0 + r) * np, np);
-      for (int i = 0; i < rF; ++i) s.ps[i * psld + r] *= dot_reg<NP>(g, s.fold + i * npmax, np);
-    }
+    if (c.tid == 0) start_phase(c, seq, TileSrc{c.gm + (long long)p.offg[d] * c.rG, als_gstride(p.nbas[d]), nullptr, 0});
+    product_pass(c, p, seq, d, false, -1, 0, kAlsWarps);
+    seq += (unsigned)c.ntiles;
     __syncthreads();
   }
-  // F Grams (FP64): CTA rank handles modes d = rank, rank+CL, ...
-  for (int d = rank; d < D; d += CL) {
+  // Grams of the starting factors (double-word), penalty
+  for (int e = c.tid; e < D * rr; e += kAlsThreads) {
+    const int d = e / rr, r = e - d * rr, i = r % rF, i2 = r / rF;
+    if (i > i2) continue;
     const int n = p.nbas[d];
-    for (int e = tid; e < rF * rF; e += kThreads) {
-      const int i = e % rF, i2 = e / rF;
-      const double* a = fbase + (long long)i * p.nD + p.off[d];
-      const double* b = fbase + (long long)i2 * p.nD + p.off[d];
-      double t = 0.0;
-      for (int q = 0; q < n; ++q) t += a[q] * b[q];
-      gram[(long long)d * rF * rF + e] = t;
-    }
+    const long long oa = (long long)i * p.nDp + p.offp[d], ob = (long long)i2 * p.nDp + p.offp[d];
+    dw s = dw_make(0.f);
+    for (int q = 0; q < n; ++q) s = dw_fma(dw_make(f32v[oa + q], f32lo_v[oa + q]), dw_make(f32v[ob + q], f32lo_v[ob + q]), s);
+    c.gram[(size_t)d * rr + i + i2 * rF] = s;
+    c.gram[(size_t)d * rr + i2 + i * rF] = s;
   }
-  if (rank == 0 && tid == 0) {
-    double pen = fcoef[0];
-    for (int i = 1; i < rF; ++i) pen = fcoef[i] > pen ? fcoef[i] : pen;
-    s.misc[0] = pen * p.pen_factor;
+  if (c.tid == 0) {
+    const double* fc = p.coef + p.term_off[c.v];
+    double mx = fc[0];
+    for (int i = 1; i < rF; ++i) mx = fc[i] > mx ? fc[i] : mx;
+    c.misc[0] = dw_from_double(mx * p.pen_factor);
   }
-  __threadfence();
-  cluster.sync();
+  __syncthreads();
+  if (c.warp < kAlsSolverWarps) {
+    dw_suffix(c);
+    solver_sync();
+    for (int e = c.tid; e < rr; e += kSolverThreads) c.sk[e] = c.suf[e];
+  }
+  load_factor(c, p, D - 1, c.fb, 0, kAlsThreads);
+  __syncthreads();
 
-  const int nib = rFp / 4;  // i-blocks of the right-hand-side register tiles
+  // ---- mode steps ----
   const int nsteps = p.nals * D;
-
   for (int t = 0; t < nsteps; ++t) {
-    const int k = t % D;
-    const int kprev = (t > 0) ? (t - 1) % D : -1;
-    const int nk = p.nbas[k], npk = round_up(nk, 4);
-    const int npp = (kprev >= 0) ? round_up(p.nbas[kprev], 4) : 0;
-    const int nnb = npk / 4;                 // n-blocks
-    const int nblk = nib * nnb;              // register blocks (<= kThreads, host-checked)
-    const int ngroups = kThreads / nblk;     // row groups
-    const int my_blk = tid % nblk, my_grp = tid / nblk;
-    const bool acc_active = my_grp < ngroups;
-    const int ib = my_blk / nnb, nb = my_blk % nnb;
-    float acc[16];
-#pragma unroll
-    for (int q = 0; q < 16; ++q) acc[q] = 0.f;
-
-    // old factor of mode k (FP32)
-    for (int e = tid; e < rFp * npk; e += kThreads) {
-      const int i = e / npk, q = e % npk;
-      s.fold[i * npmax + q] = (i < rF) ? f32[(long long)i * p.nDp + p.offp[k] + q] : 0.f;
+    const int k = t % D, kp = (k + D - 1) % D, kn = (k + 1) % D;
+    seq += phase_b(c, p, seq, k, kp, c.bpart + (size_t)(t & 1) * c.rFp * c.npmax);
+    cluster_arrive();
+    if (c.warp < kAlsSolverWarps) {
+      cluster_wait();
+      solve_step(c, p, cluster, t, k, kn);
+    } else {
+      if (t + 1 < nsteps) {
+        load_factor(c, p, kn, c.fa, kSolverThreads, kAlsThreads - kSolverThreads);
+        worker_sync();
+        if (c.tid == kSolverThreads)
+          start_phase(c, seq, TileSrc{c.gm + (long long)p.offg[kn] * c.rG, als_gstride(p.nbas[kn]), nullptr, 0});
+        product_pass(c, p, seq, kn, true, k, kAlsSolverWarps, kAlsWarps - kAlsSolverWarps);
+      }
+      cluster_wait();
     }
+    if (t + 1 < nsteps) seq += (unsigned)c.ntiles;
     __syncthreads();
-
-    const float* gmk = gm + (long long)p.offp[k] * rG;
-    const float* gmp = (kprev >= 0) ? gm + (long long)p.offp[kprev] * rG : nullptr;
-
-    const int gsd = tile_stride(npmax);
-    constexpr int kRowSlots = kTileRows / 4;  // register block = rows {rb, rb+64, rb+128, rb+192}
-    for (int tile0 = 0; tile0 < nrows; tile0 += kTileRows) {
-      const int tr = min(kTileRows, nrows - tile0);
-      // -- stage the tile's factors of modes k and kprev (coalesced float4) --
-      for (int e = tid; e < kTileRows * (npk / 4); e += kThreads) {
-        const int r = e / (npk / 4), q = (e % (npk / 4)) * 4;
-        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (r < tr) x = *reinterpret_cast<const float4*>(gmk + (long long)(row0 + tile0 + r) * npk + q);
-        *reinterpret_cast<float4*>(s.gt + r * gsd + q) = x;
-      }
-      if (kprev >= 0) {
-        for (int e = tid; e < kTileRows * (npp / 4); e += kThreads) {
-          const int r = e / (npp / 4), q = (e % (npp / 4)) * 4;
-          float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (r < tr) x = *reinterpret_cast<const float4*>(gmp + (long long)(row0 + tile0 + r) * npp + q);
-          *reinterpret_cast<float4*>(s.gp + r * gsd + q) = x;
-        }
-      }
-      __syncthreads();
-      // -- running products: fold in the new factor of kprev, divide out mode k.
-      //    Register blocks of 4 terms x 4 F terms; consecutive threads take
-      //    consecutive terms, so shared-memory accesses are conflict-free and
-      //    the F reads of a warp are broadcasts. --
-      for (int blk = tid; blk < kRowSlots * nib; blk += kThreads) {
-        const int rb = blk % kRowSlots, ibk = blk / kRowSlots;
-        float po[16], pn[16];
-#pragma unroll
-        for (int q = 0; q < 16; ++q) { po[q] = 0.f; pn[q] = 1.f; }
-        for (int q = 0; q < npk; q += 4) {
-          float4 g[4], f[4];
-#pragma unroll
-          for (int a = 0; a < 4; ++a) g[a] = *reinterpret_cast<const float4*>(s.gt + (rb + a * kRowSlots) * gsd + q);
-#pragma unroll
-          for (int c = 0; c < 4; ++c) f[c] = *reinterpret_cast<const float4*>(s.fold + (ibk * 4 + c) * npmax + q);
-#pragma unroll
-          for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              float v = po[a * 4 + c];
-              v = fmaf(g[a].x, f[c].x, v);
-              v = fmaf(g[a].y, f[c].y, v);
-              v = fmaf(g[a].z, f[c].z, v);
-              v = fmaf(g[a].w, f[c].w, v);
-              po[a * 4 + c] = v;
-            }
-        }
-        if (kprev >= 0) {
-#pragma unroll
-          for (int q = 0; q < 16; ++q) pn[q] = 0.f;
-          for (int q = 0; q < npp; q += 4) {
-            float4 g[4], f[4];
-#pragma unroll
-            for (int a = 0; a < 4; ++a) g[a] = *reinterpret_cast<const float4*>(s.gp + (rb + a * kRowSlots) * gsd + q);
-#pragma unroll
-            for (int c = 0; c < 4; ++c) f[c] = *reinterpret_cast<const float4*>(s.fnew + (ibk * 4 + c) * npmax + q);
-#pragma unroll
-            for (int a = 0; a < 4; ++a)
-#pragma unroll
-              for (int c = 0; c < 4; ++c) {
-                float v = pn[a * 4 + c];
-                v = fmaf(g[a].x, f[c].x, v);
-                v = fmaf(g[a].y, f[c].y, v);
-                v = fmaf(g[a].z, f[c].z, v);
-                v = fmaf(g[a].w, f[c].w, v);
-                pn[a * 4 + c] = v;
-              }
-          }
-        }
-        // elementwise update; the rare unsafe divisions are rebuilt after the
-        // loop so that the common path stays branch-light
-        unsigned rebuild = 0u;
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const int rt = rb + a * kRowSlots;  // row within the tile
-          const bool live = rt < tr;
-          const float cj = live ? gc[row0 + tile0 + rt] : 0.f;
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            const int i = ibk * 4 + c;
-            float psk = 0.f;
-            if (live && i < rF) {
-              const float tot = s.ps[i * psld + tile0 + rt] * pn[a * 4 + c];
-              const float d = po[a * 4 + c];
-              if (d != 0.f && fabsf(tot) >= FLT_MIN && fabsf(tot) <= FLT_MAX) {
-                psk = div_nr(tot, d);
-                s.ps[i * psld + tile0 + rt] = psk;  // holds prod_{d != k} until mode k is solved
-              } else {
-                rebuild |= 1u << (a * 4 + c);
-              }
-            }
-            s.wt[i * kWtStride + rt] = cj * psk;
-          }
-        }
-        while (rebuild) {
-          // unsafe division: rebuild prod_{d' != k} <G_j^d', F_i^d'> directly
-          const int bit = __ffs(rebuild) - 1;
-          rebuild &= rebuild - 1;
-          const int a = bit / 4, c = bit % 4;
-          const int rt = rb + a * kRowSlots, i = ibk * 4 + c;
-          const int j = row0 + tile0 + rt;
-          float psk = 1.f;
-          for (int dd = 0; dd < D; ++dd) {
-            if (dd == k) continue;
-            const int npd = round_up(p.nbas[dd], 4);
-            psk *= dot_global(gm + (long long)p.offp[dd] * rG + (long long)j * npd,
-                              f32 + (long long)i * p.nDp + p.offp[dd], npd);
-          }
-          s.ps[i * psld + tile0 + rt] = psk;
-          s.wt[i * kWtStride + rt] = gc[j] * psk;
-        }
-      }
-      __syncthreads();
-      // -- right-hand-side accumulation: acc(ib*4+a, nb*4+c) += w(r,i) g(r,n) --
-      if (acc_active) {
-        for (int rr = my_grp; rr < tr; rr += ngroups) {
-          const float w0 = s.wt[(ib * 4 + 0) * kWtStride + rr];
-          const float w1 = s.wt[(ib * 4 + 1) * kWtStride + rr];
-          const float w2 = s.wt[(ib * 4 + 2) * kWtStride + rr];
-          const float w3 = s.wt[(ib * 4 + 3) * kWtStride + rr];
-          const float4 g = *reinterpret_cast<const float4*>(s.gt + rr * gsd + nb * 4);
-          acc[0] = fmaf(w0, g.x, acc[0]);  acc[1] = fmaf(w0, g.y, acc[1]);
-          acc[2] = fmaf(w0, g.z, acc[2]);  acc[3] = fmaf(w0, g.w, acc[3]);
-          acc[4] = fmaf(w1, g.x, acc[4]);  acc[5] = fmaf(w1, g.y, acc[5]);
-          acc[6] = fmaf(w1, g.z, acc[6]);  acc[7] = fmaf(w1, g.w, acc[7]);
-          acc[8] = fmaf(w2, g.x, acc[8]);  acc[9] = fmaf(w2, g.y, acc[9]);
-          acc[10] = fmaf(w2, g.z, acc[10]); acc[11] = fmaf(w2, g.w, acc[11]);
-          acc[12] = fmaf(w3, g.x, acc[12]); acc[13] = fmaf(w3, g.y, acc[13]);
-          acc[14] = fmaf(w3, g.z, acc[14]); acc[15] = fmaf(w3, g.w, acc[15]);
-        }
-      }
-      __syncthreads();
+  }
+  // every CTA of the cluster has gathered before any shared memory goes away
+  cluster_arrive();
+  cluster_wait();
+  if (c.tid == 0) {
+    // bulk copies are all consumed by now; wait (bounded) on each stage's last fill anyway
+    for (int s = 0; s < c.stages; ++s) {
+      const int fills = c.issued[s];
+      if (fills == 0) continue;
+      for (int it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(&c.bar[s], (uint32_t)((fills - 1) & 1))) break;
     }
-    // -- reduce the row groups into this CTA's partial right-hand side --
-    if (acc_active) {
-#pragma unroll
-      for (int q = 0; q < 16; ++q) s.red[(my_grp * nblk + my_blk) * 16 + q] = acc[q];
-    }
-    __syncthreads();
-    for (int e = tid; e < nblk * 16; e += kThreads) {
-      const int blk = e / 16, q = e % 16;
-      float sum = 0.f;
-      for (int gI = 0; gI < ngroups; ++gI) sum += s.red[(gI * nblk + blk) * 16 + q];
-      const int i = (blk / nnb) * 4 + q / 4, n = (blk % nnb) * 4 + q % 4;
-      s.bpart[i * npmax + n] = sum;
-    }
-    cluster.sync();
-
-    // -- rank 0: FP64 normal equations for mode k --
-    if (rank == 0) {
-      for (int e = tid; e < rF * nk; e += kThreads) {
-        const int i = e % rF, n = e / rF;
-        double sum = 0.0;
-        for (int c = 0; c < CL; ++c) {
-          const float* bp = cluster.map_shared_rank(s.bpart, c);
-          sum += (double)bp[i * npmax + n];
-        }
-        s.X[i + n * rF] = sum;
-      }
-      if (k == 0) {
-        // sweep start: suffix products of the current Grams, empty prefix
-        for (int e = tid; e < rF * rF; e += kThreads) {
-          double a = 1.0;
-          suf[(long long)(D - 1) * rF * rF + e] = 1.0;
-          for (int d = D - 1; d >= 1; --d) {
-            a *= gram[(long long)d * rF * rF + e];
-            suf[(long long)(d - 1) * rF * rF + e] = a;
-          }
-          s.L[e] = 1.0;
-        }
-      }
-      __syncthreads();
-      const double pen = s.misc[0];
-      for (int e = tid; e < rF * rF; e += kThreads) {
-        const int i = e % rF, i2 = e / rF;
-        double bb = s.L[e] * suf[(long long)k * rF * rF + e];
-        if (i == i2) bb += pen;
-        s.BB[e] = bb;
-      }
-      __syncthreads();
-      block_ldlt(s.BB, rF, rF, s.dinv, s.u, &s.flags[0]);
-      block_ldlt_solve(s.BB, rF, rF, s.dinv, s.X, nk, rF);
-      // normalise each term's new factor (max-scaled 2-norm), write F
-      for (int i = tid; i < rF; i += kThreads) {
-        double nrm, inv;
-        scaled_norm(s.X + i, nk, rF, &nrm, &inv);
-        for (int n = 0; n < nk; ++n) s.X[i + n * rF] *= inv;
-        fcoef[i] = nrm;
-      }
-      __syncthreads();
-      for (int e = tid; e < rFp * npk; e += kThreads) {
-        const int i = e / npk, q = e % npk;
-        const double x = (i < rF && q < nk) ? s.X[i + q * rF] : 0.0;
-        const float xf = (float)x;
-        if (i < rF) {
-          if (q < nk) fbase[(long long)i * p.nD + p.off[k] + q] = x;
-          f32[(long long)i * p.nDp + p.offp[k] + q] = xf;
-        }
-        for (int c = 0; c < CL; ++c) cluster.map_shared_rank(s.fnew, c)[i * npmax + q] = xf;
-      }
-      // new Gram of mode k and prefix update
-      for (int e = tid; e < rF * rF; e += kThreads) {
-        const int i = e % rF, i2 = e / rF;
-        double t2 = 0.0;
-        for (int n = 0; n < nk; ++n) t2 += s.X[i + n * rF] * s.X[i2 + n * rF];
-        gram[(long long)k * rF * rF + e] = t2;
-        s.L[e] *= t2;
-      }
-      if (tid == 0 && s.flags[0] != 0) atomicOr(&p.status[v], 1);
-      __threadfence();
-    }
-    cluster.sync();
+    if (c.flags[0]) atomicOr(&p.status[c.v], 2);
+    if (c.flags[1]) atomicOr(&p.status[c.v], 1);
   }
 }
 
-size_t als_smem_bytes(int rows_cta, int rF, int npmax) {
-  // mirrors the carve order at the top of als_cluster_kernel
-  const int rFp = round_up(rF, 4);
-  size_t b = 0;
-  auto take = [&](size_t bytes) { b += (size_t)round_up((int)bytes, 16); };
-  take(sizeof(float) * (size_t)rows_cta * rFp);
-  take(sizeof(float) * rFp * npmax);
-  take(sizeof(float) * rFp * npmax);
-  take(sizeof(float) * kWtStride * rFp);
-  take(sizeof(float) * kTileRows * tile_stride(npmax));
-  take(sizeof(float) * kTileRows * tile_stride(npmax));
-  take(sizeof(float) * rFp * npmax);
-  take(sizeof(float) * kThreads * 16);
-  take(sizeof(double) * rF * rF);
-  take(sizeof(double) * rF * npmax);
-  take(sizeof(double) * rF * rF);
-  take(sizeof(double) * 4);
-  take(sizeof(double) * rF);
-  take(sizeof(double) * rF);
-  take(sizeof(int) * 4);
-  return b;
+size_t als_smem_bytes(int rows_cta, int rF, int npmax, int gsmax, int stages) {
+  return als_smem_layout(rows_cta, rF, npmax, gsmax, stages).total;
 }
 
-namespace {
-
-template <int NP>
-int launch_cluster(const AlsParams& prm, int cluster, size_t smem, cudaStream_t st) {
-  auto fn = als_cluster_kernel<NP>;
-  MLCP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (cluster > 8) MLCP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(prm.nvec * cluster);
-  cfg.blockDim = dim3(kThreads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = cluster;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  MLCP_CUDA_TRY(cudaLaunchKernelEx(&cfg, fn, prm));
-  return kOk;
+bool als_choose_shape(int nvec, int rGmax, int rFmax, int npmax, int gsmax, int num_sms, size_t smem_limit,
+                      AlsShape* out) {
+  // Cluster size: the largest power of two (<= 16) whose clusters for the
+  // whole batch still fit on the SMs at one CTA per SM; larger when the
+  // running products of a CTA's term range need more shared memory.  Ring
+  // depth: as many stages (2-6) as fit.
+  int cl = 1;
+  while (cl < 16 && cl * 2 * nvec <= num_sms) cl *= 2;
+  for (;;) {
+    const int rows = (rGmax + cl - 1) / cl;
+    for (int ns = 6; ns >= 2; --ns) {
+      const size_t b = als_smem_bytes(rows, rFmax, npmax, gsmax, ns);
+      if (b <= smem_limit) {
+        out->cluster = cl;
+        out->stages = ns;
+        out->rows_cta = rows;
+        out->smem = b;
+        return true;
+      }
+    }
+    if (cl >= 16) return false;
+    cl *= 2;
+  }
 }
 
-}  // namespace
-
-int als_launch(const AlsParams& p, int cluster, size_t smem, cudaStream_t st, cudaEvent_t t0, cudaEvent_t t1) {
+int als_launch(const AlsParams& p, size_t smem, cudaStream_t st, cudaEvent_t t0, cudaEvent_t t1) {
   int dev = 0, nsm = 0;
   MLCP_CUDA_TRY(cudaGetDevice(&dev));
   MLCP_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -549,12 +941,24 @@ int als_launch(const AlsParams& p, int cluster, size_t smem, cudaStream_t st, cu
   als_prep_kernel<<<(int)blocks, 256, 0, st>>>(p);
   MLCP_CUDA_TRY(cudaGetLastError());
   if (t0) MLCP_CUDA_TRY(cudaEventRecord(t0, st));
-  int rc;
-  if (p.npmax <= 16) rc = launch_cluster<16>(p, cluster, smem, st);
-  else if (p.npmax <= 32) rc = launch_cluster<32>(p, cluster, smem, st);
-  else rc = launch_cluster<64>(p, cluster, smem, st);
-  if (rc == kOk && t1) MLCP_CUDA_TRY(cudaEventRecord(t1, st));
-  return rc;
+  auto fn = als_cluster_kernel;
+  MLCP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (p.cluster > 8) MLCP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(p.nvec * p.cluster);
+  cfg.blockDim = dim3(kAlsThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = p.cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MLCP_CUDA_TRY(cudaLaunchKernelEx(&cfg, fn, p));
+  if (t1) MLCP_CUDA_TRY(cudaEventRecord(t1, st));
+  return kOk;
 }
 
 }  // namespace mlcp

@@ -119,22 +119,24 @@ constexpr int kMaxRank = 64;
 constexpr int kMaxBasis = 64;
 
 struct AlsPlan {
-  int D, nD, nDp, npmax, cluster, rows_cta_max, rFmax;
-  std::vector<int> off, offp;
+  int D, nD, nDp, nDg, npmax, gsmax, rFmax;
+  AlsShape shape;
+  std::vector<int> off, offp, offg;
   std::vector<long long> g_row_off, f_row_off, gm_off, sq_off;
-  long long total_rows, total_f, gm_floats, sq_doubles;
-  size_t smem;
+  long long total_rows, total_f, gm_floats, sq_total;
 };
 
 int plan_als(Context* ctx, int nvec, int ndof, const int* nbas, const int* rF, const int* rG, AlsPlan* P) {
-  if (nvec < 1 || ndof < 1) {
-    set_error("mlcp_als_batched: nvec (%d) and ndof (%d) must be positive", nvec, ndof);
+  if (nvec < 1 || ndof < 2) {
+    set_error("mlcp_als_batched: nvec (%d) must be positive and ndof (%d) at least 2", nvec, ndof);
     return kBadArgument;
   }
   P->D = ndof;
   P->off.assign(ndof + 1, 0);
   P->offp.assign(ndof + 1, 0);
+  P->offg.assign(ndof + 1, 0);
   P->npmax = 4;
+  P->gsmax = 4;
   for (int d = 0; d < ndof; ++d) {
     if (nbas[d] < 1 || nbas[d] > kMaxBasis) {
       set_error("mlcp_als_batched: nbas[%d] = %d outside [1, %d]", d, nbas[d], kMaxBasis);
@@ -142,10 +144,13 @@ int plan_als(Context* ctx, int nvec, int ndof, const int* nbas, const int* rF, c
     }
     P->off[d + 1] = P->off[d] + nbas[d];
     P->offp[d + 1] = P->offp[d] + round_up(nbas[d], 4);
+    P->offg[d + 1] = P->offg[d] + als_gstride(nbas[d]);
     P->npmax = std::max(P->npmax, round_up(nbas[d], 4));
+    P->gsmax = std::max(P->gsmax, als_gstride(nbas[d]));
   }
   P->nD = P->off[ndof];
   P->nDp = P->offp[ndof];
+  P->nDg = P->offg[ndof];
   P->g_row_off.resize(nvec);
   P->f_row_off.resize(nvec);
   P->gm_off.resize(nvec);
@@ -168,7 +173,7 @@ int plan_als(Context* ctx, int nvec, int ndof, const int* nbas, const int* rF, c
     P->sq_off[v] = sq;
     gr += rG[v];
     fr += rF[v];
-    gmo += (long long)rG[v] * P->nDp;
+    gmo += (long long)rG[v] * P->nDg;
     sq += (long long)rF[v] * rF[v] * ndof;
     rGmax = std::max(rGmax, rG[v]);
     P->rFmax = std::max(P->rFmax, rF[v]);
@@ -176,26 +181,12 @@ int plan_als(Context* ctx, int nvec, int ndof, const int* nbas, const int* rF, c
   P->total_rows = gr;
   P->total_f = fr;
   P->gm_floats = gmo;
-  P->sq_doubles = sq;
-  // cluster size: enough CTAs to cover the SMs, enough to fit the running
-  // products of a term range in shared memory
-  int cl = 1;
-  while (cl < 16 && cl * 2 * nvec <= ctx->num_sms) cl *= 2;
-  for (;;) {
-    const int rows = (rGmax + cl - 1) / cl;
-    const size_t smem = als_smem_bytes(rows, P->rFmax, P->npmax);
-    if (smem <= ctx->smem_optin) {
-      P->cluster = cl;
-      P->rows_cta_max = rows;
-      P->smem = smem;
-      break;
-    }
-    if (cl >= 16) {
-      set_error("mlcp_als_batched: rank-%d target with rank-%d F needs %zu bytes of shared memory per CTA "
-                "even with 16-CTA clusters (limit %zu)", rGmax, P->rFmax, smem, ctx->smem_optin);
-      return kTooLarge;
-    }
-    cl *= 2;
+  P->sq_total = sq;
+  if (!als_choose_shape(nvec, rGmax, P->rFmax, P->npmax, P->gsmax, ctx->num_sms, ctx->smem_optin, &P->shape)) {
+    set_error("mlcp_als_batched: rank-%d target with rank-%d F (padded basis %d) needs more than %zu bytes of "
+              "shared memory per CTA even with 16-CTA clusters",
+              rGmax, P->rFmax, P->gsmax, ctx->smem_optin);
+    return kTooLarge;
   }
   return kOk;
 }
@@ -218,20 +209,23 @@ int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
   AlsPlan P;
   int rc = plan_als(ctx, nvec, ndof, nbas, rF, rG, &P);
   if (rc) return rc;
+  const int CL = P.shape.cluster;
 
   // metadata block: ints then long longs (uploaded in one copy)
-  const size_t n_int = (size_t)(ndof) + 2 * (ndof + 1) + 2 * nvec;
+  const size_t n_int = (size_t)(ndof) + 3 * (ndof + 1) + 2 * nvec;
   const size_t n_ll = (size_t)6 * nvec;  // term, g_row, f_row, gm, sq, g_term offsets
   const size_t meta_bytes = align256(n_int * sizeof(int)) + n_ll * sizeof(long long);
   // workspace layout
   size_t bytes = 0;
   auto reserve = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
   const size_t o_meta = reserve(meta_bytes);
-  const size_t o_gm = reserve(sizeof(float) * (job.shared_w ? (long long)rG[0] * P.nDp : P.gm_floats));
+  const size_t o_gm = reserve(sizeof(float) * (job.shared_w ? (long long)rG[0] * P.nDg : P.gm_floats));
   const size_t o_gc = reserve(sizeof(float) * P.total_rows);
   const size_t o_f32 = reserve(sizeof(float) * P.total_f * P.nDp);
-  const size_t o_gram = reserve(sizeof(double) * P.sq_doubles);
-  const size_t o_suf = reserve(sizeof(double) * P.sq_doubles);
+  const size_t o_f32lo = reserve(sizeof(float) * P.total_f * P.nDp);
+  const size_t o_fcta = reserve(sizeof(float) * P.total_f * CL * P.nDp);
+  const size_t o_gram = reserve(sizeof(dw) * P.sq_total * CL);
+  const size_t o_suf = reserve(sizeof(dw) * P.sq_total * CL);
   const size_t o_status = reserve(sizeof(int) * nvec);
   void* ws = nullptr;
   rc = ensure_workspace(ctx, bytes, &ws);
@@ -246,11 +240,13 @@ int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
   int* p_nbas = hi;
   int* p_off = p_nbas + ndof;
   int* p_offp = p_off + (ndof + 1);
-  int* p_rF = p_offp + (ndof + 1);
+  int* p_offg = p_offp + (ndof + 1);
+  int* p_rF = p_offg + (ndof + 1);
   int* p_rG = p_rF + nvec;
   std::memcpy(p_nbas, nbas, sizeof(int) * ndof);
   std::memcpy(p_off, P.off.data(), sizeof(int) * (ndof + 1));
   std::memcpy(p_offp, P.offp.data(), sizeof(int) * (ndof + 1));
+  std::memcpy(p_offg, P.offg.data(), sizeof(int) * (ndof + 1));
   std::memcpy(p_rF, rF, sizeof(int) * nvec);
   std::memcpy(p_rG, rG, sizeof(int) * nvec);
   long long* p_term = hl;
@@ -258,12 +254,12 @@ int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
   long long* p_fro = p_gro + nvec;
   long long* p_gmo = p_fro + nvec;
   long long* p_sqo = p_gmo + nvec;
+  long long* p_gto = p_sqo + nvec;
   std::memcpy(p_term, term_off, sizeof(long long) * nvec);
   std::memcpy(p_gro, P.g_row_off.data(), sizeof(long long) * nvec);
   std::memcpy(p_fro, P.f_row_off.data(), sizeof(long long) * nvec);
   std::memcpy(p_gmo, P.gm_off.data(), sizeof(long long) * nvec);
   std::memcpy(p_sqo, P.sq_off.data(), sizeof(long long) * nvec);
-  long long* p_gto = p_sqo + nvec;
   for (int v = 0; v < nvec; ++v)
     p_gto[v] = job.shared_w ? 0 : (job.g_term_off ? job.g_term_off[v] : term_off[v] + rF[v]);
   if (job.shared_w) {
@@ -281,39 +277,47 @@ int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
   prm.ndof = ndof;
   prm.nD = P.nD;
   prm.nDp = P.nDp;
+  prm.nDg = P.nDg;
   prm.npmax = P.npmax;
+  prm.rf_max = P.rFmax;
+  prm.gsmax = P.gsmax;
   prm.nals = nals;
   prm.pen_factor = job.pen_factor;
-  prm.rows_cta_max = P.rows_cta_max;
+  prm.cluster = CL;
+  prm.stages = P.shape.stages;
+  prm.rows_cta_max = P.shape.rows_cta;
   prm.total_rows = P.total_rows;
   prm.total_f_terms = P.total_f;
   prm.nbas = d_int;
   prm.off = d_int + ndof;
   prm.offp = prm.off + (ndof + 1);
-  prm.rF = prm.offp + (ndof + 1);
+  prm.offg = prm.offp + (ndof + 1);
+  prm.rF = prm.offg + (ndof + 1);
   prm.rG = prm.rF + nvec;
   prm.term_off = d_ll;
   prm.g_row_off = d_ll + nvec;
   prm.f_row_off = d_ll + 2 * nvec;
   prm.gm_off = d_ll + 3 * nvec;
   prm.sq_off = d_ll + 4 * nvec;
+  prm.g_term_off = d_ll + 5 * nvec;
   prm.base = d_base;
   prm.coef = d_coef;
   prm.g_base = job.g_base ? job.g_base : d_base;
   prm.g_coef = job.g_coef ? job.g_coef : d_coef;
-  prm.g_term_off = d_ll + 5 * nvec;
   prm.shared_target = job.shared_w ? 1 : 0;
   prm.shared_w = job.shared_w;
   prm.gm = reinterpret_cast<float*>(w + o_gm);
   prm.gc = reinterpret_cast<float*>(w + o_gc);
   prm.f32 = reinterpret_cast<float*>(w + o_f32);
-  prm.gram = reinterpret_cast<double*>(w + o_gram);
-  prm.suf = reinterpret_cast<double*>(w + o_suf);
+  prm.f32lo = reinterpret_cast<float*>(w + o_f32lo);
+  prm.fcta = reinterpret_cast<float*>(w + o_fcta);
+  prm.gram = reinterpret_cast<dw*>(w + o_gram);
+  prm.suf = reinterpret_cast<dw*>(w + o_suf);
   prm.status = d_status ? d_status : reinterpret_cast<int*>(w + o_status);
   MLCP_CUDA_TRY(cudaMemsetAsync(prm.status, 0, sizeof(int) * nvec, st));
 
   ctx->timed = ctx->timing;
-  return als_launch(prm, P.cluster, P.smem, st, ctx->timing ? ctx->t0 : nullptr, ctx->timing ? ctx->t1 : nullptr);
+  return als_launch(prm, P.shape.smem, st, ctx->timing ? ctx->t0 : nullptr, ctx->timing ? ctx->t1 : nullptr);
 }
 
 // ---------------------------------------------------------------------------

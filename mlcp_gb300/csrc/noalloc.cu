@@ -69,13 +69,13 @@ int scratch_address(void** out) {
 int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_base, int nals, int* d_status,
         cudaStream_t st) {
   if (nals == 0) return kOk;
-  if (ndof < 1 || ndof > 1024 || rF < 1 || rF > 64 || rG < 1 || nals < 0 || !nbas || !d_coef || !d_base) {
+  if (ndof < 2 || ndof > 1024 || rF < 1 || rF > 64 || rG < 1 || nals < 0 || !nbas || !d_coef || !d_base) {
     set_error("mlcp_als_noalloc: bad arguments (ndof=%d rF=%d rG=%d nals=%d)", ndof, rF, rG, nals);
     return kBadArgument;
   }
-  int off[1025], offp[1025];
-  off[0] = offp[0] = 0;
-  int npmax = 4;
+  int off[1025], offp[1025], offg[1025];
+  off[0] = offp[0] = offg[0] = 0;
+  int npmax = 4, gsmax = 4;
   for (int d = 0; d < ndof; ++d) {
     if (nbas[d] < 1 || nbas[d] > 64) {
       set_error("mlcp_als_noalloc: nbas[%d] = %d outside [1, 64]", d, nbas[d]);
@@ -83,47 +83,45 @@ int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_bas
     }
     off[d + 1] = off[d] + nbas[d];
     offp[d + 1] = offp[d] + round_up(nbas[d], 4);
+    offg[d + 1] = offg[d] + als_gstride(nbas[d]);
     npmax = std::max(npmax, round_up(nbas[d], 4));
+    gsmax = std::max(gsmax, als_gstride(nbas[d]));
   }
-  const int nD = off[ndof], nDp = offp[ndof];
-
-  // scratch layout inside the fixed array
-  const size_t n_int = (size_t)ndof + 2 * (ndof + 1) + 2;
-  const size_t n_ll = 6;
-  size_t bytes = 0;
-  auto reserve = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
-  const size_t o_int = reserve(sizeof(int) * n_int);
-  const size_t o_ll = reserve(sizeof(long long) * n_ll);
-  const size_t o_gm = reserve(sizeof(float) * (size_t)rG * nDp);
-  const size_t o_gc = reserve(sizeof(float) * (size_t)rG);
-  const size_t o_f32 = reserve(sizeof(float) * (size_t)rF * nDp);
-  const size_t o_gram = reserve(sizeof(double) * (size_t)rF * rF * ndof);
-  const size_t o_suf = reserve(sizeof(double) * (size_t)rF * rF * ndof);
-  const size_t o_status = reserve(sizeof(int));
-  if (bytes > kNoAllocScratchBytes) {
-    set_error("mlcp_als_noalloc: a rank-%d target over %d modes (%d padded basis functions) needs %zu bytes of "
-              "scratch; the fixed scratch array holds %zu bytes (use mlcp_als_batched instead)",
-              rG, ndof, nDp, bytes, kNoAllocScratchBytes);
-    return kTooLarge;
-  }
+  const int nD = off[ndof], nDp = offp[ndof], nDg = offg[ndof];
 
   // launch shape: a cluster of up to 16 CTAs owning slices of the target terms
   int dev = 0, nsm = 0, optin = 0;
   MLCP_CUDA_TRY(cudaGetDevice(&dev));
   MLCP_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   MLCP_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  int cl = 1;
-  while (cl < 16 && cl * 2 <= nsm) cl *= 2;
-  int rows = (rG + cl - 1) / cl;
-  size_t smem = als_smem_bytes(rows, rF, npmax);
-  while (smem > (size_t)optin && cl < 16) {
-    cl *= 2;
-    rows = (rG + cl - 1) / cl;
-    smem = als_smem_bytes(rows, rF, npmax);
+  AlsShape shape;
+  if (!als_choose_shape(1, rG, rF, npmax, gsmax, nsm, (size_t)optin, &shape)) {
+    set_error("mlcp_als_noalloc: rank-%d target with rank-%d F needs more shared memory per CTA than %d bytes",
+              rG, rF, optin);
+    return kTooLarge;
   }
-  if (smem > (size_t)optin) {
-    set_error("mlcp_als_noalloc: rank-%d target with rank-%d F needs %zu bytes of shared memory per CTA (limit %d)",
-              rG, rF, smem, optin);
+  const int CL = shape.cluster;
+
+  // scratch layout inside the fixed array
+  const size_t n_int = (size_t)ndof + 3 * (ndof + 1) + 2;
+  const size_t n_ll = 6;
+  const size_t sq = (size_t)rF * rF * ndof;
+  size_t bytes = 0;
+  auto reserve = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
+  const size_t o_int = reserve(sizeof(int) * n_int);
+  const size_t o_ll = reserve(sizeof(long long) * n_ll);
+  const size_t o_gm = reserve(sizeof(float) * (size_t)rG * nDg);
+  const size_t o_gc = reserve(sizeof(float) * (size_t)rG);
+  const size_t o_f32 = reserve(sizeof(float) * (size_t)rF * nDp);
+  const size_t o_f32lo = reserve(sizeof(float) * (size_t)rF * nDp);
+  const size_t o_fcta = reserve(sizeof(float) * (size_t)rF * CL * nDp);
+  const size_t o_gram = reserve(sizeof(dw) * sq * CL);
+  const size_t o_suf = reserve(sizeof(dw) * sq * CL);
+  const size_t o_status = reserve(sizeof(int));
+  if (bytes > kNoAllocScratchBytes) {
+    set_error("mlcp_als_noalloc: a rank-%d target over %d modes (%d padded basis functions) needs %zu bytes of "
+              "scratch; the fixed scratch array holds %zu bytes (use mlcp_als_batched instead)",
+              rG, ndof, nDg, bytes, kNoAllocScratchBytes);
     return kTooLarge;
   }
 
@@ -133,13 +131,14 @@ int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_bas
   char* w = static_cast<char*>(base_ptr);
 
   // metadata from the stack (pageable copy: the call returns once it is staged)
-  int hi[1024 + 2 * 1025 + 2];
+  int hi[1024 + 3 * 1025 + 2];
   long long hl[6];
   std::memcpy(hi, nbas, sizeof(int) * ndof);
   std::memcpy(hi + ndof, off, sizeof(int) * (ndof + 1));
   std::memcpy(hi + 2 * ndof + 1, offp, sizeof(int) * (ndof + 1));
-  hi[3 * ndof + 2] = rF;
-  hi[3 * ndof + 3] = rG;
+  std::memcpy(hi + 3 * ndof + 2, offg, sizeof(int) * (ndof + 1));
+  hi[4 * ndof + 3] = rF;
+  hi[4 * ndof + 4] = rG;
   hl[0] = 0;   // F terms start at term 0
   hl[1] = 0;   // first target row
   hl[2] = 0;   // first F row
@@ -158,17 +157,23 @@ int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_bas
   prm.ndof = ndof;
   prm.nD = nD;
   prm.nDp = nDp;
+  prm.nDg = nDg;
   prm.npmax = npmax;
+  prm.rf_max = rF;
+  prm.gsmax = gsmax;
   prm.nals = nals;
   prm.pen_factor = 1.0e-10;
-  prm.rows_cta_max = rows;
+  prm.cluster = CL;
+  prm.stages = shape.stages;
+  prm.rows_cta_max = shape.rows_cta;
   prm.total_rows = rG;
   prm.total_f_terms = rF;
   prm.nbas = d_int;
   prm.off = d_int + ndof;
   prm.offp = d_int + 2 * ndof + 1;
-  prm.rF = d_int + 3 * ndof + 2;
-  prm.rG = d_int + 3 * ndof + 3;
+  prm.offg = d_int + 3 * ndof + 2;
+  prm.rF = d_int + 4 * ndof + 3;
+  prm.rG = d_int + 4 * ndof + 4;
   prm.term_off = d_ll;
   prm.g_row_off = d_ll + 1;
   prm.f_row_off = d_ll + 2;
@@ -184,10 +189,12 @@ int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_bas
   prm.gm = reinterpret_cast<float*>(w + o_gm);
   prm.gc = reinterpret_cast<float*>(w + o_gc);
   prm.f32 = reinterpret_cast<float*>(w + o_f32);
-  prm.gram = reinterpret_cast<double*>(w + o_gram);
-  prm.suf = reinterpret_cast<double*>(w + o_suf);
+  prm.f32lo = reinterpret_cast<float*>(w + o_f32lo);
+  prm.fcta = reinterpret_cast<float*>(w + o_fcta);
+  prm.gram = reinterpret_cast<dw*>(w + o_gram);
+  prm.suf = reinterpret_cast<dw*>(w + o_suf);
   prm.status = status;
-  return als_launch(prm, cl, smem, st);
+  return als_launch(prm, shape.smem, st);
 }
 
 }  // namespace

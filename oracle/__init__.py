@@ -62,6 +62,7 @@ def lib() -> ctypes.CDLL:
                                       _I, _I, ctypes.c_int, ctypes.c_int]
         L.orc_set_penalty_factor.argtypes = [ctypes.c_double]
         L.orc_set_cycle_penalties.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.orc_set_rhs_fp32.argtypes = [ctypes.c_int]
         L.orc_sygv.restype = ctypes.c_int
         L.orc_sygv.argtypes = [ctypes.c_int, _D, _D, _D, _D]
     return _lib
@@ -186,6 +187,12 @@ def set_cycle_penalties(mvp: float = PEN_FP64, gs: float = PEN_FP64, upd: float 
 
 def set_penalty_factor(f: float) -> None:
     lib().orc_set_penalty_factor(f)
+
+
+def set_rhs_fp32(on: bool) -> None:
+    """Round every ALS right-hand side to FP32 before its solve (test knob:
+    the drift of an FP64 trajectory under FP32-level noise in b)."""
+    lib().orc_set_rhs_fp32(1 if on else 0)
 
 
 def sygv(A: np.ndarray, B: np.ndarray):

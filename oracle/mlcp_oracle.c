@@ -339,6 +339,12 @@ static void work_init(work_t *w, int rk, int nmax, int nblocmax) {
 }
 static void work_free(work_t *w) { free(w->BB); free(w->BBk); free(w->bjk); free(w->tmp); free(w->ipiv); }
 
+/* Test knob (no counterpart in the reference): when set, each ALS
+ * right-hand side is rounded to FP32 before the solve, to measure how far an
+ * FP64 ALS trajectory moves under FP32-level noise in b. */
+static int g_rhs_fp32 = 0;
+void orc_set_rhs_fp32(int on) { g_rhs_fp32 = on; }
+
 static void add_penalty(double *BB, int rk, double pen) {
   for (int i = 0; i < rk; ++i) BB[i + (size_t)i * rk] += pen;
 }
@@ -366,6 +372,8 @@ static void iterate_als(cpv *Q, int rk, int nbloc, int nals, work_t *W) {
       }
       pstot(&F, &F, W->BB, j, 0, 0);
       add_penalty(W->BB, rk, pen);
+      if (g_rhs_fp32)
+        for (int e = 0; e < rk * n; ++e) W->bjk[e] = (double)(float)W->bjk[e];
       lu_solve(W->BB, W->bjk, rk, n, W->ipiv);
       replace_with_solution(&F, W->bjk, j);
       normonebase(&F, j);

@@ -75,6 +75,11 @@ void orc_als_batched(int nvec, double *const *coef, double *const *base, const i
 void orc_set_penalty_factor(double f);
 void orc_set_cycle_penalties(double mvp, double gs, double upd);
 
+/* Test knob: round every ALS right-hand side to FP32 before its solve (0 off,
+ * the default).  Measures the drift of an FP64 ALS trajectory under
+ * FP32-level noise in b, the precision of the GPU's contractions. */
+void orc_set_rhs_fp32(int on);
+
 /* Generalised symmetric eigenproblem A x = lambda B x (lower triangles of
  * column-major A, B used).  Eigenvalues ascending; X column-major with
  * X^T B X = I and the largest-magnitude entry of each column positive. */

@@ -1,10 +1,21 @@
 """GPU parity of the explicit-target ALS against the FP64 oracle.
 
-Tolerance (FP32/3xTF32-class contractions, FP64 normal-equation solves): the
-relative residual ||F - G|| / ||G|| of the GPU result agrees with the
-oracle's to within 1e-6 (absolute difference of the relative residuals), and
-the reduced vectors agree as functions: ||F_gpu - F_oracle|| / ||F_oracle||
-<= 1e-4.
+The GPU contracts in FP32 (24-bit) and solves the normal equations in
+double-word arithmetic (~48 bits).  Two checks per case:
+
+* One sweep from a common state (the GPU's state after nals-1 sweeps): the
+  relative residuals ||F - G|| / ||G|| of GPU and oracle agree to
+  SWEEP_RES_TOL = 2e-7 (absolute difference) and the two results agree as
+  functions, ||F_gpu - F_oracle|| / ||F_oracle|| <= SWEEP_VEC_TOL = 1e-5.
+  This is the per-step precision of the FP32 contractions.
+* The whole nals-sweep trajectory: residuals agree to TRAJ_RES_TOL = 5e-5
+  and the vectors to TRAJ_VEC_TOL = 5e-4.  ALS trajectories of random
+  low-rank fits converge slowly and carry perturbations forward: the FP64
+  oracle itself, with nothing changed but its right-hand sides rounded to
+  FP32 before each solve, moves by 1.7e-6 in residual and 6e-5 in distance
+  after four sweeps on the 5-mode basis-16 case (pinned on the CPU in
+  test_oracle.py::test_oracle_als_drift_under_fp32_rhs), and the GPU's
+  FP32 sums over the target terms are noisier than one rounding.
 """
 import numpy as np
 import pytest
@@ -12,8 +23,10 @@ import pytest
 import oracle
 from mlcp_gb300 import als, workloads
 
-RES_TOL = 1e-6
-VEC_TOL = 1e-4
+SWEEP_RES_TOL = 2e-7
+SWEEP_VEC_TOL = 1e-5
+TRAJ_RES_TOL = 5e-5
+TRAJ_VEC_TOL = 5e-4
 
 
 def rel_residual(fc, fb, gc, gb, nbas):
@@ -46,17 +59,25 @@ CASES = [
     (3, 6, 12, [8, 5, 8], [64, 40, 17], 10),  # rank 17 is padded with zero weights for the oracle
     (2, 30, 12, 20, 200, 3),
     (4, 3, [9, 16, 7], 6, 30, 8),
+    (40, 6, 10, 10, 2000, 3),  # 2-CTA clusters, 8 tiles per CTA: the staging ring wraps
+    (2, 5, [20, 12, 40, 7, 17], 9, 150, 4),  # bases above 16: right-hand sides in several column rounds
+    (1, 3, [6, 5, 4], 64, 256, 3),  # the largest F rank
+    (2, 2, [10, 14], 5, 60, 6),  # two modes: the previous and the next mode coincide
 ]
 
 
-@pytest.mark.gpu
-@pytest.mark.parametrize("case", CASES)
-def test_als_matches_oracle(case, cuda_device):
-    nvec, D, n, rF, rG, nals = case
-    batch = workloads.als_batch(nvec, D, n, rF, rG, seed=11 + nvec)
-    gc_, gb_, status = run_gpu(batch, nals, cuda_device)
-    assert not status.any()
-    for v in range(nvec):
+def with_f_terms(batch, coef, base):
+    """The batch with its F terms replaced by those of (coef, base)."""
+    c, b = batch.coef.copy(), batch.base.copy()
+    for v in range(batch.nvec):
+        t0, f = int(batch.term_off[v]), int(batch.rF[v])
+        c[t0:t0 + f] = coef[t0:t0 + f]
+        b[t0:t0 + f] = base[t0:t0 + f]
+    return workloads.AlsBatch(nbas=batch.nbas, rF=batch.rF, rG=batch.rG, term_off=batch.term_off, coef=c, base=b)
+
+
+def compare(batch, gc_, gb_, nals, res_tol, vec_tol):
+    for v in range(batch.nvec):
         c0, b0 = batch.vector(v)
         f = int(batch.rF[v])
         pc, pb, rGp = oracle.pad_target(c0, b0, f, int(batch.rG[v]))
@@ -67,10 +88,34 @@ def test_als_matches_oracle(case, cuda_device):
         r_orc = rel_residual(oc, ob, gcoef, gbase, batch.nbas)
         r_gpu = rel_residual(fc, fb, gcoef, gbase, batch.nbas)
         dist = rel_distance(fc, fb, oc, ob, batch.nbas)
-        assert abs(r_gpu - r_orc) <= RES_TOL, (v, r_gpu, r_orc)
-        assert dist <= VEC_TOL, (v, dist)
+        assert abs(r_gpu - r_orc) <= res_tol, (v, r_gpu, r_orc)
+        assert dist <= vec_tol, (v, dist)
         # target terms are untouched
         np.testing.assert_array_equal(gb_[t0 + f:t0 + f + int(batch.rG[v])], gbase)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_als_sweep_matches_oracle(case, cuda_device):
+    nvec, D, n, rF, rG, nals = case
+    batch = workloads.als_batch(nvec, D, n, rF, rG, seed=11 + nvec)
+    if nals > 1:
+        sc, sb, status = run_gpu(batch, nals - 1, cuda_device)
+        assert not status.any()
+        batch = with_f_terms(batch, sc, sb)
+    gc_, gb_, status = run_gpu(batch, 1, cuda_device)
+    assert not status.any()
+    compare(batch, gc_, gb_, 1, SWEEP_RES_TOL, SWEEP_VEC_TOL)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES)
+def test_als_trajectory_tracks_oracle(case, cuda_device):
+    nvec, D, n, rF, rG, nals = case
+    batch = workloads.als_batch(nvec, D, n, rF, rG, seed=11 + nvec)
+    gc_, gb_, status = run_gpu(batch, nals, cuda_device)
+    assert not status.any()
+    compare(batch, gc_, gb_, nals, TRAJ_RES_TOL, TRAJ_VEC_TOL)
 
 
 @pytest.mark.gpu
@@ -80,8 +125,18 @@ def test_alscpp_abi_matches_oracle(cuda_device):
     c, b = c0.copy(), b0.copy()
     als.alscpp(c, b, batch.nbas, 4, 24, 6)
     oc, ob = oracle.als(c0, b0, batch.nbas, 4, 24, 6)
-    assert rel_distance(c[:4], b[:4], oc, ob, batch.nbas) <= VEC_TOL
+    assert rel_distance(c[:4], b[:4], oc, ob, batch.nbas) <= TRAJ_VEC_TOL
     np.testing.assert_array_equal(b[4:], b0[4:])
+
+
+@pytest.mark.gpu
+def test_als_rejects_single_mode(cuda_device):
+    batch = workloads.als_batch(1, 2, 5, 3, 9, seed=3)
+    import torch
+    coef = torch.from_numpy(batch.coef.copy()).to(cuda_device)
+    base = torch.from_numpy(batch.base.copy()).to(cuda_device)
+    with pytest.raises(Exception, match="ndof"):
+        als.reduce_batched(coef, base, [10], batch.rF, batch.rG, batch.term_off, 2)
 
 
 @pytest.mark.gpu

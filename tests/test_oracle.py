@@ -70,6 +70,39 @@ def test_als_monotone_residual():
         prev = r
 
 
+def test_oracle_als_drift_under_fp32_rhs():
+    """How far an FP64 ALS trajectory moves when nothing changes but its
+    right-hand sides being rounded to FP32 before each solve: tiny after one
+    sweep, about 1e-6 in relative residual and 6e-5 in distance after four
+    sweeps on this slowly converging rank-9 fit of a rank-150 target.  The GPU
+    parity tests bound multi-sweep drift from this measurement."""
+    from mlcp_gb300 import workloads
+
+    def cp_dot(ab, ac, bb, bc):
+        return oracle.cp_dot(ab, ac, bb, bc, batch.nbas)
+
+    def rel(ac, ab, bc, bb):
+        aa, bbv, x = cp_dot(ab, ac, ab, ac), cp_dot(bb, bc, bb, bc), cp_dot(ab, ac, bb, bc)
+        return np.sqrt(max(aa + bbv - 2 * x, 0.0) / bbv)
+
+    batch = workloads.als_batch(2, 5, 16, 9, 150, seed=13)
+    c0, b0 = batch.vector(1)
+    pc, pb, rGp = oracle.pad_target(c0, b0, 9, 150)
+    drift = {}
+    try:
+        for nals in (1, 4):
+            oracle.set_rhs_fp32(False)
+            oc, ob = oracle.als(pc, pb, batch.nbas, 9, rGp, nals)
+            oracle.set_rhs_fp32(True)
+            qc, qb = oracle.als(pc, pb, batch.nbas, 9, rGp, nals)
+            res = abs(rel(oc, ob, c0[9:], b0[9:]) - rel(qc, qb, c0[9:], b0[9:]))
+            drift[nals] = (res, rel(qc, qb, oc, ob))
+    finally:
+        oracle.set_rhs_fp32(False)
+    assert drift[1][0] < 1e-8 and drift[1][1] < 1e-6
+    assert drift[4][0] > 5e-7 and drift[4][1] > 2e-5
+
+
 def test_sygv_matches_dense():
     rng = np.random.default_rng(2)
     n = 7
