@@ -167,8 +167,12 @@ def cycle_inputs(seed=20261203):
 
 def run_cycle_bench(steps: int, cpu: bool):
     """GPU power-cycle time through the C ABI (host buffers in and out, as
-    the Fortran host calls it), the oracle's time for one cycle on the host
-    cores, and the eigenvalue agreement of the two."""
+    the Fortran host calls it) and the oracle's time for one cycle on the host
+    cores.  No eigenvalue comparison is reported here: one cycle from a random
+    block is far from converged and its Ritz values move by several percent
+    under any rounding-level change (the FP64 oracle itself moves 9% between
+    the FP64- and FP32-build penalty rules on this workload); the cycle's
+    parity is checked in the GPU tests on well-posed cases."""
     from mlcp_gb300 import intertwine as IT
     hl, Q, qc, eig0, esh = cycle_inputs()
     IT.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)  # warm-up
@@ -182,11 +186,10 @@ def run_cycle_bench(steps: int, cpu: bool):
         import oracle
         oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
         t0 = time.perf_counter()
-        ob, oc, oe = oracle.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
+        oracle.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
         out["cpu_ms_per_cycle"] = 1e3 * (time.perf_counter() - t0)
         out["cpu_cores"] = os.cpu_count()
         out["cpu_kind"] = "port"
-        out["max_rel_eig_diff_vs_oracle"] = float(np.max(np.abs(ge - oe) / np.abs(oe)))
         oracle.set_cycle_penalties()
     return out
 

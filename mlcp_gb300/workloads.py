@@ -65,3 +65,37 @@ def als_batch(nvec: int, D: int, n, rF, rG, seed: int = ALS_SEED) -> AlsBatch:
         base[t0:t0 + f] = G[:f]
         coef[t0:t0 + f] = cg[:f]
     return AlsBatch(nbas=nbas, rF=rFa, rG=rGa, term_off=term_off, coef=coef, base=base)
+
+
+def main(argv=None) -> int:
+    """Run one batched reduction of a seeded synthetic batch on the GPU (the
+    command the profiling summaries use):
+    python -m mlcp_gb300.workloads --nvec 64 --ndof 30 --nbas 12 --rf 20 --rg 3200 --sweeps 10"""
+    import argparse
+
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--nvec", type=int, default=64)
+    ap.add_argument("--ndof", type=int, default=30)
+    ap.add_argument("--nbas", type=int, default=12)
+    ap.add_argument("--rf", type=int, default=20)
+    ap.add_argument("--rg", type=int, default=3200)
+    ap.add_argument("--sweeps", type=int, default=10)
+    a = ap.parse_args(argv)
+    import torch
+
+    from mlcp_gb300 import als
+
+    dev = torch.device("cuda", 0)
+    b = als_batch(a.nvec, a.ndof, a.nbas, a.rf, a.rg)
+    coef = torch.from_numpy(b.coef).to(dev)
+    base = torch.from_numpy(b.base).to(dev)
+    status = torch.zeros(b.nvec, dtype=torch.int32, device=dev)
+    als.reduce_batched(coef, base, b.nbas, b.rF, b.rG, b.term_off, a.sweeps, status=status)
+    torch.cuda.synchronize()
+    bad = int(status.ne(0).sum().item())
+    print(f"reduced {b.nvec} vectors ({a.sweeps} sweeps); status flags on {bad}")
+    return 1 if bad else 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
