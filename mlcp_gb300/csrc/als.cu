@@ -167,7 +167,8 @@ constexpr int kWaitLimit = 1 << 20;
 
 struct AlsSmem {
   int rFp, ldP, stage_floats;
-  size_t bar, done, issued, fillno, flags, ring, P, cw, fa, fb, bred, bpart, BB, X, L, sk, dinv, u, nrm, misc, total;
+  size_t bar, done, issued, fillno, flags, ring, P, cw, fa, fb, bred, bpart, BB, X, L, sk, dinv, u, nrm, misc, gi, b0, res,
+      red, total;
 };
 
 __host__ __device__ inline size_t carve(size_t* cursor, size_t bytes, size_t align) {
@@ -202,6 +203,10 @@ __host__ __device__ inline AlsSmem als_smem_layout(int rows_cta, int rF, int npm
   s.u = carve(&o, sizeof(dw) * (size_t)rF, 16);
   s.nrm = carve(&o, sizeof(dw) * (size_t)rF, 16);
   s.misc = carve(&o, sizeof(dw) * 4, 16);
+  s.gi = carve(&o, sizeof(float) * 2 * (size_t)rF * rF, 16);
+  s.b0 = carve(&o, sizeof(dw) * (size_t)rF * npmax, 16);
+  s.res = carve(&o, sizeof(dw) * (size_t)rF * npmax, 16);
+  s.red = carve(&o, sizeof(float) * 4, 16);
   s.total = o;
   return s;
 }
@@ -225,6 +230,10 @@ struct Cta {
   float* bred; // [warps][64] per-warp partial right-hand sides
   float* bpart;  // [2][rFp][npmax] CTA partial right-hand side (read by the cluster)
   dw *BB, *X, *L, *sk, *dinv, *u, *nrm, *misc;
+  float* gi;   // [2][rF*rF] FP32 Gauss-Jordan buffers (the inverse ends in one)
+  dw* b0;      // [rF][npmax] right-hand side (kept for the refinement residuals)
+  dw* res;     // [rF][npmax] refinement residual
+  float* red;  // [2][2] block maxima of the last refinement correction and of |X|
   const float* gm;  // this vector's FP32 target copy
   float* fcta;      // this CTA's FP32 factor copy [rF][nDp]
   dw* gram;         // this CTA's Grams [D][rF][rF]
@@ -331,8 +340,9 @@ __device__ __forceinline__ void tile_dots(const float* tile, int gs, const float
 }
 
 // prod over modes d not in {ex1, ex2} of <G_j^d, F_i^d>, straight from the
-// FP32 copies in global memory (unsafe-division fallback; rare).
-__device__ float rebuild_product(const Cta& c, const AlsParams& p, int j, int i, int ex1, int ex2) {
+// FP32 copies in global memory (unsafe-division fallback; rare, so kept out of
+// line to keep the hot loops small).
+__device__ __noinline__ float rebuild_product(const Cta& c, const AlsParams& p, int j, int i, int ex1, int ex2) {
   float s = 1.f;
   for (int d = 0; d < c.D; ++d) {
     if (d == ex1 || d == ex2) continue;
@@ -374,6 +384,48 @@ __device__ void product_pass(const Cta& c, const AlsParams& p, unsigned seq, int
       const float* tile = c.ring + (size_t)(g % (unsigned)c.stages) * c.stage_floats;
       float po[4][4];
       tile_dots(tile, gs, c.fa + iq * 4 * c.gsmax, c.gsmax, np, c.lane, po);
+      // every load before any store: a shared-memory store would order each
+      // later load behind it (the compiler cannot prove they do not alias)
+      float pv[4][4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        const int j = T * kAlsTileRows + c.lane + 32 * a;
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+          const int i = iq * 4 + cc;
+          pv[a][cc] = (j < c.nrows && i < c.rF) ? c.P[(size_t)i * c.ldP + j] : 0.f;
+        }
+      }
+      // quotients without any call in the unrolled loop (a call would keep
+      // the sixteen independent chains from overlapping); the rare unsafe
+      // ones are marked and rebuilt afterwards
+      unsigned rebuild = 0u;
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+          if (!divide) {
+            pv[a][cc] *= po[a][cc];
+          } else {
+            const float x = pv[a][cc];
+            const float qv = div_nr(x, po[a][cc]);
+            const bool ok = fabsf(x) >= FLT_MIN && fabsf(qv) <= FLT_MAX;  // also catches a zero divisor
+            const int j = T * kAlsTileRows + c.lane + 32 * a, i = iq * 4 + cc;
+            if (!ok && j < c.nrows && i < c.rF) rebuild |= 1u << (a * 4 + cc);
+            pv[a][cc] = qv;
+          }
+        }
+      while (rebuild) {
+        const int bit = __ffs(rebuild) - 1;
+        rebuild &= rebuild - 1;
+        const int a = bit >> 2, cc = bit & 3;
+        const float qv = rebuild_product(c, p, T * kAlsTileRows + c.lane + 32 * a, iq * 4 + cc, ex, d);
+#pragma unroll
+        for (int a2 = 0; a2 < 4; ++a2)
+#pragma unroll
+          for (int c2 = 0; c2 < 4; ++c2)
+            if (a2 * 4 + c2 == bit) pv[a2][c2] = qv;
+      }
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
         const int j = T * kAlsTileRows + c.lane + 32 * a;
@@ -381,21 +433,7 @@ __device__ void product_pass(const Cta& c, const AlsParams& p, unsigned seq, int
 #pragma unroll
         for (int cc = 0; cc < 4; ++cc) {
           const int i = iq * 4 + cc;
-          if (i >= c.rF) continue;
-          float* st = c.P + (size_t)i * c.ldP + j;
-          if (!divide) {
-            *st *= po[a][cc];
-          } else {
-            const float pv = *st, dv = po[a][cc];
-            float qv = 0.f;
-            bool ok = dv != 0.f && fabsf(pv) >= FLT_MIN && fabsf(pv) <= FLT_MAX;
-            if (ok) {
-              qv = div_nr(pv, dv);
-              ok = fabsf(qv) <= FLT_MAX;
-            }
-            if (!ok) qv = rebuild_product(c, p, j, i, ex, d);
-            *st = qv;
-          }
+          if (i < c.rF) c.P[(size_t)i * c.ldP + j] = pv[a][cc];
         }
       }
     }
@@ -410,20 +448,32 @@ __device__ __forceinline__ void item_b0(const Cta& c, const float* tp, int gsp, 
                                         int T, int iq, float (&acc)[4][MW]) {
   float pn[4][4];
   tile_dots(tp, gsp, c.fb + iq * 4 * c.gsmax, c.gsmax, npp, c.lane, pn);
-  float w[4][4];
+  // every load before any store (see product_pass), then the products, then
+  // the stores; w ends as the weighted products cG_j P(j,i)
+  float w[4][4], cwj[4];
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
     const int j = T * kAlsTileRows + c.lane + 32 * a;
     const bool live = j < c.nrows;
-    const float cwj = live ? c.cw[j] : 0.f;
+    cwj[a] = live ? c.cw[j] : 0.f;
 #pragma unroll
-    for (int cc = 0; cc < 4; ++cc) {
-      float* st = c.P + (size_t)(iq * 4 + cc) * c.ldP + j;
-      const float pv = live ? *st * pn[a][cc] : 0.f;
-      if (live) *st = pv;
-      w[a][cc] = cwj * pv;
-    }
+    for (int cc = 0; cc < 4; ++cc) w[a][cc] = live ? c.P[(size_t)(iq * 4 + cc) * c.ldP + j] : 0.f;
   }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) w[a][cc] *= pn[a][cc];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int j = T * kAlsTileRows + c.lane + 32 * a;
+    if (j < c.nrows)
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) c.P[(size_t)(iq * 4 + cc) * c.ldP + j] = w[a][cc];
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) w[a][cc] *= cwj[a];
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
     float4 g4[MW / 4];
@@ -684,6 +734,189 @@ __device__ void dw_new_gram(const Cta& c, int k, int nk) {
   }
 }
 
+// Walk over the entries e = tid, tid + 128, ... of a matrix with n rows
+// (column-major), tracking (row, column) = (e mod n, e div n) without dividing.
+struct Walk {
+  int i, j, di, dj, n;
+};
+__device__ __forceinline__ Walk walk_start(int t, int n) {
+  return Walk{t % n, t / n, kSolverThreads % n, kSolverThreads / n, n};
+}
+__device__ __forceinline__ void walk_next(Walk& w) {
+  w.i += w.di;
+  w.j += w.dj;
+  if (w.i >= w.n) {
+    w.i -= w.n;
+    w.j += 1;
+  }
+}
+
+// Entries a solver thread handles per batch (operands loaded before any store).
+constexpr int kSolveBatch = 4;
+
+// FP32 Gauss-Jordan inverse of the symmetric positive definite n x n matrix
+// given by the high parts of A (column-major), without pivoting (its pivots
+// are the positive Schur-complement diagonals).  Two buffers alternate so each
+// elimination step reads the previous one and needs one barrier; a thread
+// loads the operands of up to four entries before it stores any (a store
+// would otherwise order every later shared-memory load behind it).  Returns
+// the buffer holding the inverse; *ok is false when a pivot is not positive.
+__device__ const float* gj_inverse(const dw* A, int n, float* gi, bool* ok) {
+  const int t = threadIdx.x, nn = n * n;
+  for (int e = t; e < nn; e += kSolverThreads) gi[e] = A[e].hi;
+  solver_sync();
+  int cur = 0;
+  bool good = true;
+  for (int k = 0; k < n; ++k) {
+    const float* s = gi + cur * nn;
+    float* d = gi + (cur ^ 1) * nn;
+    const float piv = s[k + k * n];
+    good = good && piv > 0.f;
+    float pk = f_rcp_approx(piv);
+    pk = pk * fmaf(-piv, pk, 2.0f);
+    Walk w = walk_start(t, n);
+    for (int e0 = t; e0 < nn; e0 += kSolveBatch * kSolverThreads) {
+      float a[kSolveBatch], b[kSolveBatch], x[kSolveBatch];
+      int ii[kSolveBatch], jj[kSolveBatch];
+#pragma unroll
+      for (int q = 0; q < kSolveBatch; ++q) {
+        ii[q] = w.i;
+        jj[q] = w.j;
+        if (e0 + q * kSolverThreads < nn) {
+          a[q] = s[w.i + k * n];
+          b[q] = s[k + w.j * n];
+          x[q] = s[e0 + q * kSolverThreads];
+        }
+        walk_next(w);
+      }
+#pragma unroll
+      for (int q = 0; q < kSolveBatch; ++q) {
+        const int e = e0 + q * kSolverThreads;
+        if (e >= nn) continue;
+        const float ta = a[q] * pk;
+        float v = fmaf(-ta, b[q], x[q]);
+        if (ii[q] == k) v = (jj[q] == k) ? pk : b[q] * pk;
+        else if (jj[q] == k) v = -ta;
+        d[e] = v;
+      }
+    }
+    cur ^= 1;
+    solver_sync();
+  }
+  *ok = good;
+  return gi + cur * nn;
+}
+
+// Refinement rounds before falling back to the double-word LDL^T.
+constexpr int kRefineMax = 4;
+
+// X = A^-1 B (A n x n double-word, B and X n x nrhs, ld n) by iterative
+// refinement preconditioned with the FP32 inverse: X = inv B, then
+// X += inv (B - A X) with the residual formed in double-word, until the last
+// correction is below 1e-10 of max |X|.  Returns whether that happened within
+// kRefineMax rounds.  Each thread computes up to four entries in registers
+// before storing them.
+__device__ bool refine_solve(const dw* A, int n, const dw* B, dw* X, int nrhs, const float* inv, dw* R, float* red) {
+  const int t = threadIdx.x, nr = n * nrhs;
+  // X = inv * B
+  {
+    Walk w = walk_start(t, n);
+    for (int e0 = t; e0 < nr; e0 += kSolveBatch * kSolverThreads) {
+      int ii[kSolveBatch], jj[kSolveBatch];
+      float acc[kSolveBatch];
+#pragma unroll
+      for (int q = 0; q < kSolveBatch; ++q) {
+        ii[q] = w.i;
+        jj[q] = w.j;
+        acc[q] = 0.f;
+        walk_next(w);
+      }
+      for (int j = 0; j < n; ++j)
+#pragma unroll
+        for (int q = 0; q < kSolveBatch; ++q)
+          if (e0 + q * kSolverThreads < nr) acc[q] = fmaf(inv[ii[q] + j * n], B[j + jj[q] * n].hi, acc[q]);
+#pragma unroll
+      for (int q = 0; q < kSolveBatch; ++q)
+        if (e0 + q * kSolverThreads < nr) X[e0 + q * kSolverThreads] = dw_make(acc[q]);
+    }
+  }
+  bool ok = false;
+  for (int round = 0; round < kRefineMax && !ok; ++round) {
+    float* rd = red + 2 * (round & 1);
+    if (t == 0) rd[0] = rd[1] = 0.f;
+    solver_sync();
+    // R = B - A X (double-word); two chains per entry (even and odd j)
+    {
+      Walk w = walk_start(t, n);
+      for (int e0 = t; e0 < nr; e0 += 2 * kSolverThreads) {
+        int ii[2], jj[2];
+        dw a0[2], a1[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          ii[q] = w.i;
+          jj[q] = w.j;
+          a0[q] = (e0 + q * kSolverThreads < nr) ? B[e0 + q * kSolverThreads] : dw_make(0.f);
+          a1[q] = dw_make(0.f);
+          walk_next(w);
+        }
+        const bool two = e0 + kSolverThreads < nr;
+        int j = 0;
+        for (; j + 1 < n; j += 2) {
+          a0[0] = dw_add_sloppy(a0[0], dw_neg(dw_mul(A[ii[0] + j * n], X[j + jj[0] * n])));
+          a1[0] = dw_add_sloppy(a1[0], dw_neg(dw_mul(A[ii[0] + (j + 1) * n], X[j + 1 + jj[0] * n])));
+          if (two) {
+            a0[1] = dw_add_sloppy(a0[1], dw_neg(dw_mul(A[ii[1] + j * n], X[j + jj[1] * n])));
+            a1[1] = dw_add_sloppy(a1[1], dw_neg(dw_mul(A[ii[1] + (j + 1) * n], X[j + 1 + jj[1] * n])));
+          }
+        }
+        if (j < n) {
+          a0[0] = dw_add_sloppy(a0[0], dw_neg(dw_mul(A[ii[0] + j * n], X[j + jj[0] * n])));
+          if (two) a0[1] = dw_add_sloppy(a0[1], dw_neg(dw_mul(A[ii[1] + j * n], X[j + jj[1] * n])));
+        }
+        R[e0] = dw_add_sloppy(a0[0], a1[0]);
+        if (two) R[e0 + kSolverThreads] = dw_add_sloppy(a0[1], a1[1]);
+      }
+    }
+    solver_sync();
+    // X += inv * R
+    float mdx = 0.f, mx = 0.f;
+    {
+      Walk w = walk_start(t, n);
+      for (int e0 = t; e0 < nr; e0 += kSolveBatch * kSolverThreads) {
+        int ii[kSolveBatch], jj[kSolveBatch];
+        float acc[kSolveBatch];
+        dw xv[kSolveBatch];
+#pragma unroll
+        for (int q = 0; q < kSolveBatch; ++q) {
+          ii[q] = w.i;
+          jj[q] = w.j;
+          acc[q] = 0.f;
+          if (e0 + q * kSolverThreads < nr) xv[q] = X[e0 + q * kSolverThreads];
+          walk_next(w);
+        }
+        for (int j = 0; j < n; ++j)
+#pragma unroll
+          for (int q = 0; q < kSolveBatch; ++q)
+            if (e0 + q * kSolverThreads < nr) acc[q] = fmaf(inv[ii[q] + j * n], R[j + jj[q] * n].hi, acc[q]);
+#pragma unroll
+        for (int q = 0; q < kSolveBatch; ++q) {
+          if (e0 + q * kSolverThreads >= nr) continue;
+          const dw xn = dw_add_f(xv[q], acc[q]);
+          X[e0 + q * kSolverThreads] = xn;
+          mdx = fmaxf(mdx, (fabsf(acc[q]) <= FLT_MAX) ? fabsf(acc[q]) : INFINITY);
+          mx = fmaxf(mx, fabsf(xn.hi));
+        }
+      }
+    }
+    // non-negative floats order like their bit patterns
+    atomicMax(reinterpret_cast<int*>(rd), __float_as_int(mdx));
+    atomicMax(reinterpret_cast<int*>(rd + 1), __float_as_int(mx));
+    solver_sync();
+    ok = rd[0] <= 1e-10f * rd[1];
+  }
+  return ok;
+}
+
 // The R x R solve of step t (mode k; kn is the next step's mode), run
 // identically by every CTA of the cluster on the solver warps.
 __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& cluster, int t, int k, int kn) {
@@ -698,7 +931,7 @@ __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& 
       const float* peer = cluster.map_shared_rank(c.bpart + boff, r);
       s = dw_add_f(s, peer[i * c.npmax + n]);
     }
-    c.X[i + n * rF] = s;
+    c.b0[i + n * rF] = s;
   }
   // normal equations: prefix (this sweep) x suffix (previous sweep) + penalty
   const dw pen = c.misc[0];
@@ -708,8 +941,16 @@ __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& 
     c.BB[e] = b;
   }
   solver_sync();
-  const int bad = dw_ldlt(c.BB, rF, c.dinv, c.u);
-  dw_ldlt_solve(c.BB, rF, c.dinv, c.X, nk);
+  // FP32 inverse + double-word refinement; the double-word LDL^T when the
+  // FP32 inverse fails or the refinement does not settle (ill-conditioned BB)
+  bool gj_ok;
+  const float* inv = gj_inverse(c.BB, rF, c.gi, &gj_ok);
+  int bad = 0;
+  if (!(gj_ok && refine_solve(c.BB, rF, c.b0, c.X, nk, inv, c.res, c.red))) {
+    for (int e = c.tid; e < rF * nk; e += kSolverThreads) c.X[e] = c.b0[e];
+    bad = dw_ldlt(c.BB, rF, c.dinv, c.u);
+    dw_ldlt_solve(c.BB, rF, c.dinv, c.X, nk);
+  }
   for (int i = c.tid; i < rF; i += kSolverThreads) c.nrm[i] = dw_normalise_row(c.X + i, nk, rF);
   solver_sync();
   // new factor: FP32 copy for phase B and for this CTA's rebuilds; the
@@ -798,6 +1039,10 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
   c.u = reinterpret_cast<dw*>(smem_raw + lay.u);
   c.nrm = reinterpret_cast<dw*>(smem_raw + lay.nrm);
   c.misc = reinterpret_cast<dw*>(smem_raw + lay.misc);
+  c.gi = reinterpret_cast<float*>(smem_raw + lay.gi);
+  c.b0 = reinterpret_cast<dw*>(smem_raw + lay.b0);
+  c.res = reinterpret_cast<dw*>(smem_raw + lay.res);
+  c.red = reinterpret_cast<float*>(smem_raw + lay.red);
   c.gm = p.gm + p.gm_off[c.v];
   c.fcta = p.fcta + (p.f_row_off[c.v] * c.CL + (long long)c.rank * c.rF) * p.nDp;
   {

@@ -15,7 +15,8 @@
 //   Fast2Sum          Dekker, Numer. Math. 18 (1971) 224-242
 //   TwoProd (FMA)     exact product error by one fused multiply-add
 //   DWPlusDW          Joldes, Muller, Popescu, ACM TOMS 44(2) 2017, Alg. 6
-//                     ("AccurateDWPlusDW", relative error <= 3u^2 + 13u^3)
+//                     ("AccurateDWPlusDW", relative error <= 3u^2 + 13u^3),
+//                     and Alg. 5 ("SloppyDWPlusDW") for residual sums
 //   DWTimesDW         same paper, Alg. 12 (relative error <= 5u^2)
 //   reciprocal, sqrt  one Newton-Raphson step in double-word from an FP32
 //                     approximation (quadratic convergence: 2^-23 -> 2^-46)
@@ -94,6 +95,16 @@ MLCP_HD dw dw_add(dw x, dw y) {
   const dw v = fast_two_sum(s.hi, c);
   const float w = f_add(t.lo, v.lo);
   return fast_two_sum(v.hi, w);
+}
+
+// x + y with JMP17 Alg. 5 ("SloppyDWPlusDW"): the error is bounded by about
+// u^2 (|x| + |y|) rather than relative to the sum, which is what accumulations
+// of residuals need, for about half the operations of dw_add.
+MLCP_HD dw dw_add_sloppy(dw x, dw y) {
+  const dw s = two_sum(x.hi, y.hi);
+  const float v = f_add(x.lo, y.lo);
+  const float w = f_add(s.lo, v);
+  return fast_two_sum(s.hi, w);
 }
 
 MLCP_HD dw dw_neg(dw x) { return dw{-x.hi, -x.lo}; }

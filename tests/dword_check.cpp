@@ -45,13 +45,14 @@ static void report(const char* name, double worst) {
 
 int main() {
   const int n = 200000;
-  double e_add = 0, e_mul = 0, e_fma = 0, e_rcp = 0, e_div = 0, e_sqrt = 0, e_addf = 0, e_mulf = 0, e_conv = 0;
+  double e_adds = 0, e_add = 0, e_mul = 0, e_fma = 0, e_rcp = 0, e_div = 0, e_sqrt = 0, e_addf = 0, e_mulf = 0, e_conv = 0;
   for (int t = 0; t < n; ++t) {
     const dw a = random_dw(20, false), b = random_dw(20, false), c = random_dw(20, false);
     const dw p = random_dw(20, true);
     // sums: error relative to the operand magnitudes (|a| + |b|), the form in
     // which the bounds are stated; cancellation is then no concern
     e_add = std::fmax(e_add, scaled(ld(mlcp::dw_add(a, b)), ld(a) + ld(b), fabsl(ld(a)) + fabsl(ld(b))));
+    e_adds = std::fmax(e_adds, scaled(ld(mlcp::dw_add_sloppy(a, b)), ld(a) + ld(b), fabsl(ld(a)) + fabsl(ld(b))));
     e_mul = std::fmax(e_mul, relerr(ld(mlcp::dw_mul(a, b)), ld(a) * ld(b)));
     const long double fw = ld(a) * ld(b) + ld(c);
     e_fma = std::fmax(e_fma, scaled(ld(mlcp::dw_fma(a, b, c)), fw, fabsl(ld(a) * ld(b)) + fabsl(ld(c))));
@@ -66,6 +67,7 @@ int main() {
     e_conv = std::fmax(e_conv, relerr(ld(mlcp::dw_from_double(x)), (long double)x));
   }
   report("add", e_add);
+  report("add_sloppy", e_adds);
   report("mul", e_mul);
   report("fma", e_fma);
   report("rcp", e_rcp);

@@ -4,7 +4,8 @@ The header mlcp_gb300/csrc/dword.cuh is compiled for the host with
 -ffp-contract=off and checked against long double on 200k seeded operands.
 Bounds (relative error, as -log2): the published bounds for the algorithms
 (Joldes, Muller, Popescu, ACM TOMS 2017: DWPlusDW <= 3u^2, DWTimesDW <= 5u^2
-with u = 2^-24) give about 46 bits; the Newton-step reciprocal and square
+with u = 2^-24) give about 46 bits (the sloppy sum, Alg. 5, is measured against
+|a| + |b|, the form of its bound); the Newton-step reciprocal and square
 root lose one or two more.  The device reciprocal seed (rcp.approx, 2^-23)
 is one bit coarser than the host's rounded division, so the device ends
 about a bit lower on rcp/div; the GPU ALS tests cover that path.
@@ -18,7 +19,7 @@ import pytest
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
-BITS = {"add": 45.0, "mul": 45.0, "fma": 44.5, "rcp": 45.0, "div": 44.0, "sqrt": 44.0,
+BITS = {"add": 45.0, "add_sloppy": 45.0, "mul": 45.0, "fma": 44.5, "rcp": 45.0, "div": 44.0, "sqrt": 44.0,
         "add_f": 45.0, "mul_f": 45.0, "from_double": 47.0}
 
 

@@ -79,9 +79,11 @@ def test_noalloc_matches_allocating_entry_point(cuda_device):
 @pytest.mark.gpu
 def test_noalloc_rejects_oversized_target(cuda_device):
     import torch
-    nbas = np.full(30, 64, dtype=np.int32)
-    coef = torch.zeros(20 + 8000, dtype=torch.float64, device=cuda_device)
-    base = torch.zeros((20 + 8000) * int(nbas.sum()), dtype=torch.float64, device=cuda_device)
-    rc = _noalloc(coef, base, nbas, 20, 8000, 1, None)
+    # fits the shared-memory plan, but its FP32 target copy alone (30000 terms
+    # x 360 basis functions) exceeds the fixed scratch array
+    nbas = np.full(30, 12, dtype=np.int32)
+    coef = torch.zeros(20 + 30000, dtype=torch.float64, device=cuda_device)
+    base = torch.zeros((20 + 30000) * int(nbas.sum()), dtype=torch.float64, device=cuda_device)
+    rc = _noalloc(coef, base, nbas, 20, 30000, 1, None)
     assert rc != 0
     assert "scratch" in _lib.last_error()
