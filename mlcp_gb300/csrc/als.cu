@@ -702,10 +702,11 @@ __device__ dw dw_normalise_row(dw* x, int n, int ld) {
 }
 
 // Suffix products for the next sweep: suf[d] = prod_{d' > d} gram[d']
-// (elementwise), suf[D-1] = 1; and the prefix L reset to 1.
-__device__ void dw_suffix(const Cta& c) {
+// (elementwise), suf[D-1] = 1; and the prefix L reset to 1.  Threads t of
+// nt (the solver warps, or the one warp that does this during phase B).
+__device__ void dw_suffix(const Cta& c, int t, int nt) {
   const int rr = c.rF * c.rF;
-  for (int e = c.tid; e < rr; e += kSolverThreads) {
+  for (int e = t; e < rr; e += nt) {
     dw a = dw_make(1.f);
     c.suf[(size_t)(c.D - 1) * rr + e] = a;
     for (int d = c.D - 1; d >= 1; --d) {
@@ -718,9 +719,9 @@ __device__ void dw_suffix(const Cta& c) {
 
 // Gram matrix of the unit-normalised new factor of mode k (rows of X), stored
 // for the suffix products of the next sweep and folded into the prefix L.
-__device__ void dw_new_gram(const Cta& c, int k, int nk) {
+__device__ void dw_new_gram(const Cta& c, int k, int nk, int t, int nt) {
   const int rF = c.rF, rr = rF * rF;
-  for (int e = c.tid; e < rr; e += kSolverThreads) {
+  for (int e = t; e < rr; e += nt) {
     const int i = e % rF, i2 = e / rF;
     if (i > i2) continue;
     dw s = dw_make(0.f);
@@ -767,6 +768,15 @@ __device__ const float* gj_inverse(const dw* A, int n, float* gi, bool* ok) {
   solver_sync();
   int cur = 0;
   bool good = true;
+  // (row, column) of the first batch of entries, fixed for all steps
+  int i0[kSolveBatch], j0[kSolveBatch];
+  Walk w_later = walk_start(t, n);  // walk state at the second batch
+#pragma unroll
+  for (int q = 0; q < kSolveBatch; ++q) {
+    i0[q] = w_later.i;
+    j0[q] = w_later.j;
+    walk_next(w_later);
+  }
   for (int k = 0; k < n; ++k) {
     const float* s = gi + cur * nn;
     float* d = gi + (cur ^ 1) * nn;
@@ -774,20 +784,21 @@ __device__ const float* gj_inverse(const dw* A, int n, float* gi, bool* ok) {
     good = good && piv > 0.f;
     float pk = f_rcp_approx(piv);
     pk = pk * fmaf(-piv, pk, 2.0f);
-    Walk w = walk_start(t, n);
+    Walk w = w_later;
     for (int e0 = t; e0 < nn; e0 += kSolveBatch * kSolverThreads) {
       float a[kSolveBatch], b[kSolveBatch], x[kSolveBatch];
       int ii[kSolveBatch], jj[kSolveBatch];
+      const bool first = e0 == t;
 #pragma unroll
       for (int q = 0; q < kSolveBatch; ++q) {
-        ii[q] = w.i;
-        jj[q] = w.j;
+        ii[q] = first ? i0[q] : w.i;
+        jj[q] = first ? j0[q] : w.j;
+        if (!first) walk_next(w);
         if (e0 + q * kSolverThreads < nn) {
-          a[q] = s[w.i + k * n];
-          b[q] = s[k + w.j * n];
+          a[q] = s[ii[q] + k * n];
+          b[q] = s[k + jj[q] * n];
           x[q] = s[e0 + q * kSolverThreads];
         }
-        walk_next(w);
       }
 #pragma unroll
       for (int q = 0; q < kSolveBatch; ++q) {
@@ -813,7 +824,8 @@ constexpr int kRefineMax = 4;
 // X = A^-1 B (A n x n double-word, B and X n x nrhs, ld n) by iterative
 // refinement preconditioned with the FP32 inverse: X = inv B, then
 // X += inv (B - A X) with the residual formed in double-word, until the last
-// correction is below 1e-10 of max |X|.  Returns whether that happened within
+// correction is below 1e-10 of max |X| (or the first is below 1e-5, which
+// bounds the remaining error by 1e-10).  Returns whether that happened within
 // kRefineMax rounds.  Each thread computes up to four entries in registers
 // before storing them.
 __device__ bool refine_solve(const dw* A, int n, const dw* B, dw* X, int nrhs, const float* inv, dw* R, float* red) {
@@ -912,9 +924,36 @@ __device__ bool refine_solve(const dw* A, int n, const dw* B, dw* X, int nrhs, c
     atomicMax(reinterpret_cast<int*>(rd), __float_as_int(mdx));
     atomicMax(reinterpret_cast<int*>(rd + 1), __float_as_int(mx));
     solver_sync();
-    ok = rd[0] <= 1e-10f * rd[1];
+    // converged when the correction just applied is negligible, or when the
+    // contraction it shows (rho ~ |dX|/|X|) leaves an error of rho^2 |X| <=
+    // 1e-10 |X| (refinement converges linearly with rate rho), far below the
+    // FP32 rounding of the right-hand side
+    ok = rd[0] <= 1e-10f * rd[1] || (round == 0 && rd[0] <= 1e-5f * rd[1]);
   }
   return ok;
+}
+
+// The end of a solve: the caller's FP64 factor and weights (cluster rank 0),
+// the Gram of the new factor of mode k folded into the prefix L, the suffix
+// products when a sweep ends, and the suffix of the next mode kn.  Threads t
+// of nt; `warp_only` when they form one warp.
+__device__ void post_solve(const Cta& c, const AlsParams& p, int k, int kn, int t, int nt, bool warp_only) {
+  const int rF = c.rF, nk = p.nbas[k], rr = rF * rF;
+  if (c.rank == 0) {
+    double* fbase = p.base + p.term_off[c.v] * (long long)p.nD;
+    for (int e = t; e < rF * nk; e += nt) {
+      const int i = e / nk, q = e - i * nk;
+      fbase[(long long)i * p.nD + p.off[k] + q] = dw_to_double(c.X[i + q * rF]);
+    }
+    for (int i = t; i < rF; i += nt) p.coef[p.term_off[c.v] + i] = dw_to_double(c.nrm[i]);
+  }
+  dw_new_gram(c, k, nk, t, nt);
+  if (warp_only) __syncwarp(); else solver_sync();
+  if (k == c.D - 1) {
+    dw_suffix(c, t, nt);
+    if (warp_only) __syncwarp(); else solver_sync();
+  }
+  for (int e = t; e < rr; e += nt) c.sk[e] = c.suf[(size_t)kn * rr + e];
 }
 
 // The R x R solve of step t (mode k; kn is the next step's mode), run
@@ -961,23 +1000,14 @@ __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& 
     c.fb[i * c.gsmax + q] = x;
     if (i < rF) c.fcta[(long long)i * c.nDp + p.offp[k] + q] = x;
   }
-  if (c.rank == 0) {
-    double* fbase = p.base + p.term_off[c.v] * (long long)p.nD;
-    for (int e = c.tid; e < rF * nk; e += kSolverThreads) {
-      const int i = e / nk, q = e - i * nk;
-      fbase[(long long)i * p.nD + p.off[k] + q] = dw_to_double(c.X[i + q * rF]);
-    }
-    for (int i = c.tid; i < rF; i += kSolverThreads) p.coef[p.term_off[c.v] + i] = dw_to_double(c.nrm[i]);
-  }
-  dw_new_gram(c, k, nk);
-  solver_sync();
-  if (k == c.D - 1) {
-    dw_suffix(c);
-    solver_sync();
-  }
-  for (int e = c.tid; e < rr; e += kSolverThreads) c.sk[e] = c.suf[(size_t)kn * rr + e];
+  post_solve(c, p, k, kn, c.tid, kSolverThreads, false);
   if (c.tid == 0 && bad) c.flags[1] = 1;
 }
+
+// Warps that run phase A (the highest-numbered ones).  Phase A only has to
+// finish within the solve; the solver's dependent chains compete with its
+// warps for issue slots, so fewer of them can shorten the step.
+constexpr int kDivideWarps = 12;
 
 // Barrier among the phase-A warps only (named barrier 2).
 __device__ __forceinline__ void worker_sync() {
@@ -1101,7 +1131,7 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
   }
   __syncthreads();
   if (c.warp < kAlsSolverWarps) {
-    dw_suffix(c);
+    dw_suffix(c, c.tid, kSolverThreads);
     solver_sync();
     for (int e = c.tid; e < rr; e += kSolverThreads) c.sk[e] = c.suf[e];
   }
@@ -1123,7 +1153,8 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
         worker_sync();
         if (c.tid == kSolverThreads)
           start_phase(c, seq, TileSrc{c.gm + (long long)p.offg[kn] * c.rG, als_gstride(p.nbas[kn]), nullptr, 0});
-        product_pass(c, p, seq, kn, true, k, kAlsSolverWarps, kAlsWarps - kAlsSolverWarps);
+        if (c.warp >= kAlsWarps - kDivideWarps)
+          product_pass(c, p, seq, kn, true, k, kAlsWarps - kDivideWarps, kDivideWarps);
       }
       cluster_wait();
     }
