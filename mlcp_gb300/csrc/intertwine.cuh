@@ -62,9 +62,12 @@ struct GsParams {
   double* pscr;   // [nbloc][D+1][R][R] P(k,d) = Q_k,d F_d^T, then products over d != j
   double* g64;    // [D][R][R]
   double* gcoef;  // [nbloc]
+  double* work;   // [cluster][R*nD + D*R*R] each CTA's copy of the vector being fitted and its Grams
   int* status;
 };
 int gs_launch(const GsParams& p, cudaStream_t st);
+// Doubles of GsParams::work needed for a block of nbloc vectors.
+size_t gs_work_doubles(int nbloc, int R, int nD, int D);
 
 // Block Rayleigh-Ritz inner products: QHQ(i,j) = <Q_j, HQ_i>, S(i,j) = <Q_j, Q_i>, j <= i.
 struct GepParams {
