@@ -233,7 +233,7 @@ __global__ void update_weights_kernel(int B, int R, const double* qcoef, const d
 struct CycleBuffers {
   double *q, *qc, *hq, *hqc, *qn, *qnc;
   float *mscr, *wscr, *zscr;
-  double *pscr, *g64, *gcoef, *gsw, *A, *S, *U, *eigv, *gwork, *wts;
+  double *g64, *gsw, *A, *S, *U, *eigv, *gwork, *wts;
   int *meta, *status;
 };
 
@@ -251,9 +251,7 @@ size_t plan_cycle(const Layout& Ly, const OpTable& t, int R, int B, CycleBuffers
   cb->wscr = (float*)take(sizeof(float) * (size_t)B * t.umax * R * R);
   cb->zscr = (float*)take(sizeof(float) * (size_t)B * t.umax * R * t.npmax);
   cb->g64 = (double*)take(sizeof(double) * (size_t)B * Ly.D * R * R);
-  cb->pscr = (double*)take(sizeof(double) * (size_t)B * (Ly.D + 1) * R * R);
-  cb->gcoef = (double*)take(sizeof(double) * B);
-  cb->gsw = (double*)take(sizeof(double) * gs_work_doubles(B, R, Ly.nD, Ly.D));
+  cb->gsw = (double*)take(sizeof(double) * gs_work_doubles(B, R, Ly.nD, Ly.D, Ly.npmax));
   cb->A = (double*)take(sizeof(double) * (size_t)B * B);
   cb->S = (double*)take(sizeof(double) * (size_t)B * B);
   cb->U = (double*)take(sizeof(double) * (size_t)B * B);
@@ -346,7 +344,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
     GsParams g;
     g.D = ndof; g.R = R; g.nbloc = B; g.nD = Ly.nD; g.nDp = Ly.nDp; g.npmax = Ly.npmax; g.nals = nals;
     g.nbas = d_nbas; g.off = d_off; g.offp = d_offp; g.base = cb.q; g.coef = cb.qc;
-    g.pscr = cb.pscr; g.g64 = cb.g64; g.gcoef = cb.gcoef; g.work = cb.gsw; g.status = cb.status + B;
+    g.work = cb.gsw; g.status = cb.status + B;
     if ((rc = gs_launch(g, st))) return rc;
   }
   if (update) {

@@ -5,25 +5,36 @@
 //   F - sum_{k<iv} <Q_k, F> Q_k,
 // where F is its current iterate and the coefficients <Q_k, F> are
 // recomputed at every mode step (gramsumoverrow + sumarray in the reference).
-// The pairwise per-mode overlaps P(k,d) = Q_{k,d} F_d^T (R x R) are kept and
+// The pairwise per-mode overlaps P_k,d(r,i) = <Q_k,r^d, F_i^d> are kept and
 // only the mode just solved is refreshed, so a mode step costs
 // O(iv R^2 (D + 2n)) instead of rebuilding every product over all modes.
-// Everything here runs in FP64: once power iteration has made the block's
-// vectors nearly parallel, the target F - sum_k <Q_k,F> Q_k is a small
-// difference of large terms, and FP32 contractions lose it to cancellation.
+//
+// Precision.  Once power iteration has made the block's vectors nearly
+// parallel, the target F - sum_k <Q_k,F> Q_k is a small difference of large
+// terms, and FP32 contractions lose it to cancellation; the reference runs
+// this stage in FP64.  GB300 issues FP64 at a small fraction of its FP32
+// rate, so everything here runs in double-word arithmetic (dword.cuh: about
+// 48-bit significands on the FP32 pipes).  The R x R normal equations are
+// solved by an FP32 Gauss-Jordan inverse with double-word iterative
+// refinement, falling back to a double-word LDL^T (dwsolve.cuh).
 //
 // GB300 layout: the loop over vectors is sequential, but within a mode step
 // the work over the earlier vectors k is independent.  One thread-block
 // cluster of up to 16 CTAs runs the whole orthogonalisation in one launch;
-// CTA `rank` owns the earlier vectors k = rank (mod cluster) and computes
-// their overlaps, products, coefficients and right-hand-side contributions
-// (FP64 throughput grows with the number of SMs).  The partial right-hand
+// CTA `rank` owns the earlier vectors k = rank (mod cluster) and keeps their
+// factors, weights and overlaps resident in its shared memory (its global
+// scratch when they do not fit).  Each CTA computes its vectors' products,
+// coefficients and right-hand-side contributions; the partial right-hand
 // sides meet through distributed shared memory, and every CTA runs the same
-// small R x R solve on the same data, so each holds the identical new factor
-// and nothing is broadcast back.  One cluster barrier per mode step.
+// small solve on the same data, so each holds the identical new factor and
+// nothing is broadcast back.  One cluster barrier per mode step.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+
 #include "common.cuh"
+#include "dword.cuh"
+#include "dwsolve.cuh"
 #include "intertwine.cuh"
 
 namespace cg = cooperative_groups;
@@ -33,240 +44,389 @@ namespace mlcp {
 namespace {
 
 constexpr int kGsThreads = 512;
+constexpr int kGsWarps = kGsThreads / 32;
+static_assert(kGsWarps == 16, "block_sum reduces 16 warp partials");
 
-struct GsSmem {
-  double *X, *BB, *Gp, *selfv, *fcs, *bpart, *red, *dinv, *ucol, *misc;
-  int* flags;
+// Groups of arrays that move to global scratch (in this order) when shared
+// memory cannot hold them.
+enum : int { kGroupQ = 1, kGroupP = 2, kGroupF = 4, kGroupAll = 7 };
+
+struct GsDims {
+  int R, D, nD, npm, nkmax, gmask;
 };
 
-__host__ __device__ inline size_t gs_carve(int R, int npm, GsSmem* s, unsigned char* base) {
-  size_t o = 0;
-  auto take = [&](size_t bytes) {
-    const size_t r = o;
-    o += (bytes + 15) / 16 * 16;
-    return base ? base + r : nullptr;
+struct GsArrays {
+  dw *qf, *qw, *qc;        // [nkmax][R][nD] owned vectors' factors, the same times their weights; [nkmax][R] weights
+  dw *P, *psn, *part;      // [nkmax][D][R*R] overlaps (index r*R+i); [nkmax][R*R] products over d != j;
+                           // [nkmax+1][2][R*npm] partial dot products
+  dw *fb, *g;              // [R][nD] vector being fitted; [D][R*R] its Grams
+  dw *fcs, *wf, *Gp, *BB, *gpart, *gco, *bpart, *X, *b0, *res, *dinv, *u, *red, *misc;
+  float *gi, *rred;
+  int *nb, *off, *flags;
+};
+
+// Entries of R*R rounded up to whole warps.
+__host__ __device__ inline int gs_rrp(int R) { return (R * R + 31) / 32 * 32; }
+
+// Assigns the arrays (null bases: sizes only).  Returns the shared-memory
+// bytes; *gwork receives the global scratch entries (dw) of one CTA.
+__host__ __device__ inline size_t gs_carve(const GsDims& m, GsArrays* a, unsigned char* sbase, dw* gbase,
+                                           size_t* gwork) {
+  const int R = m.R, nkm = m.nkmax;
+  const size_t RR = (size_t)R * R, Rn = (size_t)R * m.npm;
+  size_t so = 0, go = 0;
+  auto take_s = [&](size_t bytes) -> unsigned char* {
+    const size_t r = so;
+    so += (bytes + 15) / 16 * 16;
+    return sbase ? sbase + r : nullptr;
   };
-  s->X = (double*)take(sizeof(double) * R * npm);
-  s->BB = (double*)take(sizeof(double) * R * R);
-  s->Gp = (double*)take(sizeof(double) * R * R);
-  s->selfv = (double*)take(sizeof(double) * R * npm);
-  s->fcs = (double*)take(sizeof(double) * R);
-  s->bpart = (double*)take(sizeof(double) * 2 * R * npm);
-  s->red = (double*)take(sizeof(double) * kGsThreads / 32);
-  s->dinv = (double*)take(sizeof(double) * R);
-  s->ucol = (double*)take(sizeof(double) * R);
-  s->misc = (double*)take(sizeof(double) * 4);
-  s->flags = (int*)take(sizeof(int) * 4);
-  return o;
+  auto take = [&](int group, size_t n) -> dw* {
+    if (m.gmask & group) {
+      const size_t r = go;
+      go += (n + 1) / 2 * 2;
+      return gbase ? gbase + r : nullptr;
+    }
+    return (dw*)take_s(sizeof(dw) * n);
+  };
+  a->qf = take(kGroupQ, (size_t)nkm * R * m.nD);
+  a->qw = take(kGroupQ, (size_t)nkm * R * m.nD);
+  a->qc = take(kGroupQ, (size_t)nkm * R);
+  a->P = take(kGroupP, (size_t)nkm * m.D * RR);
+  a->psn = take(kGroupP, (size_t)nkm * RR);
+  a->part = take(kGroupP, (size_t)(nkm + 1) * 2 * Rn);
+  a->fb = take(kGroupF, (size_t)R * m.nD);
+  a->g = take(kGroupF, (size_t)m.D * RR);
+  a->fcs = (dw*)take_s(sizeof(dw) * R);
+  a->wf = (dw*)take_s(sizeof(dw) * Rn);
+  a->Gp = (dw*)take_s(sizeof(dw) * RR);
+  a->BB = (dw*)take_s(sizeof(dw) * RR);
+  a->gpart = (dw*)take_s(sizeof(dw) * nkm * (gs_rrp(R) / 32));
+  a->gco = (dw*)take_s(sizeof(dw) * nkm);
+  a->bpart = (dw*)take_s(sizeof(dw) * 2 * Rn);
+  a->X = (dw*)take_s(sizeof(dw) * Rn);
+  a->b0 = (dw*)take_s(sizeof(dw) * Rn);
+  a->res = (dw*)take_s(sizeof(dw) * Rn);
+  a->dinv = (dw*)take_s(sizeof(dw) * R);
+  a->u = (dw*)take_s(sizeof(dw) * R);
+  a->red = (dw*)take_s(sizeof(dw) * kGsWarps);
+  a->misc = (dw*)take_s(sizeof(dw) * 4);
+  a->gi = (float*)take_s(sizeof(float) * 2 * RR);
+  a->rred = (float*)take_s(sizeof(float) * 4);
+  a->nb = (int*)take_s(sizeof(int) * (m.D + 1));
+  a->off = (int*)take_s(sizeof(int) * (m.D + 1));
+  a->flags = (int*)take_s(sizeof(int) * 4);
+  if (gwork) *gwork = go;
+  return so;
 }
 
 __device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
-// Sum over the block (every thread gets the result; red holds one slot per warp).
-__device__ double block_sum(double v, double* red) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+__device__ __forceinline__ dw shfl_xor_dw(dw v, int o) {
+  return dw{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+
+// Sum over the block; every thread gets the same value (dw_add is
+// commutative, so the butterflies agree across lanes and warps).
+__device__ dw block_sum(dw v, dw* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) v = dw_add(v, shfl_xor_dw(v, o));
   __syncthreads();
   if (lane == 0) red[warp] = v;
   __syncthreads();
-  double s = 0.0;
-  for (int w = 0; w < nw; ++w) s += red[w];  // same order in every thread
+  dw s = red[lane & (kGsWarps - 1)];
+  for (int o = kGsWarps / 2; o > 0; o >>= 1) s = dw_add(s, shfl_xor_dw(s, o));
   return s;
+}
+
+struct Gs {
+  GsArrays a;
+  int R, RR, RRp, D, nD, npm, CL, rank, tid;
+};
+
+// The vector iv as the working copy: factors, weights, penalty.
+__device__ void load_vector(const Gs& c, const GsParams& p, int iv) {
+  const double* fb = p.base + (size_t)iv * c.R * c.nD;
+  for (int e = c.tid; e < c.R * c.nD; e += kGsThreads) c.a.fb[e] = dw_from_double(fb[e]);
+  for (int i = c.tid; i < c.R; i += kGsThreads) c.a.fcs[i] = dw_from_double(p.coef[(size_t)iv * c.R + i]);
+  if (c.tid == 0) {
+    double pen = p.coef[(size_t)iv * c.R];
+    for (int i = 1; i < c.R; ++i) pen = fmax(pen, p.coef[(size_t)iv * c.R + i]);
+    c.a.misc[0] = dw_from_double(pen * 1.0e-10);  // FP64-build rule of the reference for this stage
+  }
+  __syncthreads();
+}
+
+// Grams of the working vector, every mode (symmetric, both triangles stored).
+__device__ void all_grams(const Gs& c) {
+  const int R = c.R, RR = c.RR;
+  for (int e = c.tid; e < c.D * RR; e += kGsThreads) {
+    const int d = e / RR, ee = e - d * RR, i = ee % R, i2 = ee / R;
+    if (i > i2) continue;
+    const dw* x = c.a.fb + (size_t)i * c.nD + c.a.off[d];
+    const dw* y = c.a.fb + (size_t)i2 * c.nD + c.a.off[d];
+    dw s = dw_make(0.f);
+    for (int q = 0; q < c.a.nb[d]; ++q) s = dw_fma(x[q], y[q], s);
+    c.a.g[(size_t)d * RR + i + i2 * R] = s;
+    c.a.g[(size_t)d * RR + i2 + i * R] = s;
+  }
+  __syncthreads();
+}
+
+// Overlaps of the owned earlier vectors with the working vector, every mode.
+__device__ void all_overlaps(const Gs& c, int nk) {
+  const int R = c.R, RR = c.RR, DRR = c.D * RR;
+  for (int e = c.tid; e < nk * DRR; e += kGsThreads) {
+    const int kl = e / DRR, rem = e - kl * DRR, d = rem / RR, ee = rem - d * RR, r = ee / R, i = ee - r * R;
+    const dw* x = c.a.qf + ((size_t)kl * R + r) * c.nD + c.a.off[d];
+    const dw* y = c.a.fb + (size_t)i * c.nD + c.a.off[d];
+    dw s = dw_make(0.f);
+    for (int q = 0; q < c.a.nb[d]; ++q) s = dw_fma(x[q], y[q], s);
+    c.a.P[(size_t)kl * DRR + rem] = s;
+  }
+  __syncthreads();
+}
+
+// Weights divided by sqrt(<F,F>).
+__device__ void normalize_weights(const Gs& c) {
+  const int R = c.R;
+  dw part = dw_make(0.f);
+  for (int e = c.tid; e < c.RR; e += kGsThreads) {
+    dw prod = dw_mul(c.a.fcs[e % R], c.a.fcs[e / R]);
+    for (int d = 0; d < c.D; ++d) prod = dw_mul(prod, c.a.g[(size_t)d * c.RR + e]);
+    part = dw_add(part, prod);
+  }
+  const dw q = dw_sqrt(dw_abs(block_sum(part, c.a.red)));
+  __syncthreads();  // every thread has read fcs
+  for (int i = c.tid; i < R; i += kGsThreads) c.a.fcs[i] = dw_div(c.a.fcs[i], q);
+  __syncthreads();
+}
+
+// The finished vector: FP64 output (rank 0), and the owner's resident copy
+// when later vectors use it.
+__device__ void finish_vector(const Gs& c, const GsParams& p, int iv, bool factors) {
+  const int R = c.R, nD = c.nD;
+  if (c.rank == 0) {
+    double* fb = p.base + (size_t)iv * R * nD;
+    if (factors)
+      for (int e = c.tid; e < R * nD; e += kGsThreads) fb[e] = dw_to_double(c.a.fb[e]);
+    for (int i = c.tid; i < R; i += kGsThreads) p.coef[(size_t)iv * R + i] = dw_to_double(c.a.fcs[i]);
+  }
+  if (iv < p.nbloc - 1 && iv % c.CL == c.rank) {
+    const int kl = iv / c.CL;
+    dw* qf = c.a.qf + (size_t)kl * R * nD;
+    dw* qw = c.a.qw + (size_t)kl * R * nD;
+    for (int e = c.tid; e < R * nD; e += kGsThreads) {
+      const dw x = c.a.fb[e];
+      qf[e] = x;
+      qw[e] = dw_mul(c.a.fcs[e / nD], x);
+    }
+    for (int i = c.tid; i < R; i += kGsThreads) c.a.qc[(size_t)kl * R + i] = c.a.fcs[i];
+  }
+  __syncthreads();
+}
+
+// Step phase 1: products over d != j of the owned overlaps (psn) and of the
+// working Grams (Gp, and BB = Gp + pen I), the weighted factor wf(r,m) =
+// c_r F_r^j(m), and per warp of psn entries the partial sums of
+// c_k,r c_i P_k(r,i) over all modes (the coefficients <Q_k, F>).
+__device__ void step_products(const Gs& c, int j, int nk) {
+  const int R = c.R, RR = c.RR, RRp = c.RRp, D = c.D, nj = c.a.nb[j], offj = c.a.off[j];
+  const int npsn = nk * RRp, ngp = npsn + RR, total = ngp + R * nj;
+  const dw pen = c.a.misc[0];
+  for (int e = c.tid; e < total; e += kGsThreads) {
+    if (e < npsn) {  // whole warps: npsn is a multiple of 32
+      const int kl = e / RRp, ee = e - kl * RRp;
+      dw contrib = dw_make(0.f);
+      if (ee < RR) {
+        const int r = ee / R, i = ee - r * R;
+        const dw* Pk = c.a.P + (size_t)kl * D * RR + ee;
+        const dw pj = Pk[(size_t)j * RR], w = dw_mul(c.a.qc[(size_t)kl * R + r], c.a.fcs[i]);
+        dw prod = dw_make(1.f);
+        for (int d = 0; d < D; ++d)
+          if (d != j) prod = dw_mul(prod, Pk[(size_t)d * RR]);
+        contrib = dw_mul(dw_mul(prod, pj), w);
+        c.a.psn[(size_t)kl * RR + ee] = prod;
+      }
+      for (int o = 16; o > 0; o >>= 1) contrib = dw_add(contrib, shfl_xor_dw(contrib, o));
+      if ((c.tid & 31) == 0) c.a.gpart[kl * (RRp / 32) + ee / 32] = contrib;
+    } else if (e < ngp) {
+      const int ee = e - npsn;
+      dw prod = dw_make(1.f);
+      for (int d = 0; d < D; ++d)
+        if (d != j) prod = dw_mul(prod, c.a.g[(size_t)d * RR + ee]);
+      c.a.Gp[ee] = prod;
+      c.a.BB[ee] = (ee % R == ee / R) ? dw_add(prod, pen) : prod;
+    } else {
+      const int ee = e - ngp, r = ee % R, m = ee / R;
+      c.a.wf[ee] = dw_mul(c.a.fcs[r], c.a.fb[(size_t)r * c.nD + offj + m]);
+    }
+  }
+  __syncthreads();
+}
+
+// Step phase 2: the dot products over r, split in two halves,
+//   source 0:        sum_r wf(r,m) Gp(r,i)                      (self term)
+//   source 1 + kl:   sum_r c_k,r Q_k,r^j(m) psn_k(r,i)          (owned k)
+// at part[(2 s + h) R nj + i + m R]; and gco_k = -<Q_k, F> from the partials.
+__device__ void step_dots(const Gs& c, int j, int nk) {
+  const int R = c.R, RR = c.RR, nj = c.a.nb[j], offj = c.a.off[j], Rn = R * nj, half = (R + 1) / 2;
+  const int total = (nk + 1) * 2 * Rn;
+  for (int e = c.tid; e < total; e += kGsThreads) {
+    const int sh = e / Rn, em = e - sh * Rn, s = sh >> 1, i = em % R, m = em / R;
+    const int r0 = (sh & 1) ? half : 0, r1 = (sh & 1) ? R : half;
+    dw acc = dw_make(0.f);
+    if (s == 0) {
+      for (int r = r0; r < r1; ++r) acc = dw_fma(c.a.wf[r + m * R], c.a.Gp[r * R + i], acc);
+    } else {
+      const dw* A = c.a.qw + (size_t)(s - 1) * R * c.nD + offj + m;
+      const dw* M = c.a.psn + (size_t)(s - 1) * RR + i;
+      for (int r = r0; r < r1; ++r) acc = dw_fma(A[(size_t)r * c.nD], M[r * R], acc);
+    }
+    c.a.part[e] = acc;
+  }
+  if (c.tid < nk) {
+    const int nch = c.RRp / 32;
+    dw s = dw_make(0.f);
+    for (int q = 0; q < nch; ++q) s = dw_add(s, c.a.gpart[c.tid * nch + q]);
+    c.a.gco[c.tid] = dw_neg(s);
+  }
+  __syncthreads();
+}
+
+// Step phase 3: this CTA's part of the right-hand side,
+//   sum_k gco_k sum_r c_k,r Q_k,r^j(m) psn_k(r,i).
+__device__ void step_rhs_part(const Gs& c, int j, int nk, dw* bp) {
+  const int Rn = c.R * c.a.nb[j];
+  for (int e = c.tid; e < Rn; e += kGsThreads) {
+    dw acc = dw_make(0.f);
+    for (int kl = 0; kl < nk; ++kl) {
+      const dw z = dw_add(c.a.part[(size_t)(2 * kl + 2) * Rn + e], c.a.part[(size_t)(2 * kl + 3) * Rn + e]);
+      acc = dw_fma(c.a.gco[kl], z, acc);
+    }
+    bp[e] = acc;
+  }
+}
+
+// Step phase 4 (after the cluster barrier): the self term plus the partial
+// right-hand sides of the cluster, summed as a fixed tree over ranks so that
+// every CTA forms the identical system.
+__device__ void step_gather(const Gs& c, cg::cluster_group& cluster, int j, dw* bp) {
+  const int Rn = c.R * c.a.nb[j];
+  for (int e = c.tid; e < Rn; e += kGsThreads) {
+    dw v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = (r < c.CL) ? cluster.map_shared_rank(bp, r)[e] : dw_make(0.f);
+#pragma unroll
+    for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+      for (int r = 0; r < w; ++r) v[r] = dw_add(v[r], v[r + w]);
+    const dw self = dw_add(c.a.part[e], c.a.part[(size_t)Rn + e]);
+    c.a.b0[e] = dw_add(self, v[0]);
+  }
+  __syncthreads();
+}
+
+// Step phase 5 (solver warps): X = BB^-1 b0, rows normalised, norms as the
+// new weights.
+__device__ void step_solve(const Gs& c, int j) {
+  if (c.tid < dwsolve::kSolverThreads) {
+    const int R = c.R, nj = c.a.nb[j];
+    bool gj_ok;
+    const float* inv = dwsolve::gj_inverse(c.a.BB, R, c.a.gi, &gj_ok);
+    int bad = 0;
+    if (!(gj_ok && dwsolve::refine_solve(c.a.BB, R, c.a.b0, c.a.X, nj, inv, c.a.res, c.a.rred))) {
+      for (int e = c.tid; e < R * nj; e += dwsolve::kSolverThreads) c.a.X[e] = c.a.b0[e];
+      bad = dwsolve::dw_ldlt(c.a.BB, R, c.a.dinv, c.a.u);
+      dwsolve::dw_ldlt_solve(c.a.BB, R, c.a.dinv, c.a.X, nj);
+    }
+    for (int i = c.tid; i < R; i += dwsolve::kSolverThreads) c.a.fcs[i] = dwsolve::dw_normalise_row(c.a.X + i, nj, R);
+    if (c.tid == 0 && bad) c.a.flags[1] = 1;
+  }
+  __syncthreads();
+}
+
+// Step phase 6: the new factor of mode j into the working vector, its Gram,
+// and the owned overlaps of mode j.
+__device__ void step_update(const Gs& c, int j, int nk) {
+  const int R = c.R, RR = c.RR, nj = c.a.nb[j], offj = c.a.off[j], Rn = R * nj;
+  const int total = Rn + RR + nk * RR;
+  for (int e = c.tid; e < total; e += kGsThreads) {
+    if (e < Rn) {
+      const int i = e % R, m = e / R;
+      c.a.fb[(size_t)i * c.nD + offj + m] = c.a.X[e];
+    } else if (e < Rn + RR) {
+      const int ee = e - Rn, i = ee % R, i2 = ee / R;
+      if (i > i2) continue;
+      dw s = dw_make(0.f);
+      for (int m = 0; m < nj; ++m) s = dw_fma(c.a.X[i + m * R], c.a.X[i2 + m * R], s);
+      c.a.g[(size_t)j * RR + i + i2 * R] = s;
+      c.a.g[(size_t)j * RR + i2 + i * R] = s;
+    } else {
+      const int ee = e - Rn - RR, kl = ee / RR, e2 = ee - kl * RR, r = e2 / R, i = e2 - r * R;
+      const dw* x = c.a.qf + ((size_t)kl * R + r) * c.nD + offj;
+      dw s = dw_make(0.f);
+      for (int m = 0; m < nj; ++m) s = dw_fma(x[m], c.a.X[i + m * R], s);
+      c.a.P[((size_t)kl * c.D + j) * RR + e2] = s;
+    }
+  }
+  __syncthreads();
 }
 
 }  // namespace
 
 __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
   cg::cluster_group cluster = cg::this_cluster();
-  const int CL = (int)cluster.num_blocks(), rank = (int)cluster.block_rank();
-  const int R = p.R, D = p.D, nD = p.nD, npm = p.npmax, B = p.nbloc, RR = R * R;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int warp = tid / 32, lane = tid % 32, nwarps = nt / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  GsSmem s;
-  gs_carve(R, npm, &s, smem_raw);
-  // this CTA's working copy of the vector being orthogonalised and its Grams
-  double* fbw = p.work + (size_t)rank * ((size_t)R * nD + (size_t)D * RR);
-  double* g64w = fbw + (size_t)R * nD;
-  double* psn_all = p.pscr + (size_t)B * D * RR;  // [B][R][R] products over d != j
-  auto P = [&](int k, int d) { return p.pscr + ((size_t)k * D + d) * RR; };
+  Gs c;
+  c.CL = (int)cluster.num_blocks();
+  c.rank = (int)cluster.block_rank();
+  c.R = p.R;
+  c.RR = p.R * p.R;
+  c.RRp = gs_rrp(p.R);
+  c.D = p.D;
+  c.nD = p.nD;
+  c.npm = p.npmax;
+  c.tid = threadIdx.x;
+  const GsDims dims{p.R, p.D, p.nD, p.npmax, p.nkmax, p.gmask};
+  gs_carve(dims, &c.a, smem_raw, reinterpret_cast<dw*>(p.work) + (size_t)c.rank * p.work_stride, nullptr);
+  for (int d = c.tid; d <= c.D; d += kGsThreads) {
+    c.a.nb[d] = d < c.D ? p.nbas[d] : 0;
+    c.a.off[d] = p.off[d];
+  }
+  if (c.tid == 0) c.a.flags[1] = 0;
+  __syncthreads();
 
-  if (tid == 0) s.flags[1] = 0;
-
-  auto load_vector = [&](int iv) {
-    const double* fb = p.base + (size_t)iv * R * nD;
-    for (int e = tid; e < R * nD; e += nt) fbw[e] = fb[e];
-    for (int i = tid; i < R; i += nt) s.fcs[i] = p.coef[(size_t)iv * R + i];
-    __syncthreads();
-  };
-  // FP64 Grams of the working vector, every mode
-  auto grams = [&]() {
-    for (int e = tid; e < D * RR; e += nt) {
-      const int d = e / RR, ii = e % RR, i = ii % R, i2 = ii / R;
-      double acc = 0.0;
-      for (int q = 0; q < p.nbas[d]; ++q) acc += fbw[(size_t)i * nD + p.off[d] + q] * fbw[(size_t)i2 * nD + p.off[d] + q];
-      g64w[e] = acc;
-    }
-    __syncthreads();
-  };
-  // weights divided by sqrt(<F,F>)
-  auto normalize_weights = [&]() {
-    double part = 0.0;
-    for (int e = tid; e < RR; e += nt) {
-      double prod = s.fcs[e % R] * s.fcs[e / R];
-      for (int d = 0; d < D; ++d) prod *= g64w[(size_t)d * RR + e];
-      part += prod;
-    }
-    const double q = sqrt(fabs(block_sum(part, s.red)));
-    __syncthreads();
-    for (int i = tid; i < R; i += nt) s.fcs[i] /= q;
-    __syncthreads();
-  };
-  auto store_vector = [&](int iv, bool factors) {
-    if (rank != 0) return;
-    double* fb = p.base + (size_t)iv * R * nD;
-    if (factors)
-      for (int e = tid; e < R * nD; e += nt) fb[e] = fbw[e];
-    for (int i = tid; i < R; i += nt) p.coef[(size_t)iv * R + i] = s.fcs[i];
-  };
-
-  load_vector(0);
-  grams();
-  normalize_weights();
-  store_vector(0, false);
-  // vector 0's weights are visible to every CTA before they read it as Q_0
-  __threadfence();
-  cl_arrive();
-  cl_wait();
+  load_vector(c, p, 0);
+  all_grams(c);
+  normalize_weights(c);
+  finish_vector(c, p, 0, false);
 
   int step = 0;
-  for (int iv = 1; iv < B && p.nals > 0; ++iv) {
-    load_vector(iv);
-    if (tid == 0) {
-      double pen = s.fcs[0];
-      for (int i = 1; i < R; ++i) pen = s.fcs[i] > pen ? s.fcs[i] : pen;
-      s.misc[0] = pen * 1.0e-10;  // FP64-build rule: this stage is FP64 throughout
-    }
-    grams();
-    // overlaps with the earlier vectors this CTA owns, every mode
-    const int nk = (iv - rank + CL - 1) / CL;  // k = rank, rank + CL, ... < iv
-    for (size_t e = tid; e < (size_t)nk * D * RR; e += nt) {
-      const int kl = (int)(e / ((size_t)D * RR)), rem = (int)(e % ((size_t)D * RR));
-      const int k = rank + kl * CL, d = rem / RR, r = (rem % RR) / R, i = rem % R;
-      const double* a = p.base + ((size_t)k * R + r) * nD + p.off[d];
-      const double* b = fbw + (size_t)i * nD + p.off[d];
-      double acc = 0.0;
-      for (int q = 0; q < p.nbas[d]; ++q) acc = fma(a[q], b[q], acc);
-      P(k, d)[r * R + i] = acc;
-    }
-    __syncthreads();
-    const double pen = s.misc[0];
-
+  for (int iv = 1; iv < p.nbloc && p.nals > 0; ++iv) {
+    load_vector(c, p, iv);
+    all_grams(c);
+    const int nk = (iv - c.rank + c.CL - 1) / c.CL;  // owned k = rank, rank + CL, ... < iv
+    all_overlaps(c, nk);
     for (int it = 0; it < p.nals; ++it) {
-      for (int j = 0; j < D; ++j, ++step) {
-        const int nj = p.nbas[j];
-        double* bp = s.bpart + (size_t)(step & 1) * R * npm;
-        // products over d != j for the owned k
-        for (size_t e = tid; e < (size_t)nk * RR; e += nt) {
-          const int k = rank + (int)(e / RR) * CL, ee = (int)(e % RR);
-          double prod = 1.0;
-          for (int d = 0; d < D; ++d)
-            if (d != j) prod *= P(k, d)[ee];
-          psn_all[(size_t)k * RR + ee] = prod;
-        }
-        // this vector's Grams over d != j: the normal equations and the self term
-        for (int e = tid; e < RR; e += nt) {
-          double g = 1.0;
-          for (int d = 0; d < D; ++d)
-            if (d != j) g *= g64w[(size_t)d * RR + e];
-          s.Gp[e] = g;
-          s.BB[e] = (e % R == e / R) ? g + pen : g;
-        }
-        __syncthreads();
-        // coefficients -<Q_k, F> (one warp per owned k)
-        for (int kl = warp; kl < nk; kl += nwarps) {
-          const int k = rank + kl * CL;
-          const double* qc = p.coef + (size_t)k * R;
-          const double* ps = psn_all + (size_t)k * RR;
-          const double* pj = P(k, j);
-          double part = 0.0;
-          for (int ee = lane; ee < RR; ee += 32) part -= qc[ee / R] * s.fcs[ee % R] * ps[ee] * pj[ee];
-          for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-          if (lane == 0) p.gcoef[k] = part;
-        }
-        // self term: sum_r c_r F_r^j(m) prod_{d != j} G_d(r, i)
-        for (int e = tid; e < R * nj; e += nt) {
-          const int i = e % R, m = e / R;
-          double acc = 0.0;
-          for (int r = 0; r < R; ++r) acc = fma(s.fcs[r] * fbw[(size_t)r * nD + p.off[j] + m], s.Gp[r * R + i], acc);
-          s.selfv[i + m * R] = acc;
-        }
-        __syncthreads();
-        // this CTA's part of sum_k gcoef_k sum_r c_kr Q_kr^j(m) psn_k(r, i)
-        for (int e = tid; e < R * nj; e += nt) {
-          const int i = e % R, m = e / R;
-          double acc = 0.0;
-          for (int kl = 0; kl < nk; ++kl) {
-            const int k = rank + kl * CL;
-            const double* qc = p.coef + (size_t)k * R;
-            const double* ps = psn_all + (size_t)k * RR;
-            double inner = 0.0;
-            for (int r = 0; r < R; ++r)
-              inner = fma(qc[r] * p.base[((size_t)k * R + r) * nD + p.off[j] + m], ps[r * R + i], inner);
-            acc = fma(p.gcoef[k], inner, acc);
-          }
-          bp[i + m * R] = acc;
-        }
+      for (int j = 0; j < c.D; ++j, ++step) {
+        dw* bp = c.a.bpart + (size_t)(step & 1) * c.R * c.npm;
+        step_products(c, j, nk);
+        step_dots(c, j, nk);
+        step_rhs_part(c, j, nk, bp);
+        // a peer's bpart of step s is rewritten at step s + 2, after every
+        // CTA has passed the barrier of step s + 1 (and so its gather of s)
         cl_arrive();
         cl_wait();
-        // every CTA: gather in rank order, then the same solve
-        for (int e = tid; e < R * nj; e += nt) {
-          const int i = e % R, m = e / R;
-          double acc = 0.0;
-          for (int c = 0; c < CL; ++c) acc += cluster.map_shared_rank(bp, c)[i + m * R];
-          s.X[i + m * R] = acc + s.selfv[i + m * R];
-        }
-        __syncthreads();
-        block_ldlt(s.BB, R, R, s.dinv, s.ucol, &s.flags[0]);
-        if (tid == 0 && s.flags[0]) s.flags[1] = 1;
-        block_ldlt_solve(s.BB, R, R, s.dinv, s.X, nj, R);
-        for (int i = tid; i < R; i += nt) {
-          double nrm, inv;
-          scaled_norm(s.X + i, nj, R, &nrm, &inv);
-          for (int m = 0; m < nj; ++m) s.X[i + m * R] *= inv;
-          s.fcs[i] = nrm;
-        }
-        __syncthreads();
-        // new factor of mode j, its Gram, and the owned overlaps of mode j
-        for (int e = tid; e < R * nj; e += nt) {
-          const int i = e / nj, m = e % nj;
-          fbw[(size_t)i * nD + p.off[j] + m] = s.X[i + m * R];
-        }
-        for (int e = tid; e < RR; e += nt) {
-          const int i = e % R, i2 = e / R;
-          double acc = 0.0;
-          for (int q = 0; q < nj; ++q) acc += s.X[i + q * R] * s.X[i2 + q * R];
-          g64w[(size_t)j * RR + e] = acc;
-        }
-        for (size_t e = tid; e < (size_t)nk * RR; e += nt) {
-          const int k = rank + (int)(e / RR) * CL, r = (int)(e % RR) / R, i = (int)(e % R);
-          const double* a = p.base + ((size_t)k * R + r) * nD + p.off[j];
-          double acc = 0.0;
-          for (int q = 0; q < nj; ++q) acc = fma(a[q], s.X[i + q * R], acc);
-          P(k, j)[r * R + i] = acc;
-        }
-        __syncthreads();
-        normalize_weights();
+        step_gather(c, cluster, j, bp);
+        step_solve(c, j);
+        step_update(c, j, nk);
+        normalize_weights(c);
       }
     }
-    // the finished vector becomes Q_iv for the next ones
-    store_vector(iv, true);
-    __threadfence();
-    cl_arrive();
-    cl_wait();
+    finish_vector(c, p, iv, true);
   }
-  if (rank == 0 && tid == 0 && s.flags[1]) atomicOr(p.status, 1);
+  if (c.rank == 0 && c.tid == 0 && c.a.flags[1]) atomicOr(p.status, 1);
   // no CTA leaves while a peer may still read its shared memory
   cl_arrive();
   cl_wait();
@@ -274,14 +434,50 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
 
 int gs_cluster_size(int nbloc) { return nbloc > 16 ? 16 : (nbloc > 1 ? nbloc - 1 : 1); }
 
-size_t gs_work_doubles(int nbloc, int R, int nD, int D) {
-  return (size_t)gs_cluster_size(nbloc) * ((size_t)R * nD + (size_t)D * R * R);
+namespace {
+
+int gs_nkmax(int nbloc) {
+  const int cl = gs_cluster_size(nbloc);
+  return std::max(1, (nbloc - 1 + cl - 1) / cl);
 }
 
-int gs_launch(const GsParams& p, cudaStream_t st) {
-  GsSmem s;
-  const size_t smem = gs_carve(p.R, p.npmax, &s, nullptr);
+// Global scratch entries (dw) of one CTA with every movable group there.
+size_t gs_cta_work(int nbloc, int R, int nD, int D, int npm) {
+  GsArrays a;
+  size_t gw = 0;
+  gs_carve(GsDims{R, D, nD, npm, gs_nkmax(nbloc), kGroupAll}, &a, nullptr, nullptr, &gw);
+  return gw;
+}
+
+}  // namespace
+
+size_t gs_work_doubles(int nbloc, int R, int nD, int D, int npm) {
+  return (size_t)gs_cluster_size(nbloc) * gs_cta_work(nbloc, R, nD, D, npm);
+}
+
+int gs_launch(const GsParams& prm, cudaStream_t st) {
+  GsParams p = prm;
   const int cl = gs_cluster_size(p.nbloc);
+  p.nkmax = gs_nkmax(p.nbloc);
+  p.work_stride = (long long)gs_cta_work(p.nbloc, p.R, p.nD, p.D, p.npmax);
+  int dev = 0, smem_max = 0;
+  MLCP_CUDA_TRY(cudaGetDevice(&dev));
+  MLCP_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  // keep as much resident as fits: the owned vectors move out first, then
+  // their overlaps, then the working vector
+  static const int masks[4] = {0, kGroupQ, kGroupQ | kGroupP, kGroupAll};
+  size_t smem = 0;
+  int q = 0;
+  for (; q < 4; ++q) {
+    GsArrays a;
+    smem = gs_carve(GsDims{p.R, p.D, p.nD, p.npmax, p.nkmax, masks[q]}, &a, nullptr, nullptr, nullptr);
+    if (smem <= (size_t)smem_max) break;
+  }
+  if (q == 4) {
+    set_error("intertwinecpp_: Gram-Schmidt needs %zu bytes of shared memory (rank %d)", smem, p.R);
+    return kTooLarge;
+  }
+  p.gmask = masks[q];
   MLCP_CUDA_TRY(cudaFuncSetAttribute(gs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (cl > 8) MLCP_CUDA_TRY(cudaFuncSetAttribute(gs_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};

@@ -59,15 +59,17 @@ struct GsParams {
   const int* offp;
   double* base;   // block, in place
   double* coef;
-  double* pscr;   // [nbloc][D+1][R][R] P(k,d) = Q_k,d F_d^T, then products over d != j
-  double* g64;    // [D][R][R]
-  double* gcoef;  // [nbloc]
-  double* work;   // [cluster][R*nD + D*R*R] each CTA's copy of the vector being fitted and its Grams
+  double* work;   // per-CTA scratch for the arrays that do not fit in shared memory (gs_work_doubles)
   int* status;
+  // set by gs_launch
+  int nkmax;             // earlier vectors owned by one CTA, at most
+  int gmask;             // array groups placed in global scratch
+  long long work_stride; // scratch entries of one CTA
 };
 int gs_launch(const GsParams& p, cudaStream_t st);
-// Doubles of GsParams::work needed for a block of nbloc vectors.
-size_t gs_work_doubles(int nbloc, int R, int nD, int D);
+// Doubles of GsParams::work needed for a block of nbloc vectors (npm: the
+// largest 4-padded basis size).
+size_t gs_work_doubles(int nbloc, int R, int nD, int D, int npm);
 
 // Block Rayleigh-Ritz inner products: QHQ(i,j) = <Q_j, HQ_i>, S(i,j) = <Q_j, Q_i>, j <= i.
 struct GepParams {

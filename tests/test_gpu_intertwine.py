@@ -60,6 +60,8 @@ CASES = [
     (lambda: H.henon_heiles(D=4, n=6), 6, 5, 3, 3, True, 1, 6.0),
     (lambda: H.random_hoplist([6, 4, 5, 3], 9, seed=8, coupling=3), 4, 3, 2, 3, False, -1, 1.5),
     (lambda: H.random_hoplist([5, 7], 4, seed=2), 3, 3, 3, 0, False, 0, 0.0),
+    # 34 vectors: a 16-CTA Gram-Schmidt cluster, up to 3 earlier vectors per CTA
+    (lambda: H.random_hoplist([4, 3, 5], 5, seed=11), 3, 34, 1, 2, False, 1, 3.0),
 ]
 
 
