@@ -162,6 +162,31 @@ MLCP_HD dw dw_sqrt(dw a) {
   return fast_two_sum(s0, f_mul(f_mul(0.5f, y0), r));
 }
 
+// Compensated accumulation of a sum of products of double-word values: the
+// FP32 running sum s and, in c, the FP32 sum of the exact errors of each
+// product (two_prod) and addition (two_sum) together with the products'
+// low-order cross terms.  This is the dot product Dot2 of Ogita, Rump and
+// Oishi ("Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005)
+// with double-word operands.  Its error is about n u^2 sum |x_i y_i|, as for
+// a chain of dw_fma, but the dependency chain through s is one FP32 addition
+// per term and a term costs about half the instructions.
+struct dw_acc {
+  float s, c;
+};
+MLCP_HD dw_acc acc_zero() { return dw_acc{0.f, 0.f}; }
+MLCP_HD void acc_fma(dw_acc& a, dw x, dw y) {
+  const dw p = two_prod(x.hi, y.hi);
+  const dw t = two_sum(a.s, p.hi);
+  a.s = t.hi;
+  a.c = f_add(a.c, f_add(f_add(t.lo, p.lo), f_fma(x.hi, y.lo, f_mul(x.lo, y.hi))));
+}
+MLCP_HD void acc_add(dw_acc& a, dw x) {
+  const dw t = two_sum(a.s, x.hi);
+  a.s = t.hi;
+  a.c = f_add(a.c, f_add(t.lo, x.lo));
+}
+MLCP_HD dw acc_value(dw_acc a) { return two_sum(a.s, a.c); }
+
 MLCP_HD dw dw_abs(dw a) { return (a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f)) ? dw_neg(a) : a; }
 MLCP_HD bool dw_gt(dw a, dw b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
 

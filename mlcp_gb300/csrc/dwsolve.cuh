@@ -118,6 +118,51 @@ __device__ inline dw dw_normalise_row(dw* x, int n, int ld) {
   return r;
 }
 
+__device__ __forceinline__ dw dw_shfl_xor(dw v, int o) {
+  return dw{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+
+// dw_normalise_row for all nr rows of X (column-major, ld nr, n columns) by
+// the solver team, G lanes of one warp per row (G the largest power of two
+// <= 32 with G nr <= 128); norms to nrm[i].  The lanes of a row combine
+// their maxima and sums of squares by butterflies, so all of them hold the
+// same norm.  Ends without a barrier.
+__device__ inline void dw_normalise_rows(dw* X, int nr, int n, dw* nrm) {
+  int G = 32;
+  while (G > 1 && G * nr > kSolverThreads) G >>= 1;
+  const int t = threadIdx.x, row = t / G, sub = t - row * G;
+  const bool live = row < nr;
+  dw* x = X + (live ? row : 0);
+  dw largest = dw_make(0.f);
+  for (int q = sub; q < n; q += G) {
+    const dw a = dw_abs(x[q * nr]);
+    if (dw_gt(a, largest)) largest = a;
+  }
+  for (int o = G / 2; o > 0; o >>= 1) {
+    const dw b = dw_shfl_xor(largest, o);
+    if (dw_gt(b, largest)) largest = b;
+  }
+  const bool zero = !(largest.hi > 0.f);
+  const dw il = dw_rcp(zero ? dw_make(1.f) : largest);
+  dw acc = dw_make(0.f);
+  for (int q = sub; q < n; q += G) {
+    const dw y = dw_mul(x[q * nr], il);
+    acc = dw_fma(y, y, acc);
+  }
+  for (int o = G / 2; o > 0; o >>= 1) acc = dw_add(acc, dw_shfl_xor(acc, o));
+  if (!live) return;
+  if (zero) {  // NaN, as the reference's zero-row norm
+    const float nan = __int_as_float(0x7fffffff);
+    for (int q = sub; q < n; q += G) x[q * nr] = dw_make(nan);
+    if (sub == 0) nrm[row] = dw_make(nan);
+    return;
+  }
+  const dw r = dw_mul(largest, dw_sqrt(acc));
+  const dw inv = dw_rcp(r);
+  for (int q = sub; q < n; q += G) x[q * nr] = dw_mul(x[q * nr], inv);
+  if (sub == 0) nrm[row] = r;
+}
+
 // Walk over the entries e = tid, tid + 128, ... of a matrix with n rows
 // (column-major), tracking (row, column) = (e mod n, e div n) without dividing.
 struct Walk {
@@ -201,6 +246,48 @@ __device__ inline const float* gj_inverse(const dw* A, int n, float* gi, bool* o
   return gi + cur * nn;
 }
 
+// The same FP32 Gauss-Jordan inverse for n <= N <= 32 by one warp, in
+// registers: lane j holds column j, and each elimination step broadcasts the
+// pivot column from its lane by shuffles, so no step touches shared memory or
+// waits at a barrier.  Writes the inverse to inv (column-major, ld n) and
+// returns whether every pivot was positive.  All 32 lanes must call it.
+template <int N>
+__device__ inline bool gj_inverse_warp_n(const dw* A, int n, float* inv) {
+  const int lane = threadIdx.x & 31;
+  const bool col = lane < n;
+  float a[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) a[i] = (col && i < n) ? A[i + lane * n].hi : 0.f;
+  bool good = true;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    if (k >= n) break;
+    const float piv = __shfl_sync(0xffffffffu, a[k], k);
+    good = good && piv > 0.f;
+    float pk = f_rcp_approx(piv);
+    pk = pk * fmaf(-piv, pk, 2.0f);
+    const float rk = a[k] * pk;  // row k of this column, scaled
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const float cik = __shfl_sync(0xffffffffu, a[i], k);  // column k, before the step
+      if (i == k) a[i] = (lane == k) ? pk : rk;
+      else a[i] = (lane == k) ? -cik * pk : fmaf(-cik, rk, a[i]);
+    }
+  }
+  if (col)
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+      if (i < n) inv[i + lane * n] = a[i];
+  return good;
+}
+
+// Register Gauss-Jordan for n <= 32, by the calling warp.
+__device__ inline bool gj_inverse_warp(const dw* A, int n, float* inv) {
+  if (n <= 8) return gj_inverse_warp_n<8>(A, n, inv);
+  if (n <= 16) return gj_inverse_warp_n<16>(A, n, inv);
+  return gj_inverse_warp_n<32>(A, n, inv);
+}
+
 // Refinement rounds before falling back to the double-word LDL^T.
 constexpr int kRefineMax = 4;
 
@@ -240,36 +327,27 @@ __device__ inline bool refine_solve(const dw* A, int n, const dw* B, dw* X, int 
     float* rd = red + 2 * (round & 1);
     if (t == 0) rd[0] = rd[1] = 0.f;
     solver_sync();
-    // R = B - A X (double-word); two chains per entry (even and odd j)
+    // R = B - A X, compensated accumulation (two entries per thread)
     {
       Walk w = walk_start(t, n);
       for (int e0 = t; e0 < nr; e0 += 2 * kSolverThreads) {
         int ii[2], jj[2];
-        dw a0[2], a1[2];
+        dw_acc acc[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
           ii[q] = w.i;
           jj[q] = w.j;
-          a0[q] = (e0 + q * kSolverThreads < nr) ? B[e0 + q * kSolverThreads] : dw_make(0.f);
-          a1[q] = dw_make(0.f);
+          acc[q] = acc_zero();
+          if (e0 + q * kSolverThreads < nr) acc_add(acc[q], B[e0 + q * kSolverThreads]);
           walk_next(w);
         }
         const bool two = e0 + kSolverThreads < nr;
-        int j = 0;
-        for (; j + 1 < n; j += 2) {
-          a0[0] = dw_add_sloppy(a0[0], dw_neg(dw_mul(A[ii[0] + j * n], X[j + jj[0] * n])));
-          a1[0] = dw_add_sloppy(a1[0], dw_neg(dw_mul(A[ii[0] + (j + 1) * n], X[j + 1 + jj[0] * n])));
-          if (two) {
-            a0[1] = dw_add_sloppy(a0[1], dw_neg(dw_mul(A[ii[1] + j * n], X[j + jj[1] * n])));
-            a1[1] = dw_add_sloppy(a1[1], dw_neg(dw_mul(A[ii[1] + (j + 1) * n], X[j + 1 + jj[1] * n])));
-          }
+        for (int j = 0; j < n; ++j) {
+          acc_fma(acc[0], dw_neg(A[ii[0] + j * n]), X[j + jj[0] * n]);
+          if (two) acc_fma(acc[1], dw_neg(A[ii[1] + j * n]), X[j + jj[1] * n]);
         }
-        if (j < n) {
-          a0[0] = dw_add_sloppy(a0[0], dw_neg(dw_mul(A[ii[0] + j * n], X[j + jj[0] * n])));
-          if (two) a0[1] = dw_add_sloppy(a0[1], dw_neg(dw_mul(A[ii[1] + j * n], X[j + jj[1] * n])));
-        }
-        R[e0] = dw_add_sloppy(a0[0], a1[0]);
-        if (two) R[e0 + kSolverThreads] = dw_add_sloppy(a0[1], a1[1]);
+        R[e0] = acc_value(acc[0]);
+        if (two) R[e0 + kSolverThreads] = acc_value(acc[1]);
       }
     }
     solver_sync();
@@ -314,6 +392,123 @@ __device__ inline bool refine_solve(const dw* A, int n, const dw* B, dw* X, int 
     ok = rd[0] <= 1e-10f * rd[1] || (round == 0 && rd[0] <= 1e-5f * rd[1]);
   }
   return ok;
+}
+
+
+__device__ __forceinline__ dw dw_shfl(dw v, int src) {
+  return dw{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+
+// Shared-memory scratch of solve_cols.
+struct ColScratch {
+  float* conv;  // [2][32] convergence partials per warp (two rounds in flight)
+  float* rmax;  // [16][32] row maxima per warp
+  dw* rsum;     // [16][32] row sums of squares per warp
+};
+
+// X = A^-1 B for n <= N rows and nrhs <= 16 columns by the first
+// solve_cols_warps(n, nrhs) warps of the block, synchronising on named
+// barrier 3: the iterative refinement of refine_solve with the rows of the
+// FP32 inverse (symmetric, so row i = column i) and of A held in registers
+// and the vectors exchanged by shuffles, so that a product costs n shuffles
+// and multiply-adds per lane and a round one barrier.  A warp holds H = 32/S
+// columns of S >= N lanes each (column m = H w + h; lane h S + i: row i).
+// When it converges, the rows of X are normalised as dw_normalise_rows does
+// (norms to nrm) and it returns true; otherwise it returns false with X
+// untouched.
+template <int N, int S>
+__device__ inline bool solve_cols(const dw* A, int n, const dw* B, dw* X, int nrhs, const float* inv, dw* nrm,
+                                  const ColScratch& s) {
+  constexpr int H = 32 / S;
+  static_assert(N <= S && S * H == 32, "column layout");
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, h = lane / S, i = lane - h * S, src = h * S;
+  const int m = H * w + h, nw = (nrhs + H - 1) / H, nthr = nw * 32;
+  const bool row = m < nrhs && i < n;
+  float iv[N];
+  dw ar[N <= 16 ? N : 1];
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    iv[j] = (row && j < n) ? inv[i + j * n] : 0.f;
+    if constexpr (N <= 16) ar[j] = (row && j < n) ? A[i + j * n] : dw_make(0.f);
+  }
+  const dw b = row ? B[i + m * n] : dw_make(0.f);
+  float x0 = 0.f;
+#pragma unroll
+  for (int j = 0; j < N; ++j) x0 = fmaf(iv[j], __shfl_sync(0xffffffffu, b.hi, src + j), x0);
+  dw x = dw_make(x0);
+  bool ok = false;
+  for (int round = 0; round < kRefineMax && !ok; ++round) {
+    // r = b - A x (compensated), then the FP32 correction inv r
+    dw_acc acc = acc_zero();
+    acc_add(acc, b);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const dw xj = dw_shfl(x, src + j);
+      dw aij;
+      if constexpr (N <= 16) aij = ar[j];
+      else aij = (row && j < n) ? A[i + j * n] : dw_make(0.f);
+      acc_fma(acc, dw_neg(aij), xj);
+    }
+    const dw r = acc_value(acc);
+    float d = 0.f;
+#pragma unroll
+    for (int j = 0; j < N; ++j) d = fmaf(iv[j], __shfl_sync(0xffffffffu, r.hi, src + j), d);
+    if (row) x = dw_add_f(x, d);
+    float mdx = row ? ((fabsf(d) <= FLT_MAX) ? fabsf(d) : INFINITY) : 0.f;
+    float mx = row ? fabsf(x.hi) : 0.f;
+    for (int o = 16; o > 0; o >>= 1) {
+      mdx = fmaxf(mdx, __shfl_xor_sync(0xffffffffu, mdx, o));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    float* cv = s.conv + (round & 1) * 32;
+    if (lane == 0) {
+      cv[w] = mdx;
+      cv[16 + w] = mx;
+    }
+    asm volatile("bar.sync 3, %0;" ::"r"(nthr) : "memory");
+    float gd = 0.f, gx = 0.f;
+    for (int q = 0; q < nw; ++q) {
+      gd = fmaxf(gd, cv[q]);
+      gx = fmaxf(gx, cv[16 + q]);
+    }
+    // the convergence rule of refine_solve
+    ok = gd <= 1e-10f * gx || (round == 0 && gd <= 1e-5f * gx);
+  }
+  if (!ok) return false;
+  // rows: scale by the largest |x|, sum the squares over the columns
+  const int slot = (m < 16 ? m : 15) * 32 + i;
+  if (m < nrhs) s.rmax[slot] = fabsf(x.hi);
+  asm volatile("bar.sync 3, %0;" ::"r"(nthr) : "memory");
+  float big = 0.f;
+  for (int q = 0; q < nrhs; ++q) big = fmaxf(big, s.rmax[q * 32 + i]);
+  const bool zero = !(big > 0.f);
+  const dw il = dw_rcp(dw_make(zero ? 1.f : big));
+  const dw y = dw_mul(x, il);
+  if (m < nrhs) s.rsum[slot] = dw_mul(y, y);
+  asm volatile("bar.sync 3, %0;" ::"r"(nthr) : "memory");
+  dw_acc sq = acc_zero();
+  for (int q = 0; q < nrhs; ++q) acc_add(sq, s.rsum[q * 32 + i]);
+  if (!row) return true;
+  if (zero) {  // NaN, as the reference's zero-row norm
+    const float nan = __int_as_float(0x7fffffff);
+    X[i + m * n] = dw_make(nan);
+    if (m == 0) nrm[i] = dw_make(nan);
+    return true;
+  }
+  const dw r = dw_mul(dw_make(big), dw_sqrt(acc_value(sq)));
+  X[i + m * n] = dw_mul(x, dw_rcp(r));
+  if (m == 0) nrm[i] = r;
+  return true;
+}
+
+// Warps used by solve_cols_any for an n-row system with nrhs columns.
+__host__ __device__ inline int solve_cols_warps(int n, int nrhs) { return n <= 16 ? (nrhs + 1) / 2 : nrhs; }
+
+// solve_cols for n <= 32 (two columns per warp when n <= 16).
+__device__ inline bool solve_cols_any(const dw* A, int n, const dw* B, dw* X, int nrhs, const float* inv, dw* nrm,
+                                      const ColScratch& s) {
+  if (n <= 16) return solve_cols<16, 16>(A, n, B, X, nrhs, inv, nrm, s);
+  return solve_cols<32, 32>(A, n, B, X, nrhs, inv, nrm, s);
 }
 
 }  // namespace dwsolve

@@ -57,11 +57,12 @@ struct GsDims {
 
 struct GsArrays {
   dw *qf, *qw, *qc;        // [nkmax][R][nD] owned vectors' factors, the same times their weights; [nkmax][R] weights
-  dw *P, *psn, *part;      // [nkmax][D][R*R] overlaps (index r*R+i); [nkmax][R*R] products over d != j;
-                           // [nkmax+1][2][R*npm] partial dot products
+  dw *P, *psn, *ppsn, *part;  // [nkmax][D][R*R] overlaps (index r*R+i); [nkmax][R*R] products over d != j,
+                               // and over d not in {j, next mode}; [nkmax+1][2][R*npm] partial dot products
   dw *fb, *g;              // [R][nD] vector being fitted; [D][R*R] its Grams
-  dw *fcs, *wf, *Gp, *BB, *gpart, *gco, *bpart, *X, *b0, *res, *dinv, *u, *red, *misc;
+  dw *fcs, *wf, *Gp, *pGp, *BB, *gpart, *gco, *bpart, *X, *b0, *res, *dinv, *u, *red, *misc;
   float *gi, *rred;
+  dwsolve::ColScratch cs;
   int *nb, *off, *flags;
 };
 
@@ -93,12 +94,14 @@ __host__ __device__ inline size_t gs_carve(const GsDims& m, GsArrays* a, unsigne
   a->qc = take(kGroupQ, (size_t)nkm * R);
   a->P = take(kGroupP, (size_t)nkm * m.D * RR);
   a->psn = take(kGroupP, (size_t)nkm * RR);
+  a->ppsn = take(kGroupP, (size_t)nkm * RR);
   a->part = take(kGroupP, (size_t)(nkm + 1) * 2 * Rn);
   a->fb = take(kGroupF, (size_t)R * m.nD);
   a->g = take(kGroupF, (size_t)m.D * RR);
   a->fcs = (dw*)take_s(sizeof(dw) * R);
   a->wf = (dw*)take_s(sizeof(dw) * Rn);
   a->Gp = (dw*)take_s(sizeof(dw) * RR);
+  a->pGp = (dw*)take_s(sizeof(dw) * RR);
   a->BB = (dw*)take_s(sizeof(dw) * RR);
   a->gpart = (dw*)take_s(sizeof(dw) * nkm * (gs_rrp(R) / 32));
   a->gco = (dw*)take_s(sizeof(dw) * nkm);
@@ -112,6 +115,9 @@ __host__ __device__ inline size_t gs_carve(const GsDims& m, GsArrays* a, unsigne
   a->misc = (dw*)take_s(sizeof(dw) * 4);
   a->gi = (float*)take_s(sizeof(float) * 2 * RR);
   a->rred = (float*)take_s(sizeof(float) * 4);
+  a->cs.conv = (float*)take_s(sizeof(float) * 64);
+  a->cs.rmax = (float*)take_s(sizeof(float) * 16 * 32);
+  a->cs.rsum = (dw*)take_s(sizeof(dw) * 16 * 32);
   a->nb = (int*)take_s(sizeof(int) * (m.D + 1));
   a->off = (int*)take_s(sizeof(int) * (m.D + 1));
   a->flags = (int*)take_s(sizeof(int) * 4);
@@ -122,20 +128,23 @@ __host__ __device__ inline size_t gs_carve(const GsDims& m, GsArrays* a, unsigne
 __device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ dw shfl_xor_dw(dw v, int o) {
-  return dw{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+// Threads outside the solver team (warps 4-15).
+constexpr int kWorkerThreads = kGsThreads - dwsolve::kSolverThreads;
+// Barrier of the threads w0..511 (named barrier 2).
+__device__ __forceinline__ void worker_sync(int w0) {
+  asm volatile("bar.sync 2, %0;" ::"r"(kGsThreads - w0) : "memory");
 }
 
 // Sum over the block; every thread gets the same value (dw_add is
 // commutative, so the butterflies agree across lanes and warps).
 __device__ dw block_sum(dw v, dw* red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int o = 16; o > 0; o >>= 1) v = dw_add(v, shfl_xor_dw(v, o));
+  for (int o = 16; o > 0; o >>= 1) v = dw_add(v, dwsolve::dw_shfl_xor(v, o));
   __syncthreads();
   if (lane == 0) red[warp] = v;
   __syncthreads();
   dw s = red[lane & (kGsWarps - 1)];
-  for (int o = kGsWarps / 2; o > 0; o >>= 1) s = dw_add(s, shfl_xor_dw(s, o));
+  for (int o = kGsWarps / 2; o > 0; o >>= 1) s = dw_add(s, dwsolve::dw_shfl_xor(s, o));
   return s;
 }
 
@@ -165,8 +174,9 @@ __device__ void all_grams(const Gs& c) {
     if (i > i2) continue;
     const dw* x = c.a.fb + (size_t)i * c.nD + c.a.off[d];
     const dw* y = c.a.fb + (size_t)i2 * c.nD + c.a.off[d];
-    dw s = dw_make(0.f);
-    for (int q = 0; q < c.a.nb[d]; ++q) s = dw_fma(x[q], y[q], s);
+    dw_acc acc = acc_zero();
+    for (int q = 0; q < c.a.nb[d]; ++q) acc_fma(acc, x[q], y[q]);
+    const dw s = acc_value(acc);
     c.a.g[(size_t)d * RR + i + i2 * R] = s;
     c.a.g[(size_t)d * RR + i2 + i * R] = s;
   }
@@ -180,9 +190,9 @@ __device__ void all_overlaps(const Gs& c, int nk) {
     const int kl = e / DRR, rem = e - kl * DRR, d = rem / RR, ee = rem - d * RR, r = ee / R, i = ee - r * R;
     const dw* x = c.a.qf + ((size_t)kl * R + r) * c.nD + c.a.off[d];
     const dw* y = c.a.fb + (size_t)i * c.nD + c.a.off[d];
-    dw s = dw_make(0.f);
-    for (int q = 0; q < c.a.nb[d]; ++q) s = dw_fma(x[q], y[q], s);
-    c.a.P[(size_t)kl * DRR + rem] = s;
+    dw_acc acc = acc_zero();
+    for (int q = 0; q < c.a.nb[d]; ++q) acc_fma(acc, x[q], y[q]);
+    c.a.P[(size_t)kl * DRR + rem] = acc_value(acc);
   }
   __syncthreads();
 }
@@ -226,13 +236,14 @@ __device__ void finish_vector(const Gs& c, const GsParams& p, int iv, bool facto
   __syncthreads();
 }
 
-// Step phase 1: products over d != j of the owned overlaps (psn) and of the
-// working Grams (Gp, and BB = Gp + pen I), the weighted factor wf(r,m) =
-// c_r F_r^j(m), and per warp of psn entries the partial sums of
+// Step phase 1.  Unless the previous step's update already formed them
+// (`pre`), the products over d != j of the owned overlaps (psn) and of the
+// working Grams (Gp, and BB = Gp + pen I).  Always: the weighted factor
+// wf(r,m) = c_r F_r^j(m), and per warp of psn entries the partial sums of
 // c_k,r c_i P_k(r,i) over all modes (the coefficients <Q_k, F>).
-__device__ void step_products(const Gs& c, int j, int nk) {
+__device__ void step_products(const Gs& c, int j, int nk, bool pre) {
   const int R = c.R, RR = c.RR, RRp = c.RRp, D = c.D, nj = c.a.nb[j], offj = c.a.off[j];
-  const int npsn = nk * RRp, ngp = npsn + RR, total = ngp + R * nj;
+  const int npsn = nk * RRp, ngp = npsn + (pre ? 0 : RR), total = ngp + R * nj;
   const dw pen = c.a.misc[0];
   for (int e = c.tid; e < total; e += kGsThreads) {
     if (e < npsn) {  // whole warps: npsn is a multiple of 32
@@ -242,13 +253,18 @@ __device__ void step_products(const Gs& c, int j, int nk) {
         const int r = ee / R, i = ee - r * R;
         const dw* Pk = c.a.P + (size_t)kl * D * RR + ee;
         const dw pj = Pk[(size_t)j * RR], w = dw_mul(c.a.qc[(size_t)kl * R + r], c.a.fcs[i]);
-        dw prod = dw_make(1.f);
-        for (int d = 0; d < D; ++d)
-          if (d != j) prod = dw_mul(prod, Pk[(size_t)d * RR]);
+        dw prod;
+        if (pre) {
+          prod = c.a.psn[(size_t)kl * RR + ee];
+        } else {
+          prod = dw_make(1.f);
+          for (int d = 0; d < D; ++d)
+            if (d != j) prod = dw_mul(prod, Pk[(size_t)d * RR]);
+        }
         contrib = dw_mul(dw_mul(prod, pj), w);
-        c.a.psn[(size_t)kl * RR + ee] = prod;
+        if (!pre) c.a.psn[(size_t)kl * RR + ee] = prod;
       }
-      for (int o = 16; o > 0; o >>= 1) contrib = dw_add(contrib, shfl_xor_dw(contrib, o));
+      for (int o = 16; o > 0; o >>= 1) contrib = dw_add(contrib, dwsolve::dw_shfl_xor(contrib, o));
       if ((c.tid & 31) == 0) c.a.gpart[kl * (RRp / 32) + ee / 32] = contrib;
     } else if (e < ngp) {
       const int ee = e - npsn;
@@ -265,46 +281,48 @@ __device__ void step_products(const Gs& c, int j, int nk) {
   __syncthreads();
 }
 
-// Step phase 2: the dot products over r, split in two halves,
+// Step phase 2 (threads w0..511, while the lower warps invert BB): the dot
+// products over r, split in two halves,
 //   source 0:        sum_r wf(r,m) Gp(r,i)                      (self term)
 //   source 1 + kl:   sum_r c_k,r Q_k,r^j(m) psn_k(r,i)          (owned k)
 // at part[(2 s + h) R nj + i + m R]; and gco_k = -<Q_k, F> from the partials.
-__device__ void step_dots(const Gs& c, int j, int nk) {
+__device__ void step_dots(const Gs& c, int j, int nk, int w0) {
   const int R = c.R, RR = c.RR, nj = c.a.nb[j], offj = c.a.off[j], Rn = R * nj, half = (R + 1) / 2;
-  const int total = (nk + 1) * 2 * Rn;
-  for (int e = c.tid; e < total; e += kGsThreads) {
+  const int total = (nk + 1) * 2 * Rn, w = c.tid - w0, nw = kGsThreads - w0;
+  for (int e = w; e < total; e += nw) {
     const int sh = e / Rn, em = e - sh * Rn, s = sh >> 1, i = em % R, m = em / R;
     const int r0 = (sh & 1) ? half : 0, r1 = (sh & 1) ? R : half;
-    dw acc = dw_make(0.f);
+    dw_acc acc = acc_zero();
     if (s == 0) {
-      for (int r = r0; r < r1; ++r) acc = dw_fma(c.a.wf[r + m * R], c.a.Gp[r * R + i], acc);
+      for (int r = r0; r < r1; ++r) acc_fma(acc, c.a.wf[r + m * R], c.a.Gp[r * R + i]);
     } else {
       const dw* A = c.a.qw + (size_t)(s - 1) * R * c.nD + offj + m;
       const dw* M = c.a.psn + (size_t)(s - 1) * RR + i;
-      for (int r = r0; r < r1; ++r) acc = dw_fma(A[(size_t)r * c.nD], M[r * R], acc);
+      for (int r = r0; r < r1; ++r) acc_fma(acc, A[(size_t)r * c.nD], M[r * R]);
     }
-    c.a.part[e] = acc;
+    c.a.part[e] = acc_value(acc);
   }
-  if (c.tid < nk) {
+  if (w < nk) {
     const int nch = c.RRp / 32;
     dw s = dw_make(0.f);
-    for (int q = 0; q < nch; ++q) s = dw_add(s, c.a.gpart[c.tid * nch + q]);
-    c.a.gco[c.tid] = dw_neg(s);
+    for (int q = 0; q < nch; ++q) s = dw_add(s, c.a.gpart[w * nch + q]);
+    c.a.gco[w] = dw_neg(s);
   }
-  __syncthreads();
+  worker_sync(w0);
 }
 
-// Step phase 3: this CTA's part of the right-hand side,
+// Step phase 3 (threads w0..511): this CTA's part of the right-hand side,
 //   sum_k gco_k sum_r c_k,r Q_k,r^j(m) psn_k(r,i).
-__device__ void step_rhs_part(const Gs& c, int j, int nk, dw* bp) {
+__device__ void step_rhs_part(const Gs& c, int j, int nk, dw* bp, int w0) {
   const int Rn = c.R * c.a.nb[j];
-  for (int e = c.tid; e < Rn; e += kGsThreads) {
-    dw acc = dw_make(0.f);
+  for (int e = c.tid - w0; e < Rn; e += kGsThreads - w0) {
+    dw_acc acc = acc_zero();
     for (int kl = 0; kl < nk; ++kl) {
-      const dw z = dw_add(c.a.part[(size_t)(2 * kl + 2) * Rn + e], c.a.part[(size_t)(2 * kl + 3) * Rn + e]);
-      acc = dw_fma(c.a.gco[kl], z, acc);
+      const dw g = c.a.gco[kl];
+      acc_fma(acc, g, c.a.part[(size_t)(2 * kl + 2) * Rn + e]);
+      acc_fma(acc, g, c.a.part[(size_t)(2 * kl + 3) * Rn + e]);
     }
-    bp[e] = acc;
+    bp[e] = acc_value(acc);
   }
 }
 
@@ -317,40 +335,57 @@ __device__ void step_gather(const Gs& c, cg::cluster_group& cluster, int j, dw* 
     dw v[16];
 #pragma unroll
     for (int r = 0; r < 16; ++r) v[r] = (r < c.CL) ? cluster.map_shared_rank(bp, r)[e] : dw_make(0.f);
+    dw_acc acc = acc_zero();
+    acc_add(acc, c.a.part[e]);
+    acc_add(acc, c.a.part[(size_t)Rn + e]);
 #pragma unroll
-    for (int w = 8; w > 0; w >>= 1)
-#pragma unroll
-      for (int r = 0; r < w; ++r) v[r] = dw_add(v[r], v[r + w]);
-    const dw self = dw_add(c.a.part[e], c.a.part[(size_t)Rn + e]);
-    c.a.b0[e] = dw_add(self, v[0]);
+    for (int r = 0; r < 16; ++r) acc_add(acc, v[r]);
+    c.a.b0[e] = acc_value(acc);
   }
   __syncthreads();
 }
 
-// Step phase 5 (solver warps): X = BB^-1 b0, rows normalised, norms as the
-// new weights.
-__device__ void step_solve(const Gs& c, int j) {
-  if (c.tid < dwsolve::kSolverThreads) {
-    const int R = c.R, nj = c.a.nb[j];
-    bool gj_ok;
-    const float* inv = dwsolve::gj_inverse(c.a.BB, R, c.a.gi, &gj_ok);
-    int bad = 0;
-    if (!(gj_ok && dwsolve::refine_solve(c.a.BB, R, c.a.b0, c.a.X, nj, inv, c.a.res, c.a.rred))) {
-      for (int e = c.tid; e < R * nj; e += dwsolve::kSolverThreads) c.a.X[e] = c.a.b0[e];
-      bad = dwsolve::dw_ldlt(c.a.BB, R, c.a.dinv, c.a.u);
-      dwsolve::dw_ldlt_solve(c.a.BB, R, c.a.dinv, c.a.X, nj);
-    }
-    for (int i = c.tid; i < R; i += dwsolve::kSolverThreads) c.a.fcs[i] = dwsolve::dw_normalise_row(c.a.X + i, nj, R);
-    if (c.tid == 0 && bad) c.a.flags[1] = 1;
+// Step phase 5 (solver warps): X = BB^-1 b0 from the FP32 inverse formed
+// during phases 2-4, rows normalised, norms as the new weights.
+__device__ void step_solve(const Gs& c, int j, const float* inv, bool gj_ok) {
+  const int R = c.R, nj = c.a.nb[j];
+  int bad = 0;
+  if (!(gj_ok && dwsolve::refine_solve(c.a.BB, R, c.a.b0, c.a.X, nj, inv, c.a.res, c.a.rred))) {
+    for (int e = c.tid; e < R * nj; e += dwsolve::kSolverThreads) c.a.X[e] = c.a.b0[e];
+    bad = dwsolve::dw_ldlt(c.a.BB, R, c.a.dinv, c.a.u);
+    dwsolve::dw_ldlt_solve(c.a.BB, R, c.a.dinv, c.a.X, nj);
   }
-  __syncthreads();
+  dwsolve::dw_normalise_rows(c.a.X, R, nj, c.a.fcs);
+  if (c.tid == 0 && bad) c.a.flags[1] = 1;
+}
+
+// When another step of this vector follows (mode jn): the products over d
+// not in {j, jn} of the owned overlaps (ppsn) and of the working Grams (pGp);
+// the update multiplies in mode j.  Threads t0, t0 + nt, ...
+__device__ void step_preproducts(const Gs& c, int j, int jn, int nk, int t0, int nt) {
+  const int RR = c.RR, D = c.D;
+  for (int e = t0; e < (nk + 1) * RR; e += nt) {
+    const int kl = e / RR, ee = e - kl * RR;
+    const bool own = kl < nk;
+    const dw* src = own ? c.a.P + (size_t)kl * D * RR + ee : c.a.g + ee;
+    dw prod = dw_make(1.f);
+    for (int d = 0; d < D; ++d)
+      if (d != j && d != jn) prod = dw_mul(prod, src[(size_t)d * RR]);
+    if (own) c.a.ppsn[(size_t)kl * RR + ee] = prod;
+    else c.a.pGp[ee] = prod;
+  }
 }
 
 // Step phase 6: the new factor of mode j into the working vector, its Gram,
-// and the owned overlaps of mode j.
-__device__ void step_update(const Gs& c, int j, int nk) {
+// and the owned overlaps of mode j; with `pre`, the next step's products
+// psn, Gp and BB (mode jn) completed by multiplying in mode j.  Then the
+// weights are divided by sqrt(<F,F>), whose terms c_i c_i' prod_d G_d(i,i')
+// come with the new Gram.
+__device__ void step_update(const Gs& c, int j, int jn, int nk, bool pre) {
   const int R = c.R, RR = c.RR, nj = c.a.nb[j], offj = c.a.off[j], Rn = R * nj;
   const int total = Rn + RR + nk * RR;
+  const dw pen = c.a.misc[0];
+  dw qpart = dw_make(0.f);
   for (int e = c.tid; e < total; e += kGsThreads) {
     if (e < Rn) {
       const int i = e % R, m = e / R;
@@ -358,23 +393,46 @@ __device__ void step_update(const Gs& c, int j, int nk) {
     } else if (e < Rn + RR) {
       const int ee = e - Rn, i = ee % R, i2 = ee / R;
       if (i > i2) continue;
-      dw s = dw_make(0.f);
-      for (int m = 0; m < nj; ++m) s = dw_fma(c.a.X[i + m * R], c.a.X[i2 + m * R], s);
-      c.a.g[(size_t)j * RR + i + i2 * R] = s;
-      c.a.g[(size_t)j * RR + i2 + i * R] = s;
+      const int et = i2 + i * R;
+      // prod_{d != j} G_d: Gp, or with `pre` pGp = prod_{d not in {j, jn}} G_d times G_jn
+      const dw gp = pre ? c.a.pGp[ee] : c.a.Gp[ee], gq = pre ? dw_mul(gp, c.a.g[(size_t)jn * RR + ee]) : gp;
+      const dw w = dw_mul(c.a.fcs[i], c.a.fcs[i2]);
+      dw_acc acc = acc_zero();
+      for (int m = 0; m < nj; ++m) acc_fma(acc, c.a.X[i + m * R], c.a.X[i2 + m * R]);
+      const dw s = acc_value(acc);
+      c.a.g[(size_t)j * RR + ee] = s;
+      c.a.g[(size_t)j * RR + et] = s;
+      dw t = dw_mul(dw_mul(gq, s), w);
+      if (i != i2) t = dw{2.f * t.hi, 2.f * t.lo};
+      qpart = dw_add(qpart, t);
+      if (pre) {
+        const dw gn = dw_mul(gp, s);
+        c.a.Gp[ee] = gn;
+        c.a.Gp[et] = gn;
+        c.a.BB[ee] = (i == i2) ? dw_add(gn, pen) : gn;
+        c.a.BB[et] = c.a.BB[ee];
+      }
     } else {
       const int ee = e - Rn - RR, kl = ee / RR, e2 = ee - kl * RR, r = e2 / R, i = e2 - r * R;
       const dw* x = c.a.qf + ((size_t)kl * R + r) * c.nD + offj;
-      dw s = dw_make(0.f);
-      for (int m = 0; m < nj; ++m) s = dw_fma(x[m], c.a.X[i + m * R], s);
+      const dw pre_k = pre ? c.a.ppsn[(size_t)kl * RR + e2] : dw_make(1.f);
+      dw_acc acc = acc_zero();
+      for (int m = 0; m < nj; ++m) acc_fma(acc, x[m], c.a.X[i + m * R]);
+      const dw s = acc_value(acc);
       c.a.P[((size_t)kl * c.D + j) * RR + e2] = s;
+      if (pre) c.a.psn[(size_t)kl * RR + e2] = dw_mul(pre_k, s);
     }
   }
+  const dw q = dw_sqrt(dw_abs(block_sum(qpart, c.a.red)));  // every thread has read fcs
+  for (int i = c.tid; i < R; i += kGsThreads) c.a.fcs[i] = dw_div(c.a.fcs[i], q);
   __syncthreads();
 }
 
 }  // namespace
 
+// kResident: every array in shared memory (the compiler then addresses them
+// as such); otherwise the groups of p.gmask live in global scratch.
+template <bool kResident>
 __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -388,7 +446,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
   c.nD = p.nD;
   c.npm = p.npmax;
   c.tid = threadIdx.x;
-  const GsDims dims{p.R, p.D, p.nD, p.npmax, p.nkmax, p.gmask};
+  const GsDims dims{p.R, p.D, p.nD, p.npmax, p.nkmax, kResident ? 0 : p.gmask};
   gs_carve(dims, &c.a, smem_raw, reinterpret_cast<dw*>(p.work) + (size_t)c.rank * p.work_stride, nullptr);
   for (int d = c.tid; d <= c.D; d += kGsThreads) {
     c.a.nb[d] = d < c.D ? p.nbas[d] : 0;
@@ -408,20 +466,64 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
     all_grams(c);
     const int nk = (iv - c.rank + c.CL - 1) / c.CL;  // owned k = rank, rank + CL, ... < iv
     all_overlaps(c, nk);
+    bool pre = false;
     for (int it = 0; it < p.nals; ++it) {
       for (int j = 0; j < c.D; ++j, ++step) {
         dw* bp = c.a.bpart + (size_t)(step & 1) * c.R * c.npm;
-        step_products(c, j, nk);
-        step_dots(c, j, nk);
-        step_rhs_part(c, j, nk, bp);
+        const bool more = it + 1 < p.nals || j + 1 < c.D;  // another step of this vector follows
+        const int jn = j + 1 < c.D ? j + 1 : 0, nj = c.a.nb[j];
+        step_products(c, j, nk, pre);
+        // FP32 inverse of BB (warp 0 in registers for R <= 32, else the
+        // solver warps) concurrently with the right-hand side (threads w0..)
+        bool gj_ok = false;
+        const float* inv = c.a.gi;
+        const int w0 = c.R <= 32 ? 32 : dwsolve::kSolverThreads;
+        if (c.tid < w0) {
+          if (c.R > 32) {
+            inv = dwsolve::gj_inverse(c.a.BB, c.R, c.a.gi, &gj_ok);
+          } else {
+            const bool good = dwsolve::gj_inverse_warp(c.a.BB, c.R, c.a.gi);
+            if (c.tid == 0) c.a.flags[2] = good;
+          }
+        } else {
+          step_dots(c, j, nk, w0);
+          step_rhs_part(c, j, nk, bp, w0);
+        }
         // a peer's bpart of step s is rewritten at step s + 2, after every
         // CTA has passed the barrier of step s + 1 (and so its gather of s)
         cl_arrive();
         cl_wait();
         step_gather(c, cluster, j, bp);
-        step_solve(c, j);
-        step_update(c, j, nk);
-        normalize_weights(c);
+        if (c.R <= 32) gj_ok = c.a.flags[2] != 0;
+        // the solve: refinement in registers (warps 0..nsw-1, one or two
+        // right-hand-side columns each), or the solver warps' refinement /
+        // LDL^T fallback; the next step's partial products on the other warps
+        bool solved = false, pre_done = !more;
+        if (gj_ok && c.R <= 32 && nj <= 16) {
+          const int nsw = dwsolve::solve_cols_warps(c.R, nj) * 32;
+          if (c.tid < nsw) {
+            const bool ok = dwsolve::solve_cols_any(c.a.BB, c.R, c.a.b0, c.a.X, nj, inv, c.a.fcs, c.a.cs);
+            if (c.tid == 0) c.a.flags[3] = ok;
+          } else if (more) {
+            step_preproducts(c, j, jn, nk, c.tid - nsw, kGsThreads - nsw);
+          }
+          __syncthreads();
+          solved = c.a.flags[3] != 0;
+          pre_done = pre_done || nsw < kGsThreads;
+          gj_ok = false;  // not converged: straight to the LDL^T
+        }
+        if (!solved) {
+          if (c.tid < dwsolve::kSolverThreads) step_solve(c, j, inv, gj_ok);
+          else if (!pre_done) step_preproducts(c, j, jn, nk, c.tid - dwsolve::kSolverThreads, kWorkerThreads);
+          __syncthreads();
+          pre_done = true;
+        }
+        if (!pre_done) {
+          step_preproducts(c, j, jn, nk, c.tid, kGsThreads);
+          __syncthreads();
+        }
+        step_update(c, j, jn, nk, more);
+        pre = more;
       }
     }
     finish_vector(c, p, iv, true);
@@ -478,8 +580,9 @@ int gs_launch(const GsParams& prm, cudaStream_t st) {
     return kTooLarge;
   }
   p.gmask = masks[q];
-  MLCP_CUDA_TRY(cudaFuncSetAttribute(gs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (cl > 8) MLCP_CUDA_TRY(cudaFuncSetAttribute(gs_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  void (*kern)(GsParams) = p.gmask == 0 ? gs_kernel<true> : gs_kernel<false>;
+  MLCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (cl > 8) MLCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cl);
   cfg.blockDim = dim3(kGsThreads);
@@ -492,7 +595,7 @@ int gs_launch(const GsParams& prm, cudaStream_t st) {
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  MLCP_CUDA_TRY(cudaLaunchKernelEx(&cfg, gs_kernel, p));
+  MLCP_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, p));
   return kOk;
 }
 

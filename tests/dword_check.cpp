@@ -73,6 +73,26 @@ int main() {
   report("rcp", e_rcp);
   report("div", e_div);
   report("sqrt", e_sqrt);
+  // compensated dot products of 1..40 terms: error relative to sum |x_i y_i|
+  double e_dot = 0, e_sum = 0;
+  for (int t = 0; t < 20000; ++t) {
+    const int nt = 1 + (int)(uniform() * 40);
+    mlcp::dw_acc acc = mlcp::acc_zero(), sacc = mlcp::acc_zero();
+    long double want = 0.0L, mag = 0.0L, swant = 0.0L, smag = 0.0L;
+    for (int q = 0; q < nt; ++q) {
+      const dw x = random_dw(10, false), y = random_dw(10, false);
+      mlcp::acc_fma(acc, x, y);
+      want += ld(x) * ld(y);
+      mag += fabsl(ld(x) * ld(y));
+      mlcp::acc_add(sacc, x);
+      swant += ld(x);
+      smag += fabsl(ld(x));
+    }
+    e_dot = std::fmax(e_dot, scaled(ld(mlcp::acc_value(acc)), want, mag));
+    e_sum = std::fmax(e_sum, scaled(ld(mlcp::acc_value(sacc)), swant, smag));
+  }
+  report("acc_dot", e_dot);
+  report("acc_sum", e_sum);
   report("add_f", e_addf);
   report("mul_f", e_mulf);
   report("from_double", e_conv);

@@ -8,7 +8,10 @@ with u = 2^-24) give about 46 bits (the sloppy sum, Alg. 5, is measured against
 |a| + |b|, the form of its bound); the Newton-step reciprocal and square
 root lose one or two more.  The device reciprocal seed (rcp.approx, 2^-23)
 is one bit coarser than the host's rounded division, so the device ends
-about a bit lower on rcp/div; the GPU ALS tests cover that path.
+about a bit lower on rcp/div; the GPU ALS tests cover that path.  The
+compensated dot product and sum (acc_*, Ogita-Rump-Oishi Dot2 with
+double-word operands) are measured on 1-40 terms against sum |x_i y_i|; their
+bound grows like n u^2, so 40 terms stay above 42 bits.
 """
 import os
 import shutil
@@ -20,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
 BITS = {"add": 45.0, "add_sloppy": 45.0, "mul": 45.0, "fma": 44.5, "rcp": 45.0, "div": 44.0, "sqrt": 44.0,
-        "add_f": 45.0, "mul_f": 45.0, "from_double": 47.0}
+        "add_f": 45.0, "mul_f": 45.0, "from_double": 47.0, "acc_dot": 42.0, "acc_sum": 42.0}
 
 
 @pytest.fixture(scope="module")

@@ -62,6 +62,12 @@ CASES = [
     (lambda: H.random_hoplist([5, 7], 4, seed=2), 3, 3, 3, 0, False, 0, 0.0),
     # 34 vectors: a 16-CTA Gram-Schmidt cluster, up to 3 earlier vectors per CTA
     (lambda: H.random_hoplist([4, 3, 5], 5, seed=11), 3, 34, 1, 2, False, 1, 3.0),
+    # rank 40: the Gram-Schmidt overlaps and earlier vectors do not fit in
+    # shared memory (global scratch); solves by the four-warp refinement
+    (lambda: H.random_hoplist([5, 4, 6, 3], 5, seed=21), 40, 20, 1, 2, False, 1, 3.0),
+    # rank 24 (one right-hand-side column per warp) and a mode of 20 basis
+    # functions (more columns than the register solve takes)
+    (lambda: H.random_hoplist([20, 5, 6], 5, seed=22), 24, 6, 2, 3, True, 1, 3.0),
 ]
 
 
