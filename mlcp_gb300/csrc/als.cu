@@ -28,7 +28,10 @@
 //    for a CTA's terms is one contiguous run; tiles of 128 terms stream into a
 //    ring of shared-memory stages with cp.async.bulk and mbarrier completion.
 //  * The R x R normal equations, the F Gram products and the normalisation run
-//    in double-word arithmetic (dword.cuh) on the FP32 pipes.
+//    in double-word arithmetic (dword.cuh) on the FP32 pipes.  The normal
+//    equations of the next step are formed when a solve ends; their FP32
+//    inverse (the refinement's preconditioner) is computed in registers by a
+//    warp that phase B leaves idle, when there is one.
 // One launch covers all sweeps; the host is not involved between steps.
 
 #include <cooperative_groups.h>
@@ -217,7 +220,7 @@ struct Cta {
   int* done;
   int* issued;
   unsigned* fillno;  // [stages] tile sequence number the stage was last armed with
-  int* flags;  // [0] pipeline abort, [1] non-positive pivot seen
+  int* flags;  // [0] pipeline abort, [1] non-positive pivot seen, [2] FP32 inverse pivots positive
   float* ring;
   float* P;    // [rFp][ldP] running products (term index fastest)
   float* cw;   // [ldP] target weights of the CTA's terms
@@ -518,6 +521,13 @@ __device__ __forceinline__ void item_bm(const Cta& c, const float* tk, int gsk, 
   }
 }
 
+// Whether the last warp has no i-quad in phase B (16 not a multiple of the
+// i-quad count) and rF <= 32: it then inverts the step's normal equations in
+// registers during the first round.
+__device__ __forceinline__ bool phase_b_inverts(const Cta& c) {
+  return c.rF <= 32 && (kAlsWarps / c.nIq) * c.nIq < kAlsWarps;
+}
+
 // One round of phase B over all tiles (all 16 warps; warp -> i-quad iq =
 // warp mod nIq, tiles T = warp / nIq (mod warps per i-quad)), ending with the
 // CTA's partial right-hand side columns [16 round, 16 round + MW) in bout.
@@ -537,6 +547,12 @@ __device__ void phase_b_round(const Cta& c, const AlsParams& p, unsigned seq, in
   for (int cc = 0; cc < 4; ++cc)
 #pragma unroll
     for (int m = 0; m < MW; ++m) acc[cc][m] = 0.f;
+  if (!active && round == 0 && c.warp == kAlsWarps - 1 && phase_b_inverts(c)) {
+    // the idle warp inverts this step's normal equations (formed at the end
+    // of the previous solve) for the solver warps
+    const bool g = dwsolve::gj_inverse_warp(c.BB, c.rF, c.gi);
+    if (c.lane == 0) c.flags[2] = g;
+  }
   if (active) {
     for (int T = sub; T < c.ntiles; T += wpi) {
       const unsigned g = seq + (unsigned)T;
@@ -655,7 +671,15 @@ __device__ void post_solve(const Cta& c, const AlsParams& p, int k, int kn, int 
     dw_suffix(c, t, nt);
     if (warp_only) __syncwarp(); else solver_sync();
   }
-  for (int e = t; e < rr; e += nt) c.sk[e] = c.suf[(size_t)kn * rr + e];
+  // suffix of the next mode, and the next step's normal equations
+  const dw pen = c.misc[0];
+  for (int e = t; e < rr; e += nt) {
+    const dw sk = c.suf[(size_t)kn * rr + e];
+    c.sk[e] = sk;
+    dw b = dw_mul(c.L[e], sk);
+    if (e % rF == e / rF) b = dw_add(b, pen);
+    c.BB[e] = b;
+  }
 }
 
 // The R x R solve of step t (mode k; kn is the next step's mode), run
@@ -674,18 +698,25 @@ __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& 
     }
     c.b0[i + n * rF] = s;
   }
-  // normal equations: prefix (this sweep) x suffix (previous sweep) + penalty
-  const dw pen = c.misc[0];
-  for (int e = c.tid; e < rr; e += kSolverThreads) {
-    dw b = dw_mul(c.L[e], c.sk[e]);
-    if (e % rF == e / rF) b = dw_add(b, pen);
-    c.BB[e] = b;
-  }
+  // the normal equations BB (prefix of this sweep x suffix of the previous
+  // one + penalty) were formed when the previous step ended
   solver_sync();
   // FP32 inverse + double-word refinement; the double-word LDL^T when the
   // FP32 inverse fails or the refinement does not settle (ill-conditioned BB)
   bool gj_ok;
-  const float* inv = gj_inverse(c.BB, rF, c.gi, &gj_ok);
+  const float* inv = c.gi;
+  if (phase_b_inverts(c)) {
+    gj_ok = c.flags[2] != 0;  // inverted during phase B
+  } else if (rF <= 32) {
+    if (c.tid < 32) {
+      const bool g = dwsolve::gj_inverse_warp(c.BB, rF, c.gi);
+      if (c.tid == 0) c.flags[2] = g;
+    }
+    solver_sync();
+    gj_ok = c.flags[2] != 0;
+  } else {
+    inv = gj_inverse(c.BB, rF, c.gi, &gj_ok);
+  }
   int bad = 0;
   if (!(gj_ok && refine_solve(c.BB, rF, c.b0, c.X, nk, inv, c.res, c.red))) {
     for (int e = c.tid; e < rF * nk; e += kSolverThreads) c.X[e] = c.b0[e];
@@ -835,7 +866,14 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
   if (c.warp < kAlsSolverWarps) {
     dw_suffix(c, c.tid, kSolverThreads);
     solver_sync();
-    for (int e = c.tid; e < rr; e += kSolverThreads) c.sk[e] = c.suf[e];
+    const dw pen = c.misc[0];
+    for (int e = c.tid; e < rr; e += kSolverThreads) {
+      const dw sk = c.suf[e];
+      c.sk[e] = sk;
+      dw b = dw_mul(c.L[e], sk);
+      if (e % rF == e / rF) b = dw_add(b, pen);
+      c.BB[e] = b;
+    }
   }
   load_factor(c, p, D - 1, c.fb, 0, kAlsThreads);
   __syncthreads();
