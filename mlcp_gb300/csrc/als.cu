@@ -277,9 +277,12 @@ __device__ bool wait_tile(const Cta& c, unsigned g) {
   const uint32_t par = (g / (unsigned)c.stages) & 1u;
   volatile int* abort_flag = c.flags;
   volatile unsigned* armed = c.fillno + st;
+  // the whole warp decides together (callers are whole warps), so that the
+  // warp stays converged for the shuffles of the consumers
   for (int it = 0; it < kWaitLimit; ++it) {
-    if (*armed == g && mbar_try_wait(&c.bar[st], par)) return true;
-    if (*abort_flag) return false;
+    const bool ready = *armed == g && mbar_try_wait(&c.bar[st], par);
+    if (__all_sync(0xffffffffu, ready)) return true;
+    if (__any_sync(0xffffffffu, *abort_flag != 0)) return false;
   }
   atomicExch(c.flags, 1);
   return false;
@@ -339,11 +342,16 @@ __device__ __forceinline__ void tile_dots(const float* tile, int gs, const float
 }
 
 // prod over modes d not in {ex1, ex2} of <G_j^d, F_i^d>, straight from the
-// FP32 copies in global memory (unsafe-division fallback; rare, so kept out of
-// line to keep the hot loops small).
+// FP32 copies in global memory (unsafe-division fallback; kept out of line to
+// keep the hot loops small).  Called by a whole warp for one (j, i): one lane
+// alone would leave its warp, and so phase A, waiting on D dependent
+// global-memory dot products.
 __device__ __noinline__ float rebuild_product(const Cta& c, const AlsParams& p, int j, int i, int ex1, int ex2) {
+  // the whole warp, lane l taking modes l, l + 32, ...; the partial
+  // products meet in a butterfly (multiplication commutes, so every lane
+  // ends with the same value)
   float s = 1.f;
-  for (int d = 0; d < c.D; ++d) {
+  for (int d = c.lane; d < c.D; d += 32) {
     if (d == ex1 || d == ex2) continue;
     const int n = p.nbas[d], gs = als_gstride(n);
     const float* g = c.gm + (long long)p.offg[d] * c.rG + (long long)(c.row0 + j) * gs;
@@ -352,6 +360,7 @@ __device__ __noinline__ float rebuild_product(const Cta& c, const AlsParams& p, 
     for (int q = 0; q < n; ++q) t = fmaf(g[q], f[q], t);
     s *= t;
   }
+  for (int o = 16; o > 0; o >>= 1) s *= __shfl_xor_sync(0xffffffffu, s, o);
   return s;
 }
 
@@ -414,16 +423,21 @@ __device__ void product_pass(const Cta& c, const AlsParams& p, unsigned seq, int
             pv[a][cc] = qv;
           }
         }
-      while (rebuild) {
-        const int bit = __ffs(rebuild) - 1;
-        rebuild &= rebuild - 1;
+      // rebuilds, one entry at a time by the whole warp
+      for (unsigned pending = __ballot_sync(0xffffffffu, rebuild != 0u); pending;
+           pending = __ballot_sync(0xffffffffu, rebuild != 0u)) {
+        const int L = __ffs(pending) - 1;
+        const int bit = __ffs(__shfl_sync(0xffffffffu, rebuild, L)) - 1;
         const int a = bit >> 2, cc = bit & 3;
-        const float qv = rebuild_product(c, p, T * kAlsTileRows + c.lane + 32 * a, iq * 4 + cc, ex, d);
+        const float qv = rebuild_product(c, p, T * kAlsTileRows + L + 32 * a, iq * 4 + cc, ex, d);
+        if (c.lane == L) {
+          rebuild &= rebuild - 1;
 #pragma unroll
-        for (int a2 = 0; a2 < 4; ++a2)
+          for (int a2 = 0; a2 < 4; ++a2)
 #pragma unroll
-          for (int c2 = 0; c2 < 4; ++c2)
-            if (a2 * 4 + c2 == bit) pv[a2][c2] = qv;
+            for (int c2 = 0; c2 < 4; ++c2)
+              if (a2 * 4 + c2 == bit) pv[a2][c2] = qv;
+        }
       }
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
@@ -686,7 +700,6 @@ __device__ void post_solve(const Cta& c, const AlsParams& p, int k, int kn, int 
 // identically by every CTA of the cluster on the solver warps.
 __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& cluster, int t, int k, int kn) {
   const int rF = c.rF, nk = p.nbas[k], npk = round_up(nk, 4);
-  const int rr = rF * rF;
   // gather the partial right-hand sides of the cluster in rank order
   const size_t boff = (size_t)(t & 1) * c.rFp * c.npmax;
   for (int e = c.tid; e < rF * nk; e += kSolverThreads) {
