@@ -149,6 +149,12 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
       : "memory");
 }
 
+// 8-byte asynchronous global -> shared copy, and the wait for this thread's copies.
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 __device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
@@ -627,7 +633,6 @@ using dwsolve::kSolverThreads;
 using dwsolve::solver_sync;
 using dwsolve::dw_ldlt;
 using dwsolve::dw_ldlt_solve;
-using dwsolve::dw_normalise_row;
 using dwsolve::gj_inverse;
 using dwsolve::refine_solve;
 
@@ -636,12 +641,22 @@ using dwsolve::refine_solve;
 // nt (the solver warps, or the one warp that does this during phase B).
 __device__ void dw_suffix(const Cta& c, int t, int nt) {
   const int rr = c.rF * c.rF;
+  const dw* __restrict__ gram = c.gram;
+  dw* __restrict__ suf = c.suf;
   for (int e = t; e < rr; e += nt) {
     dw a = dw_make(1.f);
-    c.suf[(size_t)(c.D - 1) * rr + e] = a;
-    for (int d = c.D - 1; d >= 1; --d) {
-      a = dw_mul(a, c.gram[(size_t)d * rr + e]);
-      c.suf[(size_t)(d - 1) * rr + e] = a;
+    suf[(size_t)(c.D - 1) * rr + e] = a;
+    // eight Gram entries loaded together per round (global memory)
+    for (int d0 = c.D - 1; d0 >= 1; d0 -= 8) {
+      dw gv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) gv[u] = (d0 - u >= 1) ? gram[(size_t)(d0 - u) * rr + e] : dw_make(1.f);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (d0 - u < 1) break;
+        a = dw_mul(a, gv[u]);
+        suf[(size_t)(d0 - u - 1) * rr + e] = a;
+      }
     }
     c.L[e] = dw_make(1.f);
   }
@@ -654,8 +669,9 @@ __device__ void dw_new_gram(const Cta& c, int k, int nk, int t, int nt) {
   for (int e = t; e < rr; e += nt) {
     const int i = e % rF, i2 = e / rF;
     if (i > i2) continue;
-    dw s = dw_make(0.f);
-    for (int q = 0; q < nk; ++q) s = dw_fma(c.X[i + q * rF], c.X[i2 + q * rF], s);
+    dw_acc acc = acc_zero();
+    for (int q = 0; q < nk; ++q) acc_fma(acc, c.X[i + q * rF], c.X[i2 + q * rF]);
+    const dw s = acc_value(acc);
     c.gram[(size_t)k * rr + i + i2 * rF] = s;
     c.gram[(size_t)k * rr + i2 + i * rF] = s;
     if (k < c.D - 1) {
@@ -680,16 +696,18 @@ __device__ void post_solve(const Cta& c, const AlsParams& p, int k, int kn, int 
     for (int i = t; i < rF; i += nt) p.coef[p.term_off[c.v] + i] = dw_to_double(c.nrm[i]);
   }
   dw_new_gram(c, k, nk, t, nt);
+  cp_async_wait_all();
   if (warp_only) __syncwarp(); else solver_sync();
   if (k == c.D - 1) {
     dw_suffix(c, t, nt);
     if (warp_only) __syncwarp(); else solver_sync();
+    for (int e = t; e < rr; e += nt) c.sk[e] = c.suf[(size_t)kn * rr + e];
   }
-  // suffix of the next mode, and the next step's normal equations
+  // the next step's normal equations (sk: the suffix of mode kn, copied at
+  // the start of the solve unless the sweep just ended)
   const dw pen = c.misc[0];
   for (int e = t; e < rr; e += nt) {
-    const dw sk = c.suf[(size_t)kn * rr + e];
-    c.sk[e] = sk;
+    const dw sk = c.sk[e];
     dw b = dw_mul(c.L[e], sk);
     if (e % rF == e / rF) b = dw_add(b, pen);
     c.BB[e] = b;
@@ -700,6 +718,10 @@ __device__ void post_solve(const Cta& c, const AlsParams& p, int k, int kn, int 
 // identically by every CTA of the cluster on the solver warps.
 __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& cluster, int t, int k, int kn) {
   const int rF = c.rF, nk = p.nbas[k], npk = round_up(nk, 4);
+  // the next mode's suffix products into sk, asynchronously (global memory;
+  // unchanged unless this step ends a sweep)
+  if (k < c.D - 1)
+    for (int e = c.tid; e < rF * rF; e += kSolverThreads) cp_async8(c.sk + e, c.suf + (size_t)kn * rF * rF + e);
   // gather the partial right-hand sides of the cluster in rank order
   const size_t boff = (size_t)(t & 1) * c.rFp * c.npmax;
   for (int e = c.tid; e < rF * nk; e += kSolverThreads) {
@@ -736,7 +758,7 @@ __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& 
     bad = dw_ldlt(c.BB, rF, c.dinv, c.u);
     dw_ldlt_solve(c.BB, rF, c.dinv, c.X, nk);
   }
-  for (int i = c.tid; i < rF; i += kSolverThreads) c.nrm[i] = dw_normalise_row(c.X + i, nk, rF);
+  dwsolve::dw_normalise_rows(c.X, rF, nk, c.nrm);
   solver_sync();
   // new factor: FP32 copy for phase B and for this CTA's rebuilds; the
   // caller's FP64 arrays from cluster rank 0
