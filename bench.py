@@ -328,9 +328,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-cycle", action="store_true", help="skip the power-cycle measurement")
+    ap.add_argument("--cycle-only", action="store_true",
+                    help="time only the power cycle (--steps cycles after one warm-up) and print its JSON")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.cycle_only:
+        print(json.dumps(run_cycle_bench(max(1, args.steps), cpu=not args.no_cpu)), flush=True)
+        return 0
     return run_gpu(args)
 
 
