@@ -548,6 +548,44 @@ __device__ __forceinline__ bool phase_b_inverts(const Cta& c) {
   return c.rF <= 32 && (kAlsWarps / c.nIq) * c.nIq < kAlsWarps;
 }
 
+// Sums the 4 MW accumulators of each lane over the warp into out[cc MW + m]
+// by recursive halving: at each level a lane sends the half of its values it
+// gives up to its partner and adds the half it keeps, so 64 values (padded)
+// cost 32 + 16 + 8 + 4 + 2 shuffles per lane instead of 5 per value.
+template <int MW>
+__device__ __forceinline__ void warp_sum_values(const float (&acc)[4][MW], int lane, float* out) {
+  constexpr int NV = 4 * MW;
+  constexpr int P2 = NV <= 16 ? 16 : (NV <= 32 ? 32 : 64);
+  float v[P2];
+#pragma unroll
+  for (int q = 0; q < P2; ++q) v[q] = q < NV ? acc[q / MW][q % MW] : 0.f;
+  int base = 0;
+  int n = P2;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool up = (lane & o) != 0;
+    if (n > 1) {
+      const int h = n / 2;
+#pragma unroll
+      for (int q = 0; q < P2 / 2; ++q) {
+        if (q >= h) break;
+        const float send = up ? v[q] : v[h + q];
+        const float keep = up ? v[h + q] : v[q];
+        v[q] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+      if (up) base += h;
+      n = h;
+    } else {
+      v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+    }
+  }
+  // this lane holds the totals of values base .. base + n - 1 (n = 1 or 2);
+  // with fewer than 32 slots several lanes hold the same total
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    if (q < n && base + q < NV && (P2 >= 32 || (lane & 1) == 0)) out[base + q] = v[q];
+}
+
 // One round of phase B over all tiles (all 16 warps; warp -> i-quad iq =
 // warp mod nIq, tiles T = warp / nIq (mod warps per i-quad)), ending with the
 // CTA's partial right-hand side columns [16 round, 16 round + MW) in bout.
@@ -585,19 +623,7 @@ __device__ void phase_b_round(const Cta& c, const AlsParams& p, unsigned seq, in
       }
       release_tile(c, g, T, c.nIq, src);
     }
-    // sum over the warp's lanes
-#pragma unroll
-    for (int cc = 0; cc < 4; ++cc)
-#pragma unroll
-      for (int m = 0; m < MW; ++m) {
-        float s = acc[cc][m];
-        s += __shfl_xor_sync(0xffffffffu, s, 16);
-        s += __shfl_xor_sync(0xffffffffu, s, 8);
-        s += __shfl_xor_sync(0xffffffffu, s, 4);
-        s += __shfl_xor_sync(0xffffffffu, s, 2);
-        s += __shfl_xor_sync(0xffffffffu, s, 1);
-        if (c.lane == 0) c.bred[c.warp * 64 + cc * MW + m] = s;
-      }
+    warp_sum_values<MW>(acc, c.lane, c.bred + c.warp * 64);
   }
   __syncthreads();
   // sum over the warps of each i-quad (fixed order)
