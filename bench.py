@@ -182,12 +182,21 @@ def run_cycle_bench(steps: int, cpu: bool):
     gpu_ms = 1e3 * (time.perf_counter() - t0) / steps
     out = {"workload": f"Henon-Heiles D={CYC_D} n={CYC_N}, rank {CYC_R}, block {CYC_B}, npow={CYC_NPOW}, "
                        f"nals={CYC_NALS}, update on", "gpu_ms_per_cycle": gpu_ms}
+    # the update = F step's Rayleigh quotients of the block (getqhqdiagcpp_)
+    IT.qhq_diag(gb, gc, hl.nbas, CYC_R, CYC_B, hl)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        IT.qhq_diag(gb, gc, hl.nbas, CYC_R, CYC_B, hl)
+    out["qhq_diag_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
     if cpu:
         import oracle
         oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
         t0 = time.perf_counter()
         oracle.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
         out["cpu_ms_per_cycle"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        oracle.qhq_diag(gb, gc, hl.nbas, CYC_R, CYC_B, hl)
+        out["qhq_diag_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
         out["cpu_cores"] = os.cpu_count()
         out["cpu_kind"] = "port"
         oracle.set_cycle_penalties()

@@ -32,10 +32,12 @@
 
 #ifdef __cplusplus
 #define MLCP_REF(T) const T&
+#define MLCP_INOUT(T) T&
 extern "C" {
 #else
 #include <stdbool.h>
 #define MLCP_REF(T) const T*
+#define MLCP_INOUT(T) T*
 #endif
 
 /* Replaces src/intertwining.cu:31 (intwdevicemem_): prints the device memory
@@ -62,6 +64,28 @@ MLCP_API void intertwinecpp_(double *base, double *coef, int *nbas, MLCP_REF(int
  * (terms 0..rF-1, also the starting guess).  Overwrites terms 0..rF-1. */
 MLCP_API void alscpp_(double *coef, double *base, int *nbas, MLCP_REF(int) ndof, MLCP_REF(int) rF, MLCP_REF(int) rG,
              MLCP_REF(int) nals);
+
+/* ---- The update = F path (reference CPU routines; Fortran binding in
+ * INTEGRATION.md) --------------------------------------------------------- */
+
+/* Replaces GetQHQdiag (src/BlockUtils.f90:385-408) with RayleighQuotient2
+ * (:658-688), which the reference's host runs on the CPU after
+ * intertwinecpp_ when update is false (src/Solver.f90:499-504):
+ * qhqd[i] = <Q_i|H|Q_i> / <Q_i|Q_i> for vectors i = nconv .. nbloc-1 of the
+ * block (same layout and operator list as intertwinecpp_), H applied
+ * exactly, in FP64 on the GPU.  Entries below nconv are left unchanged. */
+MLCP_API void getqhqdiagcpp_(double *base, double *coef, int *nbas, MLCP_REF(int) rk, MLCP_REF(int) ndof,
+                             MLCP_REF(int) nbloc, MLCP_REF(int) nconv, int *opid, int *mptr, double *Hcoef,
+                             double *mat, MLCP_REF(int) TxD, MLCP_REF(int) nops, MLCP_REF(int) msize,
+                             double *qhqd);
+
+/* Replaces SortVecs (src/BlockUtils.f90:520-583): reorders the block (and
+ * eigv alike) by increasing |eigv - Eref|; nconv becomes the position of
+ * the first of the first nconv vectors that moved, if any did.  Equal
+ * distances keep their order (the reference's dsort leaves ties in an
+ * unspecified order).  Host memory only; no GPU work. */
+MLCP_API void sortvecscpp_(double *base, double *coef, int *nbas, MLCP_REF(int) rk, MLCP_REF(int) ndof,
+                           MLCP_REF(int) nbloc, double *eigv, MLCP_INOUT(int) nconv, MLCP_REF(double) Eref);
 
 /* ---- Extensions (no counterpart in the reference's C layer) ---------- */
 

@@ -60,6 +60,12 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             L.intertwinecpp_.restype = None
             L.intertwinecpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I, _I, _D, _D, _I, _I, _I, _D, _I, _I, _I,
                                          ctypes.POINTER(ctypes.c_bool), _I, _D]
+        if hasattr(L, "getqhqdiagcpp_"):
+            L.getqhqdiagcpp_.restype = None
+            L.getqhqdiagcpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I, _I, _I, _D, _D, _I, _I, _I, _D]
+        if hasattr(L, "sortvecscpp_"):
+            L.sortvecscpp_.restype = None
+            L.sortvecscpp_.argtypes = [_D, _D, _I, _I, _I, _I, _D, _I, _D]
         if hasattr(L, "intwdevicemem_"):
             L.intwdevicemem_.restype = None
             L.intwdevicemem_.argtypes = [_I, _I, _I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_bool), _I]

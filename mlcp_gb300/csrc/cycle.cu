@@ -15,6 +15,7 @@
 //   batched ALS with a shared target (vector updates) -> weight normalisation.
 #include <algorithm>
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -149,22 +150,29 @@ int get_optable(Context* ctx, const Layout& Ly, const int* nbas, int R, int T, c
   const int utot = uoff[D];
   const int npm = Ly.npmax;
   std::vector<float> hmat((size_t)utot * npm * npm, 0.f);
+  std::vector<double> hmat64((size_t)utot * npm * npm, 0.0);
   std::vector<unsigned char> ident(utot, 0);
   for (int d = 0; d < D; ++d) {
     const int n = nbas[d];
     for (int u = 0; u < (int)starts[d].size(); ++u) {
       float* h = &hmat[(size_t)(uoff[d] + u) * npm * npm];
+      double* h64 = &hmat64[(size_t)(uoff[d] + u) * npm * npm];
       if (starts[d][u] < 0) {
         ident[uoff[d] + u] = 1;
-        for (int i = 0; i < n; ++i) h[i * npm + i] = 1.f;
+        for (int i = 0; i < n; ++i) {
+          h[i * npm + i] = 1.f;
+          h64[i * npm + i] = 1.0;
+        }
         continue;
       }
       const double* pk = mat + starts[d][u];
       for (int c = 0; c < n; ++c)
         for (int r = 0; r <= c; ++r) {
-          const float v = (float)pk[r + (size_t)c * (c + 1) / 2];
-          h[r * npm + c] = v;
-          h[c * npm + r] = v;
+          const double v64 = pk[r + (size_t)c * (c + 1) / 2];
+          h[r * npm + c] = (float)v64;
+          h[c * npm + r] = (float)v64;
+          h64[r * npm + c] = v64;
+          h64[c * npm + r] = v64;
         }
     }
   }
@@ -185,7 +193,8 @@ int get_optable(Context* ctx, const Layout& Ly, const int* nbas, int R, int T, c
   const size_t o_nbas = reserve(sizeof(int) * D), o_off = reserve(sizeof(int) * (D + 1)),
                o_offp = reserve(sizeof(int) * (D + 1)), o_uoff = reserve(sizeof(int) * (D + 1)),
                o_uid = reserve(sizeof(int) * uid.size()), o_ident = reserve(utot),
-               o_h = reserve(sizeof(float) * hmat.size()), o_alpha = reserve(sizeof(double) * T),
+               o_h = reserve(sizeof(float) * hmat.size()), o_h64 = reserve(sizeof(double) * hmat64.size()),
+               o_alpha = reserve(sizeof(double) * T),
                o_order = reserve(sizeof(int) * order.size()), o_gs = reserve(sizeof(int) * gstart.size());
   std::vector<char> host(bytes);
   std::memcpy(&host[o_nbas], nbas, sizeof(int) * D);
@@ -195,6 +204,7 @@ int get_optable(Context* ctx, const Layout& Ly, const int* nbas, int R, int T, c
   std::memcpy(&host[o_uid], uid.data(), sizeof(int) * uid.size());
   std::memcpy(&host[o_ident], ident.data(), utot);
   std::memcpy(&host[o_h], hmat.data(), sizeof(float) * hmat.size());
+  std::memcpy(&host[o_h64], hmat64.data(), sizeof(double) * hmat64.size());
   std::memcpy(&host[o_alpha], Hcoef, sizeof(double) * T);
   std::memcpy(&host[o_order], order.data(), sizeof(int) * order.size());
   std::memcpy(&host[o_gs], gstart.data(), sizeof(int) * gstart.size());
@@ -211,6 +221,7 @@ int get_optable(Context* ctx, const Layout& Ly, const int* nbas, int R, int T, c
   t.nbas = (const int*)(b + o_nbas); t.off = (const int*)(b + o_off); t.offp = (const int*)(b + o_offp);
   t.uoff = (const int*)(b + o_uoff); t.uid = (const int*)(b + o_uid);
   t.ident = (const unsigned char*)(b + o_ident); t.hmat = (const float*)(b + o_h);
+  t.hmat64 = (const double*)(b + o_h64);
   t.alpha = (const double*)(b + o_alpha); t.order = (const int*)(b + o_order); t.gstart = (const int*)(b + o_gs);
   hc.key = key;
   hc.R = R;
@@ -403,6 +414,90 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
 }
 
 // Device bytes one cycle of this shape needs (workspace + operator table).
+// Rayleigh quotients of vectors nconv..nbloc-1 of a block (reference
+// GetQHQdiag, src/BlockUtils.f90:385-408); host buffers in and out, entries
+// of qhqd below nconv untouched.
+int qhq_diag(Context* ctx, const double* base, const double* coef, const int* nbas, int rk, int ndof, int nbloc,
+             int nconv, const int* opid, const int* mptr, const double* Hcoef, const double* mat, int TxD, int nops,
+             int msize, double* qhqd) {
+  if (rk < 1 || rk > kMaxRankCycle) {
+    set_error("getqhqdiagcpp_: rk = %d outside [1, %d]", rk, kMaxRankCycle);
+    return rk < 1 ? kBadArgument : kTooLarge;
+  }
+  if (ndof < 1 || nbloc < 1 || nconv < 0 || TxD < ndof || TxD % ndof != 0 || nops < 1 || msize < 1) {
+    set_error("getqhqdiagcpp_: bad sizes (ndof=%d nbloc=%d nconv=%d TxD=%d nops=%d msize=%d)", ndof, nbloc, nconv,
+              TxD, nops, msize);
+    return kBadArgument;
+  }
+  if (nconv >= nbloc) return kOk;
+  Layout Ly;
+  int rc = make_layout(ndof, nbas, &Ly);
+  if (rc) return rc;
+  const int T = TxD / ndof, R = rk, B = nbloc;
+  cudaStream_t st = ctx->stream;
+  OpTable tab;
+  rc = get_optable(ctx, Ly, nbas, R, T, opid, mptr, Hcoef, mat, nops, msize, st, &tab);
+  if (rc) return rc;
+  // device buffers from the cycle workspace (calls on one context are serialised)
+  const size_t nvals = (size_t)B * R * Ly.nD;
+  size_t bytes = 0;
+  auto take = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
+  const size_t o_base = take(sizeof(double) * nvals), o_coef = take(sizeof(double) * (size_t)B * R),
+               o_out = take(sizeof(double) * B), o_work = take(sizeof(double) * (size_t)(B - nconv) * rq_work_doubles(tab));
+  if (bytes > ctx->cyc_bytes) {
+    if (ctx->cyc) {
+      MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+      MLCP_CUDA_TRY(cudaFree(ctx->cyc));
+      ctx->cyc = nullptr;
+      ctx->cyc_bytes = 0;
+    }
+    MLCP_CUDA_TRY(cudaMalloc(&ctx->cyc, bytes));
+    ctx->cyc_bytes = bytes;
+  }
+  char* b = static_cast<char*>(ctx->cyc);
+  RqParams p;
+  p.ops = tab;
+  p.v0 = nconv;
+  p.nvec = B;
+  p.nD = Ly.nD;
+  p.base = reinterpret_cast<const double*>(b + o_base);
+  p.coef = reinterpret_cast<const double*>(b + o_coef);
+  p.out = reinterpret_cast<double*>(b + o_out);
+  p.work = reinterpret_cast<double*>(b + o_work);
+  p.work_stride = 0;
+  MLCP_CUDA_TRY(cudaMemcpyAsync(b + o_base, base, sizeof(double) * nvals, cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(b + o_coef, coef, sizeof(double) * (size_t)B * R, cudaMemcpyHostToDevice, st));
+  if ((rc = rq_launch(p, st))) return rc;
+  MLCP_CUDA_TRY(cudaMemcpyAsync(qhqd + nconv, p.out + nconv, sizeof(double) * (size_t)(B - nconv),
+                                cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+  return kOk;
+}
+
+// Reference SortVecs (src/BlockUtils.f90:520-583): the block reordered by
+// increasing |eigv - Eref| (the reference's dsort with a carried index; ties
+// keep their order here), eigv permuted alike, and nconv cut back to the
+// first converged vector that moved.  Host memory only.
+void sort_vecs(double* base, double* coef, int nD, int rk, int nbloc, double* eigv, int* nconv, double eref) {
+  std::vector<int> ix(nbloc);
+  for (int i = 0; i < nbloc; ++i) ix[i] = i;
+  std::stable_sort(ix.begin(), ix.end(),
+                   [&](int a, int b) { return std::fabs(eigv[a] - eref) < std::fabs(eigv[b] - eref); });
+  const size_t vb = (size_t)rk * nD;
+  std::vector<double> ob(base, base + vb * nbloc), oc(coef, coef + (size_t)rk * nbloc), oe(eigv, eigv + nbloc);
+  for (int i = 0; i < nbloc; ++i) {
+    if (ix[i] == i) continue;
+    std::memcpy(base + vb * i, ob.data() + vb * ix[i], sizeof(double) * vb);
+    std::memcpy(coef + (size_t)rk * i, oc.data() + (size_t)rk * ix[i], sizeof(double) * rk);
+    eigv[i] = oe[ix[i]];
+  }
+  for (int i = 0; i < *nconv && i < nbloc; ++i)
+    if (ix[i] != i) {
+      *nconv = i;
+      break;
+    }
+}
+
 size_t cycle_bytes_estimate(int rk, int ndof, int nbloc, const int* nbas, int T, int msize) {
   Layout Ly;
   if (make_layout(ndof, nbas, &Ly) != kOk) return 0;
@@ -433,6 +528,34 @@ extern "C" void intertwinecpp_(double* base, double* coef, int* nbas, const int&
   }
   finish_status(rc);
   if (rc != kOk) fprintf(stderr, "intertwinecpp_: %s\n", last_error());
+}
+
+extern "C" void getqhqdiagcpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof,
+                               const int& nbloc, const int& nconv, int* opid, int* mptr, double* Hcoef, double* mat,
+                               const int& TxD, const int& nops, const int& msize, double* qhqd) {
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (ctx) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    rc = qhq_diag(ctx, base, coef, nbas, rk, ndof, nbloc, nconv, opid, mptr, Hcoef, mat, TxD, nops, msize, qhqd);
+  }
+  finish_status(rc);
+  if (rc != kOk) fprintf(stderr, "getqhqdiagcpp_: %s\n", last_error());
+}
+
+extern "C" void sortvecscpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof, const int& nbloc,
+                             double* eigv, int& nconv, const double& Eref) {
+  int rc = kOk;
+  if (rk < 1 || ndof < 1 || nbloc < 1) {
+    set_error("sortvecscpp_: bad sizes (rk=%d ndof=%d nbloc=%d)", rk, ndof, nbloc);
+    rc = kBadArgument;
+  } else {
+    int nD = 0;
+    for (int d = 0; d < ndof; ++d) nD += nbas[d];
+    sort_vecs(base, coef, nD, rk, nbloc, eigv, &nconv, Eref);
+  }
+  finish_status(rc);
+  if (rc != kOk) fprintf(stderr, "sortvecscpp_: %s\n", last_error());
 }
 
 extern "C" void intwdevicemem_(const int& rk, const int& ndof, const int& nbloc, const int& TxD, const int& nops,

@@ -22,6 +22,7 @@ struct OpTable {
   const int* uid;           // [T*D] local operator index of term t at mode d
   const unsigned char* ident;  // [utot] 1 if the operator is the identity
   const float* hmat;        // [utot][npmax][npmax] dense FP32 operators
+  const double* hmat64;     // [utot][npmax][npmax] the same in FP64 (Rayleigh quotients)
   const double* alpha;      // [T] term coefficients
   const int* order;         // [D][T] terms grouped by their operator at mode j
   const int* gstart;        // [D][umax+1] group starts in order[j]
@@ -88,6 +89,20 @@ struct GepParams {
 };
 int gep_launch(const GepParams& p, cudaStream_t st);
 size_t gep_work_doubles(int nbloc);
+
+// Rayleigh quotients <Q_v|H|Q_v>/<Q_v|Q_v> of vectors v0..nvec-1 of a block
+// (reference GetQHQdiag / RayleighQuotient2), H applied exactly, FP64.
+struct RqParams {
+  OpTable ops;
+  int v0, nvec, nD;
+  const double* base;  // block, reference layout
+  const double* coef;
+  double* work;        // rq_work_doubles(ops) per vector v0..nvec-1
+  double* out;         // [nvec] (entries v0.. written)
+  long long work_stride;  // set by rq_launch
+};
+int rq_launch(const RqParams& p, cudaStream_t st);
+size_t rq_work_doubles(const OpTable& t);
 
 // Divide the weights of each rank-R vector by its norm (FP64).
 int normalize_coefs_launch(int nvec, int R, int D, int nD, const int* nbas, const double* base, double* coef,

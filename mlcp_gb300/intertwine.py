@@ -47,6 +47,49 @@ def intertwine(base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int, hl
     return base, coef, eig
 
 
+def qhq_diag(base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int, hl, nconv: int = 0,
+             qhqd: np.ndarray | None = None) -> np.ndarray:
+    """Reference GetQHQdiag (src/BlockUtils.f90:385-408) through
+    getqhqdiagcpp_: Rayleigh quotients <Q_i|H|Q_i>/<Q_i|Q_i> of vectors
+    nconv..nbloc-1 (H applied exactly, FP64 on the GPU).  Returns a copy of
+    qhqd (zeros when None) with those entries filled."""
+    base = np.ascontiguousarray(base, dtype=np.float64)
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    out = np.zeros(nbloc) if qhqd is None else np.ascontiguousarray(qhqd, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32).copy()
+    opid = np.ascontiguousarray(hl.opid, dtype=np.int32).copy()
+    mptr = np.ascontiguousarray(hl.mptr, dtype=np.int32).copy()
+    hcoef = np.ascontiguousarray(hl.coef, dtype=np.float64).copy()
+    mat = np.ascontiguousarray(hl.mat, dtype=np.float64).copy()
+    ints = [ctypes.c_int(x) for x in (rk, nb.size, nbloc, nconv, opid.size, mptr.size, mat.size)]
+    L = _lib.load()
+    L.getqhqdiagcpp_(base.ctypes.data_as(_D), coef.ctypes.data_as(_D), nb.ctypes.data_as(_I),
+                     *[ctypes.byref(x) for x in ints[:4]], opid.ctypes.data_as(_I), mptr.ctypes.data_as(_I),
+                     hcoef.ctypes.data_as(_D), mat.ctypes.data_as(_D), *[ctypes.byref(x) for x in ints[4:]],
+                     out.ctypes.data_as(_D))
+    if L.mlcp_gb300_last_status() != 0:
+        raise _lib.MlcpError(_lib.last_error())
+    return out
+
+
+def sort_vecs(base: np.ndarray, coef: np.ndarray, nbas, rk: int, eigv: np.ndarray, nconv: int, eref: float):
+    """Reference SortVecs (src/BlockUtils.f90:520-583) through sortvecscpp_
+    on copies; returns (base, coef, eigv, nconv)."""
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    eig = np.ascontiguousarray(eigv, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32).copy()
+    ints = [ctypes.c_int(x) for x in (rk, nb.size, eig.size, nconv)]
+    e = ctypes.c_double(float(eref))
+    L = _lib.load()
+    L.sortvecscpp_(base.ctypes.data_as(_D), coef.ctypes.data_as(_D), nb.ctypes.data_as(_I),
+                   *[ctypes.byref(x) for x in ints[:3]], eig.ctypes.data_as(_D), ctypes.byref(ints[3]),
+                   ctypes.byref(e))
+    if L.mlcp_gb300_last_status() != 0:
+        raise _lib.MlcpError(_lib.last_error())
+    return base, coef, eig, ints[3].value
+
+
 def block_shift(eigv, emax: float) -> float:
     """Reference GetBlockShift (src/BlockPower.f90:20-45): half way between an
     estimate of the first eigenvalue above the block and the spectrum's top."""

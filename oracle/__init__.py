@@ -65,6 +65,10 @@ def lib() -> ctypes.CDLL:
         L.orc_set_rhs_fp32.argtypes = [ctypes.c_int]
         L.orc_sygv.restype = ctypes.c_int
         L.orc_sygv.argtypes = [ctypes.c_int, _D, _D, _D, _D]
+        L.orc_rayleigh_quotient.restype = ctypes.c_double
+        L.orc_rayleigh_quotient.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, ctypes.c_int]
+        L.orc_qhq_diag.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D,
+                                   _D, ctypes.c_int, _D, ctypes.c_int]
     return _lib
 
 
@@ -163,6 +167,41 @@ def vector_updates(base, coef, nbas, rk, nbloc, U, nals, nthreads=0):
     Ucm = np.ascontiguousarray(np.asarray(U, dtype=np.float64).T)  # column-major
     lib().orc_vector_updates(_dp(base), _dp(coef), _ip(nb), rk, len(nb), nbloc, _dp(Ucm), nals, nthreads)
     return base, coef
+
+
+def rayleigh_quotient(base, coef, nbas, hl) -> float:
+    """Reference RayleighQuotient2 (src/BlockUtils.f90:658-688): <v|H|v>/<v|v>."""
+    base = np.ascontiguousarray(base, dtype=np.float64)
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    return lib().orc_rayleigh_quotient(_dp(base), _dp(coef), _ip(nb), coef.size, len(nb), _ip(hl.opid),
+                                       _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms)
+
+
+def qhq_diag(base, coef, nbas, rk, nbloc, hl, nconv=0, qhqd=None, nthreads=0):
+    """Reference GetQHQdiag (src/BlockUtils.f90:385-408): Rayleigh quotients of
+    vectors nconv..nbloc-1; qhqd (copied) keeps its entries below nconv."""
+    base = np.ascontiguousarray(base, dtype=np.float64)
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    out = np.zeros(nbloc) if qhqd is None else np.ascontiguousarray(qhqd, dtype=np.float64).copy()
+    lib().orc_qhq_diag(_dp(base), _dp(coef), _ip(nb), rk, len(nb), nbloc, nconv, _ip(hl.opid), _ip(hl.mptr),
+                       _dp(hl.coef), _dp(hl.mat), hl.nterms, _dp(out), nthreads)
+    return out
+
+
+def sort_vecs(base, coef, rk, eigv, nconv, eref):
+    """Reference SortVecs (src/BlockUtils.f90:520-583) on copies: vectors in
+    increasing |eigv - Eref| (ties keep their order), eigv permuted alike, and
+    nconv cut back to the first converged vector that moved.  Returns
+    (base, coef, eigv, nconv)."""
+    eigv = np.asarray(eigv, dtype=np.float64)
+    nbloc = eigv.size
+    ix = np.argsort(np.abs(eigv - eref), kind="stable")
+    base = np.asarray(base, dtype=np.float64).reshape(nbloc, rk, -1)[ix].reshape(nbloc * rk, -1).copy()
+    coef = np.asarray(coef, dtype=np.float64).reshape(nbloc, rk)[ix].reshape(-1).copy()
+    moved = [i for i in range(nconv) if ix[i] != i]
+    return base, coef, eigv[ix].copy(), (moved[0] if moved else nconv)
 
 
 def cp_dot(vb, vc, wb, wc, nbas) -> float:

@@ -690,6 +690,84 @@ void orc_intertwine(double *base, double *coef, const int *nbas, int rk, int ndo
   }
 }
 
+/* RayleighQuotient2 (reference src/BlockUtils.f90:658-688): <v|H|v> / <v|v>
+ * with H applied exactly.  As the reference does, each Hamiltonian term t is
+ * applied to one rank-1 term i of v at a time (PRODHVR1: w^d = alpha_d
+ * h_{t,d} v_i^d, alpha_0 = Hcoef[t], the packed upper-triangular operators
+ * of apply_term) and the product is accumulated against v (PRODVV). */
+double orc_rayleigh_quotient(const double *base, const double *coef, const int *nbas, int rk, int ndof,
+                             const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T) {
+  int *off = make_offsets(nbas, ndof);
+  const int nD = off[ndof];
+  double *w = (double *)malloc(sizeof(double) * (size_t)nD);
+  double num = 0.0;
+  for (int i = 0; i < rk; ++i) {
+    const double *vi = base + (size_t)i * nD;
+    for (int t = 0; t < T; ++t) {
+      for (int d = 0; d < ndof; ++d) {
+        const int n = nbas[d], o = off[d];
+        const int hsft = mptr[opid[t * ndof + d] - 1] - 1;
+        const double alpha = (d == 0) ? Hcoef[t] : 1.0;
+        for (int ib = 0; ib < n; ++ib) {
+          double acc = 0.0;
+          for (int a = 0; a < n; ++a) {
+            const int ir = a < ib ? a : ib, ic = a < ib ? ib : a;
+            acc += vi[o + a] * mat[hsft + ir + ic * (ic + 1) / 2];
+          }
+          w[o + ib] = acc * alpha;
+        }
+      }
+      /* PRODVV(v, w): sum_j c_j c_i prod_d <v_j^d, w^d> */
+      double s = 0.0;
+      for (int j = 0; j < rk; ++j) {
+        const double *vj = base + (size_t)j * nD;
+        double prod = coef[j] * coef[i];
+        for (int d = 0; d < ndof; ++d) {
+          double dot = 0.0;
+          for (int a = 0; a < nbas[d]; ++a) dot += vj[off[d] + a] * w[off[d] + a];
+          prod *= dot;
+        }
+        s += prod;
+      }
+      num += s;
+    }
+  }
+  /* PRODVV(v): sum_ij c_i c_j prod_d <v_i^d, v_j^d> */
+  double den = 0.0;
+  for (int i = 0; i < rk; ++i)
+    for (int j = 0; j < rk; ++j) {
+      double prod = coef[i] * coef[j];
+      for (int d = 0; d < ndof; ++d) {
+        double dot = 0.0;
+        for (int a = 0; a < nbas[d]; ++a)
+          dot += base[(size_t)i * nD + off[d] + a] * base[(size_t)j * nD + off[d] + a];
+        prod *= dot;
+      }
+      den += prod;
+    }
+  free(w);
+  free(off);
+  return num / den;
+}
+
+/* GetQHQdiag (reference src/BlockUtils.f90:385-408): qhqd[i] =
+ * RayleighQuotient2(Q_i, H) for i = nconv .. nbloc-1; entries below nconv are
+ * left as they are. */
+void orc_qhq_diag(const double *base, const double *coef, const int *nbas, int rk, int ndof, int nbloc, int nconv,
+                  const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, double *qhqd,
+                  int nthreads) {
+  int nD = 0;
+  for (int d = 0; d < ndof; ++d) nD += nbas[d];
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+  for (int i = nconv < 0 ? 0 : nconv; i < nbloc; ++i)
+    qhqd[i] = orc_rayleigh_quotient(base + (size_t)i * rk * nD, coef + (size_t)i * rk, nbas, rk, ndof, opid, mptr,
+                                    Hcoef, mat, T);
+  (void)nthreads;
+}
+
 double orc_cp_dot(const double *vb, const double *vc, int rv, const double *wb, const double *wc, int rw,
                   const int *nbas, int ndof) {
   int *off = make_offsets(nbas, ndof);

@@ -58,6 +58,15 @@ void orc_gen_eig(const double *base, const double *coef, const int *nbas, int rk
 void orc_vector_updates(double *base, double *coef, const int *nbas, int rk, int ndof, int nbloc,
                         const double *U, int nals, int nthreads);
 
+/* Reference src/BlockUtils.f90:658-688 (RayleighQuotient2): <v|H|v>/<v|v>
+ * with H applied exactly, term by term. */
+double orc_rayleigh_quotient(const double *base, const double *coef, const int *nbas, int rk, int ndof,
+                             const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T);
+/* Reference src/BlockUtils.f90:385-408 (GetQHQdiag): qhqd[i] for i >= nconv. */
+void orc_qhq_diag(const double *base, const double *coef, const int *nbas, int rk, int ndof, int nbloc, int nconv,
+                  const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, double *qhqd,
+                  int nthreads);
+
 /* Full inner product <v,w> of two CP vectors (reference src/modvecvec.cu:724
  * constpstot with idof=-1 and both weights, summed). */
 double orc_cp_dot(const double *vb, const double *vc, int rv, const double *wb, const double *wc, int rw,

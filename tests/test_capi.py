@@ -42,3 +42,23 @@ def test_library_links_no_oracle():
     assert "orc_" not in out
     deps = subprocess.run(["ldd", _lib.lib_path()], capture_output=True, text=True).stdout
     assert "oracle" not in deps
+
+
+def test_sortvecscpp_matches_oracle():
+    """sortvecscpp_ is host code: checked here without a GPU."""
+    import numpy as np
+    import oracle
+    from mlcp_gb300 import intertwine as IT
+    rng = np.random.default_rng(5)
+    nbas = [3, 4, 2]
+    rk, nbloc, nD = 3, 9, 9
+    for trial in range(6):
+        Q, qc = rng.normal(size=(rk * nbloc, nD)), rng.uniform(0.2, 1.0, rk * nbloc)
+        eig = rng.normal(size=nbloc) * 3
+        if trial == 5:
+            eig = np.sort(np.abs(eig))  # already in order: nothing moves
+        nconv = int(rng.integers(0, nbloc + 1))
+        eref = float(rng.normal()) if trial < 5 else 0.0
+        gb, gc, ge, gn = IT.sort_vecs(Q, qc, nbas, rk, eig, nconv, eref)
+        ob, oc, oe, on = oracle.sort_vecs(Q, qc, rk, eig, nconv, eref)
+        assert np.array_equal(gb, ob) and np.array_equal(gc, oc) and np.array_equal(ge, oe) and gn == on

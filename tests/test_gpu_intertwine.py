@@ -115,3 +115,48 @@ def test_cycle_rejects_bad_operator_index(cuda_device):
     Q, qc = start_block(hl.nbas, 2, 2, seed=0)
     with pytest.raises(Exception, match="opid"):
         IT.intertwine(Q, qc, hl.nbas, 2, 2, bad, np.zeros(2), 2, 2, True, 1, 1.0)
+
+
+QHQ_CASES = [
+    # (hoplist factory, rk, nbloc, nconv)
+    (lambda: H.henon_heiles(D=3, n=5), 4, 6, 0),
+    (lambda: H.coupled_oscillators(3, 6), 1, 2, 0),
+    (lambda: H.random_hoplist([5, 4, 6, 3], 5, seed=21), 40, 3, 1),
+    (lambda: H.henon_heiles(D=6, n=10, lam=0.111803), 16, 40, 5),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", range(len(QHQ_CASES)))
+def test_qhq_diag_matches_oracle(case, cuda_device):
+    """getqhqdiagcpp_ (GetQHQdiag / RayleighQuotient2) against the oracle:
+    both FP64, so only the summation order differs (1e-11 relative)."""
+    make, rk, nbloc, nconv = QHQ_CASES[case]
+    hl = make()
+    Q, qc = start_block(hl.nbas, rk, nbloc, seed=20 + case)
+    init = np.full(nbloc, -3.0)
+    g = IT.qhq_diag(Q, qc, hl.nbas, rk, nbloc, hl, nconv, init)
+    o = oracle.qhq_diag(Q, qc, hl.nbas, rk, nbloc, hl, nconv, init)
+    assert np.all(g[:nconv] == -3.0)
+    np.testing.assert_allclose(g, o, rtol=1e-11)
+
+
+@pytest.mark.gpu
+def test_update_false_path_matches_oracle(cuda_device):
+    """The reference host's update = F step (src/Solver.f90:498-504): a cycle
+    without Rayleigh-Ritz, Rayleigh quotients of the block, then SortVecs
+    about the lower spectral bound.  Same tolerances as the cycle tests."""
+    hl = H.henon_heiles(D=4, n=6)
+    rk, nbloc = 6, 5
+    Q, qc = start_block(hl.nbas, rk, nbloc, seed=31)
+    eig0 = np.arange(nbloc, dtype=float)
+    gb, gc, _ = IT.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, eig0, 3, 3, False, 1, 6.0)
+    ob, oc, _ = oracle.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, eig0, 3, 3, False, 1, 6.0)
+    ge = IT.qhq_diag(gb, gc, hl.nbas, rk, nbloc, hl)
+    oe = oracle.qhq_diag(ob, oc, hl.nbas, rk, nbloc, hl)
+    np.testing.assert_allclose(ge, oe, rtol=EIG_RTOL)
+    gb, gc, ge, gn = IT.sort_vecs(gb, gc, hl.nbas, rk, ge, 2, 2.0)
+    ob, oc, oe, on = oracle.sort_vecs(ob, oc, rk, oe, 2, 2.0)
+    assert gn == on
+    np.testing.assert_allclose(ge, oe, rtol=EIG_RTOL)
+    compare_blocks(gb, gc, ob, oc, hl.nbas, rk, nbloc)

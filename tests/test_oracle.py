@@ -195,3 +195,46 @@ def test_pow_als_zero_iterations_is_identity():
     b, c = oracle.pow_als_block(Q, qc, hl.nbas, 2, 2, hl, npow=0)
     np.testing.assert_array_equal(b, Q)
     np.testing.assert_array_equal(c, qc)
+
+
+@pytest.mark.parametrize("make", [lambda: H.henon_heiles(D=3, n=5, lam=0.111803),
+                                  lambda: H.coupled_oscillators(3, 5),
+                                  lambda: H.random_hoplist([4, 3, 5], 6, seed=7)])
+def test_rayleigh_quotient_matches_dense(make):
+    """RayleighQuotient2 restatement = v^T H v / v^T v with the dense
+    Hamiltonian and the dense vector."""
+    hl = make()
+    Hd = H.dense_hamiltonian(hl)
+    rng = np.random.default_rng(3)
+    rk, nD = 4, int(hl.nbas.sum())
+    b, c = rng.normal(size=(rk, nD)), rng.uniform(0.3, 1.5, rk)
+    v = dense_cp(b, c, list(hl.nbas)).reshape(-1)
+    want = v @ Hd @ v / (v @ v)
+    got = oracle.rayleigh_quotient(b, c, hl.nbas, hl)
+    assert abs(got - want) <= 1e-12 * abs(want)
+
+
+def test_qhq_diag_skips_converged_vectors():
+    hl = H.random_hoplist([4, 5, 3], 5, seed=4)
+    rng = np.random.default_rng(9)
+    rk, nbloc, nD = 3, 5, int(hl.nbas.sum())
+    Q, qc = rng.normal(size=(rk * nbloc, nD)), rng.uniform(0.5, 1.0, rk * nbloc)
+    out = oracle.qhq_diag(Q, qc, hl.nbas, rk, nbloc, hl, nconv=2, qhqd=np.full(nbloc, -7.0))
+    assert np.all(out[:2] == -7.0)
+    for i in range(2, nbloc):
+        s = slice(i * rk, (i + 1) * rk)
+        assert out[i] == oracle.rayleigh_quotient(Q[s], qc[s], hl.nbas, hl)
+
+
+def test_sort_vecs_semantics():
+    """SortVecs: increasing |eigv - Eref|, vectors follow, nconv cut back."""
+    rk, nD = 2, 3
+    eig = np.array([1.0, 5.0, 2.5, 0.2])
+    Q = np.arange(4 * rk * nD, dtype=float).reshape(4 * rk, nD)
+    qc = np.arange(4 * rk, dtype=float)
+    b, c, e, nconv = oracle.sort_vecs(Q, qc, rk, eig, 3, 2.0)
+    assert list(e) == [2.5, 1.0, 0.2, 5.0]
+    assert np.array_equal(b[:rk], Q[2 * rk:3 * rk]) and np.array_equal(c[rk:2 * rk], qc[:rk])
+    assert nconv == 0
+    _, _, e2, nconv2 = oracle.sort_vecs(Q, qc, rk, np.array([0.1, 0.2, 0.3, 0.4]), 3, 0.0)
+    assert list(e2) == [0.1, 0.2, 0.3, 0.4] and nconv2 == 3
