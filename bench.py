@@ -188,8 +188,17 @@ def run_cycle_bench(steps: int, cpu: bool):
     for _ in range(steps):
         IT.qhq_diag(gb, gc, hl.nbas, CYC_R, CYC_B, hl)
     out["qhq_diag_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
+    # GetSpectralRange before a node's solve (getspectralrangecpp_): two
+    # vectors, npow power steps per round, 10 rounds
+    import oracle
+    sb, sc = oracle.spectral_start(hl.nbas, CYC_R, seed=7)
+    IT.spectral_range(sb, sc, hl.nbas, CYC_R, hl, CYC_NPOW, 10)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        _, _, bounds = IT.spectral_range(sb, sc, hl.nbas, CYC_R, hl, CYC_NPOW, 10)
+    out["spectral_range_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
+    out["spectral_range"] = [float(bounds[0]), float(bounds[1])]
     if cpu:
-        import oracle
         oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
         t0 = time.perf_counter()
         oracle.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
@@ -197,6 +206,9 @@ def run_cycle_bench(steps: int, cpu: bool):
         t0 = time.perf_counter()
         oracle.qhq_diag(gb, gc, hl.nbas, CYC_R, CYC_B, hl)
         out["qhq_diag_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        oracle.spectral_range(sb, sc, hl.nbas, CYC_R, hl, CYC_NPOW, 10)
+        out["spectral_range_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
         out["cpu_cores"] = os.cpu_count()
         out["cpu_kind"] = "port"
         oracle.set_cycle_penalties()

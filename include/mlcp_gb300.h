@@ -79,6 +79,18 @@ MLCP_API void getqhqdiagcpp_(double *base, double *coef, int *nbas, MLCP_REF(int
                              double *mat, MLCP_REF(int) TxD, MLCP_REF(int) nops, MLCP_REF(int) msize,
                              double *qhqd);
 
+/* Replaces GetSpectralRange (src/Solver.f90:563-654) for nodes of more than
+ * two modes: base/coef hold the two starting vectors of rank rk (lower and
+ * upper guesses, built by the host as the reference does); ncyc rounds of
+ * npow ALS-fitted (H - shift) steps -- shift = midpoint of the current bounds
+ * for the lower vector, 0 for the upper -- each followed by their Rayleigh
+ * quotients as the new bounds, all on the GPU.  bounds[2] receives the range
+ * padded by 0.1 % of its width on each side; base/coef the final vectors. */
+MLCP_API void getspectralrangecpp_(double *base, double *coef, int *nbas, MLCP_REF(int) rk, MLCP_REF(int) ndof,
+                                   MLCP_REF(int) npow, MLCP_REF(int) ncyc, int *opid, int *mptr, double *Hcoef,
+                                   double *mat, MLCP_REF(int) TxD, MLCP_REF(int) nops, MLCP_REF(int) msize,
+                                   double *bounds);
+
 /* Replaces SortVecs (src/BlockUtils.f90:520-583): reorders the block (and
  * eigv alike) by increasing |eigv - Eref|; nconv becomes the position of
  * the first of the first nconv vectors that moved, if any did.  Equal

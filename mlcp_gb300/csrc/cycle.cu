@@ -344,6 +344,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
   // --- matrix-vector products: POW_ALS on every vector ---
   if (npow > 0) {
     OpAlsParams p;
+    p.eshift_v = nullptr;
     p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 0; p.nsweeps = npow; p.ishift = ishift; p.eshift = Eshift;
     p.pen_factor = kPenFP32;
     p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.q; p.f_coef = cb.qc;
@@ -362,6 +363,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
     // --- <Q|H|Q>, <Q|Q>, generalised eigenproblem ---
     if (nals > 0) {
       OpAlsParams p;
+      p.eshift_v = nullptr;
       p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 1; p.nsweeps = nals; p.ishift = 0; p.eshift = 0.0;
       p.pen_factor = kPenFP32;
       p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.hq; p.f_coef = cb.hqc;
@@ -474,6 +476,110 @@ int qhq_diag(Context* ctx, const double* base, const double* coef, const int* nb
   return kOk;
 }
 
+namespace {
+// The shifts of GetSpectralRange's power steps from the current bounds:
+// the midpoint for the lower vector, none for the upper one.
+__global__ void range_shift_kernel(const double* bounds, double* shift) {
+  shift[0] = 0.5 * (bounds[0] + bounds[1]);
+  shift[1] = 0.0;
+}
+}  // namespace
+
+// Reference GetSpectralRange (src/Solver.f90:563-654), more-than-two-mode
+// branch: the two starting vectors in base/coef (rank rk each; the host
+// builds them as the reference does) are improved by ncyc rounds of npow
+// ALS-fitted steps of (H - shift) -- the lower vector shifted to the
+// midpoint of the current bounds, the upper one unshifted -- each round
+// ending with their Rayleigh quotients as the new bounds.  The whole loop
+// stays on the device.  bounds[2] receives the range padded by 0.1 % on each
+// side; base/coef the final vectors.
+int spectral_range(Context* ctx, double* base, double* coef, const int* nbas, int rk, int ndof, int npow, int ncyc,
+                   const int* opid, const int* mptr, const double* Hcoef, const double* mat, int TxD, int nops,
+                   int msize, double* bounds) {
+  if (rk < 1 || rk > kMaxRankCycle) {
+    set_error("getspectralrangecpp_: rk = %d outside [1, %d]", rk, kMaxRankCycle);
+    return rk < 1 ? kBadArgument : kTooLarge;
+  }
+  if (ndof < 3) {
+    set_error("getspectralrangecpp_: ndof = %d; nodes of two modes use the power recursion with SVD", ndof);
+    return kBadArgument;
+  }
+  if (npow < 0 || ncyc < 0 || TxD < ndof || TxD % ndof != 0 || nops < 1 || msize < 1) {
+    set_error("getspectralrangecpp_: bad sizes (npow=%d ncyc=%d TxD=%d nops=%d msize=%d)", npow, ncyc, TxD, nops,
+              msize);
+    return kBadArgument;
+  }
+  Layout Ly;
+  int rc = make_layout(ndof, nbas, &Ly);
+  if (rc) return rc;
+  const int T = TxD / ndof, R = rk, B = 2;
+  cudaStream_t st = ctx->stream;
+  OpTable tab;
+  rc = get_optable(ctx, Ly, nbas, R, T, opid, mptr, Hcoef, mat, nops, msize, st, &tab);
+  if (rc) return rc;
+  if (opals_smem_bytes(tab) > ctx->smem_optin) {
+    set_error("getspectralrangecpp_: rank %d with %d padded basis functions needs too much shared memory", R, Ly.nDp);
+    return kTooLarge;
+  }
+  CycleBuffers cb;
+  size_t bytes = plan_cycle(Ly, tab, R, B, &cb, nullptr);
+  auto take = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
+  const size_t o_rq = take(sizeof(double) * 2), o_shift = take(sizeof(double) * 2),
+               o_work = take(sizeof(double) * 2 * rq_work_doubles(tab));
+  if (bytes > ctx->cyc_bytes) {
+    if (ctx->cyc) {
+      MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+      MLCP_CUDA_TRY(cudaFree(ctx->cyc));
+      ctx->cyc = nullptr;
+      ctx->cyc_bytes = 0;
+    }
+    MLCP_CUDA_TRY(cudaMalloc(&ctx->cyc, bytes));
+    ctx->cyc_bytes = bytes;
+  }
+  char* b = static_cast<char*>(ctx->cyc);
+  plan_cycle(Ly, tab, R, B, &cb, b);
+  double* rq = reinterpret_cast<double*>(b + o_rq);
+  double* shift = reinterpret_cast<double*>(b + o_shift);
+  const size_t nvals = (size_t)B * R * Ly.nD;
+  MLCP_CUDA_TRY(cudaMemcpyAsync(cb.q, base, sizeof(double) * nvals, cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qc, coef, sizeof(double) * B * R, cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaMemsetAsync(cb.status, 0, sizeof(int) * (B + 4), st));
+  RqParams q;
+  q.ops = tab; q.v0 = 0; q.nvec = B; q.nD = Ly.nD; q.base = cb.q; q.coef = cb.qc; q.out = rq;
+  q.work = reinterpret_cast<double*>(b + o_work); q.work_stride = 0;
+  if ((rc = rq_launch(q, st))) return rc;
+  for (int i = 0; i < ncyc; ++i) {
+    range_shift_kernel<<<1, 1, 0, st>>>(rq, shift);
+    MLCP_CUDA_TRY(cudaGetLastError());
+    if (npow > 0) {
+      OpAlsParams p;
+      p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 0; p.nsweeps = npow; p.ishift = 1; p.eshift = 0.0;
+      p.eshift_v = shift;
+      p.pen_factor = kPenFP32;
+      p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.q; p.f_coef = cb.qc;
+      p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
+      if ((rc = opals_launch(p, st))) return rc;
+    }
+    if ((rc = rq_launch(q, st))) return rc;
+  }
+  double bh[2];
+  int sh[2];
+  MLCP_CUDA_TRY(cudaMemcpyAsync(bh, rq, sizeof(bh), cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(sh, cb.status, sizeof(sh), cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(base, cb.q, sizeof(double) * nvals, cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(coef, cb.qc, sizeof(double) * B * R, cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int i = 0; i < B; ++i)
+    if (sh[i]) {
+      set_error("getspectralrangecpp_: a normal-equation matrix was not positive definite (vector %d)", i);
+      return kNumerical;
+    }
+  const double pad = 0.001 * (bh[1] - bh[0]);
+  bounds[0] = bh[0] - pad;
+  bounds[1] = bh[1] + pad;
+  return kOk;
+}
+
 // Reference SortVecs (src/BlockUtils.f90:520-583): the block reordered by
 // increasing |eigv - Eref| (the reference's dsort with a carried index; ties
 // keep their order here), eigv permuted alike, and nconv cut back to the
@@ -541,6 +647,20 @@ extern "C" void getqhqdiagcpp_(double* base, double* coef, int* nbas, const int&
   }
   finish_status(rc);
   if (rc != kOk) fprintf(stderr, "getqhqdiagcpp_: %s\n", last_error());
+}
+
+extern "C" void getspectralrangecpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof,
+                                     const int& npow, const int& ncyc, int* opid, int* mptr, double* Hcoef,
+                                     double* mat, const int& TxD, const int& nops, const int& msize, double* bounds) {
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (ctx) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    rc = spectral_range(ctx, base, coef, nbas, rk, ndof, npow, ncyc, opid, mptr, Hcoef, mat, TxD, nops, msize,
+                        bounds);
+  }
+  finish_status(rc);
+  if (rc != kOk) fprintf(stderr, "getspectralrangecpp_: %s\n", last_error());
 }
 
 extern "C" void sortvecscpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof, const int& nbloc,

@@ -37,6 +37,7 @@ struct OpAlsParams {
   int nsweeps;
   int ishift;
   double eshift;
+  const double* eshift_v;  // per-vector shifts (device) overriding eshift, or null
   double pen_factor;      // penalty = pen_factor * max(Fo weights)
   const double* fo_base;  // Fo vectors (reference layout, rank R each, vector v at v*R terms)
   const double* fo_coef;

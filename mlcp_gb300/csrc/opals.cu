@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kThreads) opals_kernel(OpAlsParams p) {
             acc += prod;
           }
           if (u == 0 && p.ishift != 0) {
-            float prod = (float)(-p.eshift);
+            float prod = (float)(-(p.eshift_v ? p.eshift_v[v] : p.eshift));
             for (int d = 0; d < D; ++d)
               if (d != j) prod *= M[(size_t)t.uoff[d] * R * R + e];
             acc += prod;

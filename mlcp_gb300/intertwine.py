@@ -72,6 +72,30 @@ def qhq_diag(base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int, hl, 
     return out
 
 
+def spectral_range(base: np.ndarray, coef: np.ndarray, nbas, rk: int, hl, npow: int, ncyc: int):
+    """Reference GetSpectralRange (src/Solver.f90:563-654, more than two
+    modes) through getspectralrangecpp_, from the two starting vectors of
+    rank rk in (base, coef).  Returns (base, coef, bounds) on copies, bounds
+    padded by 0.1 % of the range on each side."""
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32).copy()
+    opid = np.ascontiguousarray(hl.opid, dtype=np.int32).copy()
+    mptr = np.ascontiguousarray(hl.mptr, dtype=np.int32).copy()
+    hcoef = np.ascontiguousarray(hl.coef, dtype=np.float64).copy()
+    mat = np.ascontiguousarray(hl.mat, dtype=np.float64).copy()
+    bounds = np.zeros(2)
+    ints = [ctypes.c_int(x) for x in (rk, nb.size, npow, ncyc, opid.size, mptr.size, mat.size)]
+    L = _lib.load()
+    L.getspectralrangecpp_(base.ctypes.data_as(_D), coef.ctypes.data_as(_D), nb.ctypes.data_as(_I),
+                           *[ctypes.byref(x) for x in ints[:4]], opid.ctypes.data_as(_I), mptr.ctypes.data_as(_I),
+                           hcoef.ctypes.data_as(_D), mat.ctypes.data_as(_D), *[ctypes.byref(x) for x in ints[4:]],
+                           bounds.ctypes.data_as(_D))
+    if L.mlcp_gb300_last_status() != 0:
+        raise _lib.MlcpError(_lib.last_error())
+    return base, coef, bounds
+
+
 def sort_vecs(base: np.ndarray, coef: np.ndarray, nbas, rk: int, eigv: np.ndarray, nconv: int, eref: float):
     """Reference SortVecs (src/BlockUtils.f90:520-583) through sortvecscpp_
     on copies; returns (base, coef, eigv, nconv)."""

@@ -67,6 +67,8 @@ def lib() -> ctypes.CDLL:
         L.orc_sygv.argtypes = [ctypes.c_int, _D, _D, _D, _D]
         L.orc_rayleigh_quotient.restype = ctypes.c_double
         L.orc_rayleigh_quotient.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, ctypes.c_int]
+        L.orc_spectral_range.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I,
+                                         _D, _D, ctypes.c_int, _D]
         L.orc_qhq_diag.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D,
                                    _D, ctypes.c_int, _D, ctypes.c_int]
     return _lib
@@ -188,6 +190,44 @@ def qhq_diag(base, coef, nbas, rk, nbloc, hl, nconv=0, qhqd=None, nthreads=0):
     lib().orc_qhq_diag(_dp(base), _dp(coef), _ip(nb), rk, len(nb), nbloc, nconv, _ip(hl.opid), _ip(hl.mptr),
                        _dp(hl.coef), _dp(hl.mat), hl.nterms, _dp(out), nthreads)
     return out
+
+
+def spectral_start(nbas, rk, seed=0):
+    """The two starting vectors of GetSpectralRange (src/Solver.f90:583-606):
+    the first (lower guess) and last (upper guess) basis function of every
+    mode, 1e-15 elsewhere, weight 1, plus (more than two modes, rk > 1) the
+    same rk - 1 seeded random terms (uniform -0.5..0.5, normalised per mode)
+    with weight 1e-7.  Returns (base, coef) of the 2 x rk terms."""
+    nbas = np.asarray(nbas, dtype=np.int32)
+    nD, D = int(nbas.sum()), nbas.size
+    offs = np.concatenate([[0], np.cumsum(nbas)])
+    rng = np.random.default_rng(seed)
+    rand = rng.uniform(-0.5, 0.5, size=(max(rk - 1, 0), nD))
+    for d in range(D):
+        blk = rand[:, offs[d]:offs[d + 1]]
+        blk /= np.linalg.norm(blk, axis=1, keepdims=True)
+    base = np.full((2 * rk, nD), 1e-15)
+    coef = np.zeros(2 * rk)
+    for j in range(2):
+        coef[j * rk] = 1.0
+        for d in range(D):
+            base[j * rk, offs[d] if j == 0 else offs[d + 1] - 1] = 1.0
+        if D > 2 and rk > 1:
+            base[j * rk + 1:(j + 1) * rk] = rand
+            coef[j * rk + 1:(j + 1) * rk] = 1e-7
+    return base, coef
+
+
+def spectral_range(base, coef, nbas, rk, hl, npow, ncyc):
+    """Reference GetSpectralRange (more than two modes) from the starting
+    vectors; returns (base, coef, bounds) with the padded bounds."""
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    bounds = np.zeros(2)
+    lib().orc_spectral_range(_dp(base), _dp(coef), _ip(nb), rk, len(nb), npow, ncyc, _ip(hl.opid), _ip(hl.mptr),
+                             _dp(hl.coef), _dp(hl.mat), hl.nterms, _dp(bounds))
+    return base, coef, bounds
 
 
 def sort_vecs(base, coef, rk, eigv, nconv, eref):

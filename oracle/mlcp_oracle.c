@@ -768,6 +768,37 @@ void orc_qhq_diag(const double *base, const double *coef, const int *nbas, int r
   (void)nthreads;
 }
 
+/* GetSpectralRange (reference src/Solver.f90:563-654), the branch for more
+ * than two modes, from the two starting vectors in base/coef: bounds from
+ * their Rayleigh quotients, then ncyc rounds of npow power steps of
+ * (H - btmp_j) -- btmp_0 the midpoint of the bounds, btmp_1 = 0 -- each
+ * round ending with new bounds; finally the range padded by 0.1 % of its
+ * width on each side.  The power step is the POW_ALS restatement above
+ * (src/intertw_mvp.cu:452; its CPU twin ALS_POW3, src/ALSPow.f90:569-660). */
+void orc_spectral_range(double *base, double *coef, const int *nbas, int rk, int ndof, int npow, int ncyc,
+                        const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T,
+                        double *bounds) {
+  int nD = 0;
+  for (int d = 0; d < ndof; ++d) nD += nbas[d];
+  double b[2], btmp[2];
+  for (int j = 0; j < 2; ++j)
+    b[j] = orc_rayleigh_quotient(base + (size_t)j * rk * nD, coef + (size_t)j * rk, nbas, rk, ndof, opid, mptr,
+                                 Hcoef, mat, T);
+  btmp[0] = 0.5 * (b[0] + b[1]);
+  btmp[1] = 0.0;
+  for (int i = 0; i < ncyc; ++i) {
+    for (int j = 0; j < 2; ++j) {
+      double *vb = base + (size_t)j * rk * nD, *vc = coef + (size_t)j * rk;
+      orc_pow_als_block(vb, vc, nbas, rk, ndof, 1, opid, mptr, Hcoef, mat, T, npow, 1, btmp[j], 1);
+      b[j] = orc_rayleigh_quotient(vb, vc, nbas, rk, ndof, opid, mptr, Hcoef, mat, T);
+    }
+    btmp[0] = 0.5 * (b[0] + b[1]);
+  }
+  const double pad = 0.001 * (b[1] - b[0]);
+  bounds[0] = b[0] - pad;
+  bounds[1] = b[1] + pad;
+}
+
 double orc_cp_dot(const double *vb, const double *vc, int rv, const double *wb, const double *wc, int rw,
                   const int *nbas, int ndof) {
   int *off = make_offsets(nbas, ndof);

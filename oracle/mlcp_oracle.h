@@ -62,6 +62,11 @@ void orc_vector_updates(double *base, double *coef, const int *nbas, int rk, int
  * with H applied exactly, term by term. */
 double orc_rayleigh_quotient(const double *base, const double *coef, const int *nbas, int rk, int ndof,
                              const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T);
+/* Reference src/Solver.f90:563-654 (GetSpectralRange, more than two modes)
+ * from the two starting vectors in base/coef (overwritten); padded bounds. */
+void orc_spectral_range(double *base, double *coef, const int *nbas, int rk, int ndof, int npow, int ncyc,
+                        const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T,
+                        double *bounds);
 /* Reference src/BlockUtils.f90:385-408 (GetQHQdiag): qhqd[i] for i >= nconv. */
 void orc_qhq_diag(const double *base, const double *coef, const int *nbas, int rk, int ndof, int nbloc, int nconv,
                   const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, double *qhqd,

@@ -160,3 +160,25 @@ def test_update_false_path_matches_oracle(cuda_device):
     assert gn == on
     np.testing.assert_allclose(ge, oe, rtol=EIG_RTOL)
     compare_blocks(gb, gc, ob, oc, hl.nbas, rk, nbloc)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ncyc", [0, 1, 6])
+def test_spectral_range_matches_oracle(ncyc, cuda_device):
+    """getspectralrangecpp_ against the oracle from the same starting vectors
+    (the power steps' FP32 contractions move the bounds by ~1e-7)."""
+    hl = H.henon_heiles(D=4, n=6)
+    b, c = oracle.spectral_start(hl.nbas, 5, seed=2)
+    gb, gc, gbd = IT.spectral_range(b, c, hl.nbas, 5, hl, 4, ncyc)
+    oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
+    ob, oc, obd = oracle.spectral_range(b, c, hl.nbas, 5, hl, 4, ncyc)
+    np.testing.assert_allclose(gbd, obd, rtol=1e-6)
+    compare_blocks(gb, gc, ob, oc, hl.nbas, 5, 2, tol=1e-5)
+
+
+@pytest.mark.gpu
+def test_spectral_range_rejects_two_modes(cuda_device):
+    hl = H.random_hoplist([5, 7], 4, seed=2)
+    b, c = oracle.spectral_start(hl.nbas, 3)
+    with pytest.raises(Exception, match="two modes"):
+        IT.spectral_range(b, c, hl.nbas, 3, hl, 2, 1)

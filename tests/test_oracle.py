@@ -238,3 +238,23 @@ def test_sort_vecs_semantics():
     assert nconv == 0
     _, _, e2, nconv2 = oracle.sort_vecs(Q, qc, rk, np.array([0.1, 0.2, 0.3, 0.4]), 3, 0.0)
     assert list(e2) == [0.1, 0.2, 0.3, 0.4] and nconv2 == 3
+
+
+@pytest.mark.parametrize("make", [lambda: H.henon_heiles(D=3, n=5, lam=0.111803),
+                                  lambda: H.coupled_oscillators(3, 5)])
+def test_spectral_range_brackets_and_converges(make):
+    """GetSpectralRange restatement: the unpadded bounds are Rayleigh
+    quotients, so they lie in [E_min, E_max]; after enough rounds they reach
+    both ends of the dense spectrum (to the accuracy a rank-4 power iteration
+    reaches: 1e-4 of the spectral width at the top, 1e-3 at the bottom, where
+    the shifted iteration converges more slowly)."""
+    hl = make()
+    ex = np.linalg.eigvalsh(H.dense_hamiltonian(hl))
+    b, c = oracle.spectral_start(hl.nbas, 4, seed=1)
+    _, _, bd = oracle.spectral_range(b, c, hl.nbas, 4, hl, 5, 20)
+    pad = 0.001 * (bd[1] - bd[0]) / 1.002
+    lo, hi = bd[0] + pad, bd[1] - pad
+    assert ex[0] - 1e-9 <= lo <= hi <= ex[-1] + 1e-9
+    width = ex[-1] - ex[0]
+    assert abs(hi - ex[-1]) < 1e-4 * width
+    assert abs(lo - ex[0]) < 1e-3 * width
