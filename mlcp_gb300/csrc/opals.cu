@@ -22,6 +22,8 @@
 // weight normalisation run in FP64; the operator Grams, term products and
 // right-hand sides run in FP32.
 #include "common.cuh"
+#include "dword.cuh"
+#include "dwsolve.cuh"
 #include "intertwine.cuh"
 
 namespace mlcp {
@@ -30,34 +32,70 @@ namespace {
 
 constexpr int kThreads = 256;
 
+constexpr int kWarps = kThreads / 32;
+
 struct OpSmem {
   float* f32;     // [R][nDp] current F (FP32)
   float* fo32;    // [R][nDp] Fo (FP32); aliases f32 for POW
   float* y;       // [R][npmax] temporary h Fo_r
-  double* X;      // [R][npmax] right-hand side / solution (column-major, ld R)
-  double* BB;     // [R][R]
-  double* cf;     // [R] weights of F
-  double* cfo;    // [R] weights of Fo
-  double* red;    // [kThreads] reduction scratch
-  double* dinv;   // [R] reciprocal pivots
-  double* u;      // [R] LDL^T scratch column
+  dw* X;          // [R][npmax] solution (column-major, ld R)
+  dw* b0;         // [R][npmax] right-hand side
+  dw* res;        // [R][npmax] refinement residual
+  dw* BB;         // [R][R] normal equations
+  float* gi;      // [2][R][R] FP32 inverse of BB
+  dw* cf;         // [R] weights of F
+  dw* cfo;        // [R] weights of Fo
+  dw* red;        // [kWarps] reduction scratch
+  dw* dinv;       // [R] LDL^T reciprocal pivots
+  dw* u;          // [R] LDL^T scratch column
+  dw* misc;       // [2] penalty
+  float* rred;    // [4] refinement scratch
+  dwsolve::ColScratch cs;
   int* flags;     // [4]
 };
 
-__device__ inline void carve(OpSmem& s, unsigned char* base, const OpTable& t, bool separate_fo) {
-  unsigned char* ptr = base;
-  auto take = [&](size_t bytes) { unsigned char* r = ptr; ptr += (bytes + 15) / 16 * 16; return r; };
+// Carves the shared memory (null base: sizes only); returns the bytes.
+__host__ __device__ inline size_t carve(OpSmem& s, unsigned char* base, const OpTable& t, bool separate_fo) {
+  size_t o = 0;
+  auto take = [&](size_t bytes) -> unsigned char* {
+    const size_t r = o;
+    o += (bytes + 15) / 16 * 16;
+    return base ? base + r : nullptr;
+  };
+  const size_t Rn = (size_t)t.R * t.npmax, RR = (size_t)t.R * t.R;
   s.f32 = (float*)take(sizeof(float) * t.R * t.nDp);
   s.fo32 = separate_fo ? (float*)take(sizeof(float) * t.R * t.nDp) : s.f32;
-  s.y = (float*)take(sizeof(float) * t.R * t.npmax);
-  s.X = (double*)take(sizeof(double) * t.R * t.npmax);
-  s.BB = (double*)take(sizeof(double) * t.R * t.R);
-  s.cf = (double*)take(sizeof(double) * t.R);
-  s.cfo = (double*)take(sizeof(double) * t.R);
-  s.red = (double*)take(sizeof(double) * kThreads);
-  s.dinv = (double*)take(sizeof(double) * t.R);
-  s.u = (double*)take(sizeof(double) * t.R);
+  s.y = (float*)take(sizeof(float) * Rn);
+  s.X = (dw*)take(sizeof(dw) * Rn);
+  s.b0 = (dw*)take(sizeof(dw) * Rn);
+  s.res = (dw*)take(sizeof(dw) * Rn);
+  s.BB = (dw*)take(sizeof(dw) * RR);
+  s.gi = (float*)take(sizeof(float) * 2 * RR);
+  s.cf = (dw*)take(sizeof(dw) * t.R);
+  s.cfo = (dw*)take(sizeof(dw) * t.R);
+  s.red = (dw*)take(sizeof(dw) * kWarps);
+  s.dinv = (dw*)take(sizeof(dw) * t.R);
+  s.u = (dw*)take(sizeof(dw) * t.R);
+  s.misc = (dw*)take(sizeof(dw) * 2);
+  s.rred = (float*)take(sizeof(float) * 4);
+  s.cs.conv = (float*)take(sizeof(float) * 64);
+  s.cs.rmax = (float*)take(sizeof(float) * 16 * 32);
+  s.cs.rsum = (dw*)take(sizeof(dw) * 16 * 32);
   s.flags = (int*)take(sizeof(int) * 4);
+  return o;
+}
+
+// Sum over the block; thread 0 gets the result (fixed order).
+__device__ dw block_sum_dw(dw v, dw* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) v = dw_add(v, dwsolve::dw_shfl_xor(v, o));
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  dw s = dw_make(0.f);
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kWarps; ++w) s = dw_add(s, red[w]);
+  return s;
 }
 
 // M(r,i) = sum_n (h Fo_r^d)(n) F_i^d(n); identity operators skip the product.
@@ -88,20 +126,20 @@ __device__ void operator_gram(const OpTable& t, int d, int ug, const OpSmem& s, 
   __syncthreads();
 }
 
-// FP64 Gram of mode d of F (global FP64 factors).
-__device__ void f_gram64(const OpTable& t, int d, const double* fb, int nD, double* G) {
+// Double-word Gram of mode d of F from the FP64 factors (set-up only).
+__device__ void f_gram_from64(const OpTable& t, int d, const double* fb, int nD, dw* G) {
   const int R = t.R, n = t.nbas[d], o = t.off[d];
   for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
     const int i = e % R, i2 = e / R;
     double acc = 0.0;
     for (int q = 0; q < n; ++q) acc += fb[(size_t)i * nD + o + q] * fb[(size_t)i2 * nD + o + q];
-    G[e] = acc;
+    G[e] = dw_from_double(acc);
   }
 }
 
 }  // namespace
 
-__global__ void __launch_bounds__(kThreads) opals_kernel(OpAlsParams p) {
+__global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
   const OpTable& t = p.ops;
   const int v = blockIdx.x;
   const int R = t.R, D = t.D, T = t.T, npm = t.npmax, nD = p.nD;
@@ -117,7 +155,7 @@ __global__ void __launch_bounds__(kThreads) opals_kernel(OpAlsParams p) {
   float* M = p.mscr + (size_t)v * t.utot * R * R;
   float* W = p.wscr + (size_t)v * t.umax * R * R;
   float* Z = p.zscr + (size_t)v * t.umax * R * npm;
-  double* G64 = p.g64 + (size_t)v * D * R * R;
+  dw* G = reinterpret_cast<dw*>(p.g64) + (size_t)v * D * R * R;  // double-word F Grams per mode
 
   // ---- set-up: F (= Fo for PRODHV), FP32 copies, Grams, penalty ----
   if (!pow_mode) {
@@ -135,20 +173,20 @@ __global__ void __launch_bounds__(kThreads) opals_kernel(OpAlsParams p) {
     if (!pow_mode) s.fo32[e] = (float)x;
   }
   for (int e = threadIdx.x; e < R; e += blockDim.x) {
-    s.cf[e] = fc[e];
-    s.cfo[e] = foc[e];
+    s.cf[e] = dw_from_double(fc[e]);
+    s.cfo[e] = dw_from_double(foc[e]);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double pen = s.cfo[0];
-    for (int i = 1; i < R; ++i) pen = s.cfo[i] > pen ? s.cfo[i] : pen;
-    s.red[0] = pen * p.pen_factor;
+    double pen = foc[0];
+    for (int i = 1; i < R; ++i) pen = foc[i] > pen ? foc[i] : pen;
+    s.misc[0] = dw_from_double(pen * p.pen_factor);
     s.flags[0] = 0;
     s.flags[1] = 0;
   }
-  for (int d = 0; d < D; ++d) f_gram64(t, d, fb, nD, G64 + (size_t)d * R * R);
+  for (int d = 0; d < D; ++d) f_gram_from64(t, d, fb, nD, G + (size_t)d * R * R);
   __syncthreads();
-  const double pen = s.red[0];
+  const dw pen = s.misc[0];
   for (int d = 0; d < D; ++d)
     for (int u = 0; u < t.uoff[d + 1] - t.uoff[d]; ++u)
       operator_gram(t, d, t.uoff[d] + u, s, M + (size_t)(t.uoff[d] + u) * R * R, nullptr);
@@ -200,45 +238,81 @@ __global__ void __launch_bounds__(kThreads) opals_kernel(OpAlsParams p) {
       }
       __syncthreads();
       // -- right-hand side b(i,n) = sum_u sum_r W_u(r,i) c_r Z_u(r,n) --
-      const double* cg = pow_mode ? s.cf : s.cfo;
+      const dw* cg = pow_mode ? s.cf : s.cfo;
       for (int e = threadIdx.x; e < R * nj; e += blockDim.x) {
         const int i = e % R, m = e / R;
         float acc = 0.f;
         for (int u = 0; u < nu; ++u)
           for (int r = 0; r < R; ++r)
-            acc = fmaf(W[(size_t)u * R * R + r * R + i] * (float)cg[r], Z[(size_t)u * R * npm + r * npm + m], acc);
-        double b = (double)acc;
-        if (p.ishift < 0) b = -b;
-        s.X[i + m * R] = b;
+            acc = fmaf(W[(size_t)u * R * R + r * R + i] * cg[r].hi, Z[(size_t)u * R * npm + r * npm + m], acc);
+        s.b0[i + m * R] = dw_make(p.ishift < 0 ? -acc : acc);
       }
-      // -- FP64 normal equations --
+      // -- normal equations (double-word): prod_{d != j} G_d + pen I --
       for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
-        double bb = 1.0;
+        dw bb = dw_make(1.f);
         for (int d = 0; d < D; ++d)
-          if (d != j) bb *= G64[(size_t)d * R * R + e];
-        if (e % R == e / R) bb += pen;
+          if (d != j) bb = dw_mul(bb, G[(size_t)d * R * R + e]);
+        if (e % R == e / R) bb = dw_add(bb, pen);
         s.BB[e] = bb;
       }
       __syncthreads();
-      block_ldlt(s.BB, R, R, s.dinv, s.u, &s.flags[2]);
-      if (threadIdx.x == 0 && s.flags[2]) s.flags[1] = 1;
-      block_ldlt_solve(s.BB, R, R, s.dinv, s.X, nj, R);
-      for (int i = threadIdx.x; i < R; i += blockDim.x) {
-        double nrm, inv;
-        scaled_norm(s.X + i, nj, R, &nrm, &inv);
-        for (int m = 0; m < nj; ++m) s.X[i + m * R] *= inv;
-        s.cf[i] = nrm;
-        fc[i] = nrm;
+      // -- FP32 inverse (one warp in registers for R <= 32), refinement
+      //    with double-word residuals, the double-word LDL^T as fallback --
+      bool gj_ok = false;
+      const float* inv = s.gi;
+      if (R <= 32) {
+        if (threadIdx.x < 32) {
+          const bool g = dwsolve::gj_inverse_warp(s.BB, R, s.gi);
+          if (threadIdx.x == 0) s.flags[2] = g;
+        }
+      } else if (threadIdx.x < dwsolve::kSolverThreads) {
+        inv = dwsolve::gj_inverse(s.BB, R, s.gi, &gj_ok);
+        if (threadIdx.x == 0) s.flags[2] = gj_ok;
       }
       __syncthreads();
+      gj_ok = s.flags[2] != 0;
+      bool solved = false;
+      const int nsw = dwsolve::solve_cols_warps(R, nj);
+      if (gj_ok && R <= 32 && nj <= 16 && nsw <= kWarps) {
+        if (threadIdx.x < nsw * 32) {
+          const bool ok = dwsolve::solve_cols_any(s.BB, R, s.b0, s.X, nj, inv, s.cf, s.cs);
+          if (threadIdx.x == 0) s.flags[3] = ok;
+        }
+        __syncthreads();
+        solved = s.flags[3] != 0;
+        gj_ok = false;  // not converged: straight to the LDL^T
+      }
+      if (!solved) {
+        if (threadIdx.x < dwsolve::kSolverThreads) {
+          int bad = 0;
+          if (!(gj_ok && dwsolve::refine_solve(s.BB, R, s.b0, s.X, nj, inv, s.res, s.rred))) {
+            for (int e = threadIdx.x; e < R * nj; e += dwsolve::kSolverThreads) s.X[e] = s.b0[e];
+            bad = dwsolve::dw_ldlt(s.BB, R, s.dinv, s.u);
+            dwsolve::dw_ldlt_solve(s.BB, R, s.dinv, s.X, nj);
+          }
+          dwsolve::dw_normalise_rows(s.X, R, nj, s.cf);
+          if (threadIdx.x == 0 && bad) s.flags[1] = 1;
+        }
+        __syncthreads();
+      }
+      // -- the new factor: FP64 output, FP32 copy, double-word Gram --
+      for (int i = threadIdx.x; i < R; i += blockDim.x) fc[i] = dw_to_double(s.cf[i]);
       for (int e = threadIdx.x; e < R * nj; e += blockDim.x) {
         const int i = e / nj, m = e % nj;
-        const double x = s.X[i + m * R];
-        fb[(size_t)i * nD + t.off[j] + m] = x;
-        s.f32[i * t.nDp + opj + m] = (float)x;
+        const dw x = s.X[i + m * R];
+        fb[(size_t)i * nD + t.off[j] + m] = dw_to_double(x);
+        s.f32[i * t.nDp + opj + m] = x.hi;
+      }
+      for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
+        const int i = e % R, i2 = e / R;
+        if (i > i2) continue;
+        dw_acc acc = acc_zero();
+        for (int m = 0; m < nj; ++m) acc_fma(acc, s.X[i + m * R], s.X[i2 + m * R]);
+        const dw g = acc_value(acc);
+        G[(size_t)j * R * R + i + i2 * R] = g;
+        G[(size_t)j * R * R + i2 + i * R] = g;
       }
       __syncthreads();
-      f_gram64(t, j, fb, nD, G64 + (size_t)j * R * R);
       // -- operator Grams of mode j with the new factor --
       for (int u = 0; u < nu; ++u) {
         const int ug = t.uoff[j] + u;
@@ -260,25 +334,19 @@ __global__ void __launch_bounds__(kThreads) opals_kernel(OpAlsParams p) {
     }
     if (pow_mode) {
       // weight renormalisation after each sweep (src/intertw_mvp.cu:491-494)
-      double part = 0.0;
+      dw part = dw_make(0.f);
       for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
-        double prod = s.cf[e % R] * s.cf[e / R];
-        for (int d = 0; d < D; ++d) prod *= G64[(size_t)d * R * R + e];
-        part += prod;
+        dw prod = dw_mul(s.cf[e % R], s.cf[e / R]);
+        for (int d = 0; d < D; ++d) prod = dw_mul(prod, G[(size_t)d * R * R + e]);
+        part = dw_add(part, prod);
       }
-      s.red[threadIdx.x] = part;
+      const dw tot = block_sum_dw(part, s.red);
+      if (threadIdx.x == 0) s.misc[1] = dw_sqrt(dw_abs(tot));
       __syncthreads();
-      if (threadIdx.x == 0) {
-        double tot = 0.0;
-        for (int k = 0; k < blockDim.x; ++k) tot += s.red[k];
-        s.red[0] = sqrt(fabs(tot));
-      }
-      __syncthreads();
-      const double q = s.red[0];
-      __syncthreads();
+      const dw q = s.misc[1];
       for (int i = threadIdx.x; i < R; i += blockDim.x) {
-        s.cf[i] /= q;
-        fc[i] = s.cf[i];
+        s.cf[i] = dw_div(s.cf[i], q);
+        fc[i] = dw_to_double(s.cf[i]);
       }
       __syncthreads();
     }
@@ -287,20 +355,8 @@ __global__ void __launch_bounds__(kThreads) opals_kernel(OpAlsParams p) {
 }
 
 size_t opals_smem_bytes(const OpTable& t) {
-  size_t b = 0;
-  auto take = [&](size_t bytes) { b += (bytes + 15) / 16 * 16; };
-  take(sizeof(float) * t.R * t.nDp);
-  take(sizeof(float) * t.R * t.nDp);
-  take(sizeof(float) * t.R * t.npmax);
-  take(sizeof(double) * t.R * t.npmax);
-  take(sizeof(double) * t.R * t.R);
-  take(sizeof(double) * t.R);
-  take(sizeof(double) * t.R);
-  take(sizeof(double) * kThreads);
-  take(sizeof(double) * t.R);
-  take(sizeof(double) * t.R);
-  take(sizeof(int) * 4);
-  return b;
+  OpSmem s;
+  return carve(s, nullptr, t, true);
 }
 
 int opals_launch(const OpAlsParams& p, cudaStream_t st) {
