@@ -51,11 +51,17 @@ struct OpSmem {
   dw* misc;       // [2] penalty
   float* rred;    // [4] refinement scratch
   dwsolve::ColScratch cs;
+  int* moff;      // [T][D] offset of each term's operator Gram per mode (null when T D is large)
+  float *Ms, *Ws, *Zs;  // operator Grams, term products, h_u Fo_j when resident in shared memory
   int* flags;     // [4]
 };
 
+// Terms x modes up to which the Gram offsets are tabulated in shared memory.
+constexpr int kMoffMax = 8192;
+
 // Carves the shared memory (null base: sizes only); returns the bytes.
-__host__ __device__ inline size_t carve(OpSmem& s, unsigned char* base, const OpTable& t, bool separate_fo) {
+__host__ __device__ inline size_t carve(OpSmem& s, unsigned char* base, const OpTable& t, bool separate_fo,
+                                        bool resident) {
   size_t o = 0;
   auto take = [&](size_t bytes) -> unsigned char* {
     const size_t r = o;
@@ -81,6 +87,10 @@ __host__ __device__ inline size_t carve(OpSmem& s, unsigned char* base, const Op
   s.cs.conv = (float*)take(sizeof(float) * 64);
   s.cs.rmax = (float*)take(sizeof(float) * 16 * 32);
   s.cs.rsum = (dw*)take(sizeof(dw) * 16 * 32);
+  s.moff = (t.T * t.D <= kMoffMax) ? (int*)take(sizeof(int) * t.T * t.D) : nullptr;
+  s.Ms = resident ? (float*)take(sizeof(float) * t.utot * RR) : nullptr;
+  s.Ws = resident ? (float*)take(sizeof(float) * t.umax * RR) : nullptr;
+  s.Zs = resident ? (float*)take(sizeof(float) * t.umax * Rn) : nullptr;
   s.flags = (int*)take(sizeof(int) * 4);
   return o;
 }
@@ -139,22 +149,28 @@ __device__ void f_gram_from64(const OpTable& t, int d, const double* fb, int nD,
 
 }  // namespace
 
+// kResident: the operator Grams, term products and h_u Fo_j in shared memory
+// (else in the per-vector global scratch of p).
+template <bool kResident>
 __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
   const OpTable& t = p.ops;
   const int v = blockIdx.x;
-  const int R = t.R, D = t.D, T = t.T, npm = t.npmax, nD = p.nD;
+  const int R = t.R, D = t.D, T = t.T, npm = t.npmax, nD = p.nD, RR = R * R;
   const bool pow_mode = (p.mode == 0);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   OpSmem s;
-  carve(s, smem_raw, t, !pow_mode);
+  carve(s, smem_raw, t, !pow_mode, kResident);
 
   const double* fob = p.fo_base + (size_t)v * R * nD;
   const double* foc = p.fo_coef + (size_t)v * R;
   double* fb = p.f_base + (size_t)v * R * nD;
   double* fc = p.f_coef + (size_t)v * R;
-  float* M = p.mscr + (size_t)v * t.utot * R * R;
-  float* W = p.wscr + (size_t)v * t.umax * R * R;
-  float* Z = p.zscr + (size_t)v * t.umax * R * npm;
+  float* M = kResident ? s.Ms : p.mscr + (size_t)v * t.utot * R * R;
+  float* W = kResident ? s.Ws : p.wscr + (size_t)v * t.umax * R * R;
+  float* Z = kResident ? s.Zs : p.zscr + (size_t)v * t.umax * R * npm;
+  const int* moff = s.moff;
+  if (moff)
+    for (int e = threadIdx.x; e < T * D; e += blockDim.x) s.moff[e] = (t.uoff[e % D] + t.uid[e]) * RR;
   dw* G = reinterpret_cast<dw*>(p.g64) + (size_t)v * D * R * R;  // double-word F Grams per mode
 
   // ---- set-up: F (= Fo for PRODHV), FP32 copies, Grams, penalty ----
@@ -197,80 +213,96 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
       const int nu = t.uoff[j + 1] - t.uoff[j];
       const int* ord = t.order + (size_t)j * T;
       const int* gs = t.gstart + (size_t)j * (t.umax + 1);
-      // -- grouped term products W_u --
-      for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
-        for (int u = 0; u < nu; ++u) {
-          float acc = 0.f;
-          for (int q = gs[u]; q < gs[u + 1]; ++q) {
-            const int term = ord[q];
-            float prod = (float)t.alpha[term];
-            const int* ut = t.uid + (size_t)term * D;
-            for (int d = 0; d < D; ++d) {
-              if (d == j) continue;
-              prod *= M[(size_t)(t.uoff[d] + ut[d]) * R * R + e];
-            }
-            acc += prod;
-          }
-          if (u == 0 && p.ishift != 0) {
-            float prod = (float)(-(p.eshift_v ? p.eshift_v[v] : p.eshift));
-            for (int d = 0; d < D; ++d)
-              if (d != j) prod *= M[(size_t)t.uoff[d] * R * R + e];
-            acc += prod;
-          }
-          W[(size_t)u * R * R + e] = acc;
-        }
-      }
-      // -- h_u Fo_j for every operator of mode j --
-      for (int u = 0; u < nu; ++u) {
-        const int ug = t.uoff[j] + u;
-        const float* h = t.hmat + (size_t)ug * npm * npm;
-        for (int e = threadIdx.x; e < R * nj; e += blockDim.x) {
-          const int r = e / nj, m = e % nj;
-          float acc;
-          if (t.ident[ug]) {
-            acc = s.fo32[r * t.nDp + opj + m];
-          } else {
-            acc = 0.f;
-            for (int k = 0; k < nj; ++k) acc = fmaf(h[m * npm + k], s.fo32[r * t.nDp + opj + k], acc);
-          }
-          Z[(size_t)u * R * npm + r * npm + m] = acc;
-        }
-      }
-      __syncthreads();
-      // -- right-hand side b(i,n) = sum_u sum_r W_u(r,i) c_r Z_u(r,n) --
-      const dw* cg = pow_mode ? s.cf : s.cfo;
-      for (int e = threadIdx.x; e < R * nj; e += blockDim.x) {
-        const int i = e % R, m = e / R;
-        float acc = 0.f;
-        for (int u = 0; u < nu; ++u)
-          for (int r = 0; r < R; ++r)
-            acc = fmaf(W[(size_t)u * R * R + r * R + i] * cg[r].hi, Z[(size_t)u * R * npm + r * npm + m], acc);
-        s.b0[i + m * R] = dw_make(p.ishift < 0 ? -acc : acc);
-      }
-      // -- normal equations (double-word): prod_{d != j} G_d + pen I --
-      for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
+      // -- normal equations (double-word) from the Grams of the previous
+      //    step: prod_{d != j} G_d + pen I --
+      for (int e = threadIdx.x; e < RR; e += blockDim.x) {
         dw bb = dw_make(1.f);
         for (int d = 0; d < D; ++d)
-          if (d != j) bb = dw_mul(bb, G[(size_t)d * R * R + e]);
+          if (d != j) bb = dw_mul(bb, G[(size_t)d * RR + e]);
         if (e % R == e / R) bb = dw_add(bb, pen);
         s.BB[e] = bb;
       }
       __syncthreads();
-      // -- FP32 inverse (one warp in registers for R <= 32), refinement
-      //    with double-word residuals, the double-word LDL^T as fallback --
-      bool gj_ok = false;
-      const float* inv = s.gi;
-      if (R <= 32) {
-        if (threadIdx.x < 32) {
+      // -- their FP32 inverse (warp 0 in registers for R <= 32, else warps
+      //    0-3) while the other warps form the right-hand side --
+      const int w0 = R <= 32 ? 32 : dwsolve::kSolverThreads;
+      if (threadIdx.x < w0) {
+        if (R <= 32) {
           const bool g = dwsolve::gj_inverse_warp(s.BB, R, s.gi);
-          if (threadIdx.x == 0) s.flags[2] = g;
+          if (threadIdx.x == 0) {
+            s.flags[2] = g;
+            s.flags[0] = 0;
+          }
+        } else {
+          bool ok;
+          const float* iv = dwsolve::gj_inverse(s.BB, R, s.gi, &ok);
+          if (threadIdx.x == 0) {
+            s.flags[2] = ok;
+            s.flags[0] = iv == s.gi ? 0 : 1;
+          }
         }
-      } else if (threadIdx.x < dwsolve::kSolverThreads) {
-        inv = dwsolve::gj_inverse(s.BB, R, s.gi, &gj_ok);
-        if (threadIdx.x == 0) s.flags[2] = gj_ok;
+      } else {
+        const int wt = threadIdx.x - w0, nw = kThreads - w0;
+        // grouped term products W_u(r,i) = sum_{t in group u} alpha_t prod_{d != j} M[d][op(t,d)](r,i),
+        // four terms at a time
+        for (int item = wt; item < nu * RR; item += nw) {
+          const int u = item / RR, e = item - u * RR;
+          float acc = 0.f;
+          for (int q = gs[u]; q < gs[u + 1]; q += 4) {
+            float pr[4];
+            int tb[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const bool live = q + k < gs[u + 1];
+              const int term = ord[live ? q + k : q];
+              pr[k] = live ? (float)t.alpha[term] : 0.f;
+              tb[k] = term * D;
+            }
+            for (int d = 0; d < D; ++d) {
+              if (d == j) continue;
+#pragma unroll
+              for (int k = 0; k < 4; ++k)
+                pr[k] *= M[(moff ? moff[tb[k] + d] : (t.uoff[d] + t.uid[tb[k] + d]) * RR) + e];
+            }
+            acc += (pr[0] + pr[1]) + (pr[2] + pr[3]);
+          }
+          if (u == 0 && p.ishift != 0) {
+            float prod = (float)(-(p.eshift_v ? p.eshift_v[v] : p.eshift));
+            for (int d = 0; d < D; ++d)
+              if (d != j) prod *= M[(size_t)t.uoff[d] * RR + e];
+            acc += prod;
+          }
+          W[(size_t)u * RR + e] = acc;
+        }
+        // h_u Fo_j for every operator of mode j
+        for (int item = wt; item < nu * R * nj; item += nw) {
+          const int u = item / (R * nj), rem = item - u * R * nj, r = rem / nj, m = rem - r * nj;
+          const int ug = t.uoff[j] + u;
+          float acc;
+          if (t.ident[ug]) {
+            acc = s.fo32[r * t.nDp + opj + m];
+          } else {
+            const float* h = t.hmat + (size_t)ug * npm * npm + (size_t)m * npm;
+            acc = 0.f;
+            for (int k = 0; k < nj; ++k) acc = fmaf(h[k], s.fo32[r * t.nDp + opj + k], acc);
+          }
+          Z[(size_t)u * R * npm + r * npm + m] = acc;
+        }
+        asm volatile("bar.sync 2, %0;" ::"r"(nw) : "memory");
+        // right-hand side b(i,n) = sum_u sum_r W_u(r,i) c_r Z_u(r,n)
+        const dw* cg = pow_mode ? s.cf : s.cfo;
+        for (int e = wt; e < R * nj; e += nw) {
+          const int i = e % R, m = e / R;
+          float acc = 0.f;
+          for (int u = 0; u < nu; ++u)
+            for (int r = 0; r < R; ++r)
+              acc = fmaf(W[(size_t)u * RR + r * R + i] * cg[r].hi, Z[(size_t)u * R * npm + r * npm + m], acc);
+          s.b0[i + m * R] = dw_make(p.ishift < 0 ? -acc : acc);
+        }
       }
       __syncthreads();
-      gj_ok = s.flags[2] != 0;
+      bool gj_ok = s.flags[2] != 0;
+      const float* inv = s.gi + (size_t)s.flags[0] * RR;
       bool solved = false;
       const int nsw = dwsolve::solve_cols_warps(R, nj);
       if (gj_ok && R <= 32 && nj <= 16 && nsw <= kWarps) {
@@ -313,22 +345,30 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
         G[(size_t)j * R * R + i2 + i * R] = g;
       }
       __syncthreads();
-      // -- operator Grams of mode j with the new factor --
-      for (int u = 0; u < nu; ++u) {
-        const int ug = t.uoff[j] + u;
-        float* Mu = M + (size_t)ug * R * R;
-        if (pow_mode) {
-          operator_gram(t, j, ug, s, Mu, nullptr);
-        } else {
-          // Fo is fixed: h_u Fo_j is still in Z
-          for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
-            const int r = e / R, i = e % R;
-            float acc = 0.f;
-            for (int m = 0; m < nj; ++m)
-              acc = fmaf(Z[(size_t)u * R * npm + r * npm + m], s.f32[i * t.nDp + opj + m], acc);
-            Mu[e] = acc;
+      // -- operator Grams of mode j with the new factor: h_u F_j for every
+      //    operator (POW; PRODHV keeps h_u Fo_j in Z), then M_u = (h_u F_j) F_j^T --
+      if (pow_mode) {
+        for (int item = threadIdx.x; item < nu * R * nj; item += blockDim.x) {
+          const int u = item / (R * nj), rem = item - u * R * nj, r = rem / nj, m = rem - r * nj;
+          const int ug = t.uoff[j] + u;
+          float acc;
+          if (t.ident[ug]) {
+            acc = s.f32[r * t.nDp + opj + m];
+          } else {
+            const float* h = t.hmat + (size_t)ug * npm * npm + (size_t)m * npm;
+            acc = 0.f;
+            for (int k = 0; k < nj; ++k) acc = fmaf(h[k], s.f32[r * t.nDp + opj + k], acc);
           }
+          Z[(size_t)u * R * npm + r * npm + m] = acc;
         }
+        __syncthreads();
+      }
+      for (int item = threadIdx.x; item < nu * RR; item += blockDim.x) {
+        const int u = item / RR, e = item - u * RR, r = e / R, i = e - r * R;
+        float acc = 0.f;
+        for (int m = 0; m < nj; ++m)
+          acc = fmaf(Z[(size_t)u * R * npm + r * npm + m], s.f32[i * t.nDp + opj + m], acc);
+        M[(size_t)(t.uoff[j] + u) * RR + e] = acc;
       }
       __syncthreads();
     }
@@ -356,13 +396,24 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
 
 size_t opals_smem_bytes(const OpTable& t) {
   OpSmem s;
-  return carve(s, nullptr, t, true);
+  return carve(s, nullptr, t, true, false);
 }
 
 int opals_launch(const OpAlsParams& p, cudaStream_t st) {
-  const size_t smem = opals_smem_bytes(p.ops);
-  MLCP_CUDA_TRY(cudaFuncSetAttribute(opals_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  opals_kernel<<<p.nvec, kThreads, smem, st>>>(p);
+  int dev = 0, limit = 0;
+  MLCP_CUDA_TRY(cudaGetDevice(&dev));
+  MLCP_CUDA_TRY(cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  OpSmem s;
+  const size_t res = carve(s, nullptr, p.ops, p.mode != 0, true);
+  if (res <= (size_t)limit) {
+    MLCP_CUDA_TRY(cudaFuncSetAttribute(opals_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)res));
+    opals_kernel<true><<<p.nvec, kThreads, res, st>>>(p);
+    MLCP_CUDA_TRY(cudaGetLastError());
+    return kOk;
+  }
+  const size_t smem = carve(s, nullptr, p.ops, p.mode != 0, false);
+  MLCP_CUDA_TRY(cudaFuncSetAttribute(opals_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  opals_kernel<false><<<p.nvec, kThreads, smem, st>>>(p);
   MLCP_CUDA_TRY(cudaGetLastError());
   return kOk;
 }
