@@ -52,7 +52,11 @@ struct OpSmem {
   float* rred;    // [4] refinement scratch
   dwsolve::ColScratch cs;
   int* moff;      // [T][D] offset of each term's operator Gram per mode (null when T D is large)
+  int* ord;       // [D][T] terms grouped by their operator at each mode (with moff)
+  int* gst;       // [D][umax+1] group starts (with moff)
+  float* alpha;   // [T] term coefficients in FP32 (with moff)
   float *Ms, *Ws, *Zs;  // operator Grams, term products, h_u Fo_j when resident in shared memory
+  float* hs;      // [utot][npmax][npmax] the FP32 operators when resident
   int* flags;     // [4]
 };
 
@@ -87,7 +91,12 @@ __host__ __device__ inline size_t carve(OpSmem& s, unsigned char* base, const Op
   s.cs.conv = (float*)take(sizeof(float) * 64);
   s.cs.rmax = (float*)take(sizeof(float) * 16 * 32);
   s.cs.rsum = (dw*)take(sizeof(dw) * 16 * 32);
-  s.moff = (t.T * t.D <= kMoffMax) ? (int*)take(sizeof(int) * t.T * t.D) : nullptr;
+  const bool tab = t.T * t.D <= kMoffMax;
+  s.moff = tab ? (int*)take(sizeof(int) * t.T * t.D) : nullptr;
+  s.ord = tab ? (int*)take(sizeof(int) * t.T * t.D) : nullptr;
+  s.gst = tab ? (int*)take(sizeof(int) * t.D * (t.umax + 1)) : nullptr;
+  s.alpha = tab ? (float*)take(sizeof(float) * t.T) : nullptr;
+  s.hs = resident ? (float*)take(sizeof(float) * t.utot * t.npmax * t.npmax) : nullptr;
   s.Ms = resident ? (float*)take(sizeof(float) * t.utot * RR) : nullptr;
   s.Ws = resident ? (float*)take(sizeof(float) * t.umax * RR) : nullptr;
   s.Zs = resident ? (float*)take(sizeof(float) * t.umax * Rn) : nullptr;
@@ -169,8 +178,17 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
   float* W = kResident ? s.Ws : p.wscr + (size_t)v * t.umax * R * R;
   float* Z = kResident ? s.Zs : p.zscr + (size_t)v * t.umax * R * npm;
   const int* moff = s.moff;
-  if (moff)
-    for (int e = threadIdx.x; e < T * D; e += blockDim.x) s.moff[e] = (t.uoff[e % D] + t.uid[e]) * RR;
+  if (moff) {
+    for (int e = threadIdx.x; e < T * D; e += blockDim.x) {
+      s.moff[e] = (t.uoff[e % D] + t.uid[e]) * RR;
+      s.ord[e] = t.order[e];
+    }
+    for (int e = threadIdx.x; e < D * (t.umax + 1); e += blockDim.x) s.gst[e] = t.gstart[e];
+    for (int e = threadIdx.x; e < T; e += blockDim.x) s.alpha[e] = (float)t.alpha[e];
+  }
+  const float* hmat = kResident ? s.hs : t.hmat;
+  if (kResident)
+    for (int e = threadIdx.x; e < t.utot * npm * npm; e += blockDim.x) s.hs[e] = t.hmat[e];
   dw* G = reinterpret_cast<dw*>(p.g64) + (size_t)v * D * R * R;  // double-word F Grams per mode
 
   // ---- set-up: F (= Fo for PRODHV), FP32 copies, Grams, penalty ----
@@ -211,8 +229,8 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
     for (int j = 0; j < D; ++j) {
       const int nj = t.nbas[j], opj = t.offp[j];
       const int nu = t.uoff[j + 1] - t.uoff[j];
-      const int* ord = t.order + (size_t)j * T;
-      const int* gs = t.gstart + (size_t)j * (t.umax + 1);
+      const int* ord = (moff ? s.ord : t.order) + (size_t)j * T;
+      const int* gs = (moff ? s.gst : t.gstart) + (size_t)j * (t.umax + 1);
       // -- normal equations (double-word) from the Grams of the previous
       //    step: prod_{d != j} G_d + pen I --
       for (int e = threadIdx.x; e < RR; e += blockDim.x) {
@@ -255,7 +273,7 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
             for (int k = 0; k < 4; ++k) {
               const bool live = q + k < gs[u + 1];
               const int term = ord[live ? q + k : q];
-              pr[k] = live ? (float)t.alpha[term] : 0.f;
+              pr[k] = live ? (moff ? s.alpha[term] : (float)t.alpha[term]) : 0.f;
               tb[k] = term * D;
             }
             for (int d = 0; d < D; ++d) {
@@ -282,7 +300,7 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
           if (t.ident[ug]) {
             acc = s.fo32[r * t.nDp + opj + m];
           } else {
-            const float* h = t.hmat + (size_t)ug * npm * npm + (size_t)m * npm;
+            const float* h = hmat + (size_t)ug * npm * npm + (size_t)m * npm;
             acc = 0.f;
             for (int k = 0; k < nj; ++k) acc = fmaf(h[k], s.fo32[r * t.nDp + opj + k], acc);
           }
@@ -355,7 +373,7 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
           if (t.ident[ug]) {
             acc = s.f32[r * t.nDp + opj + m];
           } else {
-            const float* h = t.hmat + (size_t)ug * npm * npm + (size_t)m * npm;
+            const float* h = hmat + (size_t)ug * npm * npm + (size_t)m * npm;
             acc = 0.f;
             for (int k = 0; k < nj; ++k) acc = fmaf(h[k], s.f32[r * t.nDp + opj + k], acc);
           }
