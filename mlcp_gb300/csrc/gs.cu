@@ -241,11 +241,12 @@ __device__ void finish_vector(const Gs& c, const GsParams& p, int iv, bool facto
 // working Grams (Gp, and BB = Gp + pen I).  Always: the weighted factor
 // wf(r,m) = c_r F_r^j(m), and per warp of psn entries the partial sums of
 // c_k,r c_i P_k(r,i) over all modes (the coefficients <Q_k, F>).
-__device__ void step_products(const Gs& c, int j, int nk, bool pre) {
+// Threads t0..511 (t0 a multiple of 32); ends with a barrier over them.
+__device__ void step_products(const Gs& c, int j, int nk, bool pre, int t0) {
   const int R = c.R, RR = c.RR, RRp = c.RRp, D = c.D, nj = c.a.nb[j], offj = c.a.off[j];
   const int npsn = nk * RRp, ngp = npsn + (pre ? 0 : RR), total = ngp + R * nj;
   const dw pen = c.a.misc[0];
-  for (int e = c.tid; e < total; e += kGsThreads) {
+  for (int e = c.tid - t0; e < total; e += kGsThreads - t0) {
     if (e < npsn) {  // whole warps: npsn is a multiple of 32
       const int kl = e / RRp, ee = e - kl * RRp;
       dw contrib = dw_make(0.f);
@@ -278,7 +279,8 @@ __device__ void step_products(const Gs& c, int j, int nk, bool pre) {
       c.a.wf[ee] = dw_mul(c.a.fcs[r], c.a.fb[(size_t)r * c.nD + offj + m]);
     }
   }
-  __syncthreads();
+  if (t0 == 0) __syncthreads();
+  else worker_sync(t0);
 }
 
 // Step phase 2 (threads w0..511, while the lower warps invert BB): the dot
@@ -329,12 +331,21 @@ __device__ void step_rhs_part(const Gs& c, int j, int nk, dw* bp, int w0) {
 // Step phase 4 (after the cluster barrier): the self term plus the partial
 // right-hand sides of the cluster, summed as a fixed tree over ranks so that
 // every CTA forms the identical system.
-__device__ void step_gather(const Gs& c, cg::cluster_group& cluster, int j, dw* bp) {
+// (ranks >= nown own no earlier vector yet; their parts are exact zeros)
+__device__ void step_gather(const Gs& c, int j, dw* bp, int nown) {
   const int Rn = c.R * c.a.nb[j];
   for (int e = c.tid; e < Rn; e += kGsThreads) {
+    const uint32_t local = (uint32_t)__cvta_generic_to_shared(bp + e);
     dw v[16];
 #pragma unroll
-    for (int r = 0; r < 16; ++r) v[r] = (r < c.CL) ? cluster.map_shared_rank(bp, r)[e] : dw_make(0.f);
+    for (int r = 0; r < 16; ++r) {
+      v[r] = dw_make(0.f);
+      if (r < nown) {
+        uint32_t remote;
+        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(r));
+        asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v[r].hi), "=f"(v[r].lo) : "r"(remote) : "memory");
+      }
+    }
     dw_acc acc = acc_zero();
     acc_add(acc, c.a.part[e]);
     acc_add(acc, c.a.part[(size_t)Rn + e]);
@@ -472,12 +483,15 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
         dw* bp = c.a.bpart + (size_t)(step & 1) * c.R * c.npm;
         const bool more = it + 1 < p.nals || j + 1 < c.D;  // another step of this vector follows
         const int jn = j + 1 < c.D ? j + 1 : 0, nj = c.a.nb[j];
-        step_products(c, j, nk, pre);
         // FP32 inverse of BB (warp 0 in registers for R <= 32, else the
-        // solver warps) concurrently with the right-hand side (threads w0..)
+        // solver warps) concurrently with the right-hand side (threads w0..);
+        // when the previous update already formed BB, also concurrently with
+        // the products
         bool gj_ok = false;
         const float* inv = c.a.gi;
         const int w0 = c.R <= 32 ? 32 : dwsolve::kSolverThreads;
+        const bool early = pre && c.R <= 32;
+        if (!early) step_products(c, j, nk, pre, 0);
         if (c.tid < w0) {
           if (c.R > 32) {
             inv = dwsolve::gj_inverse(c.a.BB, c.R, c.a.gi, &gj_ok);
@@ -486,6 +500,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
             if (c.tid == 0) c.a.flags[2] = good;
           }
         } else {
+          if (early) step_products(c, j, nk, pre, w0);
           step_dots(c, j, nk, w0);
           step_rhs_part(c, j, nk, bp, w0);
         }
@@ -493,7 +508,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
         // CTA has passed the barrier of step s + 1 (and so its gather of s)
         cl_arrive();
         cl_wait();
-        step_gather(c, cluster, j, bp);
+        step_gather(c, j, bp, iv < c.CL ? iv : c.CL);
         if (c.R <= 32) gj_ok = c.a.flags[2] != 0;
         // the solve: refinement in registers (warps 0..nsw-1, one or two
         // right-hand-side columns each), or the solver warps' refinement /
