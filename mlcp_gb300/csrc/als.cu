@@ -750,13 +750,25 @@ __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& 
     for (int e = c.tid; e < rF * rF; e += kSolverThreads) cp_async8(c.sk + e, c.suf + (size_t)kn * rF * rF + e);
   // gather the partial right-hand sides of the cluster in rank order
   const size_t boff = (size_t)(t & 1) * c.rFp * c.npmax;
+  // (mapa + ld.shared::cluster: explicit distributed-shared-memory loads,
+  // all issued before the sums)
   for (int e = c.tid; e < rF * nk; e += kSolverThreads) {
     const int i = e % rF, n = e / rF;
-    dw s = dw_make(0.f);
-    for (int r = 0; r < c.CL; ++r) {
-      const float* peer = cluster.map_shared_rank(c.bpart + boff, r);
-      s = dw_add_f(s, peer[i * c.npmax + n]);
+    const uint32_t local = smem_addr(c.bpart + boff + i * c.npmax + n);
+    float v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      v[r] = 0.f;
+      if (r < c.CL) {
+        uint32_t remote;
+        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(r));
+        asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v[r]) : "r"(remote) : "memory");
+      }
     }
+    dw s = dw_make(0.f);
+#pragma unroll
+    for (int r = 0; r < 16; ++r)
+      if (r < c.CL) s = dw_add_f(s, v[r]);
     c.b0[i + n * rF] = s;
   }
   // the normal equations BB (prefix of this sweep x suffix of the previous
