@@ -511,5 +511,95 @@ __device__ inline bool solve_cols_any(const dw* A, int n, const dw* B, dw* X, in
   return solve_cols<32, 32>(A, n, B, X, nrhs, inv, nrm, s);
 }
 
+// solve_cols for n <= 16 with one column per warp and each row's sums split
+// over the two half-warps (lane h 16 + i: row i, terms j of half h), so that
+// every dependency chain is half as long; the halves combine their partial
+// results in a fixed order, so both hold identical values.  Uses warps
+// 0..nrhs-1 (named barrier 3); same results contract as solve_cols.
+__device__ __forceinline__ dw_acc acc_merge(dw_acc a, dw_acc b) {
+  const dw t = two_sum(a.s, b.s);
+  return dw_acc{t.hi, f_add(f_add(a.c, b.c), t.lo)};
+}
+__device__ inline bool solve_cols_split(const dw* A, int n, const dw* B, dw* X, int nrhs, const float* inv, dw* nrm,
+                                        const ColScratch& s) {
+  constexpr int NH = 8;
+  const int lane = threadIdx.x & 31, m = threadIdx.x >> 5, i = lane & 15, h = lane >> 4, j0 = h * NH;
+  const int nthr = nrhs * 32;
+  const bool row = i < n;
+  float iv[NH];
+  dw ar[NH];
+#pragma unroll
+  for (int q = 0; q < NH; ++q) {
+    const int j = j0 + q;
+    iv[q] = (row && j < n) ? inv[i + j * n] : 0.f;
+    ar[q] = (row && j < n) ? A[i + j * n] : dw_make(0.f);
+  }
+  const dw b = row ? B[i + m * n] : dw_make(0.f);
+  auto combine = [&](float v) {  // fixed order: half 0's part first
+    const float o = __shfl_xor_sync(0xffffffffu, v, 16);
+    return h == 0 ? v + o : o + v;
+  };
+  float p0 = 0.f;
+#pragma unroll
+  for (int q = 0; q < NH; ++q) p0 = fmaf(iv[q], __shfl_sync(0xffffffffu, b.hi, j0 + q), p0);
+  dw x = dw_make(combine(p0));
+  bool ok = false;
+  for (int round = 0; round < kRefineMax && !ok; ++round) {
+    dw_acc acc = acc_zero();
+    if (h == 0) acc_add(acc, b);
+#pragma unroll
+    for (int q = 0; q < NH; ++q) acc_fma(acc, dw_neg(ar[q]), dw_shfl(x, j0 + q));
+    const dw_acc other{__shfl_xor_sync(0xffffffffu, acc.s, 16), __shfl_xor_sync(0xffffffffu, acc.c, 16)};
+    const dw r = acc_value(h == 0 ? acc_merge(acc, other) : acc_merge(other, acc));
+    float dp = 0.f;
+#pragma unroll
+    for (int q = 0; q < NH; ++q) dp = fmaf(iv[q], __shfl_sync(0xffffffffu, r.hi, j0 + q), dp);
+    const float d = combine(dp);
+    if (row) x = dw_add_f(x, d);
+    float mdx = row ? ((fabsf(d) <= FLT_MAX) ? fabsf(d) : INFINITY) : 0.f;
+    float mx = row ? fabsf(x.hi) : 0.f;
+    for (int o = 16; o > 0; o >>= 1) {
+      mdx = fmaxf(mdx, __shfl_xor_sync(0xffffffffu, mdx, o));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    float* cv = s.conv + (round & 1) * 32;
+    if (lane == 0) {
+      cv[m] = mdx;
+      cv[16 + m] = mx;
+    }
+    asm volatile("bar.sync 3, %0;" ::"r"(nthr) : "memory");
+    float gd = 0.f, gx = 0.f;
+    for (int w = 0; w < nrhs; ++w) {
+      gd = fmaxf(gd, cv[w]);
+      gx = fmaxf(gx, cv[16 + w]);
+    }
+    ok = gd <= 1e-10f * gx || (round == 0 && gd <= 1e-5f * gx);
+  }
+  if (!ok) return false;
+  const int slot = m * 32 + i;
+  if (h == 0) s.rmax[slot] = fabsf(x.hi);
+  asm volatile("bar.sync 3, %0;" ::"r"(nthr) : "memory");
+  float big = 0.f;
+  for (int w = 0; w < nrhs; ++w) big = fmaxf(big, s.rmax[w * 32 + i]);
+  const bool zero = !(big > 0.f);
+  const dw il = dw_rcp(dw_make(zero ? 1.f : big));
+  const dw y = dw_mul(x, il);
+  if (h == 0) s.rsum[slot] = dw_mul(y, y);
+  asm volatile("bar.sync 3, %0;" ::"r"(nthr) : "memory");
+  dw_acc sq = acc_zero();
+  for (int w = 0; w < nrhs; ++w) acc_add(sq, s.rsum[w * 32 + i]);
+  if (!row || h != 0) return true;
+  if (zero) {  // NaN, as the reference's zero-row norm
+    const float nan = __int_as_float(0x7fffffff);
+    X[i + m * n] = dw_make(nan);
+    if (m == 0) nrm[i] = dw_make(nan);
+    return true;
+  }
+  const dw rn = dw_mul(dw_make(big), dw_sqrt(acc_value(sq)));
+  X[i + m * n] = dw_mul(x, dw_rcp(rn));
+  if (m == 0) nrm[i] = rn;
+  return true;
+}
+
 }  // namespace dwsolve
 }  // namespace mlcp

@@ -515,9 +515,12 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
         // LDL^T fallback; the next step's partial products on the other warps
         bool solved = false, pre_done = !more;
         if (gj_ok && c.R <= 32 && nj <= 16) {
-          const int nsw = dwsolve::solve_cols_warps(c.R, nj) * 32;
+          // rank <= 16: one column per warp, sums split over the half-warps
+          const bool split = c.R <= 16;
+          const int nsw = (split ? nj : dwsolve::solve_cols_warps(c.R, nj)) * 32;
           if (c.tid < nsw) {
-            const bool ok = dwsolve::solve_cols_any(c.a.BB, c.R, c.a.b0, c.a.X, nj, inv, c.a.fcs, c.a.cs);
+            const bool ok = split ? dwsolve::solve_cols_split(c.a.BB, c.R, c.a.b0, c.a.X, nj, inv, c.a.fcs, c.a.cs)
+                                  : dwsolve::solve_cols_any(c.a.BB, c.R, c.a.b0, c.a.X, nj, inv, c.a.fcs, c.a.cs);
             if (c.tid == 0) c.a.flags[3] = ok;
           } else if (more) {
             step_preproducts(c, j, jn, nk, c.tid - nsw, kGsThreads - nsw);
