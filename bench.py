@@ -197,6 +197,19 @@ def run_cycle_bench(steps: int, cpu: bool):
     for _ in range(steps):
         _, _, bounds = IT.spectral_range(sb, sc, hl.nbas, CYC_R, hl, CYC_NPOW, 10)
     out["spectral_range_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
+    # the next layer's operator update (updateopermatcpp_): three operators of mode 1
+    rng = np.random.default_rng(11)
+    xm = []
+    for _ in range(3):
+        X = rng.normal(size=(CYC_N, CYC_N))
+        X = X + X.T
+        xm.append([X[i, j] for j in range(CYC_N) for i in range(j + 1)])
+    xm = np.array(xm)
+    IT.update_opermat(1, gb, gc, hl.nbas, CYC_R, CYC_B, xm)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        IT.update_opermat(1, gb, gc, hl.nbas, CYC_R, CYC_B, xm)
+    out["update_opermat_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
     out["spectral_range"] = [float(bounds[0]), float(bounds[1])]
     if cpu:
         oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
@@ -209,6 +222,9 @@ def run_cycle_bench(steps: int, cpu: bool):
         t0 = time.perf_counter()
         oracle.spectral_range(sb, sc, hl.nbas, CYC_R, hl, CYC_NPOW, 10)
         out["spectral_range_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        oracle.update_opermat(1, gb, gc, hl.nbas, CYC_R, CYC_B, xm)
+        out["update_opermat_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
         out["cpu_cores"] = os.cpu_count()
         out["cpu_kind"] = "port"
         oracle.set_cycle_penalties()

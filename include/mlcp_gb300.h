@@ -91,6 +91,17 @@ MLCP_API void getspectralrangecpp_(double *base, double *coef, int *nbas, MLCP_R
                                    double *mat, MLCP_REF(int) TxD, MLCP_REF(int) nops, MLCP_REF(int) msize,
                                    double *bounds);
 
+/* Replaces UpdateOperMat (src/Updater.f90:110-151) for the nx primitive
+ * operators of mode imode (1-based) of the block, on the GPU in FP64:
+ * qxq[x] = the nbloc x nbloc matrix <Q_j, X_x Q_i>, each xmats[x] and qxq[x]
+ * packed upper-triangular column by column (n(n+1)/2 and
+ * nbloc(nbloc+1)/2 entries, back to back), as dspmv('U') reads and
+ * SymPackMat2Vec writes them.  UpdateH calls it once per mode with all the
+ * operators that the reference passes to UpdateOperMat one at a time. */
+MLCP_API void updateopermatcpp_(MLCP_REF(int) imode, double *base, double *coef, int *nbas, MLCP_REF(int) rk,
+                                MLCP_REF(int) ndof, MLCP_REF(int) nbloc, MLCP_REF(int) nx, double *xmats,
+                                double *qxq);
+
 /* Replaces SortVecs (src/BlockUtils.f90:520-583): reorders the block (and
  * eigv alike) by increasing |eigv - Eref|; nconv becomes the position of
  * the first of the first nconv vectors that moved, if any did.  Equal

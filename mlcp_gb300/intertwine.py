@@ -96,6 +96,27 @@ def spectral_range(base: np.ndarray, coef: np.ndarray, nbas, rk: int, hl, npow: 
     return base, coef, bounds
 
 
+def update_opermat(imode: int, base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int,
+                   xmats: np.ndarray) -> np.ndarray:
+    """Reference UpdateOperMat (src/Updater.f90:110-151) through
+    updateopermatcpp_ for the operators xmats (one packed upper triangle per
+    row) of mode imode (1-based): returns the packed nbloc x nbloc matrices
+    <Q_j, X Q_i>, one row per operator."""
+    base = np.ascontiguousarray(base, dtype=np.float64)
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32).copy()
+    xm = np.ascontiguousarray(np.atleast_2d(xmats), dtype=np.float64)
+    out = np.zeros((xm.shape[0], nbloc * (nbloc + 1) // 2))
+    ints = [ctypes.c_int(x) for x in (imode, rk, nb.size, nbloc, xm.shape[0])]
+    L = _lib.load()
+    L.updateopermatcpp_(ctypes.byref(ints[0]), base.ctypes.data_as(_D), coef.ctypes.data_as(_D),
+                        nb.ctypes.data_as(_I), *[ctypes.byref(x) for x in ints[1:]], xm.ctypes.data_as(_D),
+                        out.ctypes.data_as(_D))
+    if L.mlcp_gb300_last_status() != 0:
+        raise _lib.MlcpError(_lib.last_error())
+    return out
+
+
 def sort_vecs(base: np.ndarray, coef: np.ndarray, nbas, rk: int, eigv: np.ndarray, nconv: int, eref: float):
     """Reference SortVecs (src/BlockUtils.f90:520-583) through sortvecscpp_
     on copies; returns (base, coef, eigv, nconv)."""

@@ -67,6 +67,8 @@ def lib() -> ctypes.CDLL:
         L.orc_sygv.argtypes = [ctypes.c_int, _D, _D, _D, _D]
         L.orc_rayleigh_quotient.restype = ctypes.c_double
         L.orc_rayleigh_quotient.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, _I, _I, _D, _D, ctypes.c_int]
+        L.orc_update_opermat.argtypes = [ctypes.c_int, _D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, _D, _D]
         L.orc_spectral_range.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I,
                                          _D, _D, ctypes.c_int, _D]
         L.orc_qhq_diag.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D,
@@ -190,6 +192,31 @@ def qhq_diag(base, coef, nbas, rk, nbloc, hl, nconv=0, qhqd=None, nthreads=0):
     lib().orc_qhq_diag(_dp(base), _dp(coef), _ip(nb), rk, len(nb), nbloc, nconv, _ip(hl.opid), _ip(hl.mptr),
                        _dp(hl.coef), _dp(hl.mat), hl.nterms, _dp(out), nthreads)
     return out
+
+
+def update_opermat(imode, base, coef, nbas, rk, nbloc, xmats):
+    """Reference UpdateOperMat (src/Updater.f90:110-151) for the operators
+    xmats (each packed upper-triangular, n(n+1)/2) of mode imode (1-based);
+    returns the packed nbloc x nbloc matrices, one row per operator."""
+    base = np.ascontiguousarray(base, dtype=np.float64)
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    xm = np.ascontiguousarray(np.atleast_2d(xmats), dtype=np.float64)
+    out = np.zeros((xm.shape[0], nbloc * (nbloc + 1) // 2))
+    lib().orc_update_opermat(imode, _dp(base), _dp(coef), _ip(nb), rk, len(nb), nbloc, xm.shape[0], _dp(xm),
+                             _dp(out))
+    return out
+
+
+def unpack_sym(v, n):
+    """Symmetric matrix from its packed upper triangle (column by column)."""
+    M = np.zeros((n, n))
+    k = 0
+    for j in range(n):
+        for i in range(j + 1):
+            M[i, j] = M[j, i] = v[k]
+            k += 1
+    return M
 
 
 def spectral_start(nbas, rk, seed=0):

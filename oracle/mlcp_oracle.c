@@ -799,6 +799,42 @@ void orc_spectral_range(double *base, double *coef, const int *nbas, int rk, int
   bounds[1] = b[1] + pad;
 }
 
+/* UpdateOperMat (reference src/Updater.f90:110-151) for nx operators of
+ * mode imode (1-based) given packed upper-triangular (as dspmv 'U', column
+ * by column) back to back: for each i, XQ = X applied to mode imode of every
+ * term of Q_i (PRODXV, :155-189), then QXQ(i,j) = <Q_j, XQ> (PRODVV) for
+ * j >= i, packed upper-triangular (SymPackMat2Vec, src/Utils.f90:559-595)
+ * into qxq[x][i + j(j+1)/2]. */
+void orc_update_opermat(int imode, const double *base, const double *coef, const int *nbas, int rk, int ndof,
+                        int nbloc, int nx, const double *xmats, double *qxq) {
+  int *off = make_offsets(nbas, ndof);
+  const int nD = off[ndof], m = imode - 1, n = nbas[m], o = off[m];
+  const size_t np = (size_t)n * (n + 1) / 2, nq = (size_t)nbloc * (nbloc + 1) / 2;
+  double *xq = (double *)malloc(sizeof(double) * (size_t)rk * nD);
+  for (int x = 0; x < nx; ++x) {
+    const double *X = xmats + (size_t)x * np;
+    for (int i = 0; i < nbloc; ++i) {
+      const double *qi = base + (size_t)i * rk * nD;
+      memcpy(xq, qi, sizeof(double) * (size_t)rk * nD);
+      for (int r = 0; r < rk; ++r)
+        for (int a = 0; a < n; ++a) {
+          double acc = 0.0;
+          for (int b = 0; b < n; ++b) {
+            const int ir = a < b ? a : b, ic = a < b ? b : a;
+            acc += X[ir + ic * (ic + 1) / 2] * qi[(size_t)r * nD + o + b];
+          }
+          xq[(size_t)r * nD + o + a] = acc;
+        }
+      for (int j = i; j < nbloc; ++j)
+        qxq[(size_t)x * nq + i + (size_t)j * (j + 1) / 2] =
+            orc_cp_dot(base + (size_t)j * rk * nD, coef + (size_t)j * rk, rk, xq, coef + (size_t)i * rk, rk, nbas,
+                       ndof);
+    }
+  }
+  free(xq);
+  free(off);
+}
+
 double orc_cp_dot(const double *vb, const double *vc, int rv, const double *wb, const double *wc, int rw,
                   const int *nbas, int ndof) {
   int *off = make_offsets(nbas, ndof);

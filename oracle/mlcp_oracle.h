@@ -62,6 +62,11 @@ void orc_vector_updates(double *base, double *coef, const int *nbas, int rk, int
  * with H applied exactly, term by term. */
 double orc_rayleigh_quotient(const double *base, const double *coef, const int *nbas, int rk, int ndof,
                              const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T);
+/* Reference src/Updater.f90:110-151 (UpdateOperMat) for nx operators of mode
+ * imode (1-based), packed upper-triangular back to back; qxq[x] packed the
+ * same way (nbloc x nbloc). */
+void orc_update_opermat(int imode, const double *base, const double *coef, const int *nbas, int rk, int ndof,
+                        int nbloc, int nx, const double *xmats, double *qxq);
 /* Reference src/Solver.f90:563-654 (GetSpectralRange, more than two modes)
  * from the two starting vectors in base/coef (overwritten); padded bounds. */
 void orc_spectral_range(double *base, double *coef, const int *nbas, int rk, int ndof, int npow, int ncyc,

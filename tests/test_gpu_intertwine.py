@@ -182,3 +182,24 @@ def test_spectral_range_rejects_two_modes(cuda_device):
     b, c = oracle.spectral_start(hl.nbas, 3)
     with pytest.raises(Exception, match="two modes"):
         IT.spectral_range(b, c, hl.nbas, 3, hl, 2, 1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("imode,rk,nbloc,nx", [(1, 4, 6, 1), (3, 16, 40, 3), (2, 5, 9, 20)])
+def test_update_opermat_matches_oracle(imode, rk, nbloc, nx, cuda_device):
+    """updateopermatcpp_ (UpdateOperMat for nx operators at once) against the
+    oracle; both FP64 (1e-12 of the largest entry).  20 operators take two
+    passes of the pair kernel."""
+    rng = np.random.default_rng(imode + nx)
+    nbas = [5, 6, 4, 3]
+    n = nbas[imode - 1]
+    Q, qc = start_block(nbas, rk, nbloc, seed=imode)
+    xm = []
+    for _ in range(nx):
+        X = rng.normal(size=(n, n))
+        X = X + X.T
+        xm.append([X[i, j] for j in range(n) for i in range(j + 1)])
+    xm = np.array(xm)
+    g = IT.update_opermat(imode, Q, qc, nbas, rk, nbloc, xm)
+    o = oracle.update_opermat(imode, Q, qc, nbas, rk, nbloc, xm)
+    assert np.max(np.abs(g - o)) <= 1e-12 * np.max(np.abs(o))

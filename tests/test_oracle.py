@@ -258,3 +258,25 @@ def test_spectral_range_brackets_and_converges(make):
     width = ex[-1] - ex[0]
     assert abs(hi - ex[-1]) < 1e-4 * width
     assert abs(lo - ex[0]) < 1e-3 * width
+
+
+def test_update_opermat_matches_dense():
+    """UpdateOperMat restatement = Q X_m Q^T with dense vectors and X acting
+    on mode m (identity elsewhere), packed upper-triangular."""
+    rng = np.random.default_rng(0)
+    nbas, rk, nbloc = [3, 4, 2], 2, 3
+    nD = sum(nbas)
+    Q, qc = rng.normal(size=(nbloc * rk, nD)), rng.uniform(0.5, 1.0, nbloc * rk)
+    Qd = np.array([dense_cp(Q[i * rk:(i + 1) * rk], qc[i * rk:(i + 1) * rk], nbas).reshape(-1)
+                   for i in range(nbloc)])
+    for imode in (1, 2, 3):
+        n = nbas[imode - 1]
+        X = rng.normal(size=(n, n))
+        X = X + X.T
+        packed = np.array([X[i, j] for j in range(n) for i in range(j + 1)])
+        out = oracle.update_opermat(imode, Q, qc, nbas, rk, nbloc, packed)[0]
+        eyes = [np.eye(m) for m in nbas]
+        eyes[imode - 1] = X
+        Xf = np.kron(np.kron(eyes[0], eyes[1]), eyes[2])
+        want = Qd @ Xf @ Qd.T
+        assert np.max(np.abs(oracle.unpack_sym(out, nbloc) - want)) <= 1e-12 * np.max(np.abs(want))
