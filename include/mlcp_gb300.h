@@ -166,6 +166,29 @@ MLCP_API int mlcp_cp_dot_batched(int nvec, int ndof, const int *nbas, const long
                         const long long *y_off, const int *ry, const double *d_coef, const double *d_base,
                         double *d_out, void *stream);
 
+/* Restart files (replace SavePsiFile / ReadPsiFile, src/Restart.f90:614-793;
+ * the reference does this I/O in Fortran, so these have no C counterpart).
+ * The file is the reference's gfortran unformatted sequential file: records
+ * (isavi, nev) | bounds(2) | eigv(nev) | delta(nev), then per vector
+ * (ndof, rank) | nbas(ndof) | coef(rank) | base(nD x rank), each framed by
+ * its 4-byte length before and after.  Host memory only; no GPU work.
+ * ranks[nev]: terms of each vector; coef/base hold the vectors one after the
+ * other (sum(ranks) terms, nD = sum(nbas) values per term). */
+MLCP_API int mlcp_save_psi(const char *path, int isavi, const double *bounds, int nev, const double *eigv,
+                           const double *delta, int ndof, const int *nbas, const int *ranks, const double *coef,
+                           const double *base);
+
+/* Reads a restart file written by SavePsiFile or mlcp_save_psi.  As
+ * ReadPsiFile, *success = 1 and the caller's isavi, bounds, eigv, delta,
+ * ranks, coef and base are replaced only when the whole file was read and
+ * its nev, and every vector's ndof and nbas, equal the caller's; otherwise
+ * *success = 0 and nothing is changed (a missing file is not an error).
+ * max_terms bounds sum(ranks) (the capacity of coef/base in terms); a file
+ * with more terms reads as a mismatch. */
+MLCP_API int mlcp_read_psi(const char *path, int *isavi, double *bounds, int nev, double *eigv, double *delta,
+                           int ndof, const int *nbas, int max_terms, int *ranks, double *coef, double *base,
+                           int *success);
+
 #ifdef __cplusplus
 }
 #endif

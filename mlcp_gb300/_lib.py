@@ -72,6 +72,13 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         if hasattr(L, "sortvecscpp_"):
             L.sortvecscpp_.restype = None
             L.sortvecscpp_.argtypes = [_D, _D, _I, _I, _I, _I, _D, _I, _D]
+        if hasattr(L, "mlcp_save_psi"):
+            L.mlcp_save_psi.restype = ctypes.c_int
+            L.mlcp_save_psi.argtypes = [ctypes.c_char_p, ctypes.c_int, _D, ctypes.c_int, _D, _D, ctypes.c_int, _I,
+                                        _I, _D, _D]
+            L.mlcp_read_psi.restype = ctypes.c_int
+            L.mlcp_read_psi.argtypes = [ctypes.c_char_p, _I, _D, ctypes.c_int, _D, _D, ctypes.c_int, _I,
+                                        ctypes.c_int, _I, _D, _D, _I]
         if hasattr(L, "intwdevicemem_"):
             L.intwdevicemem_.restype = None
             L.intwdevicemem_.argtypes = [_I, _I, _I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_bool), _I]

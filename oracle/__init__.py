@@ -271,6 +271,79 @@ def sort_vecs(base, coef, rk, eigv, nconv, eref):
     return base, coef, eigv[ix].copy(), (moved[0] if moved else nconv)
 
 
+def fortran_records(path):
+    """The records of a gfortran unformatted sequential file, as bytes: each
+    record is a 4-byte little-endian length, the data, and the length again.
+    Raises ValueError on a broken frame."""
+    import struct
+    out = []
+    with open(path, "rb") as f:
+        data = f.read()
+    pos = 0
+    while pos < len(data):
+        if pos + 4 > len(data):
+            raise ValueError("truncated record marker")
+        (n,) = struct.unpack_from("<i", data, pos)
+        if n < 0 or pos + 8 + n > len(data):
+            raise ValueError("bad record length")
+        (m,) = struct.unpack_from("<i", data, pos + 4 + n)
+        if m != n:
+            raise ValueError("record markers differ")
+        out.append(data[pos + 4:pos + 4 + n])
+        pos += 8 + n
+    return out
+
+
+def psi_write(path, isavi, bounds, eigv, delta, nbas, ranks, coef, base) -> None:
+    """Reference SavePsiFile (src/Restart.f90:759-793) restated: the WRITE
+    statements (isavi, nev), bounds, eigv, delta and per vector
+    (ndof, nrk), nbas, coef, base, as gfortran frames them.  coef/base hold
+    the vectors back to back (base: nD values per term)."""
+    import struct
+    nb = np.asarray(nbas, dtype="<i4")
+    nD = int(nb.sum())
+    eigv = np.asarray(eigv, dtype="<f8")
+    coef = np.asarray(coef, dtype="<f8").ravel()
+    base = np.asarray(base, dtype="<f8").ravel()
+    recs = [struct.pack("<ii", int(isavi), eigv.size), np.asarray(bounds, dtype="<f8").tobytes(), eigv.tobytes(),
+            np.asarray(delta, dtype="<f8").tobytes()]
+    t = 0
+    for r in ranks:
+        r = int(r)
+        recs += [struct.pack("<ii", nb.size, r), nb.tobytes(), coef[t:t + r].tobytes(),
+                 base[t * nD:(t + r) * nD].tobytes()]
+        t += r
+    with open(path, "wb") as f:
+        for rec in recs:
+            f.write(struct.pack("<i", len(rec)) + rec + struct.pack("<i", len(rec)))
+
+
+def psi_read(path):
+    """Reference ReadPsiFile (src/Restart.f90:614-731) restated without its
+    checks against the caller's block: returns a dict with isavi, bounds,
+    eigv, delta, nbas (per vector), ranks, coef and base, read as a Fortran
+    READ reads (a record longer than the list is accepted)."""
+    import struct
+    recs = fortran_records(path)
+    isavi, nev = struct.unpack_from("<ii", recs[0])
+    out = {"isavi": isavi, "bounds": np.frombuffer(recs[1], "<f8", 2).copy(),
+           "eigv": np.frombuffer(recs[2], "<f8", nev).copy(), "delta": np.frombuffer(recs[3], "<f8", nev).copy(),
+           "nbas": [], "ranks": [], "coef": [], "base": []}
+    k = 4
+    for _ in range(nev):
+        ndof, nrk = struct.unpack_from("<ii", recs[k])
+        nb = np.frombuffer(recs[k + 1], "<i4", ndof).copy()
+        out["nbas"].append(nb)
+        out["ranks"].append(nrk)
+        out["coef"].append(np.frombuffer(recs[k + 2], "<f8", nrk))
+        out["base"].append(np.frombuffer(recs[k + 3], "<f8", nrk * int(nb.sum())))
+        k += 4
+    out["coef"] = np.concatenate(out["coef"]) if nev else np.zeros(0)
+    out["base"] = np.concatenate(out["base"]) if nev else np.zeros(0)
+    out["ranks"] = np.asarray(out["ranks"], dtype=np.int32)
+    return out
+
+
 def cp_dot(vb, vc, wb, wc, nbas) -> float:
     vb = np.ascontiguousarray(vb, dtype=np.float64)
     vc = np.ascontiguousarray(vc, dtype=np.float64)
