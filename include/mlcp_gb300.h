@@ -79,13 +79,17 @@ MLCP_API void getqhqdiagcpp_(double *base, double *coef, int *nbas, MLCP_REF(int
                              double *mat, MLCP_REF(int) TxD, MLCP_REF(int) nops, MLCP_REF(int) msize,
                              double *qhqd);
 
-/* Replaces GetSpectralRange (src/Solver.f90:563-654) for nodes of more than
- * two modes: base/coef hold the two starting vectors of rank rk (lower and
- * upper guesses, built by the host as the reference does); ncyc rounds of
- * npow ALS-fitted (H - shift) steps -- shift = midpoint of the current bounds
- * for the lower vector, 0 for the upper -- each followed by their Rayleigh
- * quotients as the new bounds, all on the GPU.  bounds[2] receives the range
- * padded by 0.1 % of its width on each side; base/coef the final vectors. */
+/* Replaces GetSpectralRange (src/Solver.f90:563-654): base/coef hold the
+ * two starting vectors of rank rk (lower and upper guesses, built by the host
+ * as the reference does); ncyc rounds of npow (H - shift) steps -- shift =
+ * midpoint of the current bounds for the lower vector, 0 for the upper --
+ * each followed by their Rayleigh quotients as the new bounds, all on the
+ * GPU.  More than two modes: ALS-fitted steps (ALS_POW_alg).  Two modes:
+ * PowrRecurse -- the exact product, its SVD reduction to at most rk terms
+ * (redtol 1e-12) and NORMCOEF; the reference starts these vectors at rank 1,
+ * so terms past the first carry weight 0, and the result's unused terms are
+ * zero.  bounds[2] receives the range padded by 0.1 % of its width on each
+ * side; base/coef the final vectors. */
 MLCP_API void getspectralrangecpp_(double *base, double *coef, int *nbas, MLCP_REF(int) rk, MLCP_REF(int) ndof,
                                    MLCP_REF(int) npow, MLCP_REF(int) ncyc, int *opid, int *mptr, double *Hcoef,
                                    double *mat, MLCP_REF(int) TxD, MLCP_REF(int) nops, MLCP_REF(int) msize,
@@ -101,6 +105,18 @@ MLCP_API void getspectralrangecpp_(double *base, double *coef, int *nbas, MLCP_R
 MLCP_API void updateopermatcpp_(MLCP_REF(int) imode, double *base, double *coef, int *nbas, MLCP_REF(int) rk,
                                 MLCP_REF(int) ndof, MLCP_REF(int) nbloc, MLCP_REF(int) nx, double *xmats,
                                 double *qxq);
+
+/* Replaces reduc_SVDa / reduc_SVDb (src/REDUCTIONML.f90:296-392), the
+ * reduction of two-mode vectors (reduc with red2D = 'SVD'), batched: each of
+ * the nvec vectors of rG terms (base[nvec][rG][nbas[0] + nbas[1]],
+ * coef[nvec][rG]) is multiplied out to A = sum_k c_k a_k b_k^T, A's SVD taken
+ * (FP64 one-sided Jacobi on the GPU), and its leading singular triplets
+ * written as at most rF terms: obase[nvec][rF][nD], ocoef[nvec][rF] = s_i
+ * (mode 1 = U(:, i), mode 2 = V(:, i)), orank[v] = min(nr, nc, rF, ncomp),
+ * ncomp = the leading singular values >= redtol * s_1.  Terms past orank[v]
+ * are zero.  Limits: min(nr, nc) <= 256, max(nr, nc) <= 4096. */
+MLCP_API void reducsvdcpp_(double *base, double *coef, int *nbas, MLCP_REF(int) rG, MLCP_REF(int) nvec,
+                           MLCP_REF(int) rF, MLCP_REF(double) redtol, double *obase, double *ocoef, int *orank);
 
 /* Replaces SortVecs (src/BlockUtils.f90:520-583): reorders the block (and
  * eigv alike) by increasing |eigv - Eref|; nconv becomes the position of

@@ -485,6 +485,91 @@ __global__ void range_shift_kernel(const double* bounds, double* shift) {
 }
 }  // namespace
 
+// Reduction threshold of the reference's solver (redtol, src/Solver.f90:326).
+constexpr double kRedTol = 1.0e-12;
+
+// Reference GetSpectralRange (src/Solver.f90:563-654), two-mode branch: each
+// of the two vectors runs PowrRecurse (src/BlockPower.f90:49-73) -- npow
+// times the exact product w = (H - shift) v (PRODHV with ishift = 1), its
+// reduction by SVD to at most rk terms (reduc_SVD with redtol 1e-12) and
+// NORMCOEF -- and each round ends with the Rayleigh quotients as the new
+// bounds.  The vectors live at rank rk with zero-weight padding (the
+// reference starts them at rank 1; a zero-weight term adds nothing to A).
+int spectral_range_2mode(Context* ctx, double* base, double* coef, const int* nbas, int rk, int npow, int ncyc,
+                         const int* opid, const int* mptr, const double* Hcoef, const double* mat, int TxD, int nops,
+                         int msize, double* bounds) {
+  Layout Ly;
+  int rc = make_layout(2, nbas, &Ly);
+  if (rc) return rc;
+  const int T = TxD / 2, R = rk, B = 2;
+  cudaStream_t st = ctx->stream;
+  OpTable tab;
+  rc = get_optable(ctx, Ly, nbas, R, T, opid, mptr, Hcoef, mat, nops, msize, st, &tab);
+  if (rc) return rc;
+  const size_t nvals = (size_t)B * R * Ly.nD;
+  size_t bytes = 0;
+  auto take = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
+  const size_t o_q = take(sizeof(double) * nvals), o_qc = take(sizeof(double) * B * R),
+               o_y = take(sizeof(double) * (size_t)B * tab.utot * R * tab.npmax),
+               o_w = take(sizeof(double) * B * svd2_work_doubles(nbas[0], nbas[1])),
+               o_rqw = take(sizeof(double) * B * rq_work_doubles(tab)), o_rq = take(sizeof(double) * B),
+               o_shift = take(sizeof(double) * B), o_st = take(sizeof(int) * B);
+  if (bytes > ctx->cyc_bytes) {
+    if (ctx->cyc) {
+      MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+      MLCP_CUDA_TRY(cudaFree(ctx->cyc));
+      ctx->cyc = nullptr;
+      ctx->cyc_bytes = 0;
+    }
+    MLCP_CUDA_TRY(cudaMalloc(&ctx->cyc, bytes));
+    ctx->cyc_bytes = bytes;
+  }
+  char* b = static_cast<char*>(ctx->cyc);
+  double* q = reinterpret_cast<double*>(b + o_q);
+  double* qc = reinterpret_cast<double*>(b + o_qc);
+  double* y = reinterpret_cast<double*>(b + o_y);
+  double* rq = reinterpret_cast<double*>(b + o_rq);
+  double* shift = reinterpret_cast<double*>(b + o_shift);
+  int* status = reinterpret_cast<int*>(b + o_st);
+  MLCP_CUDA_TRY(cudaMemcpyAsync(q, base, sizeof(double) * nvals, cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(qc, coef, sizeof(double) * B * R, cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int) * B, st));
+  RqParams rp;
+  rp.ops = tab; rp.v0 = 0; rp.nvec = B; rp.nD = Ly.nD; rp.base = q; rp.coef = qc; rp.out = rq;
+  rp.work = reinterpret_cast<double*>(b + o_rqw); rp.work_stride = 0;
+  if ((rc = rq_launch(rp, st))) return rc;
+  Svd2Params sp{};
+  sp.nvec = B; sp.nr = nbas[0]; sp.nc = nbas[1]; sp.rout = R; sp.redtol = kRedTol; sp.normalize = 1;
+  sp.K = (T + 1) * R; sp.hv = 1; sp.ops = tab; sp.y = y; sp.v_coef = qc; sp.shift = shift;
+  sp.out_base = q; sp.out_coef = qc; sp.out_rank = nullptr; sp.status = status;
+  sp.work = reinterpret_cast<double*>(b + o_w);
+  for (int i = 0; i < ncyc; ++i) {
+    range_shift_kernel<<<1, 1, 0, st>>>(rq, shift);
+    MLCP_CUDA_TRY(cudaGetLastError());
+    for (int s = 0; s < npow; ++s) {
+      if ((rc = svd2_apply_launch(tab, B, Ly.nD, q, y, st))) return rc;
+      if ((rc = svd2_launch(sp, (int)ctx->smem_optin, st))) return rc;
+    }
+    if ((rc = rq_launch(rp, st))) return rc;
+  }
+  double bh[2];
+  int sh[2];
+  MLCP_CUDA_TRY(cudaMemcpyAsync(bh, rq, sizeof(bh), cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(sh, status, sizeof(sh), cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(base, q, sizeof(double) * nvals, cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(coef, qc, sizeof(double) * B * R, cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int i = 0; i < B; ++i)
+    if (sh[i]) {
+      set_error("getspectralrangecpp_: the SVD of vector %d did not converge", i);
+      return kNumerical;
+    }
+  const double pad = 0.001 * (bh[1] - bh[0]);
+  bounds[0] = bh[0] - pad;
+  bounds[1] = bh[1] + pad;
+  return kOk;
+}
+
 // Reference GetSpectralRange (src/Solver.f90:563-654), more-than-two-mode
 // branch: the two starting vectors in base/coef (rank rk each; the host
 // builds them as the reference does) are improved by ncyc rounds of npow
@@ -500,8 +585,8 @@ int spectral_range(Context* ctx, double* base, double* coef, const int* nbas, in
     set_error("getspectralrangecpp_: rk = %d outside [1, %d]", rk, kMaxRankCycle);
     return rk < 1 ? kBadArgument : kTooLarge;
   }
-  if (ndof < 3) {
-    set_error("getspectralrangecpp_: ndof = %d; nodes of two modes use the power recursion with SVD", ndof);
+  if (ndof < 2) {
+    set_error("getspectralrangecpp_: ndof = %d; the range needs at least two modes", ndof);
     return kBadArgument;
   }
   if (npow < 0 || ncyc < 0 || TxD < ndof || TxD % ndof != 0 || nops < 1 || msize < 1) {
@@ -509,6 +594,9 @@ int spectral_range(Context* ctx, double* base, double* coef, const int* nbas, in
               msize);
     return kBadArgument;
   }
+  if (ndof == 2)
+    return spectral_range_2mode(ctx, base, coef, nbas, rk, npow, ncyc, opid, mptr, Hcoef, mat, TxD, nops, msize,
+                                bounds);
   Layout Ly;
   int rc = make_layout(ndof, nbas, &Ly);
   if (rc) return rc;

@@ -105,6 +105,37 @@ struct RqParams {
 int rq_launch(const RqParams& p, cudaStream_t st);
 size_t rq_work_doubles(const OpTable& t);
 
+// Two-mode reduction by SVD (reference reduc_SVDa/b, src/REDUCTIONML.f90:
+// 296-392): per vector, the nr x nc matrix A of a CP sum is formed, its SVD
+// computed, and the leading singular triplets written back as CP terms.
+// The input is either K plain CP terms per vector (hv = 0) or the terms of
+// (H - shift_v) v for a rank-R two-mode vector v (hv = 1: PRODHV with
+// ishift = 1, K = (T + 1) R, operator applications from svd2_apply_launch).
+struct Svd2Params {
+  int nvec, nr, nc;
+  int rout;           // output terms per vector (the reduction rank)
+  double redtol;      // singular values below redtol * s_1 are dropped
+  int normalize;      // 1: NORMCOEF the result (unit factors, unit norm)
+  int K;              // input terms per vector
+  const double* in_base;  // hv = 0: [nvec][K][nr + nc]
+  const double* in_coef;  // hv = 0: [nvec][K]
+  int hv;
+  OpTable ops;            // hv = 1: the operator list (D = 2)
+  const double* y;        // hv = 1: [nvec][utot][R][npmax] operators applied to v's factors
+  const double* v_coef;   // hv = 1: [nvec][R]
+  const double* shift;    // hv = 1: [nvec] energy shifts (device)
+  double* out_base;       // [nvec][rout][nr + nc]
+  double* out_coef;       // [nvec][rout]
+  int* out_rank;          // [nvec] terms kept (rest zero), or null
+  int* status;            // [nvec] bit 2: the Jacobi sweeps did not converge
+  double* work;           // svd2_work_doubles(nr, nc) per vector
+};
+int svd2_launch(const Svd2Params& p, int smem_optin, cudaStream_t st);
+size_t svd2_work_doubles(int nr, int nc);
+// y[v][g][r][:] = h_g x_r^d(g) for every operator slot g of a two-mode
+// table and term r of vector v (the identity copies).
+int svd2_apply_launch(const OpTable& t, int nvec, int nD, const double* base, double* y, cudaStream_t st);
+
 // Divide the weights of each rank-R vector by its norm (FP64).
 int normalize_coefs_launch(int nvec, int R, int D, int nD, const int* nbas, const double* base, double* coef,
                            cudaStream_t st);

@@ -73,10 +73,12 @@ def qhq_diag(base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int, hl, 
 
 
 def spectral_range(base: np.ndarray, coef: np.ndarray, nbas, rk: int, hl, npow: int, ncyc: int):
-    """Reference GetSpectralRange (src/Solver.f90:563-654, more than two
-    modes) through getspectralrangecpp_, from the two starting vectors of
-    rank rk in (base, coef).  Returns (base, coef, bounds) on copies, bounds
-    padded by 0.1 % of the range on each side."""
+    """Reference GetSpectralRange (src/Solver.f90:563-654) through
+    getspectralrangecpp_, from the two starting vectors of rank rk in
+    (base, coef) -- for two modes the rank-1 starts padded with zero-weight
+    terms, which the SVD power recursion fills up to rank rk.  Returns
+    (base, coef, bounds) on copies, bounds padded by 0.1 % of the range on
+    each side."""
     base = np.ascontiguousarray(base, dtype=np.float64).copy()
     coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
     nb = np.ascontiguousarray(nbas, dtype=np.int32).copy()
@@ -115,6 +117,32 @@ def update_opermat(imode: int, base: np.ndarray, coef: np.ndarray, nbas, rk: int
     if L.mlcp_gb300_last_status() != 0:
         raise _lib.MlcpError(_lib.last_error())
     return out
+
+
+def reduc_svd(base: np.ndarray, coef: np.ndarray, nbas, rG: int, rF: int, redtol: float = 1.0e-12):
+    """Reference reduc_SVDa/b (src/REDUCTIONML.f90:296-392) through
+    reducsvdcpp_ for a batch of two-mode vectors of rG terms each
+    (base [nvec * rG, nD], coef [nvec * rG]).  Returns (base [nvec, rF, nD],
+    coef [nvec, rF], rank [nvec]); terms past rank[v] are zero."""
+    nb = np.ascontiguousarray(nbas, dtype=np.int32).copy()
+    if nb.size != 2:
+        raise ValueError("reduc_svd reduces two-mode vectors")
+    nD = int(nb.sum())
+    base = np.ascontiguousarray(base, dtype=np.float64).reshape(-1, rG, nD)
+    coef = np.ascontiguousarray(coef, dtype=np.float64).reshape(-1, rG)
+    nvec = base.shape[0]
+    obase = np.zeros((nvec, rF, nD))
+    ocoef = np.zeros((nvec, rF))
+    orank = np.zeros(nvec, dtype=np.int32)
+    ints = [ctypes.c_int(x) for x in (rG, nvec, rF)]
+    tol = ctypes.c_double(float(redtol))
+    L = _lib.load()
+    L.reducsvdcpp_(base.ctypes.data_as(_D), coef.ctypes.data_as(_D), nb.ctypes.data_as(_I),
+                   *[ctypes.byref(x) for x in ints], ctypes.byref(tol), obase.ctypes.data_as(_D),
+                   ocoef.ctypes.data_as(_D), orank.ctypes.data_as(_I))
+    if L.mlcp_gb300_last_status() != 0:
+        raise _lib.MlcpError(_lib.last_error())
+    return obase, ocoef, orank
 
 
 def sort_vecs(base: np.ndarray, coef: np.ndarray, nbas, rk: int, eigv: np.ndarray, nconv: int, eref: float):

@@ -257,6 +257,91 @@ def spectral_range(base, coef, nbas, rk, hl, npow, ncyc):
     return base, coef, bounds
 
 
+def cp2d_dense(base, coef, nbas):
+    """Reference CP2DtoMat (src/SepdRepn.f90:518-558): the nr x nc matrix
+    sum_k c_k a_k b_k^T of a two-mode CP vector."""
+    nr, nc = int(nbas[0]), int(nbas[1])
+    base = np.asarray(base, dtype=np.float64).reshape(-1, nr + nc)
+    coef = np.asarray(coef, dtype=np.float64).ravel()
+    return (base[:, :nr] * coef[:, None]).T @ base[:, nr:]
+
+
+def reduc_svd(base, coef, nbas, rF, redtol=1.0e-12):
+    """Reference reduc_SVDa (src/REDUCTIONML.f90:296-333): CP2DtoMat, the SVD
+    (SolveWithSVD, src/LinAlg.f90:432-466, LAPACK through numpy), ncomp = the
+    leading singular values >= redtol * s_1 (at least one), nrk =
+    min(nr, nc, rF, ncomp) and RebuildfromSVD (src/REDUCTIONML.f90:394-439):
+    coef = s_i, mode 1 = U(:, i), mode 2 = V(:, i).  Returns (base, coef)
+    with nrk terms."""
+    nr, nc = int(nbas[0]), int(nbas[1])
+    U, s, Vt = np.linalg.svd(cp2d_dense(base, coef, nbas), full_matrices=False)
+    cut = redtol * s[0]
+    ncomp = 1
+    for i in range(1, s.size):
+        if abs(s[i]) < cut:
+            break
+        ncomp = i + 1
+    nrk = min(nr, nc, rF, ncomp)
+    return np.concatenate([U[:, :nrk].T, Vt[:nrk, :]], axis=1), s[:nrk].copy()
+
+
+def normcoef(base, coef, nbas):
+    """Reference NORMCOEF (src/MODVECVECML.f90:295-352): unit factors with
+    their norms moved into the weights, then the weights divided by the
+    vector's norm.  Returns copies."""
+    nbas = np.asarray(nbas)
+    offs = np.concatenate([[0], np.cumsum(nbas)])
+    base = np.array(base, dtype=np.float64).reshape(-1, int(nbas.sum()))
+    coef = np.array(coef, dtype=np.float64).ravel()
+    G = np.ones((coef.size, coef.size))
+    for d in range(nbas.size):
+        blk = base[:, offs[d]:offs[d + 1]]
+        nrm = np.linalg.norm(blk, axis=1)
+        blk /= nrm[:, None]
+        coef *= nrm
+        G *= blk @ blk.T
+    return base, coef / np.sqrt(abs(coef @ G @ coef))
+
+
+def prodhv_2mode(base, coef, nbas, hl, eshift):
+    """Reference PRODHV (src/MODHVECML.f90:50-111) with ishift = 1: the terms
+    of H v followed by those of -eshift v, for a two-mode v."""
+    nr = int(nbas[0])
+    base = np.asarray(base, dtype=np.float64).reshape(-1, int(np.sum(nbas)))
+    coef = np.asarray(coef, dtype=np.float64).ravel()
+    bs, cs = [], []
+    for t in range(hl.nterms):
+        h1, h2 = hl.operator(t, 0), hl.operator(t, 1)
+        bs.append(np.concatenate([base[:, :nr] @ h1.T, base[:, nr:] @ h2.T], axis=1))
+        cs.append(hl.coef[t] * coef)
+    bs.append(base.copy())
+    cs.append(-eshift * coef)
+    return np.concatenate(bs), np.concatenate(cs)
+
+
+def spectral_range_2mode(nbas, rk, hl, npow, ncyc):
+    """Reference GetSpectralRange (src/Solver.f90:563-654), two-mode branch:
+    rank-1 starting vectors, PowrRecurse (src/BlockPower.f90:49-73: PRODHV,
+    reduc by SVD to at most rk terms with redtol 1e-12, NORMCOEF) and the
+    Rayleigh quotients.  Returns ([(base, coef)] * 2, padded bounds)."""
+    b0, c0 = spectral_start(nbas, rk)
+    vecs = [(b0[j * rk:j * rk + 1].copy(), c0[j * rk:j * rk + 1].copy()) for j in range(2)]
+    bounds = np.array([rayleigh_quotient(b, c, nbas, hl) for b, c in vecs])
+    shift = [0.5 * (bounds[0] + bounds[1]), 0.0]
+    for _ in range(ncyc):
+        for j in range(2):
+            b, c = vecs[j]
+            for _ in range(npow):
+                wb, wc = prodhv_2mode(b, c, nbas, hl, shift[j])
+                b, c = reduc_svd(wb, wc, nbas, rk)
+                b, c = normcoef(b, c, nbas)
+            vecs[j] = (b, c)
+            bounds[j] = rayleigh_quotient(b, c, nbas, hl)
+        shift[0] = 0.5 * (bounds[0] + bounds[1])
+    pad = 0.001 * (bounds[1] - bounds[0])
+    return vecs, np.array([bounds[0] - pad, bounds[1] + pad])
+
+
 def sort_vecs(base, coef, rk, eigv, nconv, eref):
     """Reference SortVecs (src/BlockUtils.f90:520-583) on copies: vectors in
     increasing |eigv - Eref| (ties keep their order), eigv permuted alike, and

@@ -177,8 +177,29 @@ def test_spectral_range_matches_oracle(ncyc, cuda_device):
 
 
 @pytest.mark.gpu
-def test_spectral_range_rejects_two_modes(cuda_device):
-    hl = H.random_hoplist([5, 7], 4, seed=2)
+@pytest.mark.parametrize("case", [("random", [9, 7], 6, 4, 3), ("random", [7, 11], 5, 3, 2),
+                                  ("oscillators", [8, 8], 8, 10, 5), ("random", [40, 33], 12, 3, 2)])
+def test_spectral_range_two_modes_matches_oracle(case, cuda_device):
+    """Two-mode getspectralrangecpp_ (PowrRecurse: exact H v, SVD reduction,
+    NORMCOEF; all FP64) against the oracle's restatement: bounds to 1e-10
+    relative, each final vector as a matrix to 1e-9 of its largest entry
+    (the SVD's sign freedom cancels in U S V^T).  [7, 11] takes the
+    transposed orientation (nr < nc); [40, 33] a 40 x 33 SVD per step."""
+    kind, nbas, rk, npow, ncyc = case
+    hl = H.coupled_oscillators(2, nbas[0]) if kind == "oscillators" else H.random_hoplist(nbas, 5, seed=rk)
+    b, c = oracle.spectral_start(hl.nbas, rk)
+    gb, gc, gbd = IT.spectral_range(b, c, hl.nbas, rk, hl, npow, ncyc)
+    vecs, obd = oracle.spectral_range_2mode(hl.nbas, rk, hl, npow, ncyc)
+    np.testing.assert_allclose(gbd, obd, rtol=1e-10)
+    for j in range(2):
+        G = oracle.cp2d_dense(gb[j * rk:(j + 1) * rk], gc[j * rk:(j + 1) * rk], hl.nbas)
+        O = oracle.cp2d_dense(*vecs[j], hl.nbas)
+        assert np.abs(G - O).max() <= 1e-9 * np.abs(O).max()
+
+
+@pytest.mark.gpu
+def test_spectral_range_rejects_one_mode(cuda_device):
+    hl = H.random_hoplist([5], 4, seed=2)
     b, c = oracle.spectral_start(hl.nbas, 3)
     with pytest.raises(Exception, match="two modes"):
         IT.spectral_range(b, c, hl.nbas, 3, hl, 2, 1)

@@ -280,3 +280,45 @@ def test_update_opermat_matches_dense():
         Xf = np.kron(np.kron(eyes[0], eyes[1]), eyes[2])
         want = Qd @ Xf @ Qd.T
         assert np.max(np.abs(oracle.unpack_sym(out, nbloc) - want)) <= 1e-12 * np.max(np.abs(want))
+
+
+def test_reduc_svd_restatement():
+    """reduc_SVD restatement: an exact rank-3 input comes back as the same
+    matrix with 3 terms (the zero singular values fall below redtol * s_1);
+    truncation to rF terms leaves the Eckart-Young error; the factors are
+    orthonormal; a zero vector keeps min(nr, nc, rF) zero-weight terms."""
+    rng = np.random.default_rng(3)
+    nbas = [7, 5]
+    b3, c3 = rng.normal(size=(3, 12)), rng.uniform(0.5, 2.0, 3)
+    b = np.concatenate([b3, b3[:2]])
+    c = np.concatenate([c3, [0.5, -0.25]])  # rank 3, five terms
+    A = oracle.cp2d_dense(b, c, nbas)
+    ob, oc = oracle.reduc_svd(b, c, nbas, 10)
+    assert oc.size == 3
+    np.testing.assert_allclose(oracle.cp2d_dense(ob, oc, nbas), A, atol=1e-13 * np.abs(A).max())
+    np.testing.assert_allclose(ob[:, :7] @ ob[:, :7].T, np.eye(3), atol=1e-14)
+    np.testing.assert_allclose(ob[:, 7:] @ ob[:, 7:].T, np.eye(3), atol=1e-14)
+    s = np.linalg.svd(A, compute_uv=False)
+    ob2, oc2 = oracle.reduc_svd(b, c, nbas, 2)
+    err = np.linalg.norm(oracle.cp2d_dense(ob2, oc2, nbas) - A)
+    assert abs(err - s[2]) < 1e-12 * s[0]
+    ob0, oc0 = oracle.reduc_svd(b, np.zeros(5), nbas, 4)
+    assert oc0.size == 4 and not np.any(oc0)
+
+
+@pytest.mark.parametrize("make", [lambda: H.coupled_oscillators(2, 8),
+                                  lambda: H.random_hoplist([9, 7], 5, seed=4)])
+def test_spectral_range_2mode_brackets(make):
+    """Two-mode GetSpectralRange restatement (PowrRecurse with SVD): the
+    unpadded bounds are Rayleigh quotients inside [E_min, E_max] and reach
+    both ends of the dense spectrum (1e-6 of the width: the SVD reduction is
+    exact up to the rank cut, unlike ALS)."""
+    hl = make()
+    ex = np.linalg.eigvalsh(H.dense_hamiltonian(hl))
+    _, bd = oracle.spectral_range_2mode(hl.nbas, 8, hl, 10, 12)
+    pad = 0.001 * (bd[1] - bd[0]) / 1.002
+    lo, hi = bd[0] + pad, bd[1] - pad
+    assert ex[0] - 1e-9 <= lo <= hi <= ex[-1] + 1e-9
+    width = ex[-1] - ex[0]
+    assert abs(hi - ex[-1]) < 1e-6 * width
+    assert abs(lo - ex[0]) < 1e-6 * width
