@@ -151,6 +151,10 @@ def run_reference(args):
 # 6-mode level (10 HO functions per mode, lambda = 0.111803), rank 16, a
 # block of 40 vectors, npow = nals = 10, update on.
 CYC_D, CYC_N, CYC_R, CYC_B, CYC_NPOW, CYC_NALS = 6, 10, 16, 40, 10, 10
+# Two-mode node (40 x 40 functions, as the upper layers of a mode tree
+# combine 40-state modes); SVD reductions of 64 vectors of 16 x (20 + 1)
+# terms (the size of (H - E) v for a 20-term H).
+SVD_NBAS, SVD_T, SVD_NVEC = [40, 40], 20, 64
 
 
 def cycle_inputs(seed=20261203):
@@ -211,6 +215,29 @@ def run_cycle_bench(steps: int, cpu: bool):
         IT.update_opermat(1, gb, gc, hl.nbas, CYC_R, CYC_B, xm)
     out["update_opermat_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
     out["spectral_range"] = [float(bounds[0]), float(bounds[1])]
+    # two-mode nodes: GetSpectralRange as the solver calls it (rank 16,
+    # npow 10, 5 rounds) on a 40 x 40 two-mode quartic force field, and a
+    # batch of 64 SVD reductions of 336-term vectors to 16 terms
+    from mlcp_gb300 import hoplist as H
+    h2 = H.synthetic_qff(2, SVD_NBAS[0], seed=5)
+    tb, tc = oracle.spectral_start(h2.nbas, CYC_R)
+    IT.spectral_range(tb, tc, h2.nbas, CYC_R, h2, CYC_NPOW, 5)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        _, _, b2 = IT.spectral_range(tb, tc, h2.nbas, CYC_R, h2, CYC_NPOW, 5)
+    out["spectral_range_2mode_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
+    out["spectral_range_2mode"] = [float(b2[0]), float(b2[1])]
+    rg = CYC_R * (SVD_T + 1)
+    srng = np.random.default_rng(13)
+    svb = srng.normal(size=(SVD_NVEC * rg, sum(SVD_NBAS)))
+    svc = srng.uniform(0.1, 1.0, SVD_NVEC * rg)
+    IT.reduc_svd(svb, svc, SVD_NBAS, rg, CYC_R)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        IT.reduc_svd(svb, svc, SVD_NBAS, rg, CYC_R)
+    out["reduc_svd_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
+    out["workload_2mode"] = (f"two-mode quartic force field {SVD_NBAS[0]}x{SVD_NBAS[1]} ({h2.nterms} terms), "
+                             f"rank {CYC_R}; reduc_svd: {SVD_NVEC} vectors of {rg} terms -> {CYC_R}")
     if cpu:
         oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
         t0 = time.perf_counter()
@@ -225,6 +252,13 @@ def run_cycle_bench(steps: int, cpu: bool):
         t0 = time.perf_counter()
         oracle.update_opermat(1, gb, gc, hl.nbas, CYC_R, CYC_B, xm)
         out["update_opermat_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        oracle.spectral_range_2mode(h2.nbas, CYC_R, h2, CYC_NPOW, 5)
+        out["spectral_range_2mode_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        for v in range(SVD_NVEC):
+            oracle.reduc_svd(svb[v * rg:(v + 1) * rg], svc[v * rg:(v + 1) * rg], SVD_NBAS, CYC_R)
+        out["reduc_svd_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
         out["cpu_cores"] = os.cpu_count()
         out["cpu_kind"] = "port"
         oracle.set_cycle_penalties()

@@ -110,7 +110,8 @@ MLCP_API void updateopermatcpp_(MLCP_REF(int) imode, double *base, double *coef,
  * reduction of two-mode vectors (reduc with red2D = 'SVD'), batched: each of
  * the nvec vectors of rG terms (base[nvec][rG][nbas[0] + nbas[1]],
  * coef[nvec][rG]) is multiplied out to A = sum_k c_k a_k b_k^T, A's SVD taken
- * (FP64 one-sided Jacobi on the GPU), and its leading singular triplets
+ * (one-sided Jacobi on the GPU: A formed in FP64, sweeps in double-word
+ * arithmetic of about 48 bits), and its leading singular triplets
  * written as at most rF terms: obase[nvec][rF][nD], ocoef[nvec][rF] = s_i
  * (mode 1 = U(:, i), mode 2 = V(:, i)), orank[v] = min(nr, nc, rF, ncomp),
  * ncomp = the leading singular values >= redtol * s_1.  Terms past orank[v]

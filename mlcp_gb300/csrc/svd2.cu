@@ -10,10 +10,10 @@
 // factors), so both are this one routine; results agree up to rounding and
 // the signs of singular-vector pairs.
 //
-// GB300 mapping (FP64 throughout, as the reference):
+// GB300 mapping:
 //   svd2_form_kernel   many CTAs per vector: the matrix M (A, or A^T when
-//                      nr < nc, so that M is m x n with m >= n) in column
-//                      order into global scratch;
+//                      nr < nc, so that M is m x n with m >= n) in FP64, in
+//                      column order into global scratch;
 //   svd2_jacobi_kernel one CTA per vector: one-sided Jacobi (Hestenes) on
 //                      the n columns of M in shared memory (global memory
 //                      when it does not fit), with the parallel
@@ -21,10 +21,15 @@
 //                      round, one warp per pair -- until a sweep makes no
 //                      rotation; then column norms = singular values, a
 //                      stable descending sort, the reference's truncation,
-//                      the rebuild and (optionally) NORMCOEF.
-// One-sided Jacobi computes every singular value to high relative accuracy
-// (Demmel and Veselic, SIAM J. Matrix Anal. Appl. 13 (1992) 1204-1245), so
-// the truncation decision sees the same values as LAPACK's up to rounding.
+//                      the rebuild and (optionally) NORMCOEF, in FP64.
+// The sweeps run in double-word arithmetic (about 48 bits, dword.cuh) on M
+// scaled by a power of two: an FP64 instruction holds this part's FP64 pipe
+// for 64 cycles per warp, which made FP64 sweeps slower than one CPU core,
+// while double-word operations issue on the FP32 pipes.  One-sided Jacobi
+// computes every singular value to high relative accuracy (Demmel and
+// Veselic, SIAM J. Matrix Anal. Appl. 13 (1992) 1204-1245); with 48-bit
+// arithmetic the results agree with LAPACK's FP64 SVD to about 1e-13 of s_1,
+// far inside the reference's rank cut of 1e-12 s_1.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -34,6 +39,7 @@
 #include "../../include/mlcp_gb300.h"
 #include "common.cuh"
 #include "context.cuh"
+#include "dword.cuh"
 #include "intertwine.cuh"
 
 namespace mlcp {
@@ -42,12 +48,12 @@ int finish_status(int status);
 
 namespace {
 
-constexpr int kSvdThreads = 256;
+constexpr int kSvdThreads = 512;
 constexpr int kSvdWarps = kSvdThreads / 32;
 constexpr int kMaxN = 256;       // min(nr, nc)
 constexpr int kMaxM = 4096;      // max(nr, nc)
 constexpr int kMaxSweeps = 40;
-constexpr double kEps = 2.220446049250313e-16;  // DBL_EPSILON
+constexpr float kTinySq = 7.8886091e-31f;        // (2^-50)^2
 constexpr long long kApplyMaxBlocks = 2048;     // grid-stride cap of the apply kernel
 
 struct Shape {
@@ -116,23 +122,57 @@ __global__ void __launch_bounds__(256) svd2_form_kernel(Svd2Params p) {
 
 // Jacobi rotation that makes columns x and y orthogonal, from their Gram
 // entries (Rutishauser's formulas: t the smaller root of
-// t^2 + 2 zeta t - 1 = 0, zeta = (beta - alpha) / (2 gamma)).
-__device__ __forceinline__ void jacobi_rotation(double al, double be, double ga, double* c, double* s) {
-  const double zeta = (be - al) / (2.0 * ga);
-  const double az = fabs(zeta);
-  double t;
-  if (az > 1.0e150)
-    t = 0.5 / zeta;
+// t^2 + 2 zeta t - 1 = 0, zeta = (beta - alpha) / (2 gamma)).  t is taken in
+// FP32 (beta - alpha formed in double-word first, so near-equal norms do not
+// cancel); c = 1 / sqrt(1 + t^2) and s = c t are then double-word, so that
+// c^2 + s^2 = 1 to double-word accuracy whatever t's own rounding.  A t off
+// by 1e-7 relative still cuts gamma by seven digits; the sweeps repeat.
+__device__ __forceinline__ void jacobi_rotation(dw al, dw be, dw ga, dw* c, dw* s) {
+  const float zeta = __fdiv_rn(dw_sub(be, al).hi, __fmul_rn(2.f, ga.hi));
+  const float az = fabsf(zeta);
+  float t;
+  if (az > 1.0e15f)
+    t = __fdiv_rn(0.5f, zeta);
   else
-    t = (zeta >= 0.0 ? 1.0 : -1.0) / (az + sqrt(1.0 + zeta * zeta));
-  *c = 1.0 / sqrt(1.0 + t * t);
-  *s = *c * t;
+    t = __fdiv_rn(zeta >= 0.f ? 1.f : -1.f, __fadd_rn(az, __fsqrt_rn(__fmaf_rn(zeta, zeta, 1.f))));
+  // c = (1 + t^2)^-1/2 by two Newton steps in double-word from the FP32
+  // seed (2^-22 -> 2^-44 -> double-word rounding): a one-step c would make
+  // c^2 + s^2 - 1 about 1e-13 and scale the columns at every rotation
+  const dw u = dw_add_f(two_prod(t, t), 1.f);
+  dw r{f_rsqrt_approx(u.hi), 0.f};
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const dw e = dw_add_f(dw_neg(dw_mul(u, dw_mul(r, r))), 1.f);
+    r = dw_add(r, dw_mul(r, dw_mul_f(e, 0.5f)));
+  }
+  *c = r;
+  *s = dw_mul_f(r, t);
+}
+
+// all lanes end with the same double-word sum (dw_add_sloppy is symmetric
+// in its arguments: its two-sums are exact)
+__device__ __forceinline__ dw warp_sum_dw(dw v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const dw w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = dw_add_sloppy(v, w);
+  }
+  return v;
+}
+
+// x <- c x - s y, y <- s x + c y over n entries (lane-strided)
+__device__ __forceinline__ void rotate_cols(dw* x, dw* y, int n, dw c, dw s, int lane) {
+  for (int i = lane; i < n; i += 32) {
+    const dw xi = x[i], yi = y[i];
+    x[i] = dw_add_sloppy(dw_mul(c, xi), dw_neg(dw_mul(s, yi)));
+    y[i] = dw_add_sloppy(dw_mul(s, xi), dw_mul(c, yi));
+  }
 }
 
 template <bool kShared>
 __global__ void __launch_bounds__(kSvdThreads) svd2_jacobi_kernel(Svd2Params p) {
   extern __shared__ __align__(16) double smem[];
-  __shared__ double sig[kMaxN];
+  __shared__ double sig[kMaxN], vnorm[kMaxN], mnorm[kMaxN];
   __shared__ int ord[kMaxN];
   __shared__ double red[kSvdWarps];
   __shared__ int flag, nkeep;
@@ -140,17 +180,39 @@ __global__ void __launch_bounds__(kSvdThreads) svd2_jacobi_kernel(Svd2Params p) 
   const int m = sh.m, n = sh.n, n2 = sh.n2;
   const int v = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   double* gw = p.work + (size_t)v * work_doubles(sh);
-  double* M = kShared ? smem : gw;
-  double* V = kShared ? smem + (size_t)n2 * m : gw + (size_t)n2 * m;
-  // M (plus a zero column when n is odd) and V = I
-  for (int e = tid; e < n2 * m; e += kSvdThreads) {
-    const double x = e < n * m ? gw[e] : 0.0;
-    if (kShared || e >= n * m) M[e] = x;
+  // the sweeps run on double-word copies of M and V, in place of the FP64
+  // values (same 8 bytes per entry)
+  dw* M = reinterpret_cast<dw*>(kShared ? smem : gw);
+  dw* V = M + (size_t)n2 * m;
+  // scale M by a power of two so that its largest entry lies in [0.5, 1):
+  // the FP32 exponent range then covers every square the sweeps form
+  double amax = 0.0;
+  for (int e = tid; e < n * m; e += kSvdThreads) amax = fmax(amax, fabs(gw[e]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  if (lane == 0) red[warp] = amax;
+  __syncthreads();
+  if (tid == 0) {
+    double a = 0.0;
+    for (int w = 0; w < kSvdWarps; ++w) a = fmax(a, red[w]);
+    int ex = 0;
+    if (a > 0.0) frexp(a, &ex);
+    sig[0] = ldexp(1.0, -ex);
   }
-  for (int e = tid; e < n2 * n2; e += kSvdThreads) V[e] = (e % n2 == e / n2) ? 1.0 : 0.0;
+  __syncthreads();
+  const double scale = sig[0];
+  __syncthreads();
+  for (int e = tid; e < n2 * m; e += kSvdThreads) {
+    const double x = e < n * m ? gw[e] * scale : 0.0;
+    M[e] = dw_from_double(x);
+  }
+  for (int e = tid; e < n2 * n2; e += kSvdThreads) V[e] = dw{(e % n2 == e / n2) ? 1.f : 0.f, 0.f};
   __syncthreads();
 
-  const double tol = sqrt((double)m) * kEps;
+  // rotate while |x.y| > sqrt(m) 2^-46 |x| |y|: about the orthogonality that
+  // double-word columns can hold, reached in the same number of sweeps as a
+  // looser bound
+  const float tol = sqrtf((float)m) * 1.4210855e-14f;
   bool converged = false;
   for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
     if (tid == 0) flag = 0;
@@ -165,33 +227,24 @@ __global__ void __launch_bounds__(kSvdThreads) svd2_jacobi_kernel(Svd2Params p) 
           a = (k + q) % (n2 - 1);
           b = (k - q + n2 - 1) % (n2 - 1);
         }
-        double* x = M + (size_t)a * m;
-        double* y = M + (size_t)b * m;
-        double al = 0.0, be = 0.0, ga = 0.0;
+        dw* x = M + (size_t)a * m;
+        dw* y = M + (size_t)b * m;
+        dw_acc aa = acc_zero(), ab = acc_zero(), ag = acc_zero();
         for (int i = lane; i < m; i += 32) {
-          const double xi = x[i], yi = y[i];
-          al = fma(xi, xi, al);
-          be = fma(yi, yi, be);
-          ga = fma(xi, yi, ga);
+          const dw xi = x[i], yi = y[i];
+          acc_fma(aa, xi, xi);
+          acc_fma(ab, yi, yi);
+          acc_fma(ag, xi, yi);
         }
-        al = warp_sum(al);
-        be = warp_sum(be);
-        ga = warp_sum(ga);
-        if (ga != 0.0 && fabs(ga) > tol * sqrt(al) * sqrt(be)) {
-          double c, s;
+        const dw al = warp_sum_dw(acc_value(aa)), be = warp_sum_dw(acc_value(ab)), ga = warp_sum_dw(acc_value(ag));
+        // columns below 2^-50 of the largest entry stay as they are: they
+        // cannot move a singular value above the rank cut
+        if (al.hi > kTinySq && be.hi > kTinySq &&
+            fabsf(ga.hi) > tol * __fsqrt_rn(al.hi) * __fsqrt_rn(be.hi)) {
+          dw c, s;
           jacobi_rotation(al, be, ga, &c, &s);
-          for (int i = lane; i < m; i += 32) {
-            const double xi = x[i], yi = y[i];
-            x[i] = c * xi - s * yi;
-            y[i] = fma(s, xi, c * yi);
-          }
-          double* vx = V + (size_t)a * n2;
-          double* vy = V + (size_t)b * n2;
-          for (int i = lane; i < n2; i += 32) {
-            const double xi = vx[i], yi = vy[i];
-            vx[i] = c * xi - s * yi;
-            vy[i] = fma(s, xi, c * yi);
-          }
+          rotate_cols(x, y, m, c, s, lane);
+          rotate_cols(V + (size_t)a * n2, V + (size_t)b * n2, n2, c, s, lane);
           if (lane == 0) flag = 1;
         }
       }
@@ -205,13 +258,22 @@ __global__ void __launch_bounds__(kSvdThreads) svd2_jacobi_kernel(Svd2Params p) 
     }
   }
 
-  // singular values = column norms (fixed order per column)
+  // singular values: M = M0 V holds for the computed V, whose columns carry
+  // the same rounding-level norm drift as M's, so s_j = |M_j| / |V_j|
+  // (unscaled); the rebuild divides M_j by |M_j| and V_j by |V_j|
   for (int j = warp; j < n; j += kSvdWarps) {
-    const double* x = M + (size_t)j * m;
-    double a = 0.0;
-    for (int i = lane; i < m; i += 32) a = fma(x[i], x[i], a);
-    a = warp_sum(a);
-    if (lane == 0) sig[j] = sqrt(a);
+    const dw* x = M + (size_t)j * m;
+    const dw* y = V + (size_t)j * n2;
+    dw_acc a = acc_zero(), b = acc_zero();
+    for (int i = lane; i < m; i += 32) acc_fma(a, x[i], x[i]);
+    for (int i = lane; i < n2; i += 32) acc_fma(b, y[i], y[i]);
+    const dw ta = warp_sum_dw(acc_value(a)), tb = warp_sum_dw(acc_value(b));
+    if (lane == 0) {
+      const double mn = sqrt(dw_to_double(ta)), vn = sqrt(dw_to_double(tb));
+      sig[j] = mn / vn / scale;
+      vnorm[j] = vn;
+      mnorm[j] = mn;
+    }
   }
   __syncthreads();
   // stable descending order
@@ -249,15 +311,16 @@ __global__ void __launch_bounds__(kSvdThreads) svd2_jacobi_kernel(Svd2Params p) 
     }
     const int j = ord[k];
     const double s = sig[j];
-    const double* x = M + (size_t)j * m;
+    const dw* x = M + (size_t)j * m;
     if (s > 0.0) {
-      const double inv = 1.0 / s;
-      for (int i = lane; i < m; i += 32) ou[i] = x[i] * inv;
+      const double inv = 1.0 / mnorm[j];
+      for (int i = lane; i < m; i += 32) ou[i] = dw_to_double(x[i]) * inv;
     } else {  // all of A is zero: unit vectors, weight zero
       for (int i = lane; i < m; i += 32) ou[i] = (i == k % m) ? 1.0 : 0.0;
     }
-    const double* vc = V + (size_t)j * n2;
-    for (int i = lane; i < n; i += 32) ov[i] = vc[i];
+    const dw* vc = V + (size_t)j * n2;
+    const double vinv = 1.0 / vnorm[j];
+    for (int i = lane; i < n; i += 32) ov[i] = dw_to_double(vc[i]) * vinv;
     if (lane == 0) oc[k] = s;
   }
   if (!p.normalize) return;
@@ -352,7 +415,7 @@ int svd2_launch(const Svd2Params& p, int smem_optin, cudaStream_t st) {
   MLCP_CUDA_TRY(cudaGetLastError());
   const size_t smem = sizeof(double) * work_doubles(s);
   // static shared arrays of the kernel, with room for their alignment
-  const size_t stat = sizeof(double) * (kMaxN + kSvdWarps) + sizeof(int) * (kMaxN + 2) + 64;
+  const size_t stat = sizeof(double) * (3 * kMaxN + kSvdWarps) + sizeof(int) * (kMaxN + 2) + 64;
   if (smem + stat <= (size_t)smem_optin) {
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;

@@ -180,8 +180,9 @@ def test_spectral_range_matches_oracle(ncyc, cuda_device):
 @pytest.mark.parametrize("case", [("random", [9, 7], 6, 4, 3), ("random", [7, 11], 5, 3, 2),
                                   ("oscillators", [8, 8], 8, 10, 5), ("random", [40, 33], 12, 3, 2)])
 def test_spectral_range_two_modes_matches_oracle(case, cuda_device):
-    """Two-mode getspectralrangecpp_ (PowrRecurse: exact H v, SVD reduction,
-    NORMCOEF; all FP64) against the oracle's restatement: bounds to 1e-10
+    """Two-mode getspectralrangecpp_ (PowrRecurse: exact H v in FP64, SVD
+    reduction with double-word Jacobi sweeps, NORMCOEF) against the oracle's
+    FP64 restatement: bounds to 1e-10
     relative, each final vector as a matrix to 1e-9 of its largest entry
     (the SVD's sign freedom cancels in U S V^T).  [7, 11] takes the
     transposed orientation (nr < nc); [40, 33] a 40 x 33 SVD per step."""

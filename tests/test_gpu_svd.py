@@ -2,10 +2,11 @@
 src/REDUCTIONML.f90:296-392) on the GPU against the oracle's restatement
 (CP2DtoMat, LAPACK SVD through numpy, the reference's truncation rule).
 
-Both are FP64.  Singular vectors are unique only up to the sign of each
-(u_i, v_i) pair, so results are compared as the kept rank, the singular
-values (1e-12 of s_1), the reduced vector as a matrix (1e-12 of its
-largest entry) and the orthonormality of each mode's factors (1e-13).
+The GPU forms A in FP64 and runs the Jacobi sweeps in double-word (about
+48-bit) arithmetic.  Singular vectors are unique only up to the sign of
+each (u_i, v_i) pair, so results are compared as the kept rank, the
+singular values (1e-12 of s_1), the reduced vector as a matrix (1e-12 of
+its largest entry) and the orthonormality of each mode's factors (1e-12).
 """
 import numpy as np
 import pytest
@@ -36,8 +37,8 @@ def check(gb, gc, gr, base, coef, nbas, rF, redtol=1e-12):
         O = oracle.cp2d_dense(ob, oc, nbas)
         assert np.abs(G - O).max() <= 1e-12 * max(np.abs(O).max(), 1e-300)
         U, W = gb[v, :k, :nr], gb[v, :k, nr:]
-        np.testing.assert_allclose(U @ U.T, np.eye(k), atol=1e-13)
-        np.testing.assert_allclose(W @ W.T, np.eye(k), atol=1e-13)
+        np.testing.assert_allclose(U @ U.T, np.eye(k), atol=1e-12)
+        np.testing.assert_allclose(W @ W.T, np.eye(k), atol=1e-12)
 
 
 @pytest.mark.gpu
