@@ -63,23 +63,34 @@ __device__ inline int owner(const long long* row_off, int nvec, long long row) {
 }
 
 // One thread per (term, mode) element run; grid-stride.
+// Target factors to the mode-major FP32 copy.  Block row y is one
+// (vector, mode) pair, whose destination [rG][gs] is contiguous: consecutive
+// threads write consecutive floats and read consecutive doubles of a factor.
+// With a shared target only vector 0's terms are converted.
+__global__ void __launch_bounds__(256) als_prep_target_kernel(AlsParams p) {
+  const int nv = p.shared_target ? 1 : p.nvec;
+  const long long x0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long xs = (long long)gridDim.x * blockDim.x;
+  for (long long vd = blockIdx.y; vd < (long long)nv * p.ndof; vd += gridDim.y) {
+    const int v = (int)(vd / p.ndof), d = (int)(vd - (long long)v * p.ndof);
+    const int rG = p.rG[v], n = p.nbas[d], gs = als_gstride(n);
+    const double* src = p.g_base + p.g_term_off[v] * (long long)p.nD + p.off[d];
+    float* dst = p.gm + p.gm_off[v] + (long long)p.offg[d] * rG;
+    const long long cnt = (long long)rG * gs;
+    for (long long e = x0; e < cnt; e += xs) {
+      const long long j = e / gs;
+      const int q = (int)(e - j * gs);
+      dst[e] = (q < n) ? (float)src[j * p.nD + q] : 0.f;
+    }
+    if (d == 0 && !p.shared_target)
+      for (long long j = x0; j < rG; j += xs) p.gc[p.g_row_off[v] + j] = (float)p.g_coef[p.g_term_off[v] + j];
+  }
+}
+
+// The target weights of a shared target, and F's factors.
 __global__ void als_prep_kernel(AlsParams p) {
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  // target factors; with a shared target only vector 0's terms are converted
-  const long long grows = p.shared_target ? (long long)p.rG[0] : p.total_rows;
-  for (long long e = tid; e < grows * p.ndof; e += stride) {
-    const long long row = e / p.ndof;
-    const int d = (int)(e % p.ndof);
-    const int v = p.shared_target ? 0 : owner(p.g_row_off, p.nvec, row);
-    const int j = (int)(row - p.g_row_off[v]);
-    const int rG = p.rG[v];
-    const int n = p.nbas[d], gs = als_gstride(n);
-    const double* src = p.g_base + (p.g_term_off[v] + j) * (long long)p.nD + p.off[d];
-    float* dst = p.gm + p.gm_off[v] + (long long)p.offg[d] * rG + (long long)j * gs;
-    for (int q = 0; q < gs; ++q) dst[q] = (q < n) ? (float)src[q] : 0.f;
-    if (d == 0 && !p.shared_target) p.gc[p.g_row_off[v] + j] = (float)p.g_coef[p.g_term_off[v] + j];
-  }
   if (p.shared_target)
     for (long long e = tid; e < p.total_rows; e += stride) p.gc[e] = (float)p.shared_w[e];
   // F: each factor scaled to unit 2-norm (a zero factor stays zero), split
@@ -1023,7 +1034,10 @@ int als_launch(const AlsParams& p, size_t smem, cudaStream_t st, cudaEvent_t t0,
   int dev = 0, nsm = 0;
   MLCP_CUDA_TRY(cudaGetDevice(&dev));
   MLCP_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const long long work = (p.total_rows > p.total_f_terms ? p.total_rows : p.total_f_terms) * p.ndof;
+  const long long nvd = (long long)(p.shared_target ? 1 : p.nvec) * p.ndof;
+  als_prep_target_kernel<<<dim3(16, (unsigned)std::min<long long>(nvd, 65535)), 256, 0, st>>>(p);
+  MLCP_CUDA_TRY(cudaGetLastError());
+  const long long work = std::max<long long>(p.shared_target ? p.total_rows : 0, p.total_f_terms * p.ndof);
   long long blocks = (work + 255) / 256;
   if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
   if (blocks < 1) blocks = 1;

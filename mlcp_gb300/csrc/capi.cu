@@ -530,12 +530,33 @@ extern "C" int mlcp_als_batched_host(int nvec, int ndof, const int* nbas, const 
   job.term_off = term_off; job.d_base = d_base; job.d_coef = d_coef;
   rc = als_run(ctx, job, st);
   if (rc) return finish(rc);
-  for (int v = 0; v < nvec; ++v) {
-    const size_t t0 = (size_t)term_off[v];
-    if ((rc = cpy(h_base + t0 * nD, d_base + t0 * nD, sizeof(double) * (size_t)rF[v] * nD, cudaMemcpyDeviceToHost)))
-      return finish(rc);
-    if ((rc = cpy(h_coef + t0, d_coef + t0, sizeof(double) * (size_t)rF[v], cudaMemcpyDeviceToHost)))
-      return finish(rc);
+  // the F terms back: one strided copy per array when the vectors are evenly
+  // spaced with equal rF (the usual batch), else one copy per vector
+  bool even = nvec > 1;
+  for (int v = 1; v < nvec && even; ++v)
+    even = rF[v] == rF[0] && term_off[v] - term_off[v - 1] == term_off[1] - term_off[0];
+  const long long step = nvec > 1 ? term_off[1] - term_off[0] : 0;
+  if (even && step >= rF[0]) {
+    const size_t t0 = (size_t)term_off[0];
+    cudaError_t e = cudaMemcpy2DAsync(h_base + t0 * nD, sizeof(double) * (size_t)step * nD, d_base + t0 * nD,
+                                      sizeof(double) * (size_t)step * nD, sizeof(double) * (size_t)rF[0] * nD, nvec,
+                                      cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(h_coef + t0, sizeof(double) * (size_t)step, d_coef + t0, sizeof(double) * (size_t)step,
+                            sizeof(double) * (size_t)rF[0], nvec, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) {
+      set_error("cudaMemcpy2DAsync failed: %s", cudaGetErrorString(e));
+      return finish(kCudaError);
+    }
+  } else {
+    for (int v = 0; v < nvec; ++v) {
+      const size_t t0 = (size_t)term_off[v];
+      if ((rc = cpy(h_base + t0 * nD, d_base + t0 * nD, sizeof(double) * (size_t)rF[v] * nD,
+                    cudaMemcpyDeviceToHost)))
+        return finish(rc);
+      if ((rc = cpy(h_coef + t0, d_coef + t0, sizeof(double) * (size_t)rF[v], cudaMemcpyDeviceToHost)))
+        return finish(rc);
+    }
   }
   if (!stream) {
     cudaError_t e = cudaStreamSynchronize(st);

@@ -181,3 +181,22 @@ def test_cp_dot_matches_oracle(cuda_device):
         f = int(batch.rF[v])
         ref = oracle.cp_dot(b0[:f], c0[:f], b0[f:], c0[f:], batch.nbas)
         assert abs(got[v] - ref) <= 1e-12 * max(1.0, abs(ref))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [(6, 5, 8, 6, 90), (3, 4, [7, 5, 9, 6], [5, 8, 3], [40, 70, 25])])
+def test_host_entry_matches_device_entry(case, cuda_device):
+    """mlcp_als_batched_host (host buffers in and out) returns bit-for-bit
+    what mlcp_als_batched returns on the same data, and writes back only the
+    F terms: evenly spaced vectors with equal ranks take the strided
+    copy-back, the ragged batch one copy per vector."""
+    nvec, D, n, rF, rG = case
+    batch = workloads.als_batch(nvec, D, n, rF, rG, seed=17)
+    dc, db, _ = run_gpu(batch, 3, cuda_device)
+    hc, hb = batch.coef.copy(), batch.base.copy()
+    als.reduce_batched_host(hc, hb, batch.nbas, batch.rF, batch.rG, batch.term_off, 3)
+    np.testing.assert_array_equal(hc, dc)
+    np.testing.assert_array_equal(hb, db)
+    for v in range(batch.nvec):
+        t0, f = int(batch.term_off[v]), int(batch.rF[v])
+        np.testing.assert_array_equal(hb[t0 + f:t0 + f + int(batch.rG[v])], batch.base[t0 + f:t0 + f + int(batch.rG[v])])
