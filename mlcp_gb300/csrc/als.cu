@@ -76,11 +76,19 @@ __global__ void __launch_bounds__(256) als_prep_target_kernel(AlsParams p) {
     const int rG = p.rG[v], n = p.nbas[d], gs = als_gstride(n);
     const double* src = p.g_base + p.g_term_off[v] * (long long)p.nD + p.off[d];
     float* dst = p.gm + p.gm_off[v] + (long long)p.offg[d] * rG;
-    const long long cnt = (long long)rG * gs;
+    // four entries per thread (gs is a multiple of 4): one 16-byte store
+    const int g4 = gs / 4;
+    const long long cnt = (long long)rG * g4;
     for (long long e = x0; e < cnt; e += xs) {
-      const long long j = e / gs;
-      const int q = (int)(e - j * gs);
-      dst[e] = (q < n) ? (float)src[j * p.nD + q] : 0.f;
+      const long long j = e / g4;
+      const int q = 4 * (int)(e - j * g4);
+      const double* s = src + j * p.nD + q;
+      float4 o;
+      o.x = (q < n) ? (float)s[0] : 0.f;
+      o.y = (q + 1 < n) ? (float)s[1] : 0.f;
+      o.z = (q + 2 < n) ? (float)s[2] : 0.f;
+      o.w = (q + 3 < n) ? (float)s[3] : 0.f;
+      reinterpret_cast<float4*>(dst)[e] = o;
     }
     if (d == 0 && !p.shared_target)
       for (long long j = x0; j < rG; j += xs) p.gc[p.g_row_off[v] + j] = (float)p.g_coef[p.g_term_off[v] + j];

@@ -70,7 +70,8 @@ def als_batch(nvec: int, D: int, n, rF, rG, seed: int = ALS_SEED) -> AlsBatch:
 def main(argv=None) -> int:
     """Run one batched reduction of a seeded synthetic batch on the GPU (the
     command the profiling summaries use):
-    python -m mlcp_gb300.workloads --nvec 64 --ndof 30 --nbas 12 --rf 20 --rg 3200 --sweeps 10"""
+    python -m mlcp_gb300.workloads --nvec 64 --ndof 30 --nbas 12 --rf 20 --rg 3200 --sweeps 10
+    python -m mlcp_gb300.workloads --svd --nvec 64 --nbas 40 --rf 16 --rg 336"""
     import argparse
 
     ap = argparse.ArgumentParser(description=main.__doc__)
@@ -80,7 +81,19 @@ def main(argv=None) -> int:
     ap.add_argument("--rf", type=int, default=20)
     ap.add_argument("--rg", type=int, default=3200)
     ap.add_argument("--sweeps", type=int, default=10)
+    ap.add_argument("--svd", action="store_true",
+                    help="instead: one two-mode SVD reduction (reducsvdcpp_) of nvec vectors of rg terms on an "
+                         "nbas x nbas basis to rank rf")
     a = ap.parse_args(argv)
+    if a.svd:
+        from mlcp_gb300 import intertwine
+        rng = np.random.default_rng(ALS_SEED)
+        nb = [a.nbas, a.nbas]
+        base = rng.standard_normal((a.nvec * a.rg, 2 * a.nbas))
+        coef = rng.uniform(0.1, 1.0, a.nvec * a.rg)
+        _, _, rank = intertwine.reduc_svd(base, coef, nb, a.rg, a.rf)
+        print(f"reduced {a.nvec} two-mode vectors; ranks {int(rank.min())}..{int(rank.max())}")
+        return 0
     import torch
 
     from mlcp_gb300 import als
