@@ -95,6 +95,49 @@ __global__ void __launch_bounds__(256) als_prep_target_kernel(AlsParams p) {
   }
 }
 
+// The same conversion for targets in mapped host memory: entries are read in
+// the caller's term-major order (consecutive threads, consecutive doubles of
+// one vector's target terms), so the host link moves long contiguous runs;
+// each goes to its mode's row of the mode-major copy, and the last entry of a
+// mode's row also writes the row's zero padding.  Dynamic shared memory: the
+// mode of every column, then the per-mode offsets.
+__global__ void __launch_bounds__(256) als_prep_target_rows_kernel(AlsParams p) {
+  extern __shared__ int prep_smem[];
+  int* cmode = prep_smem;            // [nD]
+  int* soff = cmode + p.nD;          // [D+1] reference-layout offsets
+  int* soffg = soff + p.ndof + 1;    // [D+1] target-copy offsets
+  for (int c = threadIdx.x; c <= p.ndof; c += blockDim.x) {
+    soff[c] = p.off[c];
+    soffg[c] = p.offg[c];
+  }
+  for (int c = threadIdx.x; c < p.nD; c += blockDim.x) {
+    int d = 0;
+    while (p.off[d + 1] <= c) ++d;
+    cmode[c] = d;
+  }
+  __syncthreads();
+  const int nv = p.shared_target ? 1 : p.nvec;
+  const long long x0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long xs = (long long)gridDim.x * blockDim.x;
+  for (int v = blockIdx.y; v < nv; v += gridDim.y) {
+    const int rG = p.rG[v];
+    const double* src = p.g_base + p.g_term_off[v] * (long long)p.nD;
+    float* dst = p.gm + p.gm_off[v];
+    const long long total = (long long)rG * p.nD;
+    for (long long e = x0; e < total; e += xs) {
+      const long long j = e / p.nD;
+      const int c = (int)(e - j * p.nD), d = cmode[c], q = c - soff[d];
+      const int n = soff[d + 1] - soff[d], gs = als_gstride(n);
+      float* row = dst + (long long)soffg[d] * rG + j * gs;
+      row[q] = (float)src[e];
+      if (q == n - 1)
+        for (int z = n; z < gs; ++z) row[z] = 0.f;
+    }
+    if (!p.shared_target)
+      for (long long j = x0; j < rG; j += xs) p.gc[p.g_row_off[v] + j] = (float)p.g_coef[p.g_term_off[v] + j];
+  }
+}
+
 // The target weights of a shared target, and F's factors.
 __global__ void als_prep_kernel(AlsParams p) {
   const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -726,13 +769,16 @@ __device__ void dw_new_gram(const Cta& c, int k, int nk, int t, int nt) {
   }
 }
 
-// The end of a solve: the caller's FP64 factor and weights (cluster rank 0),
-// the Gram of the new factor of mode k folded into the prefix L, the suffix
+// The end of a solve: the caller's FP64 factor and weights (cluster rank 0,
+// in the last sweep only: earlier values of a mode are overwritten unseen,
+// and the conversions would hold the FP64 pipe on the critical path), the
+// Gram of the new factor of mode k folded into the prefix L, the suffix
 // products when a sweep ends, and the suffix of the next mode kn.  Threads t
 // of nt; `warp_only` when they form one warp.
-__device__ void post_solve(const Cta& c, const AlsParams& p, int k, int kn, int t, int nt, bool warp_only) {
+__device__ void post_solve(const Cta& c, const AlsParams& p, int k, int kn, int t, int nt, bool warp_only,
+                           bool last_sweep) {
   const int rF = c.rF, nk = p.nbas[k], rr = rF * rF;
-  if (c.rank == 0) {
+  if (c.rank == 0 && last_sweep) {
     double* fbase = p.base + p.term_off[c.v] * (long long)p.nD;
     for (int e = t; e < rF * nk; e += nt) {
       const int i = e / nk, q = e - i * nk;
@@ -825,7 +871,7 @@ __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& 
     c.fb[i * c.gsmax + q] = x;
     if (i < rF) c.fcta[(long long)i * c.nDp + p.offp[k] + q] = x;
   }
-  post_solve(c, p, k, kn, c.tid, kSolverThreads, false);
+  post_solve(c, p, k, kn, c.tid, kSolverThreads, false, t >= (p.nals - 1) * c.D);
   if (c.tid == 0 && bad) c.flags[1] = 1;
 }
 
@@ -1042,8 +1088,14 @@ int als_launch(const AlsParams& p, size_t smem, cudaStream_t st, cudaEvent_t t0,
   int dev = 0, nsm = 0;
   MLCP_CUDA_TRY(cudaGetDevice(&dev));
   MLCP_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const long long nvd = (long long)(p.shared_target ? 1 : p.nvec) * p.ndof;
-  als_prep_target_kernel<<<dim3(16, (unsigned)std::min<long long>(nvd, 65535)), 256, 0, st>>>(p);
+  const long long nv = p.shared_target ? 1 : p.nvec;
+  const size_t rows_smem = sizeof(int) * ((size_t)p.nD + 2 * (p.ndof + 1));
+  if (p.g_host && rows_smem <= 48 * 1024) {
+    als_prep_target_rows_kernel<<<dim3(32, (unsigned)std::min<long long>(nv, 65535)), 256, rows_smem, st>>>(p);
+  } else {
+    const long long nvd = nv * p.ndof;
+    als_prep_target_kernel<<<dim3(16, (unsigned)std::min<long long>(nvd, 65535)), 256, 0, st>>>(p);
+  }
   MLCP_CUDA_TRY(cudaGetLastError());
   const long long work = std::max<long long>(p.shared_target ? p.total_rows : 0, p.total_f_terms * p.ndof);
   long long blocks = (work + 255) / 256;

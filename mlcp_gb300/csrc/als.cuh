@@ -58,6 +58,7 @@ struct AlsParams {
   int shared_target;            // 1: every vector fits the same target terms (those
                                 //    of vector 0) with its own weights from shared_w
   const double* shared_w;       // [nvec][rG] per-vector target weights (shared_target only)
+  int g_host;                   // 1: g_base/g_coef are mapped host memory (read in term order)
   float* gm;         // FP32 mode-major target factors: mode d of term j at
                      //   gm + gm_off[v] + offg[d]*rG + j*gstride(n_d)
   float* gc;         // FP32 target weights [total_rows]
@@ -93,6 +94,7 @@ struct AlsJob {
   const double* g_base = nullptr;        // device; null: targets follow F in d_base
   const double* g_coef = nullptr;
   const long long* g_term_off = nullptr; // host [nvec]; null: term_off + rF
+  bool g_host = false;                   // g_base/g_coef: mapped host memory
   const double* shared_w = nullptr;      // device [nvec][rG]: shared target of vector 0
   double pen_factor = 1.0e-10;           // reference FP64-build penalty rule
   int* d_status = nullptr;

@@ -305,6 +305,7 @@ int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
   prm.g_base = job.g_base ? job.g_base : d_base;
   prm.g_coef = job.g_coef ? job.g_coef : d_coef;
   prm.shared_target = job.shared_w ? 1 : 0;
+  prm.g_host = job.g_host ? 1 : 0;
   prm.shared_w = job.shared_w;
   prm.gm = reinterpret_cast<float*>(w + o_gm);
   prm.gc = reinterpret_cast<float*>(w + o_gc);
@@ -492,11 +493,28 @@ extern "C" int mlcp_als_batched_host(int nvec, int ndof, const int* nbas, const 
   cudaStream_t st = pick_stream(ctx, stream);
   int nD = 0;
   for (int d = 0; d < ndof; ++d) nD += nbas[d];
-  long long nterms = 0;
-  for (int v = 0; v < nvec; ++v) nterms = std::max(nterms, term_off[v] + rF[v] + rG[v]);
-  // device copies of the caller's buffers live in their own allocation so the
-  // ALS workspace can grow independently
-  const size_t need = sizeof(double) * (size_t)nterms * (nD + 1);
+  long long nterms = 0, nf = 0;
+  for (int v = 0; v < nvec; ++v) {
+    if (rF[v] < 1 || rG[v] < 1) {
+      set_error("mlcp_als_batched_host: vector %d has rF=%d rG=%d (both must be positive)", v, rF[v], rG[v]);
+      return finish(kBadArgument);
+    }
+    nterms = std::max(nterms, term_off[v] + rF[v] + rG[v]);
+    nf += rF[v];
+  }
+  // Page-locked, mapped caller arrays (cudaHostAlloc, cudaHostRegister,
+  // pinned torch tensors): the conversion kernel reads the target terms
+  // straight from host memory, so crossing the host link and the FP64 ->
+  // FP32 conversion are one pass, and only the F terms go through a device
+  // buffer.  Other host memory: one copy of the whole batch.
+  cudaPointerAttributes ab{}, ac{};
+  const bool mapped = cudaPointerGetAttributes(&ab, h_base) == cudaSuccess && ab.type == cudaMemoryTypeHost &&
+                      ab.devicePointer && cudaPointerGetAttributes(&ac, h_coef) == cudaSuccess &&
+                      ac.type == cudaMemoryTypeHost && ac.devicePointer;
+  (void)cudaGetLastError();
+  // device copies live in their own allocation so the ALS workspace can grow
+  // independently: the F terms only (mapped) or the whole batch
+  const size_t need = sizeof(double) * (size_t)(mapped ? nf : nterms) * (nD + 1);
   if (need > ctx->io_bytes) {
     if (ctx->io) {
       cudaError_t e0 = cudaStreamSynchronize(st);
@@ -517,47 +535,82 @@ extern "C" int mlcp_als_batched_host(int nvec, int ndof, const int* nbas, const 
   }
   double* d_buf = static_cast<double*>(ctx->io);
   double* d_base = d_buf;
-  double* d_coef = d_buf + (size_t)nterms * nD;
-  auto cpy = [&](void* dst, const void* src, size_t b, cudaMemcpyKind k) {
-    cudaError_t e = cudaMemcpyAsync(dst, src, b, k, st);
-    if (e != cudaSuccess) set_error("cudaMemcpyAsync failed: %s", cudaGetErrorString(e));
-    return e == cudaSuccess ? kOk : kCudaError;
-  };
-  if ((rc = cpy(d_base, h_base, sizeof(double) * (size_t)nterms * nD, cudaMemcpyHostToDevice))) return finish(rc);
-  if ((rc = cpy(d_coef, h_coef, sizeof(double) * (size_t)nterms, cudaMemcpyHostToDevice))) return finish(rc);
-  AlsJob job;
-  job.nvec = nvec; job.ndof = ndof; job.nals = nals; job.nbas = nbas; job.rF = rF; job.rG = rG;
-  job.term_off = term_off; job.d_base = d_base; job.d_coef = d_coef;
-  rc = als_run(ctx, job, st);
-  if (rc) return finish(rc);
-  // the F terms back: one strided copy per array when the vectors are evenly
-  // spaced with equal rF (the usual batch), else one copy per vector
+  double* d_coef = d_buf + (size_t)(mapped ? nf : nterms) * nD;
+  // F terms of vector v: host terms term_off[v].., device terms doff[v]..
+  std::vector<long long> doff(nvec), gto(nvec);
+  {
+    long long o = 0;
+    for (int v = 0; v < nvec; ++v) {
+      doff[v] = mapped ? o : term_off[v];
+      gto[v] = term_off[v] + rF[v];
+      o += rF[v];
+    }
+  }
+  // the F terms between host and device: one strided copy per array when the
+  // vectors are evenly spaced with equal rF (the usual batch), else one copy
+  // per vector
   bool even = nvec > 1;
   for (int v = 1; v < nvec && even; ++v)
     even = rF[v] == rF[0] && term_off[v] - term_off[v - 1] == term_off[1] - term_off[0];
-  const long long step = nvec > 1 ? term_off[1] - term_off[0] : 0;
-  if (even && step >= rF[0]) {
-    const size_t t0 = (size_t)term_off[0];
-    cudaError_t e = cudaMemcpy2DAsync(h_base + t0 * nD, sizeof(double) * (size_t)step * nD, d_base + t0 * nD,
-                                      sizeof(double) * (size_t)step * nD, sizeof(double) * (size_t)rF[0] * nD, nvec,
-                                      cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpy2DAsync(h_coef + t0, sizeof(double) * (size_t)step, d_coef + t0, sizeof(double) * (size_t)step,
-                            sizeof(double) * (size_t)rF[0], nvec, cudaMemcpyDeviceToHost, st);
+  const long long hstep = nvec > 1 ? term_off[1] - term_off[0] : 0;
+  even = even && hstep >= rF[0];
+  auto copy_f = [&](cudaMemcpyKind kind) -> int {
+    const bool h2d = kind == cudaMemcpyHostToDevice;
+    const long long dstep = mapped ? rF[0] : hstep;
+    cudaError_t e = cudaSuccess;
+    if (even) {
+      const size_t t0 = (size_t)term_off[0], w = sizeof(double) * (size_t)rF[0];
+      double* hb = h_base + t0 * nD;
+      double* hc = h_coef + t0;
+      double* db = d_base + (size_t)doff[0] * nD;
+      double* dc = d_coef + (size_t)doff[0];
+      const size_t hpb = sizeof(double) * (size_t)hstep * nD, dpb = sizeof(double) * (size_t)dstep * nD;
+      const size_t hpc = sizeof(double) * (size_t)hstep, dpc = sizeof(double) * (size_t)dstep;
+      e = h2d ? cudaMemcpy2DAsync(db, dpb, hb, hpb, w * nD, nvec, kind, st)
+              : cudaMemcpy2DAsync(hb, hpb, db, dpb, w * nD, nvec, kind, st);
+      if (e == cudaSuccess)
+        e = h2d ? cudaMemcpy2DAsync(dc, dpc, hc, hpc, w, nvec, kind, st)
+                : cudaMemcpy2DAsync(hc, hpc, dc, dpc, w, nvec, kind, st);
+    } else {
+      for (int v = 0; v < nvec && e == cudaSuccess; ++v) {
+        double* hb = h_base + (size_t)term_off[v] * nD;
+        double* db = d_base + (size_t)doff[v] * nD;
+        const size_t bb = sizeof(double) * (size_t)rF[v] * nD, bc = sizeof(double) * (size_t)rF[v];
+        e = h2d ? cudaMemcpyAsync(db, hb, bb, kind, st) : cudaMemcpyAsync(hb, db, bb, kind, st);
+        if (e == cudaSuccess)
+          e = h2d ? cudaMemcpyAsync(d_coef + doff[v], h_coef + term_off[v], bc, kind, st)
+                  : cudaMemcpyAsync(h_coef + term_off[v], d_coef + doff[v], bc, kind, st);
+      }
+    }
     if (e != cudaSuccess) {
-      set_error("cudaMemcpy2DAsync failed: %s", cudaGetErrorString(e));
+      set_error("copying the F terms failed: %s", cudaGetErrorString(e));
+      return kCudaError;
+    }
+    return kOk;
+  };
+  AlsJob job;
+  job.nvec = nvec; job.ndof = ndof; job.nals = nals; job.nbas = nbas; job.rF = rF; job.rG = rG;
+  job.d_base = d_base; job.d_coef = d_coef;
+  if (mapped) {
+    if ((rc = copy_f(cudaMemcpyHostToDevice))) return finish(rc);
+    job.term_off = doff.data();
+    job.g_base = static_cast<const double*>(ab.devicePointer);
+    job.g_coef = static_cast<const double*>(ac.devicePointer);
+    job.g_term_off = gto.data();
+    job.g_host = true;
+  } else {
+    cudaError_t e = cudaMemcpyAsync(d_base, h_base, sizeof(double) * (size_t)nterms * nD, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(d_coef, h_coef, sizeof(double) * (size_t)nterms, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+      set_error("cudaMemcpyAsync failed: %s", cudaGetErrorString(e));
       return finish(kCudaError);
     }
-  } else {
-    for (int v = 0; v < nvec; ++v) {
-      const size_t t0 = (size_t)term_off[v];
-      if ((rc = cpy(h_base + t0 * nD, d_base + t0 * nD, sizeof(double) * (size_t)rF[v] * nD,
-                    cudaMemcpyDeviceToHost)))
-        return finish(rc);
-      if ((rc = cpy(h_coef + t0, d_coef + t0, sizeof(double) * (size_t)rF[v], cudaMemcpyDeviceToHost)))
-        return finish(rc);
-    }
+    job.term_off = term_off;
   }
+  rc = als_run(ctx, job, st);
+  if (rc) return finish(rc);
+  if ((rc = copy_f(cudaMemcpyDeviceToHost))) return finish(rc);
   if (!stream) {
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {

@@ -185,6 +185,7 @@ int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_bas
   prm.g_base = d_base;
   prm.g_coef = d_coef;
   prm.shared_target = 0;
+  prm.g_host = 0;
   prm.shared_w = nullptr;
   prm.gm = reinterpret_cast<float*>(w + o_gm);
   prm.gc = reinterpret_cast<float*>(w + o_gc);

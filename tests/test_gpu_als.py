@@ -184,16 +184,24 @@ def test_cp_dot_matches_oracle(cuda_device):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("case", [(6, 5, 8, 6, 90), (3, 4, [7, 5, 9, 6], [5, 8, 3], [40, 70, 25])])
-def test_host_entry_matches_device_entry(case, cuda_device):
+def test_host_entry_matches_device_entry(case, pinned, cuda_device):
     """mlcp_als_batched_host (host buffers in and out) returns bit-for-bit
     what mlcp_als_batched returns on the same data, and writes back only the
-    F terms: evenly spaced vectors with equal ranks take the strided
-    copy-back, the ragged batch one copy per vector."""
+    F terms: evenly spaced vectors with equal ranks take the strided copies,
+    the ragged batch one copy per vector.  Pinned (mapped) arrays take the
+    path whose conversion kernel reads the target terms from host memory;
+    pageable ones are copied whole."""
+    import torch
     nvec, D, n, rF, rG = case
     batch = workloads.als_batch(nvec, D, n, rF, rG, seed=17)
     dc, db, _ = run_gpu(batch, 3, cuda_device)
-    hc, hb = batch.coef.copy(), batch.base.copy()
+    if pinned:
+        hc = torch.from_numpy(batch.coef.copy()).pin_memory().numpy()
+        hb = torch.from_numpy(batch.base.copy()).pin_memory().numpy()
+    else:
+        hc, hb = batch.coef.copy(), batch.base.copy()
     als.reduce_batched_host(hc, hb, batch.nbas, batch.rF, batch.rG, batch.term_off, 3)
     np.testing.assert_array_equal(hc, dc)
     np.testing.assert_array_equal(hb, db)
