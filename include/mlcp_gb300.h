@@ -148,8 +148,13 @@ MLCP_API int mlcp_gb300_last_status(void);
 MLCP_API int mlcp_als_batched(int nvec, int ndof, const int *nbas, const int *rF, const int *rG, const long long *term_off,
                      double *d_coef, double *d_base, int nals, int *d_status, void *stream);
 
-/* Same computation on host buffers: copies the batch to the device, reduces,
- * and copies the F terms back (pinned host memory gives asynchronous copies). */
+/* Same computation on host buffers, F terms written back in place.  Page-locked
+ * mapped arrays (cudaHostAlloc, cudaHostRegister, pinned tensors) are read by
+ * the GPU directly: the target terms cross the host link once, inside the
+ * FP32 conversion, and only the F terms use device copies.  Other host memory
+ * is copied to the device whole.  With a stream the call is asynchronous and
+ * the arrays must stay unchanged until the stream reaches the end of the call;
+ * with stream NULL it returns when the results are in place. */
 MLCP_API int mlcp_als_batched_host(int nvec, int ndof, const int *nbas, const int *rF, const int *rG,
                           const long long *term_off, double *h_coef, double *h_base, int nals, void *stream);
 
