@@ -48,7 +48,7 @@ int finish_status(int status);
 
 namespace {
 
-constexpr int kSvdThreads = 512;
+constexpr int kSvdThreads = 1024;
 constexpr int kSvdWarps = kSvdThreads / 32;
 constexpr int kMaxN = 256;       // min(nr, nc)
 constexpr int kMaxM = 4096;      // max(nr, nc)
