@@ -95,6 +95,21 @@ MLCP_API void getspectralrangecpp_(double *base, double *coef, int *nbas, MLCP_R
                                    double *mat, MLCP_REF(int) TxD, MLCP_REF(int) nops, MLCP_REF(int) msize,
                                    double *bounds);
 
+/* Replaces Diagonalize(Q, H, eigv, .FALSE., ...) (src/BlockUtils.f90:184-225),
+ * the pre-diagonalisation of the block that the solver runs before its
+ * cycles (src/Solver.f90:363-369), on the GPU: A = <Q|H|Q> and S = <Q|Q>
+ * with H applied exactly (FP64), the generalised eigenproblem (eigenvalues
+ * ascending into eigv), and each vector replaced by the reduction of
+ * sum_i U(i, m) Q_i to at most rk terms followed by NORMCOEF: the SVD
+ * (redtol 1e-12) for two modes, nals ALS sweeps started from the old Q_m for
+ * more (the reference starts from a randomised decomposition; nals = 0
+ * keeps the vectors).  Terms the SVD does not need carry weight 0.
+ * Same layout and operator list as intertwinecpp_; at most 160 vectors. */
+MLCP_API void diagonalizecpp_(double *base, double *coef, int *nbas, MLCP_REF(int) rk, MLCP_REF(int) ndof,
+                              MLCP_REF(int) nbloc, int *opid, int *mptr, double *Hcoef, double *mat,
+                              MLCP_REF(int) TxD, MLCP_REF(int) nops, MLCP_REF(int) msize, double *eigv,
+                              MLCP_REF(int) nals);
+
 /* Replaces UpdateOperMat (src/Updater.f90:110-151) for the nx primitive
  * operators of mode imode (1-based) of the block, on the GPU in FP64:
  * qxq[x] = the nbloc x nbloc matrix <Q_j, X_x Q_i>, each xmats[x] and qxq[x]

@@ -69,6 +69,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         if hasattr(L, "updateopermatcpp_"):
             L.updateopermatcpp_.restype = None
             L.updateopermatcpp_.argtypes = [_I, _D, _D, _I, _I, _I, _I, _I, _D, _D]
+        if hasattr(L, "diagonalizecpp_"):
+            L.diagonalizecpp_.restype = None
+            L.diagonalizecpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I, _I, _D, _D, _I, _I, _I, _D, _I]
         if hasattr(L, "reducsvdcpp_"):
             L.reducsvdcpp_.restype = None
             L.reducsvdcpp_.argtypes = [_D, _D, _I, _I, _I, _I, _D, _D, _D, _I]

@@ -488,6 +488,129 @@ __global__ void range_shift_kernel(const double* bounds, double* shift) {
 // Reduction threshold of the reference's solver (redtol, src/Solver.f90:326).
 constexpr double kRedTol = 1.0e-12;
 
+// Reference Diagonalize with intw = .FALSE. (src/BlockUtils.f90:184-225), the
+// solver's pre-diagonalisation (src/Solver.f90:363-369): A = <Q|H|Q> and
+// S = <Q|Q> with H applied exactly (GetQHQ, GetOverlaps; the reference
+// reduces H Q before the inner products to save CPU time, here the products
+// are exact), the generalised eigenproblem (SolveGenEigval: eigenvalues
+// ascending into eigv), and UpdateVecs (:437-475): Q_m <- the reduction of
+// sum_i U(i, m) Q_i to at most rk terms, then NORMCOEF.  Two modes reduce by
+// SVD (reduc_SVD, redtol 1e-12: the reference's red2D = 'SVD' choice);
+// more modes by nals ALS sweeps from the old Q_m (the reference starts its
+// reduc_ALS from a randomised interpolative decomposition, which no fixed
+// input reproduces); nals = 0 leaves the vectors as they are.
+int diagonalize(Context* ctx, double* base, double* coef, const int* nbas, int rk, int ndof, int nbloc,
+                const int* opid, const int* mptr, const double* Hcoef, const double* mat, int TxD, int nops, int msize,
+                double* eigv, int nals) {
+  if (rk < 1 || rk > kMaxRankCycle) {
+    set_error("diagonalizecpp_: rk = %d outside [1, %d]", rk, kMaxRankCycle);
+    return rk < 1 ? kBadArgument : kTooLarge;
+  }
+  if (ndof < 2 || nbloc < 1 || nals < 0 || TxD < ndof || TxD % ndof != 0 || nops < 1 || msize < 1) {
+    set_error("diagonalizecpp_: bad sizes (ndof=%d nbloc=%d nals=%d TxD=%d nops=%d msize=%d)", ndof, nbloc, nals, TxD,
+              nops, msize);
+    return kBadArgument;
+  }
+  if (nbloc > 160) {
+    set_error("diagonalizecpp_: block size %d exceeds the 160 vectors of the on-chip Rayleigh-Ritz solver", nbloc);
+    return kTooLarge;
+  }
+  Layout Ly;
+  int rc = make_layout(ndof, nbas, &Ly);
+  if (rc) return rc;
+  const int T = TxD / ndof, R = rk, B = nbloc;
+  cudaStream_t st = ctx->stream;
+  OpTable tab;
+  rc = get_optable(ctx, Ly, nbas, R, T, opid, mptr, Hcoef, mat, nops, msize, st, &tab);
+  if (rc) return rc;
+  CycleBuffers cb;
+  size_t bytes = plan_cycle(Ly, tab, R, B, &cb, nullptr);
+  auto take = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
+  const size_t o_y = take(sizeof(double) * (size_t)B * tab.utot * R * tab.npmax);
+  const size_t o_sv = take(ndof == 2 ? sizeof(double) * B * svd2_work_doubles(nbas[0], nbas[1]) : 0);
+  if (bytes > ctx->cyc_bytes) {
+    if (ctx->cyc) {
+      MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+      MLCP_CUDA_TRY(cudaFree(ctx->cyc));
+      ctx->cyc = nullptr;
+      ctx->cyc_bytes = 0;
+    }
+    MLCP_CUDA_TRY(cudaMalloc(&ctx->cyc, bytes));
+    ctx->cyc_bytes = bytes;
+  }
+  char* b = static_cast<char*>(ctx->cyc);
+  plan_cycle(Ly, tab, R, B, &cb, b);
+  double* y = reinterpret_cast<double*>(b + o_y);
+  const size_t nvals = (size_t)B * R * Ly.nD;
+  MLCP_CUDA_TRY(cudaMemcpyAsync(cb.q, base, sizeof(double) * nvals, cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qc, coef, sizeof(double) * B * R, cudaMemcpyHostToDevice, st));
+  std::vector<int> meta(3 * (ndof + 1), 0);
+  std::memcpy(meta.data(), nbas, sizeof(int) * ndof);
+  std::memcpy(meta.data() + (ndof + 1), Ly.off.data(), sizeof(int) * (ndof + 1));
+  std::memcpy(meta.data() + 2 * (ndof + 1), Ly.offp.data(), sizeof(int) * (ndof + 1));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(cb.meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaMemsetAsync(cb.status, 0, sizeof(int) * (B + 4), st));
+  const int* d_nbas = cb.meta;
+  // A, S with H applied exactly; then the generalised eigenproblem
+  if ((rc = rq_apply_launch(tab, B, Ly.nD, cb.q, y, st))) return rc;
+  RqPairParams rp;
+  rp.ops = tab; rp.nvec = B; rp.nD = Ly.nD; rp.base = cb.q; rp.coef = cb.qc; rp.y = y; rp.A = cb.A; rp.S = cb.S;
+  if ((rc = rq_pair_launch(rp, (int)ctx->smem_optin, st))) return rc;
+  GepParams gp;
+  gp.D = ndof; gp.R = R; gp.nbloc = B; gp.nD = Ly.nD; gp.nbas = d_nbas;
+  gp.q_base = cb.q; gp.q_coef = cb.qc; gp.hq_base = nullptr; gp.hq_coef = nullptr;
+  gp.A = cb.A; gp.S = cb.S; gp.eigv = cb.eigv; gp.U = cb.U; gp.work = cb.gwork; gp.status = cb.status + B + 1;
+  if ((rc = gep_solve_launch(gp, st))) return rc;
+  // UpdateVecs: weights w[m][i R + r] = c(i, r) U(i, m) of sum_i U(i, m) Q_i
+  const bool update = ndof == 2 || nals > 0;
+  if (update) {
+    update_weights_kernel<<<std::min(ctx->num_sms * 8, (B * B * R + 255) / 256), 256, 0, st>>>(B, R, cb.qc, cb.U,
+                                                                                                cb.wts);
+    MLCP_CUDA_TRY(cudaGetLastError());
+  }
+  if (ndof == 2) {
+    Svd2Params sp{};
+    sp.nvec = B; sp.nr = nbas[0]; sp.nc = nbas[1]; sp.rout = R; sp.redtol = kRedTol; sp.normalize = 1;
+    sp.K = B * R; sp.in_base = cb.q; sp.in_coef = cb.wts; sp.shared_base = 1; sp.hv = 0;
+    sp.out_base = cb.qn; sp.out_coef = cb.qnc; sp.out_rank = nullptr; sp.status = cb.status;
+    sp.work = reinterpret_cast<double*>(b + o_sv);
+    if ((rc = svd2_launch(sp, (int)ctx->smem_optin, st))) return rc;
+    std::swap(cb.q, cb.qn);
+    std::swap(cb.qc, cb.qnc);
+  } else if (nals > 0) {
+    MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qn, cb.q, sizeof(double) * nvals, cudaMemcpyDeviceToDevice, st));
+    MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qnc, cb.qc, sizeof(double) * B * R, cudaMemcpyDeviceToDevice, st));
+    std::vector<int> rF(B, R), rG(B, B * R);
+    std::vector<long long> toff(B), gtoff(B, 0);
+    for (int v = 0; v < B; ++v) toff[v] = (long long)v * R;
+    AlsJob job;
+    job.nvec = B; job.ndof = ndof; job.nals = nals; job.nbas = nbas; job.rF = rF.data(); job.rG = rG.data();
+    job.term_off = toff.data(); job.d_base = cb.qn; job.d_coef = cb.qnc;
+    job.g_base = cb.q; job.g_coef = cb.qc; job.g_term_off = gtoff.data(); job.shared_w = cb.wts;
+    job.d_status = cb.status;
+    job.pen_factor = kPenFP32;
+    if ((rc = als_run(ctx, job, st))) return rc;
+    if ((rc = normalize_coefs_launch(B, R, ndof, Ly.nD, d_nbas, cb.qn, cb.qnc, st))) return rc;
+    std::swap(cb.q, cb.qn);
+    std::swap(cb.qc, cb.qnc);
+  }
+  MLCP_CUDA_TRY(cudaMemcpyAsync(eigv, cb.eigv, sizeof(double) * B, cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(base, cb.q, sizeof(double) * nvals, cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(coef, cb.qc, sizeof(double) * B * R, cudaMemcpyDeviceToHost, st));
+  std::vector<int> status(B + 4);
+  MLCP_CUDA_TRY(cudaMemcpyAsync(status.data(), cb.status, sizeof(int) * (B + 4), cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int i = 0; i < B + 2; ++i)
+    if (status[i]) {
+      set_error("diagonalizecpp_: %s (flag %d at %d)",
+                i == B + 1 ? "the overlap matrix was not positive definite"
+                           : (ndof == 2 ? "an SVD did not converge" : "a normal-equation matrix was not positive definite"),
+                status[i], i);
+      return kNumerical;
+    }
+  return kOk;
+}
+
 // Reference GetSpectralRange (src/Solver.f90:563-654), two-mode branch: each
 // of the two vectors runs PowrRecurse (src/BlockPower.f90:49-73) -- npow
 // times the exact product w = (H - shift) v (PRODHV with ishift = 1), its
@@ -749,6 +872,19 @@ extern "C" void getspectralrangecpp_(double* base, double* coef, int* nbas, cons
   }
   finish_status(rc);
   if (rc != kOk) fprintf(stderr, "getspectralrangecpp_: %s\n", last_error());
+}
+
+extern "C" void diagonalizecpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof,
+                                const int& nbloc, int* opid, int* mptr, double* Hcoef, double* mat, const int& TxD,
+                                const int& nops, const int& msize, double* eigv, const int& nals) {
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (ctx) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    rc = diagonalize(ctx, base, coef, nbas, rk, ndof, nbloc, opid, mptr, Hcoef, mat, TxD, nops, msize, eigv, nals);
+  }
+  finish_status(rc);
+  if (rc != kOk) fprintf(stderr, "diagonalizecpp_: %s\n", last_error());
 }
 
 extern "C" void sortvecscpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof, const int& nbloc,

@@ -296,6 +296,11 @@ int gep_launch(const GepParams& p, cudaStream_t st) {
   const int npairs = B * (B + 1) / 2;
   gep_inner_kernel<<<npairs, kPairThreads, 0, st>>>(p);
   MLCP_CUDA_TRY(cudaGetLastError());
+  return gep_solve_launch(p, st);
+}
+
+int gep_solve_launch(const GepParams& p, cudaStream_t st) {
+  const int B = p.nbloc;
   const int Bp = (B + 1) / 2 * 2;
   const size_t smem = sizeof(float) * ((size_t)2 * Bp * Bp + Bp) + sizeof(int) * Bp + 64;
   MLCP_CUDA_TRY(cudaFuncSetAttribute(gep_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

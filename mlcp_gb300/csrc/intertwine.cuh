@@ -105,6 +105,26 @@ struct RqParams {
 int rq_launch(const RqParams& p, cudaStream_t st);
 size_t rq_work_doubles(const OpTable& t);
 
+// The block's H and overlap matrices with H applied exactly (reference GetQHQ
+// and GetOverlaps, src/BlockUtils.f90:229-264, :347-381): A(i, j) =
+// <Q_j|H|Q_i>, S(i, j) = <Q_j|Q_i> for i >= j, column-major [nvec][nvec], in
+// FP64.  y: the operators applied to every factor (rq_apply_launch).
+struct RqPairParams {
+  OpTable ops;
+  int nvec, nD;
+  const double* base;
+  const double* coef;
+  const double* y;  // [nvec][utot][R][npmax]
+  double* A;
+  double* S;
+};
+int rq_apply_launch(const OpTable& t, int nvec, int nD, const double* base, double* y, cudaStream_t st);
+int rq_pair_launch(const RqPairParams& p, int smem_optin, cudaStream_t st);
+
+// The generalised eigensolver of the Rayleigh-Ritz step alone, on A and S
+// already formed (lower triangles).
+int gep_solve_launch(const GepParams& p, cudaStream_t st);
+
 // Two-mode reduction by SVD (reference reduc_SVDa/b, src/REDUCTIONML.f90:
 // 296-392): per vector, the nr x nc matrix A of a CP sum is formed, its SVD
 // computed, and the leading singular triplets written back as CP terms.
@@ -117,8 +137,9 @@ struct Svd2Params {
   double redtol;      // singular values below redtol * s_1 are dropped
   int normalize;      // 1: NORMCOEF the result (unit factors, unit norm)
   int K;              // input terms per vector
-  const double* in_base;  // hv = 0: [nvec][K][nr + nc]
+  const double* in_base;  // hv = 0: [nvec][K][nr + nc], or [K][nr + nc] for every vector (shared_base)
   const double* in_coef;  // hv = 0: [nvec][K]
+  int shared_base;        // hv = 0: every vector combines the same K terms with its own weights
   int hv;
   OpTable ops;            // hv = 1: the operator list (D = 2)
   const double* y;        // hv = 1: [nvec][utot][R][npmax] operators applied to v's factors

@@ -13,6 +13,8 @@
 //   <v|v>   = sum_ij c_i c_j prod_d M_d,0(i, j).
 // Everything is FP64, as in the reference: the work per vector is small and
 // the result is an eigenvalue estimate compared at the 1e-7 relative level.
+#include <algorithm>
+
 #include "common.cuh"
 #include "intertwine.cuh"
 
@@ -99,7 +101,127 @@ __global__ void __launch_bounds__(kRqThreads) rq_kernel(RqParams p) {
   if (threadIdx.x == 0) p.out[v] = num / den;
 }
 
+constexpr int kPairChunk = 128;  // (r, s) entries per pass of a pair CTA
+
+// y[v][g][s][a] = (h_g x_s^d)(a), d the mode of slot g (identity slots copy
+// the factor; entries a >= n_d are zero).
+__global__ void __launch_bounds__(256) rq_apply_kernel(OpTable t, int nvec, int nD, const double* base, double* y) {
+  const int R = t.R, npm = t.npmax;
+  const long long total = (long long)nvec * t.utot * R * npm;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int a = (int)(e % npm);
+    const long long q = e / npm;
+    const int r = (int)(q % R);
+    const long long q2 = q / R;
+    const int g = (int)(q2 % t.utot), v = (int)(q2 / t.utot);
+    const int d = slot_mode(t, g), n = t.nbas[d];
+    double acc = 0.0;
+    if (a < n) {
+      const double* x = base + ((size_t)v * R + r) * nD + t.off[d];
+      if (t.ident[g]) {
+        acc = x[a];
+      } else {
+        const double* h = t.hmat64 + (size_t)g * npm * npm + (size_t)a * npm;
+        for (int b = 0; b < n; ++b) acc = fma(h[b], x[b], acc);
+      }
+    }
+    y[e] = acc;
+  }
+}
+
+// One CTA per pair i >= j of the block:
+//   A(i, j) = <Q_j|H|Q_i> = sum_t alpha_t sum_rs c_j,r c_i,s prod_d M_d,op(t,d)(r, s)
+//   S(i, j) = <Q_j|Q_i>   = sum_rs c_j,r c_i,s prod_d M_d,0(r, s)
+// with M_g(r, s) = <q_j,r^d, h_g q_i,s^d> from the applied factors y.  Each
+// thread takes one (r, s) per pass and keeps its M values in a shared-memory
+// column ([utot][kPairChunk]); FP64, fixed-order block sums.
+__global__ void __launch_bounds__(kPairChunk) rq_pair_kernel(RqPairParams p) {
+  const OpTable& t = p.ops;
+  extern __shared__ double msm[];  // [utot][kPairChunk]
+  __shared__ double red[2][kPairChunk / 32];
+  const int e = blockIdx.x;
+  int i = (int)((sqrt(8.0 * e + 1.0) - 1.0) / 2.0);
+  while ((i + 1) * (i + 2) / 2 <= e) ++i;
+  while (i * (i + 1) / 2 > e) --i;
+  const int j = e - i * (i + 1) / 2;
+  const int R = t.R, RR = R * R, D = t.D, U = t.utot, npm = t.npmax, tid = threadIdx.x;
+  const double* qj = p.base + (size_t)j * R * p.nD;
+  const double* cj = p.coef + (size_t)j * R;
+  const double* ci = p.coef + (size_t)i * R;
+  const double* yi = p.y + (size_t)i * U * R * npm;
+  double* col = msm + tid;
+  double accA = 0.0, accS = 0.0;
+  for (int rs0 = 0; rs0 < RR; rs0 += kPairChunk) {
+    const int rs = rs0 + tid;
+    if (rs < RR) {
+      const int r = rs / R, sv = rs - r * R;
+      for (int g = 0; g < U; ++g) {
+        const int d = slot_mode(t, g), n = t.nbas[d];
+        const double* x = qj + (size_t)r * p.nD + t.off[d];
+        const double* yv = yi + ((size_t)g * R + sv) * npm;
+        double m = 0.0;
+        for (int a = 0; a < n; ++a) m = fma(x[a], yv[a], m);
+        col[(size_t)g * kPairChunk] = m;
+      }
+      const double cc = cj[r] * ci[sv];
+      double ps = cc;
+      for (int d = 0; d < D; ++d) ps *= col[(size_t)t.uoff[d] * kPairChunk];
+      accS += ps;
+      double pa = 0.0;
+      for (int tt = 0; tt < t.T; ++tt) {
+        double prod = t.alpha[tt];
+        for (int d = 0; d < D; ++d) prod *= col[(size_t)(t.uoff[d] + t.uid[(size_t)tt * D + d]) * kPairChunk];
+        pa += prod;
+      }
+      accA = fma(cc, pa, accA);
+    }
+  }
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    accA += __shfl_xor_sync(0xffffffffu, accA, o);
+    accS += __shfl_xor_sync(0xffffffffu, accS, o);
+  }
+  if (lane == 0) {
+    red[0][warp] = accA;
+    red[1][warp] = accS;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double a = 0.0, sv = 0.0;
+    for (int w = 0; w < kPairChunk / 32; ++w) {
+      a += red[0][w];
+      sv += red[1][w];
+    }
+    p.A[i + (size_t)j * p.nvec] = a;
+    p.S[i + (size_t)j * p.nvec] = sv;
+  }
+}
+
 }  // namespace
+
+int rq_apply_launch(const OpTable& t, int nvec, int nD, const double* base, double* y, cudaStream_t st) {
+  const long long total = (long long)nvec * t.utot * t.R * t.npmax;
+  const int blocks = (int)std::min<long long>((total + 255) / 256, 4096LL);
+  rq_apply_kernel<<<blocks, 256, 0, st>>>(t, nvec, nD, base, y);
+  MLCP_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+size_t rq_pair_smem(const OpTable& t) { return sizeof(double) * (size_t)t.utot * kPairChunk; }
+
+int rq_pair_launch(const RqPairParams& p, int smem_optin, cudaStream_t st) {
+  const size_t smem = rq_pair_smem(p.ops);
+  if (smem + 1024 > (size_t)smem_optin) {
+    set_error("the block's H matrix: %d distinct operators exceed the shared memory of one pair", p.ops.utot);
+    return kTooLarge;
+  }
+  MLCP_CUDA_TRY(cudaFuncSetAttribute(rq_pair_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long long npairs = (long long)p.nvec * (p.nvec + 1) / 2;
+  rq_pair_kernel<<<(unsigned)npairs, kPairChunk, smem, st>>>(p);
+  MLCP_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
 
 size_t rq_work_doubles(const OpTable& t) {
   return (size_t)t.utot * t.R * t.R + (size_t)t.utot * t.npmax * t.R;

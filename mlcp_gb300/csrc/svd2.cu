@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(256) svd2_form_kernel(Svd2Params p) {
   double acc = 0.0;
   if (!p.hv) {
     const int nD = p.nr + p.nc;
-    const double* b = p.in_base + (size_t)v * p.K * nD;
+    const double* b = p.in_base + (p.shared_base ? (size_t)0 : (size_t)v * p.K * nD);
     const double* c = p.in_coef + (size_t)v * p.K;
     for (int k = 0; k < p.K; ++k) acc = fma(c[k] * b[(size_t)k * nD + ia], b[(size_t)k * nD + p.nr + ib], acc);
   } else {

@@ -98,6 +98,29 @@ def spectral_range(base: np.ndarray, coef: np.ndarray, nbas, rk: int, hl, npow: 
     return base, coef, bounds
 
 
+def diagonalize(base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int, hl, nals: int):
+    """Reference Diagonalize with intw = .FALSE. (src/BlockUtils.f90:184-225)
+    through diagonalizecpp_ on copies: the exact block Rayleigh-Ritz problem
+    and the reduced eigenvector combinations.  Returns (base, coef, eigv)."""
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32).copy()
+    opid = np.ascontiguousarray(hl.opid, dtype=np.int32).copy()
+    mptr = np.ascontiguousarray(hl.mptr, dtype=np.int32).copy()
+    hcoef = np.ascontiguousarray(hl.coef, dtype=np.float64).copy()
+    mat = np.ascontiguousarray(hl.mat, dtype=np.float64).copy()
+    eigv = np.zeros(nbloc)
+    ints = [ctypes.c_int(x) for x in (rk, nb.size, nbloc, opid.size, mptr.size, mat.size, nals)]
+    L = _lib.load()
+    L.diagonalizecpp_(base.ctypes.data_as(_D), coef.ctypes.data_as(_D), nb.ctypes.data_as(_I),
+                      *[ctypes.byref(x) for x in ints[:3]], opid.ctypes.data_as(_I), mptr.ctypes.data_as(_I),
+                      hcoef.ctypes.data_as(_D), mat.ctypes.data_as(_D), *[ctypes.byref(x) for x in ints[3:6]],
+                      eigv.ctypes.data_as(_D), ctypes.byref(ints[6]))
+    if L.mlcp_gb300_last_status() != 0:
+        raise _lib.MlcpError(_lib.last_error())
+    return base, coef, eigv
+
+
 def update_opermat(imode: int, base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int,
                    xmats: np.ndarray) -> np.ndarray:
     """Reference UpdateOperMat (src/Updater.f90:110-151) through

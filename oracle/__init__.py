@@ -257,6 +257,58 @@ def spectral_range(base, coef, nbas, rk, hl, npow, ncyc):
     return base, coef, bounds
 
 
+def cp_dense(base, coef, nbas):
+    """The full tensor of a CP vector, flattened (mode 0 slowest)."""
+    nbas = [int(n) for n in nbas]
+    offs = np.concatenate([[0], np.cumsum(nbas)])
+    base = np.asarray(base, dtype=np.float64).reshape(-1, offs[-1])
+    coef = np.asarray(coef, dtype=np.float64).ravel()
+    out = np.zeros(int(np.prod(nbas)))
+    for r in range(coef.size):
+        t = np.array([coef[r]])
+        for d in range(len(nbas)):
+            t = np.multiply.outer(t, base[r, offs[d]:offs[d + 1]]).ravel()
+        out += t
+    return out
+
+
+def diagonalize_dense(base, coef, nbas, rk, nbloc, hl, nals=0):
+    """Reference Diagonalize with intw = .FALSE. (src/BlockUtils.f90:184-225)
+    on small cases through dense tensors: A = <Q_j|H|Q_i> and S = <Q_j|Q_i>
+    (GetQHQ, GetOverlaps, H exact), the generalised eigenproblem
+    (SolveGenEigval: ascending; each eigenvector scaled to X^T S X = I and its
+    largest-magnitude entry made positive, the library's convention), then
+    UpdateVecs (:437-475): for two modes the SVD reduction of
+    sum_i U(i, m) Q_i to at most rk terms and NORMCOEF; for more modes the
+    ALS update of the restated vector updates from the old vectors (nals
+    sweeps).  Returns (base, coef, eigv, U); for two modes base/coef list the
+    new vectors' (base, coef) pairs."""
+    import scipy.linalg
+    from mlcp_gb300 import hoplist as H
+    nD = int(np.sum(nbas))
+    base = np.asarray(base, dtype=np.float64).reshape(nbloc * rk, nD)
+    coef = np.asarray(coef, dtype=np.float64).ravel()
+    Qd = np.array([cp_dense(base[i * rk:(i + 1) * rk], coef[i * rk:(i + 1) * rk], nbas) for i in range(nbloc)])
+    Hd = H.dense_hamiltonian(hl)
+    A = Qd @ Hd @ Qd.T
+    S = Qd @ Qd.T
+    lam, U = scipy.linalg.eigh(0.5 * (A + A.T), 0.5 * (S + S.T))
+    for m in range(nbloc):
+        if U[np.argmax(np.abs(U[:, m])), m] < 0:
+            U[:, m] = -U[:, m]
+    if len(nbas) == 2:
+        vecs = []
+        for m in range(nbloc):
+            w = (U[:, m][:, None] * coef.reshape(nbloc, rk)).ravel()
+            b, c = reduc_svd(base, w, nbas, rk)
+            vecs.append(normcoef(b, c, nbas))
+        return vecs, None, lam, U
+    if nals > 0:
+        nb, nc = vector_updates(base, coef, nbas, rk, nbloc, U, nals)
+        return nb, nc, lam, U
+    return base.copy(), coef.copy(), lam, U
+
+
 def cp2d_dense(base, coef, nbas):
     """Reference CP2DtoMat (src/SepdRepn.f90:518-558): the nr x nc matrix
     sum_k c_k a_k b_k^T of a two-mode CP vector."""

@@ -322,3 +322,28 @@ def test_spectral_range_2mode_brackets(make):
     width = ex[-1] - ex[0]
     assert abs(hi - ex[-1]) < 1e-6 * width
     assert abs(lo - ex[0]) < 1e-6 * width
+
+
+def test_diagonalize_dense_restatement():
+    """Diagonalize restatement: a block of all the product functions of a
+    two-mode node (the solver's diag case) gives the exact spectrum, and the
+    SVD-reduced eigenfunctions are the exact eigenvectors (rank <= 3 = the
+    smaller mode, so the reduction is exact)."""
+    hl = H.random_hoplist([4, 3], 5, seed=9)
+    nb = [4, 3]
+    rk, B = 3, 12
+    base = np.full((B * rk, 7), 0.0)
+    coef = np.zeros(B * rk)
+    for a in range(4):
+        for b in range(3):
+            i = a * 3 + b
+            base[i * rk, a] = 1.0
+            base[i * rk, 4 + b] = 1.0
+            coef[i * rk] = 1.0
+    vecs, _, lam, U = oracle.diagonalize_dense(base, coef, nb, rk, B, hl)
+    Hd = H.dense_hamiltonian(hl)
+    ex, X = np.linalg.eigh(Hd)
+    np.testing.assert_allclose(lam, ex, rtol=1e-12, atol=1e-12)
+    for m in range(B):
+        v = oracle.cp_dense(*vecs[m], nb)
+        assert abs(abs(v @ X[:, m]) - 1.0) < 1e-10
