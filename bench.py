@@ -155,6 +155,24 @@ CYC_D, CYC_N, CYC_R, CYC_B, CYC_NPOW, CYC_NALS = 6, 10, 16, 40, 10, 10
 # combine 40-state modes); SVD reductions of 64 vectors of 16 x (20 + 1)
 # terms (the size of (H - E) v for a 20-term H).
 SVD_NBAS, SVD_T, SVD_NVEC = [40, 40], 20, 64
+# Pre-diagonalisation of a two-mode node whose block is all its product
+# functions (12 x 12 = 144 vectors: the solver's direct-diagonalisation case).
+DIAG_N = 12
+
+
+def diag_product_block(n, rk):
+    """Every product function of an n x n node as a rank-1 vector padded to
+    rank rk with zero weights."""
+    B = n * n
+    base = np.zeros((B * rk, 2 * n))
+    coef = np.zeros(B * rk)
+    for a in range(n):
+        for b in range(n):
+            i = a * n + b
+            base[i * rk, a] = 1.0
+            base[i * rk, n + b] = 1.0
+            coef[i * rk] = 1.0
+    return base, coef, B
 
 
 def cycle_inputs(seed=20261203):
@@ -238,6 +256,23 @@ def run_cycle_bench(steps: int, cpu: bool):
     out["reduc_svd_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
     out["workload_2mode"] = (f"two-mode quartic force field {SVD_NBAS[0]}x{SVD_NBAS[1]} ({h2.nterms} terms), "
                              f"rank {CYC_R}; reduc_svd: {SVD_NVEC} vectors of {rg} terms -> {CYC_R}")
+    # pre-diagonalisation (diagonalizecpp_): a two-mode node whose block is
+    # every product function (the solver's diag case, 12 x 12 = 144 states),
+    # and the 40-vector Henon-Heiles block with ALS updates
+    hd = H.synthetic_qff(2, DIAG_N, seed=6)
+    db, dc, nbd = diag_product_block(DIAG_N, CYC_R)
+    IT.diagonalize(db, dc, hd.nbas, CYC_R, nbd, hd, 0)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        IT.diagonalize(db, dc, hd.nbas, CYC_R, nbd, hd, 0)
+    out["diagonalize_2mode_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
+    IT.diagonalize(gb, gc, hl.nbas, CYC_R, CYC_B, hl, CYC_NALS)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        IT.diagonalize(gb, gc, hl.nbas, CYC_R, CYC_B, hl, CYC_NALS)
+    out["diagonalize_hh6_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
+    out["workload_diagonalize"] = (f"two-mode quartic force field {DIAG_N}x{DIAG_N}, all {nbd} product functions, "
+                                   f"rank {CYC_R}; Henon-Heiles block as the cycle with nals={CYC_NALS}")
     if cpu:
         oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
         t0 = time.perf_counter()
@@ -259,6 +294,9 @@ def run_cycle_bench(steps: int, cpu: bool):
         for v in range(SVD_NVEC):
             oracle.reduc_svd(svb[v * rg:(v + 1) * rg], svc[v * rg:(v + 1) * rg], SVD_NBAS, CYC_R)
         out["reduc_svd_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        oracle.diagonalize_dense(db, dc, hd.nbas, CYC_R, nbd, hd)
+        out["diagonalize_2mode_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
         out["cpu_cores"] = os.cpu_count()
         out["cpu_kind"] = "port"
         oracle.set_cycle_penalties()
