@@ -196,6 +196,14 @@ MLCP_API int mlcp_als_noalloc(int ndof, const int *nbas, int rF, int rG, double 
 MLCP_API void mlcp_gb300_set_kernel_timing(int enable);
 MLCP_API double mlcp_gb300_last_kernel_ms(void);
 
+/* Failure-path self-test (extension): a one-warp kernel sets up the batched
+ * ALS kernel's tile ring and waits, with that kernel's bounded wait, for a
+ * tile that is never issued.  The wait must give up after its iteration limit
+ * (tens of milliseconds); *flags_out receives the status bit the ALS kernel
+ * reports for such a vector (2) and the context stays usable.  No GPU fault,
+ * trap or hang is involved. */
+MLCP_API int mlcp_gb300_wait_selftest(int *flags_out);
+
 /* Full CP inner products out[v] = <X_v, Y_v> for nvec pairs of CP vectors in
  * the reference layout on the device (FP64 arithmetic), used for residuals
  * ||F - G|| = sqrt(<F,F> + <G,G> - 2<F,G>). */

@@ -50,6 +50,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mlcp_als_noalloc.argtypes = [ctypes.c_int, _I, ctypes.c_int, ctypes.c_int, _V, _V, ctypes.c_int, _V, _V]
         L.mlcp_cp_dot_batched.restype = ctypes.c_int
         L.mlcp_cp_dot_batched.argtypes = [ctypes.c_int, ctypes.c_int, _I, _LL, _I, _LL, _I, _V, _V, _V, _V]
+        L.mlcp_gb300_wait_selftest.restype = ctypes.c_int
+        L.mlcp_gb300_wait_selftest.argtypes = [_I]
         L.mlcp_gb300_set_kernel_timing.restype = None
         L.mlcp_gb300_set_kernel_timing.argtypes = [ctypes.c_int]
         L.mlcp_gb300_last_kernel_ms.restype = ctypes.c_double

@@ -1084,6 +1084,66 @@ bool als_choose_shape(int nvec, int rGmax, int rFmax, int npmax, int gsmax, int 
   }
 }
 
+namespace {
+
+// Failure-path self-test of the pipeline wait: one warp sets up a one-stage
+// ring exactly as the cluster kernel does and waits for a tile that nobody
+// issues.  wait_tile must give up after its iteration limit and raise the
+// abort flag; out[0] receives the status bit the cluster kernel would report
+// (2), out[1] whether the wait returned false.
+__global__ void als_wait_selftest_kernel(int* out) {
+  __shared__ __align__(8) uint64_t bar[1];
+  __shared__ int done[1], issued[1], flags[8];
+  __shared__ unsigned fillno[1];
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    done[0] = 0;
+    issued[0] = 0;
+    fillno[0] = 0xffffffffu;
+  }
+  if (threadIdx.x < 8) flags[threadIdx.x] = 0;
+  __syncwarp();
+  Cta c{};
+  c.tid = threadIdx.x;
+  c.lane = threadIdx.x & 31;
+  c.stages = 1;
+  c.bar = bar;
+  c.done = done;
+  c.issued = issued;
+  c.fillno = fillno;
+  c.flags = flags;
+  const bool got = wait_tile(c, 0u);
+  __syncwarp();
+  if (threadIdx.x == 0) {
+    out[0] = flags[0] ? 2 : 0;
+    out[1] = got ? 0 : 1;
+  }
+}
+
+}  // namespace
+
+int als_wait_selftest(cudaStream_t st, int* flags_out) {
+  int* d = nullptr;
+  MLCP_CUDA_TRY(cudaMalloc(&d, 2 * sizeof(int)));
+  als_wait_selftest_kernel<<<1, 32, 0, st>>>(d);
+  cudaError_t e = cudaGetLastError();
+  int h[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    set_error("wait self-test failed: %s", cudaGetErrorString(e));
+    return kCudaError;
+  }
+  if (!h[1]) {
+    set_error("wait self-test: the wait for a tile that was never issued reported success");
+    return kNumerical;
+  }
+  *flags_out = h[0];
+  return kOk;
+}
+
 int als_launch(const AlsParams& p, size_t smem, cudaStream_t st, cudaEvent_t t0, cudaEvent_t t1) {
   int dev = 0, nsm = 0;
   MLCP_CUDA_TRY(cudaGetDevice(&dev));

@@ -105,5 +105,8 @@ struct AlsJob {
 // When t0/t1 are non-null they are recorded around the cluster kernel.
 int als_launch(const AlsParams& p, size_t smem, cudaStream_t st, cudaEvent_t t0 = nullptr,
                cudaEvent_t t1 = nullptr);
+// Failure-path self-test of the cluster kernel's bounded tile wait: a wait
+// for a tile nobody issues must give up and report the abort status (2).
+int als_wait_selftest(cudaStream_t st, int* flags_out);
 
 }  // namespace mlcp

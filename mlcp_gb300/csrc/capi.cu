@@ -35,6 +35,10 @@ const char* last_error() { return t_error.c_str(); }
 static int finish(int status) {
   t_status = status;
   if (status == kOk) t_error.clear();
+  // a failed call leaves no stale runtime error behind (a refused allocation
+  // would otherwise surface at the next call's launch check); errors that
+  // poison the context persist whatever is read here
+  if (status == kCudaError) (void)cudaGetLastError();
   return status;
 }
 int finish_status(int status) { return finish(status); }
@@ -438,6 +442,18 @@ int cp_dot_device(Context* ctx, int nvec, int ndof, const int* nbas, const long 
 using namespace mlcp;
 
 extern "C" const char* mlcp_gb300_last_error(void) { return last_error(); }
+
+extern "C" int mlcp_gb300_wait_selftest(int* flags_out) {
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (!ctx) return finish(rc);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!flags_out) {
+    set_error("mlcp_gb300_wait_selftest: null output");
+    return finish(kBadArgument);
+  }
+  return finish(als_wait_selftest(ctx->stream, flags_out));
+}
 
 extern "C" void mlcp_gb300_set_kernel_timing(int enable) {
   int rc = kOk;
