@@ -50,6 +50,8 @@ namespace {
 
 constexpr int kSvdThreads = 1024;
 constexpr int kSvdWarps = kSvdThreads / 32;
+constexpr int kPairLanes = 16;                  // lanes per column pair in the sweeps
+constexpr int kGroupsPerWarp = 32 / kPairLanes;
 constexpr int kMaxN = 256;       // min(nr, nc)
 constexpr int kMaxM = 4096;      // max(nr, nc)
 constexpr int kMaxSweeps = 40;
@@ -160,9 +162,20 @@ __device__ __forceinline__ dw warp_sum_dw(dw v) {
   return v;
 }
 
-// x <- c x - s y, y <- s x + c y over n entries (lane-strided)
+// The same over the kPairLanes lanes of a pair group (xor offsets below the
+// group width stay inside the group).
+__device__ __forceinline__ dw group_sum_dw(dw v) {
+#pragma unroll
+  for (int o = kPairLanes / 2; o > 0; o >>= 1) {
+    const dw w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = dw_add_sloppy(v, w);
+  }
+  return v;
+}
+
+// x <- c x - s y, y <- s x + c y over n entries (strided by the pair group)
 __device__ __forceinline__ void rotate_cols(dw* x, dw* y, int n, dw c, dw s, int lane) {
-  for (int i = lane; i < n; i += 32) {
+  for (int i = lane; i < n; i += kPairLanes) {
     const dw xi = x[i], yi = y[i];
     x[i] = dw_add_sloppy(dw_mul(c, xi), dw_neg(dw_mul(s, yi)));
     y[i] = dw_add_sloppy(dw_mul(s, xi), dw_mul(c, yi));
@@ -208,6 +221,31 @@ __global__ void __launch_bounds__(kSvdThreads) svd2_jacobi_kernel(Svd2Params p) 
   }
   for (int e = tid; e < n2 * n2; e += kSvdThreads) V[e] = dw{(e % n2 == e / n2) ? 1.f : 0.f, 0.f};
   __syncthreads();
+  // Columns whose norm falls below skip = 0.01 redtol / sqrt(n) of the
+  // largest starting column norm take no further rotations: together they
+  // span singular values below 0.01 redtol s_1 (s_1 is at least the largest
+  // column norm), which the rank cut drops, and leaving them unorthogonalised
+  // moves the kept singular values by less than that.  A low-rank input
+  // (the usual H v) would otherwise spend most sweeps rotating rounding noise.
+  float cmax = 0.f;
+  for (int j = warp; j < n; j += kSvdWarps) {
+    const dw* x = M + (size_t)j * m;
+    float a = 0.f;
+    for (int i = lane; i < m; i += 32) a = fmaf(x[i].hi, x[i].hi, a);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    cmax = fmaxf(cmax, a);
+  }
+  if (lane == 0) red[warp] = (double)cmax;
+  __syncthreads();
+  float tiny = kTinySq;
+  {
+    double mx = 0.0;
+    for (int w = 0; w < kSvdWarps; ++w) mx = fmax(mx, red[w]);
+    const double rel = 0.01 * p.redtol / sqrt((double)n);
+    tiny = fmaxf(tiny, (float)(rel * rel * mx));
+  }
+  __syncthreads();
 
   // rotate while |x.y| > sqrt(m) 2^-46 |x| |y|: about the orthogonality that
   // double-word columns can hold, reached in the same number of sweeps as a
@@ -218,34 +256,39 @@ __global__ void __launch_bounds__(kSvdThreads) svd2_jacobi_kernel(Svd2Params p) 
     if (tid == 0) flag = 0;
     __syncthreads();
     for (int k = 0; k < n2 - 1; ++k) {
-      for (int q = warp; q < n2 / 2; q += kSvdWarps) {
-        int a, b;
+      // a group of kPairLanes lanes per column pair, two pairs per warp
+      // instruction; every lane of a warp runs the same number of slots so
+      // that the group shuffles stay converged
+      for (int q0 = warp * kGroupsPerWarp; q0 < n2 / 2; q0 += kSvdWarps * kGroupsPerWarp) {
+        const int q = q0 + lane / kPairLanes, gl = lane % kPairLanes;
+        const bool live = q < n2 / 2;
+        int a = 0, b = 0;
         if (q == 0) {
           a = n2 - 1;
           b = k;
-        } else {
+        } else if (live) {
           a = (k + q) % (n2 - 1);
           b = (k - q + n2 - 1) % (n2 - 1);
         }
         dw* x = M + (size_t)a * m;
         dw* y = M + (size_t)b * m;
         dw_acc aa = acc_zero(), ab = acc_zero(), ag = acc_zero();
-        for (int i = lane; i < m; i += 32) {
+        for (int i = gl; live && i < m; i += kPairLanes) {
           const dw xi = x[i], yi = y[i];
           acc_fma(aa, xi, xi);
           acc_fma(ab, yi, yi);
           acc_fma(ag, xi, yi);
         }
-        const dw al = warp_sum_dw(acc_value(aa)), be = warp_sum_dw(acc_value(ab)), ga = warp_sum_dw(acc_value(ag));
-        // columns below 2^-50 of the largest entry stay as they are: they
-        // cannot move a singular value above the rank cut
-        if (al.hi > kTinySq && be.hi > kTinySq &&
-            fabsf(ga.hi) > tol * __fsqrt_rn(al.hi) * __fsqrt_rn(be.hi)) {
+        const dw al = group_sum_dw(acc_value(aa)), be = group_sum_dw(acc_value(ab)),
+                 ga = group_sum_dw(acc_value(ag));
+        // columns below the skip norm (or 2^-50 of the largest entry) stay
+        // as they are: they cannot move a singular value above the rank cut
+        if (live && al.hi > tiny && be.hi > tiny && fabsf(ga.hi) > tol * __fsqrt_rn(al.hi) * __fsqrt_rn(be.hi)) {
           dw c, s;
           jacobi_rotation(al, be, ga, &c, &s);
-          rotate_cols(x, y, m, c, s, lane);
-          rotate_cols(V + (size_t)a * n2, V + (size_t)b * n2, n2, c, s, lane);
-          if (lane == 0) flag = 1;
+          rotate_cols(x, y, m, c, s, gl);
+          rotate_cols(V + (size_t)a * n2, V + (size_t)b * n2, n2, c, s, gl);
+          if (gl == 0) flag = 1;
         }
       }
       __syncthreads();
