@@ -148,6 +148,18 @@ __device__ dw block_sum(dw v, dw* red) {
   return s;
 }
 
+// block_sum without its leading barrier, for callers after which no thread
+// can still be reading red from an earlier sum (many barriers since).
+__device__ dw block_sum_ready(dw v, dw* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) v = dw_add(v, dwsolve::dw_shfl_xor(v, o));
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  dw s = red[lane & (kGsWarps - 1)];
+  for (int o = kGsWarps / 2; o > 0; o >>= 1) s = dw_add(s, dwsolve::dw_shfl_xor(s, o));
+  return s;
+}
+
 struct Gs {
   GsArrays a;
   int R, RR, RRp, D, nD, npm, CL, rank, tid;
@@ -242,7 +254,7 @@ __device__ void finish_vector(const Gs& c, const GsParams& p, int iv, bool facto
 // wf(r,m) = c_r F_r^j(m), and per warp of psn entries the partial sums of
 // c_k,r c_i P_k(r,i) over all modes (the coefficients <Q_k, F>).
 // Threads t0..511 (t0 a multiple of 32); ends with a barrier over them.
-__device__ void step_products(const Gs& c, int j, int nk, bool pre, int t0) {
+__device__ void step_products(const Gs& c, int j, int nk, bool pre, int t0, dw qinv) {
   const int R = c.R, RR = c.RR, RRp = c.RRp, D = c.D, nj = c.a.nb[j], offj = c.a.off[j];
   const int npsn = nk * RRp, ngp = npsn + (pre ? 0 : RR), total = ngp + R * nj;
   const dw pen = c.a.misc[0];
@@ -253,7 +265,7 @@ __device__ void step_products(const Gs& c, int j, int nk, bool pre, int t0) {
       if (ee < RR) {
         const int r = ee / R, i = ee - r * R;
         const dw* Pk = c.a.P + (size_t)kl * D * RR + ee;
-        const dw pj = Pk[(size_t)j * RR], w = dw_mul(c.a.qc[(size_t)kl * R + r], c.a.fcs[i]);
+        const dw pj = Pk[(size_t)j * RR], w = dw_mul(c.a.qc[(size_t)kl * R + r], dw_mul(c.a.fcs[i], qinv));
         dw prod;
         if (pre) {
           prod = c.a.psn[(size_t)kl * RR + ee];
@@ -276,7 +288,7 @@ __device__ void step_products(const Gs& c, int j, int nk, bool pre, int t0) {
       c.a.BB[ee] = (ee % R == ee / R) ? dw_add(prod, pen) : prod;
     } else {
       const int ee = e - ngp, r = ee % R, m = ee / R;
-      c.a.wf[ee] = dw_mul(c.a.fcs[r], c.a.fb[(size_t)r * c.nD + offj + m]);
+      c.a.wf[ee] = dw_mul(dw_mul(c.a.fcs[r], qinv), c.a.fb[(size_t)r * c.nD + offj + m]);
     }
   }
   if (t0 == 0) __syncthreads();
@@ -392,7 +404,7 @@ __device__ void step_preproducts(const Gs& c, int j, int jn, int nk, int t0, int
 // psn, Gp and BB (mode jn) completed by multiplying in mode j.  Then the
 // weights are divided by sqrt(<F,F>), whose terms c_i c_i' prod_d G_d(i,i')
 // come with the new Gram.
-__device__ void step_update(const Gs& c, int j, int jn, int nk, bool pre) {
+__device__ dw step_update(const Gs& c, int j, int jn, int nk, bool pre) {
   const int R = c.R, RR = c.RR, nj = c.a.nb[j], offj = c.a.off[j], Rn = R * nj;
   const int total = Rn + RR + nk * RR;
   const dw pen = c.a.misc[0];
@@ -434,9 +446,11 @@ __device__ void step_update(const Gs& c, int j, int jn, int nk, bool pre) {
       if (pre) c.a.psn[(size_t)kl * RR + e2] = dw_mul(pre_k, s);
     }
   }
-  const dw q = dw_sqrt(dw_abs(block_sum(qpart, c.a.red)));  // every thread has read fcs
-  for (int i = c.tid; i < R; i += kGsThreads) c.a.fcs[i] = dw_div(c.a.fcs[i], q);
-  __syncthreads();
+  // 1 / sqrt(<F,F>) for every thread: the next step's products apply it to
+  // the weights as they read them (the solve then writes new weights), so
+  // the weights need no rewrite and no barrier of their own here; the sum's
+  // barrier also orders every write above before the next phase
+  return dw_rcp(dw_sqrt(dw_abs(block_sum_ready(qpart, c.a.red))));
 }
 
 }  // namespace
@@ -478,6 +492,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
     const int nk = (iv - c.rank + c.CL - 1) / c.CL;  // owned k = rank, rank + CL, ... < iv
     all_overlaps(c, nk);
     bool pre = false;
+    dw qinv = dw_make(1.f);  // 1 / |F| not yet applied to the weights (see step_update)
     for (int it = 0; it < p.nals; ++it) {
       for (int j = 0; j < c.D; ++j, ++step) {
         dw* bp = c.a.bpart + (size_t)(step & 1) * c.R * c.npm;
@@ -491,7 +506,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
         const float* inv = c.a.gi;
         const int w0 = c.R <= 32 ? 32 : dwsolve::kSolverThreads;
         const bool early = pre && c.R <= 32;
-        if (!early) step_products(c, j, nk, pre, 0);
+        if (!early) step_products(c, j, nk, pre, 0, qinv);
         if (c.tid < w0) {
           if (c.R > 32) {
             inv = dwsolve::gj_inverse(c.a.BB, c.R, c.a.gi, &gj_ok);
@@ -500,7 +515,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
             if (c.tid == 0) c.a.flags[2] = good;
           }
         } else {
-          if (early) step_products(c, j, nk, pre, w0);
+          if (early) step_products(c, j, nk, pre, w0, qinv);
           step_dots(c, j, nk, w0);
           step_rhs_part(c, j, nk, bp, w0);
         }
@@ -540,10 +555,12 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
           step_preproducts(c, j, jn, nk, c.tid, kGsThreads);
           __syncthreads();
         }
-        step_update(c, j, jn, nk, more);
+        qinv = step_update(c, j, jn, nk, more);
         pre = more;
       }
     }
+    for (int i = c.tid; i < c.R; i += kGsThreads) c.a.fcs[i] = dw_mul(c.a.fcs[i], qinv);
+    __syncthreads();
     finish_vector(c, p, iv, true);
   }
   if (c.rank == 0 && c.tid == 0 && c.a.flags[1]) atomicOr(p.status, 1);
