@@ -37,6 +37,17 @@ METRIC = "ALS reductions/s"
 UNIT = "reductions/s"
 
 
+def max_over_ranks(x: float, dist=None, device=None) -> float:
+    """The largest x over the ranks of the process group (x itself without
+    one): every timing of a replicated run is the slowest rank's."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -355,10 +366,7 @@ def run_gpu(args):
     barrier()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop() if clocks else None
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist, dev)
     value = NVEC * ws * args.steps / (ms / 1e3)
 
     # dominant-kernel timing (cluster ALS kernel) on the launching stream
@@ -391,6 +399,8 @@ def run_gpu(args):
     for _ in range(args.steps):
         e2e_step()
     e2e_s = time.perf_counter() - t0
+    barrier()
+    e2e_s = max_over_ranks(e2e_s, dist, dev)
     h2d = int(batch.coef.nbytes + batch.base.nbytes)
     d2h = int(NVEC * RF * (batch.nD + 1) * 8)
     e2e_value = NVEC * ws * args.steps / e2e_s
