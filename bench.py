@@ -169,6 +169,8 @@ SVD_NBAS, SVD_T, SVD_NVEC = [40, 40], 20, 64
 # Pre-diagonalisation of a two-mode node whose block is all its product
 # functions (12 x 12 = 144 vectors: the solver's direct-diagonalisation case).
 DIAG_N = 12
+# Power cycles of the solver loop measured to convergence against Lanczos.
+SOLVE_CYCLES = 60
 
 
 def diag_product_block(n, rk):
@@ -282,6 +284,21 @@ def run_cycle_bench(steps: int, cpu: bool):
     for _ in range(steps):
         IT.diagonalize(gb, gc, hl.nbas, CYC_R, CYC_B, hl, CYC_NALS)
     out["diagonalize_hh6_gpu_ms"] = 1e3 * (time.perf_counter() - t0) / steps
+    # the solver loop to convergence (SolveHPsi with the GPU cycle): 60
+    # cycles from the product-function guess, eigenvalues against the
+    # Lanczos values of the full 10^6 basis
+    from mlcp_gb300 import solver
+    t0 = time.perf_counter()
+    _, _, seig, _, shist = solver.solve(hl, CYC_B, CYC_R, SOLVE_CYCLES, CYC_NPOW, CYC_NALS)
+    s_sec = time.perf_counter() - t0
+    with open(os.path.join(ROOT, "tests", "golden", "hh6_n10_lowest40.json")) as f:
+        ex = np.array(json.load(f)["eigenvalues"])
+    serr = seig - ex
+    out["solver"] = {"cycles": SOLVE_CYCLES, "seconds": s_sec, "e0_abs_error": float(serr[0]),
+                     "max_abs_error_0_1_quanta": float(np.abs(serr[:7]).max()),
+                     "max_abs_error_0_2_quanta": float(np.abs(serr[:28]).max()),
+                     "max_abs_error_all_40": float(np.abs(serr).max()), "last_rms_change": shist[-1],
+                     "reference": "ARPACK Lanczos, full 10^6 basis (tests/golden/hh6_n10_lowest40.json)"}
     out["workload_diagonalize"] = (f"two-mode quartic force field {DIAG_N}x{DIAG_N}, all {nbd} product functions, "
                                    f"rank {CYC_R}; Henon-Heiles block as the cycle with nals={CYC_NALS}")
     if cpu:
