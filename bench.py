@@ -299,6 +299,20 @@ def run_cycle_bench(steps: int, cpu: bool):
                      "max_abs_error_0_2_quanta": float(np.abs(serr[:28]).max()),
                      "max_abs_error_all_40": float(np.abs(serr).max()), "last_rms_change": shist[-1],
                      "reference": "ARPACK Lanczos, full 10^6 basis (tests/golden/hh6_n10_lowest40.json)"}
+    # the benchmark's whole tree (three two-mode nodes of 30 states, a
+    # three-mode top layer of 40 states; ncycle = npow = nals = 10, rank 16),
+    # every solve and operator update on the GPU, against the same Lanczos values
+    from mlcp_gb300 import tree
+    t0 = time.perf_counter()
+    teig, tinfo = tree.hh_tree(D=CYC_D, n=CYC_N, keep=30, top_nev=CYC_B, rk=CYC_R, ncycle=10, npow=CYC_NPOW,
+                               nals=CYC_NALS)
+    terr = teig - ex
+    out["tree"] = {"workload": "Henon-Heiles D=6 n=10, tree (0 1)(2 3)(4 5) keeping 30 states each / top 40 states, "
+                               "rank 16, ncycle=npow=nals=10", "seconds": time.perf_counter() - t0,
+                   "e0_abs_error": float(terr[0]), "max_abs_error_0_1_quanta": float(np.abs(terr[:7]).max()),
+                   "max_abs_error_0_2_quanta": float(np.abs(terr[:28]).max()),
+                   "max_abs_error_all_40": float(np.abs(terr).max()),
+                   "reference": "ARPACK Lanczos, full 10^6 basis (tests/golden/hh6_n10_lowest40.json)"}
     out["workload_diagonalize"] = (f"two-mode quartic force field {DIAG_N}x{DIAG_N}, all {nbd} product functions, "
                                    f"rank {CYC_R}; Henon-Heiles block as the cycle with nals={CYC_NALS}")
     if cpu:

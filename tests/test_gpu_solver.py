@@ -47,3 +47,21 @@ def test_solver_converges_to_lanczos(cuda_device):
     assert np.abs(err).max() < 0.15, np.abs(err).max()
     assert err.min() > -1e-6, err.min()
     assert hist[-1] < 1e-3
+
+
+@pytest.mark.gpu
+def test_tree_matches_lanczos(cuda_device):
+    """The benchmark's tree -- pairs (0 1)(2 3)(4 5) solved for 30 states each
+    by the GPU solver loop, their coupling operators carried into the pair
+    bases by updateopermatcpp_, a three-mode top layer solved for 40 states --
+    against the full-basis Lanczos values: with the configuration's 10 cycles
+    per layer the ground state lands within 5e-5, the one-quantum states
+    within 2e-4 and the two-quanta states within 2e-3 (tree contraction and
+    rank 16 together)."""
+    from mlcp_gb300 import tree
+    eig, info = tree.hh_tree(D=6, n=10, keep=30, top_nev=40, rk=16, ncycle=10, npow=10, nals=10)
+    err = eig - exact()
+    assert abs(err[0]) < 5e-5, err[0]
+    assert np.abs(err[:7]).max() < 2e-4, err[:7]
+    assert np.abs(err[:28]).max() < 2e-3, np.abs(err[:28]).max()
+    assert len(info["pairs"]) == 3
