@@ -50,6 +50,32 @@ def spectral_start(nbas, rk: int, seed: int = 0):
     return base, coef
 
 
+def _with_quanta(nbas, q, prefix=()):
+    """Index tuples over the modes with total q, in lexicographic order."""
+    d = len(prefix)
+    if d == len(nbas):
+        if q == 0:
+            yield prefix
+        return
+    rest = sum(n - 1 for n in nbas[d + 1:])
+    for i in range(max(0, q - rest), min(q, nbas[d] - 1) + 1):
+        yield from _with_quanta(nbas, q - i, prefix + (i,))
+
+
+def _lowest_products(nbas, nev):
+    """The nev product states of lowest total quanta (ties lexicographic),
+    generated shell by shell rather than from the whole product space."""
+    out = []
+    for q in itertools.count():
+        if q > sum(n - 1 for n in nbas):
+            break
+        for st in _with_quanta(nbas, q):
+            out.append(st)
+            if len(out) == nev:
+                return out
+    return out
+
+
 def product_guess(nbas, nev: int, rk: int, seed: int = 0):
     """nev product functions of lowest total quanta (ties in lexicographic
     order) as rank-rk vectors: the product term with weight 1, then rk - 1
@@ -57,7 +83,7 @@ def product_guess(nbas, nev: int, rk: int, seed: int = 0):
     nbas = [int(n) for n in nbas]
     offs = np.concatenate([[0], np.cumsum(nbas)])
     nD = int(offs[-1])
-    states = sorted(itertools.product(*[range(n) for n in nbas]), key=lambda s: (sum(s), s))[:nev]
+    states = _lowest_products(nbas, nev)
     rng = np.random.default_rng(seed)
     base = np.zeros((nev * rk, nD))
     coef = np.zeros(nev * rk)

@@ -65,3 +65,17 @@ def test_tree_matches_lanczos(cuda_device):
     assert np.abs(err[:7]).max() < 2e-4, err[:7]
     assert np.abs(err[:28]).max() < 2e-3, np.abs(err[:28]).max()
     assert len(info["pairs"]) == 3
+
+
+def test_product_guess_order():
+    """The starting block takes the product states of lowest total quanta,
+    ties in lexicographic order, generated shell by shell (no enumeration of
+    the product space: 8^24 states at the third configuration's shape)."""
+    import itertools
+    for nb, nev in [([4, 3, 5], 30), ([6, 6, 6], 40), ([3, 3], 9)]:
+        want = sorted(itertools.product(*[range(n) for n in nb]), key=lambda s: (sum(s), s))[:nev]
+        assert solver._lowest_products(nb, nev) == want
+    st = solver._lowest_products([8] * 24, 100)
+    assert len(st) == 100 and sum(st[-1]) == 2
+    base, coef = solver.product_guess([8] * 24, 100, 30)
+    assert base.shape == (3000, 192) and coef[0] == 1.0 and coef[1] == 1e-12
