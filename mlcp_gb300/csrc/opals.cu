@@ -117,6 +117,25 @@ __device__ dw block_sum_dw(dw v, dw* red) {
   return s;
 }
 
+// In-place POW applies (H - E) once per mode step, so within a sweep the
+// weights grow (or shrink) by about ||H - E|| per step: a 12-mode quartic
+// force field in cm^-1 passes the FP32 exponent range after nine steps, and a
+// 400-term random Hamiltonian over 24 modes overflows the squared row norms
+// (weights above 1.8e19).  The end-of-sweep renormalisation divides out any
+// common factor, so after each step the weights are multiplied by the power
+// of two that brings the largest into [0.5, 1): exact, and the solve is linear
+// in the weights, so the sweep's result is unchanged.  Warp 0 only; each lane
+// rescales the entries it read.
+__device__ void rescale_weights_warp(dw* cf, int R) {
+  float m = 0.f;
+  for (int i = threadIdx.x; i < R; i += 32) m = fmaxf(m, fabsf(cf[i].hi));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (!(m > 0.f && m <= 3.4028235e38f)) return;  // zero, or non-finite (reported by the next solve)
+  int e;
+  frexpf(m, &e);
+  for (int i = threadIdx.x; i < R; i += 32) cf[i] = dw_make(ldexpf(cf[i].hi, -e), ldexpf(cf[i].lo, -e));
+}
+
 // M(r,i) = sum_n (h Fo_r^d)(n) F_i^d(n); identity operators skip the product.
 __device__ void operator_gram(const OpTable& t, int d, int ug, const OpSmem& s, float* M, float* zout) {
   const int R = t.R, n = t.nbas[d], op = t.offp[d], npm = t.npmax;
@@ -345,8 +364,13 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
         }
         __syncthreads();
       }
-      // -- the new factor: FP64 output, FP32 copy, double-word Gram --
-      for (int i = threadIdx.x; i < R; i += blockDim.x) fc[i] = dw_to_double(s.cf[i]);
+      // -- the new factor: FP64 output, FP32 copy, double-word Gram (warp 0
+      //    rescales the POW weights first; no other thread reads them before
+      //    the next barrier) --
+      if (threadIdx.x < 32) {
+        if (pow_mode) rescale_weights_warp(s.cf, R);
+        for (int i = threadIdx.x; i < R; i += 32) fc[i] = dw_to_double(s.cf[i]);
+      }
       for (int e = threadIdx.x; e < R * nj; e += blockDim.x) {
         const int i = e / nj, m = e % nj;
         const dw x = s.X[i + m * R];
