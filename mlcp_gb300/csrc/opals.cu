@@ -20,7 +20,9 @@
 // to 1e10 and the CP weights blow up over successive cycles.  The R x R normal equations
 // (prod_{d!=j} F_d F_d^T + pen I), their Cholesky solve, the F Grams and the
 // weight normalisation run in FP64; the operator Grams, term products and
-// right-hand sides run in FP32.
+// right-hand sides run in FP32.  In POW the weights are rescaled by a power
+// of two after every mode step (rescale_weights_warp), which keeps them in
+// the FP32 exponent range without changing the sweep's result.
 #include "common.cuh"
 #include "dword.cuh"
 #include "dwsolve.cuh"

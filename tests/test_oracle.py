@@ -347,3 +347,21 @@ def test_diagonalize_dense_restatement():
     for m in range(B):
         v = oracle.cp_dense(*vecs[m], nb)
         assert abs(abs(v @ X[:, m]) - 1.0) < 1e-10
+
+
+@pytest.mark.parametrize("ishift,esh", [(1, 6.0), (-1, 1.5)])
+def test_pow_sweep_is_scale_free(ishift, esh):
+    """The in-place power sweep fits (H - E) F and renormalises the weights at
+    the end of each sweep, so scaling H and E by a power of two (2^40) leaves
+    its output bit-identical in FP64.  The GPU sweep's weight rescaling relies
+    on exactly this invariance (its test compares H with 2^40 H)."""
+    hl = H.henon_heiles(D=4, n=6)
+    big = H.HopList(nbas=hl.nbas, opid=hl.opid, mptr=hl.mptr, coef=hl.coef * 2.0 ** 40, mat=hl.mat)
+    rk, nbloc = 6, 3
+    rng = np.random.default_rng(5)
+    Q = rng.uniform(-0.5, 0.5, size=(rk * nbloc, int(np.sum(hl.nbas))))
+    qc = np.ones(rk * nbloc)
+    a = oracle.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, np.zeros(nbloc), 3, 0, False, ishift, esh)
+    b = oracle.intertwine(Q, qc, hl.nbas, rk, nbloc, big, np.zeros(nbloc), 3, 0, False, ishift, esh * 2.0 ** 40)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
