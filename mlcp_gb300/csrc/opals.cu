@@ -18,8 +18,10 @@
 // (1e-5 max c, src/als.cu:248-267): with the FP64 rule (1e-10) the rounding
 // noise in near-null directions of the normal equations is amplified by up
 // to 1e10 and the CP weights blow up over successive cycles.  The R x R normal equations
-// (prod_{d!=j} F_d F_d^T + pen I), their Cholesky solve, the F Grams and the
-// weight normalisation run in FP64; the operator Grams, term products and
+// (prod_{d!=j} F_d F_d^T + pen I), their solve (FP32 inverse with
+// double-word refinement, or a double-word LDL^T), the F Grams and the weight
+// normalisation run in double-word (float-float, about 48 bits; the factors
+// are written out in FP64); the operator Grams, term products and
 // right-hand sides run in FP32.  In POW the weights are rescaled by a power
 // of two after every mode step (rescale_weights_warp), which keeps them in
 // the FP32 exponent range without changing the sweep's result.
