@@ -117,6 +117,16 @@ def test_cycle_rejects_bad_operator_index(cuda_device):
         IT.intertwine(Q, qc, hl.nbas, 2, 2, bad, np.zeros(2), 2, 2, True, 1, 1.0)
 
 
+@pytest.mark.gpu
+def test_cycle_rejects_block_above_rayleigh_ritz_limit(cuda_device):
+    """The one-CTA Rayleigh-Ritz solve takes at most 160 vectors; a larger
+    block with update = T is an error return (checked before any device work)."""
+    hl = H.random_hoplist([4, 3], 3, seed=1)
+    Q, qc = start_block(hl.nbas, 2, 161, seed=0)
+    with pytest.raises(Exception, match="160 vectors"):
+        IT.intertwine(Q, qc, hl.nbas, 2, 161, hl, np.zeros(161), 1, 1, True, 1, 1.0)
+
+
 QHQ_CASES = [
     # (hoplist factory, rk, nbloc, nconv)
     (lambda: H.henon_heiles(D=3, n=5), 4, 6, 0),
