@@ -65,8 +65,8 @@ MLCP_API void intertwinecpp_(double *base, double *coef, int *nbas, MLCP_REF(int
 MLCP_API void alscpp_(double *coef, double *base, int *nbas, MLCP_REF(int) ndof, MLCP_REF(int) rF, MLCP_REF(int) rG,
              MLCP_REF(int) nals);
 
-/* ---- The update = F path (reference CPU routines; Fortran binding in
- * INTEGRATION.md) --------------------------------------------------------- */
+/* ---- The update = F path (reference CPU routines, called from the Fortran
+ * host through a bind(C) interface) ---------------------------------------- */
 
 /* Replaces GetQHQdiag (src/BlockUtils.f90:385-408) with RayleighQuotient2
  * (:658-688), which the reference's host runs on the CPU after
@@ -177,15 +177,17 @@ MLCP_API int mlcp_als_batched_host(int nvec, int ndof, const int *nbas, const in
  * alscpp_ reduction of one vector held in caller-provided DEVICE buffers
  * (d_coef/d_base in the reference layout: rF F terms, then rG target terms;
  * the F terms are overwritten).  For callers that cannot allocate device
- * memory at call time (inside stream capture, under an allocator that owns the
- * device, in latency-critical loops): all scratch comes from a fixed 32 MiB
- * array inside the library, held by every GPU that loads it.  The first call
- * on a device looks up that array's address and must come before any stream
- * capture.  Calls share the array: calls whose work overlaps on the GPU race.
- * Sizes whose scratch exceeds the array return an error.  Enqueued on stream
- * (NULL: the legacy default stream); d_status (optional, device int) receives
- * bit 0 when a normal-equation matrix was not positive definite and bit 1
- * when an internal pipeline wait timed out (result not valid). */
+ * memory at call time (a host whose device memory another allocator or pool
+ * owns up front, a latency-critical loop that must stay out of the driver's
+ * allocator): all scratch comes from a fixed 32 MiB array inside the library,
+ * held by every GPU that loads it.  The first call on a device looks up that
+ * array's address and must come before any stream capture.  Calls share the
+ * array: calls whose work overlaps on the GPU race.  Sizes whose scratch
+ * exceeds the array return an error; arguments are checked even when
+ * nals = 0.  Enqueued on stream (NULL: the legacy default stream).  d_status
+ * (required, a device int, cleared by the call) receives bit 0 when a
+ * normal-equation matrix was not positive definite and bit 1 when an internal
+ * pipeline wait timed out; either bit means the result is not valid. */
 MLCP_API int mlcp_als_noalloc(int ndof, const int *nbas, int rF, int rG, double *d_coef, double *d_base, int nals,
                               int *d_status, void *stream);
 

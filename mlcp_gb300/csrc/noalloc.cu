@@ -3,11 +3,10 @@
 // from a fixed array compiled into the library.
 //
 // Who needs it: callers that cannot call cudaMalloc at the moment they reduce
-// a vector, such as code running while a stream is being captured into a CUDA
-// graph, hosts whose device memory is owned up front by another allocator or
-// memory pool (a framework that reserves the card, an MPS client with a hard
-// memory limit), and latency-critical loops that must not enter the driver's
-// allocator (cudaFree synchronises the device).
+// a vector: hosts whose device memory is owned up front by another allocator
+// or memory pool (a framework that reserves the card, an MPS client with a
+// hard memory limit), and latency-critical loops that must not enter the
+// driver's allocator (cudaFree synchronises the device).
 //
 // Contract:
 //  * Scratch lives in g_noalloc_scratch (kNoAllocScratchBytes = 32 MiB).  Every
@@ -15,15 +14,20 @@
 //  * The first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current).  Make that first call
 //    before any stream capture begins.
-//  * All calls share the array and it keeps the previous call's contents.  The
-//    status word is cleared on every call, and every other scratch region is
-//    fully written before it is read.  Calls whose work overlaps on the GPU (two
-//    streams, or two host threads) race on the array and give wrong results;
-//    serialise them.
+//  * All calls share the array and it keeps the previous call's contents.
+//    Every scratch region is fully written before it is read.  Calls whose
+//    work overlaps on the GPU (two streams, or two host threads) race on the
+//    array and give wrong results; serialise them.
+//  * The caller's status word (d_status, required) is cleared by every call and
+//    receives the kernel's flags: bit 0 when a normal-equation matrix was not
+//    positive definite, bit 1 when an internal pipeline wait timed out.  Either
+//    bit means the reduced vector is not valid.
 //  * Sizes whose scratch exceeds the array are rejected with kTooLarge and a
-//    message naming the limit; nothing is truncated.
+//    message naming the limit; nothing is truncated.  Arguments are checked
+//    before anything else, also when nals = 0 (which then does nothing).
 //  * No cudaMalloc, cudaFree, cudaMallocHost or other allocating routine is
-//    called.  Metadata is copied from the caller's stack with cudaMemcpyAsync.
+//    called.  Metadata is copied from the caller's stack with cudaMemcpyAsync
+//    (a pageable copy: the call returns once the runtime has staged it).
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -68,9 +72,12 @@ int scratch_address(void** out) {
 
 int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_base, int nals, int* d_status,
         cudaStream_t st) {
-  if (nals == 0) return kOk;
   if (ndof < 2 || ndof > 1024 || rF < 1 || rF > 64 || rG < 1 || nals < 0 || !nbas || !d_coef || !d_base) {
     set_error("mlcp_als_noalloc: bad arguments (ndof=%d rF=%d rG=%d nals=%d)", ndof, rF, rG, nals);
+    return kBadArgument;
+  }
+  if (!d_status) {
+    set_error("mlcp_als_noalloc: d_status is required (a device int that reports an invalid result)");
     return kBadArgument;
   }
   int off[1025], offp[1025], offg[1025];
@@ -87,6 +94,7 @@ int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_bas
     npmax = std::max(npmax, round_up(nbas[d], 4));
     gsmax = std::max(gsmax, als_gstride(nbas[d]));
   }
+  if (nals == 0) return kOk;
   const int nD = off[ndof], nDp = offp[ndof], nDg = offg[ndof];
 
   // launch shape: a cluster of up to 16 CTAs owning slices of the target terms
@@ -117,7 +125,6 @@ int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_bas
   const size_t o_fcta = reserve(sizeof(float) * (size_t)rF * CL * nDp);
   const size_t o_gram = reserve(sizeof(dw) * sq * CL);
   const size_t o_suf = reserve(sizeof(dw) * sq * CL);
-  const size_t o_status = reserve(sizeof(int));
   if (bytes > kNoAllocScratchBytes) {
     set_error("mlcp_als_noalloc: a rank-%d target over %d modes (%d padded basis functions) needs %zu bytes of "
               "scratch; the fixed scratch array holds %zu bytes (use mlcp_als_batched instead)",
@@ -147,7 +154,7 @@ int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_bas
   hl[5] = rF;  // target terms follow F
   MLCP_CUDA_TRY(cudaMemcpyAsync(w + o_int, hi, sizeof(int) * n_int, cudaMemcpyHostToDevice, st));
   MLCP_CUDA_TRY(cudaMemcpyAsync(w + o_ll, hl, sizeof(long long) * n_ll, cudaMemcpyHostToDevice, st));
-  int* status = d_status ? d_status : reinterpret_cast<int*>(w + o_status);
+  int* status = d_status;
   MLCP_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
 
   const int* d_int = reinterpret_cast<const int*>(w + o_int);

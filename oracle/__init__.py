@@ -520,3 +520,110 @@ def sygv(A: np.ndarray, B: np.ndarray):
     X = np.zeros(n * n)
     info = lib().orc_sygv(n, _dp(Acm), _dp(Bcm), _dp(w), _dp(X))
     return w, X.reshape(n, n).T.copy(), info
+
+
+# --- the reference's own FP64 CUDA library (oracle/ref_build.py, oracle/ref_run.py) ---
+
+def reference_staged() -> bool:
+    """True when the reference's CUDA sources are staged under oracle/_ref/src."""
+    from . import ref_build
+    return ref_build.staged()
+
+
+def reference_built() -> bool:
+    from . import ref_build
+    return os.path.exists(ref_build.LIB)
+
+
+class Reference:
+    """The reference's FP64 CUDA entry points, served by a child process
+    (``oracle/ref_run.py``; the reference resets the device after each call).
+
+    ``als`` runs ``alscpp_`` (src/intertwining.cu:180) once per vector;
+    ``intertwine`` runs one ``intertwinecpp_`` cycle (src/intertwining.cu:98).
+    Both return the reference's outputs and the host wall time of each call.
+    Test and baseline infrastructure only."""
+
+    def __init__(self, timeout: float = 1800.0):
+        import subprocess as sp
+        import sys
+        from . import ref_build
+        if not os.path.exists(ref_build.LIB):
+            raise RuntimeError("reference library not built (oracle/ref_build.py)")
+        self.timeout = timeout
+        env = dict(os.environ, OMP_NUM_THREADS="1")
+        self.proc = sp.Popen([sys.executable, os.path.join(_HERE, "ref_run.py")], stdin=sp.PIPE, stdout=sp.PIPE,
+                             env=env)
+
+    def _call(self, req: dict) -> dict:
+        import io
+        import select
+        import struct
+        import time as _t
+        buf = io.BytesIO()
+        np.savez(buf, **req)
+        data = buf.getvalue()
+        self.proc.stdin.write(struct.pack("<Q", len(data)) + data)
+        self.proc.stdin.flush()
+        fd = self.proc.stdout.fileno()
+        deadline = _t.monotonic() + self.timeout
+
+        def read(n):
+            out = bytearray()
+            while len(out) < n:
+                left = deadline - _t.monotonic()
+                if left <= 0 or not select.select([fd], [], [], left)[0]:
+                    self.close(kill=True)
+                    raise TimeoutError("reference runner did not answer in time")
+                chunk = os.read(fd, n - len(out))
+                if not chunk:
+                    raise RuntimeError(f"reference runner exited (code {self.proc.poll()})")
+                out += chunk
+            return bytes(out)
+        (n,) = struct.unpack("<Q", read(8))
+        rep = dict(np.load(io.BytesIO(read(n)), allow_pickle=False))
+        if "error" in rep:
+            raise RuntimeError(f"reference runner: {rep['error']}")
+        return rep
+
+    def als(self, coefs, bases, nbas, rF: int, rG: int, nals: int):
+        """coefs (nv, rF+rG), bases (nv, rF+rG, nD): F then G per vector, as
+        the host passes them to alscpp_.  Returns (coef (nv, rF), base (nv, rF,
+        nD), seconds (nv))."""
+        rep = self._call({"op": np.array("als"), "coef": np.asarray(coefs, dtype=np.float64),
+                          "base": np.asarray(bases, dtype=np.float64),
+                          "nbas": np.asarray(nbas, dtype=np.int32), "rF": np.array(rF), "rG": np.array(rG),
+                          "nals": np.array(nals)})
+        return rep["coef"], rep["base"], rep["seconds"]
+
+    def intertwine(self, base, coef, nbas, rk, nbloc, hl, eigv, npow, nals, update=True, ishift=1, Eshift=0.0):
+        """One intertwinecpp_ cycle; returns (base, coef, eigv, seconds)."""
+        rep = self._call({"op": np.array("cycle"), "base": np.asarray(base, dtype=np.float64),
+                          "coef": np.asarray(coef, dtype=np.float64), "eigv": np.asarray(eigv, dtype=np.float64),
+                          "nbas": np.asarray(nbas, dtype=np.int32), "opid": np.asarray(hl.opid, dtype=np.int32),
+                          "mptr": np.asarray(hl.mptr, dtype=np.int32),
+                          "hcoef": np.asarray(hl.coef, dtype=np.float64),
+                          "mat": np.asarray(hl.mat, dtype=np.float64), "rk": np.array(rk),
+                          "nbloc": np.array(nbloc), "npow": np.array(npow), "nals": np.array(nals),
+                          "update": np.array(bool(update)), "ishift": np.array(ishift),
+                          "eshift": np.array(float(Eshift))})
+        return rep["base"], rep["coef"], rep["eigv"], float(rep["seconds"])
+
+    def close(self, kill: bool = False):
+        if self.proc is None:
+            return
+        try:
+            if kill:
+                self.proc.kill()
+            else:
+                self.proc.stdin.close()
+            self.proc.wait(timeout=60)
+        except Exception:
+            self.proc.kill()
+        self.proc = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
