@@ -13,6 +13,13 @@ restored from a pristine copy at the start of every step).  The FP64 target
 --impl reference times the reference algorithm's CPU implementation (the C
 restatement in oracle/, OpenMP over vectors, all host threads) on a bounded
 sample of the same workload.
+
+Baseline legs beside the GPU measurement (never inside its timed regions):
+the CPU oracle on a sample of the batch (cpu_baseline, whose FP64 results
+also give the GPU's residual errors on the headline workload), and the
+reference's own FP64 CUDA library (fp64_gpu_baseline: oracle/ref_build.py,
+run in a child process on the same GPU) on a smaller sample and on one power
+cycle, with the GPU's errors against it.
 """
 from __future__ import annotations
 
@@ -113,8 +120,9 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def cpu_sample_rate(batch, nvec_sample: int, threads: int):
-    """Oracle (C restatement of the reference algorithm) on nvec_sample vectors."""
+def cpu_sample_rate(batch, nvec_sample: int, threads: int, keep: bool = False):
+    """Oracle (C restatement of the reference algorithm) on nvec_sample
+    vectors; with keep, also the reduced (coef, base) of each vector."""
     import oracle
     coefs, bases, rfs, rgs = [], [], [], []
     for v in range(nvec_sample):
@@ -126,7 +134,74 @@ def cpu_sample_rate(batch, nvec_sample: int, threads: int):
     t0 = time.perf_counter()
     oracle.als_batched(coefs, bases, batch.nbas, rfs, rgs, NALS, nthreads=threads)
     dt = time.perf_counter() - t0
+    if keep:
+        return nvec_sample / dt, dt, [(coefs[v][:rfs[v]], bases[v][:rfs[v]]) for v in range(nvec_sample)]
     return nvec_sample / dt, dt
+
+
+def als_errors(batch, gcoef, gbase, results):
+    """Largest relative difference of the residuals ||F - G|| / ||G|| and
+    largest relative distance of the reduced vectors, GPU against FP64
+    results [(coef, base)] of the first len(results) vectors."""
+    import oracle
+    rerr, dist = 0.0, 0.0
+    for v, (fc, fb) in enumerate(results):
+        c0, b0 = batch.vector(v)
+        f = int(batch.rF[v])
+        t = int(batch.term_off[v])
+        gc, gb = gcoef[t:t + f], gbase[t:t + f]
+        gg = oracle.cp_dot(b0[f:], c0[f:], b0[f:], c0[f:], batch.nbas)
+
+        def res(xc, xb):
+            xx = oracle.cp_dot(xb, xc, xb, xc, batch.nbas)
+            xg = oracle.cp_dot(xb, xc, b0[f:], c0[f:], batch.nbas)
+            return np.sqrt(max(xx + gg - 2 * xg, 0.0) / gg)
+        r_ref, r_gpu = res(fc, fb), res(gc, gb)
+        rerr = max(rerr, abs(r_gpu - r_ref) / r_ref)
+        aa = oracle.cp_dot(gb, gc, gb, gc, batch.nbas)
+        bb = oracle.cp_dot(fb, fc, fb, fc, batch.nbas)
+        ab = oracle.cp_dot(gb, gc, fb, fc, batch.nbas)
+        dist = max(dist, float(np.sqrt(max(aa + bb - 2 * ab, 0.0) / bb)))
+    return float(rerr), dist
+
+
+FP64_SAMPLE = 4  # vectors the reference FP64 GPU library reduces (about 5 s each)
+
+
+def fp64_gpu_baseline(batch, gcoef, gbase, gpu_value, cycle_gpu_ms=None):
+    """The reference's own FP64 CUDA library on the same GPU: seconds per
+    alscpp_ reduction on FP64_SAMPLE vectors of the batch (its residuals
+    against the GPU's), and one intertwinecpp_ power cycle on the cycle
+    workload (its eigenvalues against the GPU's).  None when the library is
+    not built."""
+    import oracle
+    if not oracle.reference_built():
+        return None
+    out = {"kind": "reference CUDA library, FP64 build (-DUSE_DOUBLES=1), sm_103a, same GPU, child process",
+           "timing": "host wall time of each entry-point call after the context exists (its device "
+                     "allocations, copies, kernels, cuSOLVER solves and closing cudaDeviceReset)"}
+    with oracle.Reference(timeout=1200) as ref:
+        vs = list(range(FP64_SAMPLE))
+        cs = np.stack([batch.vector(v)[0] for v in vs])
+        bs = np.stack([batch.vector(v)[1] for v in vs])
+        rc, rb, sec = ref.als(cs, bs, batch.nbas, RF, RG, NALS)
+        rate = 1.0 / float(np.mean(sec))
+        rerr, dist = als_errors(batch, gcoef, gbase, [(rc[k], rb[k]) for k in range(len(vs))])
+        out["als"] = {"value": rate, "unit": UNIT, "seconds_per_reduction": float(np.mean(sec)),
+                      "sample": f"vectors 0-{FP64_SAMPLE - 1} of the batch, one alscpp_ call each",
+                      "gpu_over_fp64": gpu_value / rate, "gpu_residual_rel_err_max": rerr,
+                      "gpu_vec_rel_dist_max": dist}
+        if cycle_gpu_ms is not None:
+            hl, Q, qc, eig0, esh = cycle_inputs()
+            from mlcp_gb300 import intertwine as IT
+            _, _, ge = IT.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
+            _, _, re, rsec = ref.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1,
+                                            esh)
+            out["power_cycle"] = {"ms_per_cycle": 1e3 * rsec, "gpu_ms_per_cycle": cycle_gpu_ms,
+                                  "fp64_over_gpu_time": 1e3 * rsec / cycle_gpu_ms,
+                                  "gpu_eig_rel_err_max": float(np.max(np.abs(ge - re) / np.abs(re))),
+                                  "workload": "the power_cycle workload, one cycle from its seeded block"}
+    return out
 
 
 def run_reference(args):
@@ -316,7 +391,6 @@ def run_cycle_bench(steps: int, cpu: bool):
     out["workload_diagonalize"] = (f"two-mode quartic force field {DIAG_N}x{DIAG_N}, all {nbd} product functions, "
                                    f"rank {CYC_R}; Henon-Heiles block as the cycle with nals={CYC_NALS}")
     if cpu:
-        oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
         t0 = time.perf_counter()
         oracle.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
         out["cpu_ms_per_cycle"] = 1e3 * (time.perf_counter() - t0)
@@ -341,7 +415,6 @@ def run_cycle_bench(steps: int, cpu: bool):
         out["diagonalize_2mode_cpu_ms"] = 1e3 * (time.perf_counter() - t0)
         out["cpu_cores"] = os.cpu_count()
         out["cpu_kind"] = "port"
-        oracle.set_cycle_penalties()
     return out
 
 
@@ -408,6 +481,8 @@ def run_gpu(args):
         kms.append(L.mlcp_gb300_last_kernel_ms())
     L.mlcp_gb300_set_kernel_timing(0)
     kernel_ms = float(np.mean(kms))
+    torch.cuda.synchronize()
+    gcoef, gbase = coef.cpu().numpy(), base.cpu().numpy()  # the last step's reduced batch
     alg_bytes = NALS * batch.g_bytes(4)  # FP32 target slice streamed once per mode visit
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
@@ -444,19 +519,29 @@ def run_gpu(args):
 
     # CPU baseline: the oracle on a bounded sample (rank 0, N=1 only)
     cpu = None
+    accuracy = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         sample = min(NVEC, threads)
-        rate, dt = cpu_sample_rate(batch, sample, threads)
+        rate, dt, fp64 = cpu_sample_rate(batch, sample, threads, keep=True)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{sample} of the {NVEC} vectors (full 10 sweeps each) in {dt:.1f} s"}
+        rerr, dist = als_errors(batch, gcoef, gbase, fp64)
+        accuracy = {"against": "FP64 oracle (the reference's algorithm; pinned to the reference library by "
+                               "tests/test_gpu_reference.py)", "sample": f"vectors 0-{sample - 1}",
+                    "als_residual_rel_err_max": rerr, "als_vec_rel_dist_max": dist}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
-                "config": dict(CONFIG, parallelism=f"replicas x{ws}"),
-                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+dw48", "data": "synthetic (seeded)",
+                "dtype_note": "FP32 contractions with FP32 accumulation; normal equations, solves and norms in "
+                              "double-word FP32 pairs (~48-bit significand, FP32 exponent range); FP64 in and out",
+                "config": dict(CONFIG),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "note": "alscpp_ keeps the target on the host: its FP64 copy crosses the host link every "
+                                "step, read by the GPU from mapped pinned memory"},
+                "accuracy": accuracy,
                 "gpu_launches": 3 * args.steps,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
@@ -465,6 +550,9 @@ def run_gpu(args):
                 "cpu_baseline": cpu, "clocks": clk}
         if not args.no_cycle and ws == 1:
             line["power_cycle"] = run_cycle_bench(max(1, min(args.steps, 5)), cpu=not args.no_cpu)
+        if not args.no_fp64 and ws == 1:
+            cyc_ms = line["power_cycle"]["gpu_ms_per_cycle"] if "power_cycle" in line else None
+            line["fp64_gpu_baseline"] = fp64_gpu_baseline(batch, gcoef, gbase, e2e_value, cyc_ms)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -479,6 +567,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-cycle", action="store_true", help="skip the power-cycle measurement")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the reference FP64 GPU library's timing (fp64_gpu_baseline)")
     ap.add_argument("--cycle-only", action="store_true",
                     help="time only the power cycle (--steps cycles after one warm-up) and print its JSON")
     args = ap.parse_args()

@@ -35,10 +35,11 @@ int finish_status(int status);
 namespace {
 
 constexpr int kMaxRankCycle = 64;
-// Penalty factors (reference src/als.cu:248-267): the FP32-build rule for the
-// stages whose right-hand sides are FP32 contractions, the FP64-build rule for
-// the FP64 Gram-Schmidt (applied inside gs.cu).
-constexpr double kPenFP32 = 1.0e-5;
+// Penalty factor of the power sweeps, H-applications and vector updates: the
+// reference's FP64-build rule (src/als.cu:248-267), as in the Gram-Schmidt
+// (applied inside gs.cu).  These stages run in double-word arithmetic, which
+// this rule needs (opals.cu, upd.cu).
+constexpr double kPen = 1.0e-10;
 constexpr int kMaxBasisCycle = 64;
 
 uint64_t fnv1a(uint64_t h, const void* data, size_t bytes) {
@@ -149,18 +150,18 @@ int get_optable(Context* ctx, const Layout& Ly, const int* nbas, int R, int T, c
   }
   const int utot = uoff[D];
   const int npm = Ly.npmax;
-  std::vector<float> hmat((size_t)utot * npm * npm, 0.f);
+  std::vector<dw> hmat((size_t)utot * npm * npm, dw{0.f, 0.f});
   std::vector<double> hmat64((size_t)utot * npm * npm, 0.0);
   std::vector<unsigned char> ident(utot, 0);
   for (int d = 0; d < D; ++d) {
     const int n = nbas[d];
     for (int u = 0; u < (int)starts[d].size(); ++u) {
-      float* h = &hmat[(size_t)(uoff[d] + u) * npm * npm];
+      dw* h = &hmat[(size_t)(uoff[d] + u) * npm * npm];
       double* h64 = &hmat64[(size_t)(uoff[d] + u) * npm * npm];
       if (starts[d][u] < 0) {
         ident[uoff[d] + u] = 1;
         for (int i = 0; i < n; ++i) {
-          h[i * npm + i] = 1.f;
+          h[i * npm + i] = dw{1.f, 0.f};
           h64[i * npm + i] = 1.0;
         }
         continue;
@@ -169,8 +170,8 @@ int get_optable(Context* ctx, const Layout& Ly, const int* nbas, int R, int T, c
       for (int c = 0; c < n; ++c)
         for (int r = 0; r <= c; ++r) {
           const double v64 = pk[r + (size_t)c * (c + 1) / 2];
-          h[r * npm + c] = (float)v64;
-          h[c * npm + r] = (float)v64;
+          h[r * npm + c] = dw_from_double(v64);
+          h[c * npm + r] = dw_from_double(v64);
           h64[r * npm + c] = v64;
           h64[c * npm + r] = v64;
         }
@@ -193,7 +194,7 @@ int get_optable(Context* ctx, const Layout& Ly, const int* nbas, int R, int T, c
   const size_t o_nbas = reserve(sizeof(int) * D), o_off = reserve(sizeof(int) * (D + 1)),
                o_offp = reserve(sizeof(int) * (D + 1)), o_uoff = reserve(sizeof(int) * (D + 1)),
                o_uid = reserve(sizeof(int) * uid.size()), o_ident = reserve(utot),
-               o_h = reserve(sizeof(float) * hmat.size()), o_h64 = reserve(sizeof(double) * hmat64.size()),
+               o_h = reserve(sizeof(dw) * hmat.size()), o_h64 = reserve(sizeof(double) * hmat64.size()),
                o_alpha = reserve(sizeof(double) * T),
                o_order = reserve(sizeof(int) * order.size()), o_gs = reserve(sizeof(int) * gstart.size());
   std::vector<char> host(bytes);
@@ -203,7 +204,7 @@ int get_optable(Context* ctx, const Layout& Ly, const int* nbas, int R, int T, c
   std::memcpy(&host[o_uoff], uoff.data(), sizeof(int) * (D + 1));
   std::memcpy(&host[o_uid], uid.data(), sizeof(int) * uid.size());
   std::memcpy(&host[o_ident], ident.data(), utot);
-  std::memcpy(&host[o_h], hmat.data(), sizeof(float) * hmat.size());
+  std::memcpy(&host[o_h], hmat.data(), sizeof(dw) * hmat.size());
   std::memcpy(&host[o_h64], hmat64.data(), sizeof(double) * hmat64.size());
   std::memcpy(&host[o_alpha], Hcoef, sizeof(double) * T);
   std::memcpy(&host[o_order], order.data(), sizeof(int) * order.size());
@@ -220,7 +221,7 @@ int get_optable(Context* ctx, const Layout& Ly, const int* nbas, int R, int T, c
   t.D = D; t.T = T; t.R = R; t.nDp = Ly.nDp; t.npmax = npm; t.umax = umax; t.utot = utot;
   t.nbas = (const int*)(b + o_nbas); t.off = (const int*)(b + o_off); t.offp = (const int*)(b + o_offp);
   t.uoff = (const int*)(b + o_uoff); t.uid = (const int*)(b + o_uid);
-  t.ident = (const unsigned char*)(b + o_ident); t.hmat = (const float*)(b + o_h);
+  t.ident = (const unsigned char*)(b + o_ident); t.hdw = (const dw*)(b + o_h);
   t.hmat64 = (const double*)(b + o_h64);
   t.alpha = (const double*)(b + o_alpha); t.order = (const int*)(b + o_order); t.gstart = (const int*)(b + o_gs);
   hc.key = key;
@@ -243,7 +244,7 @@ __global__ void update_weights_kernel(int B, int R, const double* qcoef, const d
 
 struct CycleBuffers {
   double *q, *qc, *hq, *hqc, *qn, *qnc;
-  float *mscr, *wscr, *zscr;
+  dw *mscr, *wscr, *zscr, *uwork, *qdw;
   double *g64, *gsw, *A, *S, *U, *eigv, *gwork, *wts;
   int *meta, *status;
 };
@@ -258,9 +259,9 @@ size_t plan_cycle(const Layout& Ly, const OpTable& t, int R, int B, CycleBuffers
   cb->hqc = (double*)take(sizeof(double) * vec);
   cb->qn = (double*)take(sizeof(double) * vec * Ly.nD);
   cb->qnc = (double*)take(sizeof(double) * vec);
-  cb->mscr = (float*)take(sizeof(float) * (size_t)B * t.utot * R * R);
-  cb->wscr = (float*)take(sizeof(float) * (size_t)B * t.umax * R * R);
-  cb->zscr = (float*)take(sizeof(float) * (size_t)B * t.umax * R * t.npmax);
+  cb->mscr = (dw*)take(sizeof(dw) * (size_t)B * t.utot * R * R);
+  cb->wscr = (dw*)take(sizeof(dw) * (size_t)B * t.umax * R * R);
+  cb->zscr = (dw*)take(sizeof(dw) * (size_t)B * t.umax * R * t.npmax);
   cb->g64 = (double*)take(sizeof(double) * (size_t)B * Ly.D * R * R);
   cb->gsw = (double*)take(sizeof(double) * gs_work_doubles(B, R, Ly.nD, Ly.D, Ly.npmax));
   cb->A = (double*)take(sizeof(double) * (size_t)B * B);
@@ -269,9 +270,22 @@ size_t plan_cycle(const Layout& Ly, const OpTable& t, int R, int B, CycleBuffers
   cb->eigv = (double*)take(sizeof(double) * B);
   cb->gwork = (double*)take(sizeof(double) * gep_work_doubles(B));
   cb->wts = (double*)take(sizeof(double) * (size_t)B * B * R);
+  cb->uwork = (dw*)take(sizeof(dw) * upd_work_dw(B, R, Ly.D));
+  cb->qdw = (dw*)take(sizeof(dw) * upd_qdw_dw(B, R, Ly.nD));
   cb->meta = (int*)take(sizeof(int) * 3 * (Ly.D + 1));
   cb->status = (int*)take(sizeof(int) * (B + 4));
   return bytes;
+}
+
+// New block: vector i fits sum_k U(k,i) Q_k (cb.U from the Rayleigh-Ritz
+// solve), nals sweeps from Q_i, into cb.qn / cb.qnc.
+int run_updates(Context* ctx, const Layout& Ly, const CycleBuffers& cb, const int* d_nbas, const int* d_off, int R,
+                int B, int nals, cudaStream_t st) {
+  UpdParams u;
+  u.D = Ly.D; u.R = R; u.B = B; u.nD = Ly.nD; u.npmax = Ly.npmax; u.nals = nals; u.tile = 0;
+  u.nbas = d_nbas; u.off = d_off; u.q = cb.q; u.qc = cb.qc; u.U = cb.U; u.qn = cb.qn; u.qnc = cb.qnc;
+  u.qdw = cb.qdw; u.work = cb.uwork; u.pen_factor = kPen; u.status = cb.status;
+  return upd_launch(u, (int)ctx->smem_optin, st);
 }
 
 }  // namespace
@@ -346,7 +360,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
     OpAlsParams p;
     p.eshift_v = nullptr;
     p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 0; p.nsweeps = npow; p.ishift = ishift; p.eshift = Eshift;
-    p.pen_factor = kPenFP32;
+    p.pen_factor = kPen;
     p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.q; p.f_coef = cb.qc;
     p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
     if ((rc = opals_launch(p, st))) return rc;
@@ -365,7 +379,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
       OpAlsParams p;
       p.eshift_v = nullptr;
       p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 1; p.nsweeps = nals; p.ishift = 0; p.eshift = 0.0;
-      p.pen_factor = kPenFP32;
+      p.pen_factor = kPen;
       p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.hq; p.f_coef = cb.hqc;
       p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
       if ((rc = opals_launch(p, st))) return rc;
@@ -380,22 +394,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
     if ((rc = gep_launch(gp, st))) return rc;
     // --- vector updates: new Q_i fits sum_k U(k,i) Q_k, starting from Q_i ---
     if (nals > 0) {
-      MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qn, cb.q, sizeof(double) * nvals, cudaMemcpyDeviceToDevice, st));
-      MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qnc, cb.qc, sizeof(double) * B * R, cudaMemcpyDeviceToDevice, st));
-      update_weights_kernel<<<std::min(ctx->num_sms * 8, (B * B * R + 255) / 256), 256, 0, st>>>(B, R, cb.qc, cb.U,
-                                                                                                  cb.wts);
-      MLCP_CUDA_TRY(cudaGetLastError());
-      std::vector<int> rF(B, R), rG(B, B * R);
-      std::vector<long long> toff(B), gtoff(B, 0);
-      for (int v = 0; v < B; ++v) toff[v] = (long long)v * R;
-      AlsJob job;
-      job.nvec = B; job.ndof = ndof; job.nals = nals; job.nbas = nbas; job.rF = rF.data(); job.rG = rG.data();
-      job.term_off = toff.data(); job.d_base = cb.qn; job.d_coef = cb.qnc;
-      job.g_base = cb.q; job.g_coef = cb.qc; job.g_term_off = gtoff.data(); job.shared_w = cb.wts;
-      job.d_status = cb.status;
-      job.pen_factor = kPenFP32;
-      if ((rc = als_run(ctx, job, st))) return rc;
-      if ((rc = normalize_coefs_launch(B, R, ndof, Ly.nD, d_nbas, cb.qn, cb.qnc, st))) return rc;
+      if ((rc = run_updates(ctx, Ly, cb, d_nbas, d_off, R, B, nals, st))) return rc;
       std::swap(cb.q, cb.qn);
       std::swap(cb.qc, cb.qnc);
     }
@@ -551,6 +550,7 @@ int diagonalize(Context* ctx, double* base, double* coef, const int* nbas, int r
   MLCP_CUDA_TRY(cudaMemcpyAsync(cb.meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, st));
   MLCP_CUDA_TRY(cudaMemsetAsync(cb.status, 0, sizeof(int) * (B + 4), st));
   const int* d_nbas = cb.meta;
+  const int* d_off = cb.meta + (ndof + 1);
   // A, S with H applied exactly; then the generalised eigenproblem
   if ((rc = rq_apply_launch(tab, B, Ly.nD, cb.q, y, st))) return rc;
   RqPairParams rp;
@@ -578,19 +578,7 @@ int diagonalize(Context* ctx, double* base, double* coef, const int* nbas, int r
     std::swap(cb.q, cb.qn);
     std::swap(cb.qc, cb.qnc);
   } else if (nals > 0) {
-    MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qn, cb.q, sizeof(double) * nvals, cudaMemcpyDeviceToDevice, st));
-    MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qnc, cb.qc, sizeof(double) * B * R, cudaMemcpyDeviceToDevice, st));
-    std::vector<int> rF(B, R), rG(B, B * R);
-    std::vector<long long> toff(B), gtoff(B, 0);
-    for (int v = 0; v < B; ++v) toff[v] = (long long)v * R;
-    AlsJob job;
-    job.nvec = B; job.ndof = ndof; job.nals = nals; job.nbas = nbas; job.rF = rF.data(); job.rG = rG.data();
-    job.term_off = toff.data(); job.d_base = cb.qn; job.d_coef = cb.qnc;
-    job.g_base = cb.q; job.g_coef = cb.qc; job.g_term_off = gtoff.data(); job.shared_w = cb.wts;
-    job.d_status = cb.status;
-    job.pen_factor = kPenFP32;
-    if ((rc = als_run(ctx, job, st))) return rc;
-    if ((rc = normalize_coefs_launch(B, R, ndof, Ly.nD, d_nbas, cb.qn, cb.qnc, st))) return rc;
+    if ((rc = run_updates(ctx, Ly, cb, d_nbas, d_off, R, B, nals, st))) return rc;
     std::swap(cb.q, cb.qn);
     std::swap(cb.qc, cb.qnc);
   }
@@ -766,7 +754,7 @@ int spectral_range(Context* ctx, double* base, double* coef, const int* nbas, in
       OpAlsParams p;
       p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 0; p.nsweeps = npow; p.ishift = 1; p.eshift = 0.0;
       p.eshift_v = shift;
-      p.pen_factor = kPenFP32;
+      p.pen_factor = kPen;
       p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.q; p.f_coef = cb.qc;
       p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
       if ((rc = opals_launch(p, st))) return rc;

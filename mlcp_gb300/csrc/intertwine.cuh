@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include "dword.cuh"
+
 namespace mlcp {
 
 // Operator list prepared once per distinct HopList (cached on the device).
@@ -21,7 +23,7 @@ struct OpTable {
   const int* uoff;          // [D+1] first global operator slot of each mode
   const int* uid;           // [T*D] local operator index of term t at mode d
   const unsigned char* ident;  // [utot] 1 if the operator is the identity
-  const float* hmat;        // [utot][npmax][npmax] dense FP32 operators
+  const dw* hdw;            // [utot][npmax][npmax] dense operators in double-word (power sweeps)
   const double* hmat64;     // [utot][npmax][npmax] the same in FP64 (Rayleigh quotients)
   const double* alpha;      // [T] term coefficients
   const int* order;         // [D][T] terms grouped by their operator at mode j
@@ -38,14 +40,14 @@ struct OpAlsParams {
   int ishift;
   double eshift;
   const double* eshift_v;  // per-vector shifts (device) overriding eshift, or null
-  double pen_factor;      // penalty = pen_factor * max(Fo weights)
+  double pen_factor;      // penalty = pen_factor * max(Fo weights) (1e-10: the reference's FP64 rule)
   const double* fo_base;  // Fo vectors (reference layout, rank R each, vector v at v*R terms)
   const double* fo_coef;
   double* f_base;         // F output (may alias fo for POW)
   double* f_coef;
-  float* mscr;            // [nvec][utot][R][R] operator Grams M = Fo^T h F
-  float* wscr;            // [nvec][umax][R][R] grouped term products W
-  float* zscr;            // [nvec][umax][R][npmax] h Fo_j
+  dw* mscr;               // [nvec][utot][R][R] operator Grams M = Fo^T h F
+  dw* wscr;               // [nvec][umax][R][R] grouped term products W
+  dw* zscr;               // [nvec][umax][R][npmax] h Fo_j
   double* g64;            // [nvec][D][R][R] FP64 Grams of F
   int* status;            // [nvec]
 };
@@ -72,6 +74,28 @@ int gs_launch(const GsParams& p, cudaStream_t st);
 // Doubles of GsParams::work needed for a block of nbloc vectors (npm: the
 // largest 4-padded basis size).
 size_t gs_work_doubles(int nbloc, int R, int nD, int D, int npm);
+
+// Vector updates (reference VectorUpdates / UPDATES_ALS, src/intertw_lcv.cu:
+// 209-304): vector i of the new block is the nals-sweep ALS fit, started from
+// Q_i, of sum_k U(k,i) Q_k, weights then divided by its norm; double-word.
+struct UpdParams {
+  int D, R, B, nD, npmax, nals;
+  int tile;               // block terms per shared-memory tile (set by upd_launch)
+  const int* nbas;        // [D] (device)
+  const int* off;         // [D+1] reference-layout offsets (device)
+  const double* q;        // old block (reference layout)
+  const double* qc;
+  const double* U;        // [B][B] column-major: U(k, i) = U[k + i B]
+  double* qn;             // new block
+  double* qnc;
+  dw* qdw;                // upd_qdw_dw(B, R, nD): the old block's factors, double-word, mode-major
+  dw* work;               // upd_work_dw(B, R, D): per-vector overlaps, Grams, target weights
+  double pen_factor;      // penalty = pen_factor * max(weights of Q_i)
+  int* status;            // [B] bit 0: non-positive pivot
+};
+int upd_launch(UpdParams p, int smem_optin, cudaStream_t st);
+size_t upd_work_dw(int B, int R, int D);
+size_t upd_qdw_dw(int B, int R, int nD);
 
 // Block Rayleigh-Ritz inner products: QHQ(i,j) = <Q_j, HQ_i>, S(i,j) = <Q_j, Q_i>, j <= i.
 struct GepParams {

@@ -13,18 +13,23 @@
 //   b(i,n) = sum_u sum_r c_r W_u(r,i) (h_u Fo_r^j)(n)
 // so a mode step costs O(T R^2 D) instead of O(T R (sum_d n_d^2 + R nD)).
 // The energy shift enters as an identity term with weight -E; for ishift < 0
-// b changes sign, as in the reference.  Because the right-hand sides carry
-// FP32 rounding, the penalty follows the reference's FP32-build rule
-// (1e-5 max c, src/als.cu:248-267): with the FP64 rule (1e-10) the rounding
-// noise in near-null directions of the normal equations is amplified by up
-// to 1e10 and the CP weights blow up over successive cycles.  The R x R normal equations
-// (prod_{d!=j} F_d F_d^T + pen I), their solve (FP32 inverse with
-// double-word refinement, or a double-word LDL^T), the F Grams and the weight
-// normalisation run in double-word (float-float, about 48 bits; the factors
-// are written out in FP64); the operator Grams, term products and
-// right-hand sides run in FP32.  In POW the weights are rescaled by a power
-// of two after every mode step (rescale_weights_warp), which keeps them in
-// the FP32 exponent range without changing the sweep's result.
+// b changes sign, as in the reference.
+//
+// Precision.  The penalty is the reference's FP64-build rule (1e-10 max c,
+// src/als.cu:248-267).  With it the normal equations of a nearly converged
+// vector (whose terms are close to linearly dependent) have condition
+// numbers up to 1e10, so any noise in b along their near-null directions is
+// amplified by up to 1e10: FP32 right-hand sides (24 bits) made the weights
+// blow up over successive cycles.  Everything here therefore runs in
+// double-word arithmetic (dword.cuh, about 48 bits): the factors of F and Fo,
+// the operators, the operator Grams M, the term products W, h_u Fo_j, the
+// right-hand sides, the normal equations (prod_{d!=j} F_d F_d^T + pen I),
+// their solve (FP32 inverse as the preconditioner of a double-word
+// refinement, or a double-word LDL^T), the F Grams and the weight
+// normalisation; the factors are written out in FP64.  In POW the weights
+// are rescaled by a power of two after every mode step
+// (rescale_weights_warp), which keeps them in the FP32 exponent range of
+// the double-word values without changing the sweep's result.
 #include "common.cuh"
 #include "dword.cuh"
 #include "dwsolve.cuh"
@@ -39,9 +44,9 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 
 struct OpSmem {
-  float* f32;     // [R][nDp] current F (FP32)
-  float* fo32;    // [R][nDp] Fo (FP32); aliases f32 for POW
-  float* y;       // [R][npmax] temporary h Fo_r
+  dw* f;          // [R][nDp] current F
+  dw* fo;         // [R][nDp] Fo; aliases f for POW
+  dw* y;          // [R][npmax] temporary h Fo_r
   dw* X;          // [R][npmax] solution (column-major, ld R)
   dw* b0;         // [R][npmax] right-hand side
   dw* res;        // [R][npmax] refinement residual
@@ -52,15 +57,15 @@ struct OpSmem {
   dw* red;        // [kWarps] reduction scratch
   dw* dinv;       // [R] LDL^T reciprocal pivots
   dw* u;          // [R] LDL^T scratch column
-  dw* misc;       // [2] penalty
+  dw* misc;       // [2] penalty, norm
   float* rred;    // [4] refinement scratch
   dwsolve::ColScratch cs;
   int* moff;      // [T][D] offset of each term's operator Gram per mode (null when T D is large)
   int* ord;       // [D][T] terms grouped by their operator at each mode (with moff)
   int* gst;       // [D][umax+1] group starts (with moff)
-  float* alpha;   // [T] term coefficients in FP32 (with moff)
-  float *Ms, *Ws, *Zs;  // operator Grams, term products, h_u Fo_j when resident in shared memory
-  float* hs;      // [utot][npmax][npmax] the FP32 operators when resident
+  dw* alpha;      // [T] term coefficients (with moff)
+  dw *Ms, *Ws, *Zs;  // operator Grams, term products, h_u Fo_j when resident in shared memory
+  dw* hs;         // [utot][npmax][npmax] the operators when resident
   int* flags;     // [4]
 };
 
@@ -77,9 +82,9 @@ __host__ __device__ inline size_t carve(OpSmem& s, unsigned char* base, const Op
     return base ? base + r : nullptr;
   };
   const size_t Rn = (size_t)t.R * t.npmax, RR = (size_t)t.R * t.R;
-  s.f32 = (float*)take(sizeof(float) * t.R * t.nDp);
-  s.fo32 = separate_fo ? (float*)take(sizeof(float) * t.R * t.nDp) : s.f32;
-  s.y = (float*)take(sizeof(float) * Rn);
+  s.f = (dw*)take(sizeof(dw) * t.R * t.nDp);
+  s.fo = separate_fo ? (dw*)take(sizeof(dw) * t.R * t.nDp) : s.f;
+  s.y = (dw*)take(sizeof(dw) * Rn);
   s.X = (dw*)take(sizeof(dw) * Rn);
   s.b0 = (dw*)take(sizeof(dw) * Rn);
   s.res = (dw*)take(sizeof(dw) * Rn);
@@ -99,11 +104,11 @@ __host__ __device__ inline size_t carve(OpSmem& s, unsigned char* base, const Op
   s.moff = tab ? (int*)take(sizeof(int) * t.T * t.D) : nullptr;
   s.ord = tab ? (int*)take(sizeof(int) * t.T * t.D) : nullptr;
   s.gst = tab ? (int*)take(sizeof(int) * t.D * (t.umax + 1)) : nullptr;
-  s.alpha = tab ? (float*)take(sizeof(float) * t.T) : nullptr;
-  s.hs = resident ? (float*)take(sizeof(float) * t.utot * t.npmax * t.npmax) : nullptr;
-  s.Ms = resident ? (float*)take(sizeof(float) * t.utot * RR) : nullptr;
-  s.Ws = resident ? (float*)take(sizeof(float) * t.umax * RR) : nullptr;
-  s.Zs = resident ? (float*)take(sizeof(float) * t.umax * Rn) : nullptr;
+  s.alpha = tab ? (dw*)take(sizeof(dw) * t.T) : nullptr;
+  s.hs = resident ? (dw*)take(sizeof(dw) * t.utot * t.npmax * t.npmax) : nullptr;
+  s.Ms = resident ? (dw*)take(sizeof(dw) * t.utot * RR) : nullptr;
+  s.Ws = resident ? (dw*)take(sizeof(dw) * t.umax * RR) : nullptr;
+  s.Zs = resident ? (dw*)take(sizeof(dw) * t.umax * Rn) : nullptr;
   s.flags = (int*)take(sizeof(int) * 4);
   return o;
 }
@@ -141,29 +146,29 @@ __device__ void rescale_weights_warp(dw* cf, int R) {
 }
 
 // M(r,i) = sum_n (h Fo_r^d)(n) F_i^d(n); identity operators skip the product.
-__device__ void operator_gram(const OpTable& t, int d, int ug, const OpSmem& s, float* M, float* zout) {
+__device__ void operator_gram(const OpTable& t, const dw* hmat, int d, int ug, const OpSmem& s, dw* M) {
   const int R = t.R, n = t.nbas[d], op = t.offp[d], npm = t.npmax;
   const bool ident = t.ident[ug];
-  const float* h = t.hmat + (size_t)ug * npm * npm;
+  const dw* h = hmat + (size_t)ug * npm * npm;
   // y(r, m) = sum_k h(m, k) Fo_r(k)
   for (int e = threadIdx.x; e < R * n; e += blockDim.x) {
     const int r = e / n, m = e % n;
-    float acc;
+    dw val;
     if (ident) {
-      acc = s.fo32[r * t.nDp + op + m];
+      val = s.fo[r * t.nDp + op + m];
     } else {
-      acc = 0.f;
-      for (int k = 0; k < n; ++k) acc = fmaf(h[m * npm + k], s.fo32[r * t.nDp + op + k], acc);
+      dw_acc acc = acc_zero();
+      for (int k = 0; k < n; ++k) acc_fma(acc, h[m * npm + k], s.fo[r * t.nDp + op + k]);
+      val = acc_value(acc);
     }
-    s.y[r * npm + m] = acc;
-    if (zout) zout[r * npm + m] = acc;
+    s.y[r * npm + m] = val;
   }
   __syncthreads();
   for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
     const int r = e / R, i = e % R;
-    float acc = 0.f;
-    for (int m = 0; m < n; ++m) acc = fmaf(s.y[r * npm + m], s.f32[i * t.nDp + op + m], acc);
-    M[e] = acc;
+    dw_acc acc = acc_zero();
+    for (int m = 0; m < n; ++m) acc_fma(acc, s.y[r * npm + m], s.f[i * t.nDp + op + m]);
+    M[e] = acc_value(acc);
   }
   __syncthreads();
 }
@@ -181,8 +186,8 @@ __device__ void f_gram_from64(const OpTable& t, int d, const double* fb, int nD,
 
 }  // namespace
 
-// kResident: the operator Grams, term products and h_u Fo_j in shared memory
-// (else in the per-vector global scratch of p).
+// kResident: the operator Grams, term products, h_u Fo_j and the operators in
+// shared memory (else in the per-vector global scratch of p and the table).
 template <bool kResident>
 __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
   const OpTable& t = p.ops;
@@ -197,9 +202,9 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
   const double* foc = p.fo_coef + (size_t)v * R;
   double* fb = p.f_base + (size_t)v * R * nD;
   double* fc = p.f_coef + (size_t)v * R;
-  float* M = kResident ? s.Ms : p.mscr + (size_t)v * t.utot * R * R;
-  float* W = kResident ? s.Ws : p.wscr + (size_t)v * t.umax * R * R;
-  float* Z = kResident ? s.Zs : p.zscr + (size_t)v * t.umax * R * npm;
+  dw* M = kResident ? s.Ms : p.mscr + (size_t)v * t.utot * R * R;
+  dw* W = kResident ? s.Ws : p.wscr + (size_t)v * t.umax * R * R;
+  dw* Z = kResident ? s.Zs : p.zscr + (size_t)v * t.umax * R * npm;
   const int* moff = s.moff;
   if (moff) {
     for (int e = threadIdx.x; e < T * D; e += blockDim.x) {
@@ -207,14 +212,14 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
       s.ord[e] = t.order[e];
     }
     for (int e = threadIdx.x; e < D * (t.umax + 1); e += blockDim.x) s.gst[e] = t.gstart[e];
-    for (int e = threadIdx.x; e < T; e += blockDim.x) s.alpha[e] = (float)t.alpha[e];
+    for (int e = threadIdx.x; e < T; e += blockDim.x) s.alpha[e] = dw_from_double(t.alpha[e]);
   }
-  const float* hmat = kResident ? s.hs : t.hmat;
+  const dw* hmat = kResident ? s.hs : t.hdw;
   if (kResident)
-    for (int e = threadIdx.x; e < t.utot * npm * npm; e += blockDim.x) s.hs[e] = t.hmat[e];
+    for (int e = threadIdx.x; e < t.utot * npm * npm; e += blockDim.x) s.hs[e] = t.hdw[e];
   dw* G = reinterpret_cast<dw*>(p.g64) + (size_t)v * D * R * R;  // double-word F Grams per mode
 
-  // ---- set-up: F (= Fo for PRODHV), FP32 copies, Grams, penalty ----
+  // ---- set-up: F (= Fo for PRODHV), double-word copies, Grams, penalty ----
   if (!pow_mode) {
     for (int e = threadIdx.x; e < R * nD; e += blockDim.x) fb[e] = fob[e];
     for (int e = threadIdx.x; e < R; e += blockDim.x) fc[e] = foc[e];
@@ -225,9 +230,9 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
     int d = 0;
     while (d + 1 < D && t.offp[d + 1] <= q) ++d;
     const int k = q - t.offp[d];
-    const double x = (k < t.nbas[d]) ? fob[(size_t)r * nD + t.off[d] + k] : 0.0;
-    s.f32[e] = (float)x;
-    if (!pow_mode) s.fo32[e] = (float)x;
+    const dw x = dw_from_double((k < t.nbas[d]) ? fob[(size_t)r * nD + t.off[d] + k] : 0.0);
+    s.f[e] = x;
+    if (!pow_mode) s.fo[e] = x;
   }
   for (int e = threadIdx.x; e < R; e += blockDim.x) {
     s.cf[e] = dw_from_double(fc[e]);
@@ -246,7 +251,8 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
   const dw pen = s.misc[0];
   for (int d = 0; d < D; ++d)
     for (int u = 0; u < t.uoff[d + 1] - t.uoff[d]; ++u)
-      operator_gram(t, d, t.uoff[d] + u, s, M + (size_t)(t.uoff[d] + u) * R * R, nullptr);
+      operator_gram(t, hmat, d, t.uoff[d] + u, s, M + (size_t)(t.uoff[d] + u) * R * R);
+  const dw eshift = dw_from_double(-(p.eshift_v ? p.eshift_v[v] : p.eshift));
 
   for (int sw = 0; sw < p.nsweeps; ++sw) {
     for (int j = 0; j < D; ++j) {
@@ -254,8 +260,8 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
       const int nu = t.uoff[j + 1] - t.uoff[j];
       const int* ord = (moff ? s.ord : t.order) + (size_t)j * T;
       const int* gs = (moff ? s.gst : t.gstart) + (size_t)j * (t.umax + 1);
-      // -- normal equations (double-word) from the Grams of the previous
-      //    step: prod_{d != j} G_d + pen I --
+      // -- normal equations from the Grams of the previous step:
+      //    prod_{d != j} G_d + pen I --
       for (int e = threadIdx.x; e < RR; e += blockDim.x) {
         dw bb = dw_make(1.f);
         for (int d = 0; d < D; ++d)
@@ -288,57 +294,60 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
         // four terms at a time
         for (int item = wt; item < nu * RR; item += nw) {
           const int u = item / RR, e = item - u * RR;
-          float acc = 0.f;
+          dw_acc acc = acc_zero();
           for (int q = gs[u]; q < gs[u + 1]; q += 4) {
-            float pr[4];
+            dw pr[4];
             int tb[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
               const bool live = q + k < gs[u + 1];
               const int term = ord[live ? q + k : q];
-              pr[k] = live ? (moff ? s.alpha[term] : (float)t.alpha[term]) : 0.f;
+              pr[k] = live ? (moff ? s.alpha[term] : dw_from_double(t.alpha[term])) : dw_make(0.f);
               tb[k] = term * D;
             }
             for (int d = 0; d < D; ++d) {
               if (d == j) continue;
 #pragma unroll
               for (int k = 0; k < 4; ++k)
-                pr[k] *= M[(moff ? moff[tb[k] + d] : (t.uoff[d] + t.uid[tb[k] + d]) * RR) + e];
+                pr[k] = dw_mul(pr[k], M[(moff ? moff[tb[k] + d] : (t.uoff[d] + t.uid[tb[k] + d]) * RR) + e]);
             }
-            acc += (pr[0] + pr[1]) + (pr[2] + pr[3]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc_add(acc, pr[k]);
           }
           if (u == 0 && p.ishift != 0) {
-            float prod = (float)(-(p.eshift_v ? p.eshift_v[v] : p.eshift));
+            dw prod = eshift;
             for (int d = 0; d < D; ++d)
-              if (d != j) prod *= M[(size_t)t.uoff[d] * RR + e];
-            acc += prod;
+              if (d != j) prod = dw_mul(prod, M[(size_t)t.uoff[d] * RR + e]);
+            acc_add(acc, prod);
           }
-          W[(size_t)u * RR + e] = acc;
+          W[(size_t)u * RR + e] = acc_value(acc);
         }
         // h_u Fo_j for every operator of mode j
         for (int item = wt; item < nu * R * nj; item += nw) {
           const int u = item / (R * nj), rem = item - u * R * nj, r = rem / nj, m = rem - r * nj;
           const int ug = t.uoff[j] + u;
-          float acc;
+          dw val;
           if (t.ident[ug]) {
-            acc = s.fo32[r * t.nDp + opj + m];
+            val = s.fo[r * t.nDp + opj + m];
           } else {
-            const float* h = hmat + (size_t)ug * npm * npm + (size_t)m * npm;
-            acc = 0.f;
-            for (int k = 0; k < nj; ++k) acc = fmaf(h[k], s.fo32[r * t.nDp + opj + k], acc);
+            const dw* h = hmat + (size_t)ug * npm * npm + (size_t)m * npm;
+            dw_acc acc = acc_zero();
+            for (int k = 0; k < nj; ++k) acc_fma(acc, h[k], s.fo[r * t.nDp + opj + k]);
+            val = acc_value(acc);
           }
-          Z[(size_t)u * R * npm + r * npm + m] = acc;
+          Z[(size_t)u * R * npm + r * npm + m] = val;
         }
         asm volatile("bar.sync 2, %0;" ::"r"(nw) : "memory");
         // right-hand side b(i,n) = sum_u sum_r W_u(r,i) c_r Z_u(r,n)
         const dw* cg = pow_mode ? s.cf : s.cfo;
         for (int e = wt; e < R * nj; e += nw) {
           const int i = e % R, m = e / R;
-          float acc = 0.f;
+          dw_acc acc = acc_zero();
           for (int u = 0; u < nu; ++u)
             for (int r = 0; r < R; ++r)
-              acc = fmaf(W[(size_t)u * RR + r * R + i] * cg[r].hi, Z[(size_t)u * R * npm + r * npm + m], acc);
-          s.b0[i + m * R] = dw_make(p.ishift < 0 ? -acc : acc);
+              acc_fma(acc, dw_mul(W[(size_t)u * RR + r * R + i], cg[r]), Z[(size_t)u * R * npm + r * npm + m]);
+          const dw b = acc_value(acc);
+          s.b0[i + m * R] = p.ishift < 0 ? dw_neg(b) : b;
         }
       }
       __syncthreads();
@@ -368,7 +377,7 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
         }
         __syncthreads();
       }
-      // -- the new factor: FP64 output, FP32 copy, double-word Gram (warp 0
+      // -- the new factor: FP64 output, double-word copy and Gram (warp 0
       //    rescales the POW weights first; no other thread reads them before
       //    the next barrier) --
       if (threadIdx.x < 32) {
@@ -379,7 +388,7 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
         const int i = e / nj, m = e % nj;
         const dw x = s.X[i + m * R];
         fb[(size_t)i * nD + t.off[j] + m] = dw_to_double(x);
-        s.f32[i * t.nDp + opj + m] = x.hi;
+        s.f[i * t.nDp + opj + m] = x;
       }
       for (int e = threadIdx.x; e < R * R; e += blockDim.x) {
         const int i = e % R, i2 = e / R;
@@ -397,24 +406,24 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
         for (int item = threadIdx.x; item < nu * R * nj; item += blockDim.x) {
           const int u = item / (R * nj), rem = item - u * R * nj, r = rem / nj, m = rem - r * nj;
           const int ug = t.uoff[j] + u;
-          float acc;
+          dw val;
           if (t.ident[ug]) {
-            acc = s.f32[r * t.nDp + opj + m];
+            val = s.f[r * t.nDp + opj + m];
           } else {
-            const float* h = hmat + (size_t)ug * npm * npm + (size_t)m * npm;
-            acc = 0.f;
-            for (int k = 0; k < nj; ++k) acc = fmaf(h[k], s.f32[r * t.nDp + opj + k], acc);
+            const dw* h = hmat + (size_t)ug * npm * npm + (size_t)m * npm;
+            dw_acc acc = acc_zero();
+            for (int k = 0; k < nj; ++k) acc_fma(acc, h[k], s.f[r * t.nDp + opj + k]);
+            val = acc_value(acc);
           }
-          Z[(size_t)u * R * npm + r * npm + m] = acc;
+          Z[(size_t)u * R * npm + r * npm + m] = val;
         }
         __syncthreads();
       }
       for (int item = threadIdx.x; item < nu * RR; item += blockDim.x) {
         const int u = item / RR, e = item - u * RR, r = e / R, i = e - r * R;
-        float acc = 0.f;
-        for (int m = 0; m < nj; ++m)
-          acc = fmaf(Z[(size_t)u * R * npm + r * npm + m], s.f32[i * t.nDp + opj + m], acc);
-        M[(size_t)(t.uoff[j] + u) * RR + e] = acc;
+        dw_acc acc = acc_zero();
+        for (int m = 0; m < nj; ++m) acc_fma(acc, Z[(size_t)u * R * npm + r * npm + m], s.f[i * t.nDp + opj + m]);
+        M[(size_t)(t.uoff[j] + u) * RR + e] = acc_value(acc);
       }
       __syncthreads();
     }

@@ -1,17 +1,15 @@
 """GPU intertwined power cycle (intertwinecpp_ through the C ABI) against the
 FP64 oracle.
 
-The GPU cycle uses the reference's FP32-build penalty rule (1e-5 max c,
-src/als.cu:248-267) in the stages whose right-hand sides are FP32
-contractions (power sweeps, H-applications, vector updates) and the FP64
-rule (1e-10) in the FP64 Gram-Schmidt; the oracle is run with the same
-per-stage rule.
+Both sides use the reference's FP64-build penalty rule (1e-10 max c,
+src/als.cu:248-267) in every stage; the oracle is the reference's FP64
+algorithm (pinned against the reference library in test_gpu_reference.py).
 
-Tolerances (FP32 contractions, FP64 normal equations and Rayleigh-Ritz):
-eigenvalues agree to 1e-6 relative; each output vector agrees with the
-oracle's as a function, |<a,b>| / (|a| |b|) >= 1 - 1e-6 (sign-insensitive:
-the eigenvector sign convention is fixed identically on both sides, but a
-vector's factors may carry compensating signs).
+Tolerances (double-word power sweeps, Gram-Schmidt and updates, FP64
+Rayleigh-Ritz): eigenvalues agree to 1e-6 relative; each output vector
+agrees with the oracle's as a function, |<a,b>| / (|a| |b|) >= 1 - 1e-6
+(sign-insensitive: the eigenvector sign convention is fixed identically on
+both sides, but a vector's factors may carry compensating signs).
 """
 import numpy as np
 import pytest
@@ -22,13 +20,6 @@ from mlcp_gb300 import intertwine as IT
 
 EIG_RTOL = 1e-6
 COS_TOL = 1e-6
-
-
-@pytest.fixture(autouse=True)
-def cycle_penalties():
-    oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
-    yield
-    oracle.set_cycle_penalties()
 
 
 def cos_sim(ab, ac, bb, bc, nbas):
@@ -175,12 +166,10 @@ def test_update_false_path_matches_oracle(cuda_device):
 @pytest.mark.gpu
 @pytest.mark.parametrize("ncyc", [0, 1, 6])
 def test_spectral_range_matches_oracle(ncyc, cuda_device):
-    """getspectralrangecpp_ against the oracle from the same starting vectors
-    (the power steps' FP32 contractions move the bounds by ~1e-7)."""
+    """getspectralrangecpp_ against the oracle from the same starting vectors."""
     hl = H.henon_heiles(D=4, n=6)
     b, c = oracle.spectral_start(hl.nbas, 5, seed=2)
     gb, gc, gbd = IT.spectral_range(b, c, hl.nbas, 5, hl, 4, ncyc)
-    oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
     ob, oc, obd = oracle.spectral_range(b, c, hl.nbas, 5, hl, 4, ncyc)
     np.testing.assert_allclose(gbd, obd, rtol=1e-6)
     compare_blocks(gb, gc, ob, oc, hl.nbas, 5, 2, tol=1e-5)

@@ -159,3 +159,54 @@ def test_cycle_oracle_matches_reference(ref):
     worst = min(cos_sim(ob[i * 16:(i + 1) * 16], oc[i * 16:(i + 1) * 16], rbq[i * 16:(i + 1) * 16],
                         rcq[i * 16:(i + 1) * 16], hl.nbas) for i in range(40))
     assert 1 - worst <= 1e-8, worst
+
+
+def converged_block(ncycle=40):
+    """The bench cycle's block after ncycle solver cycles on the GPU (from the
+    product-function guess), with the spectral bounds of that run."""
+    from mlcp_gb300 import hoplist as H
+    from mlcp_gb300 import solver
+    hl = H.henon_heiles(D=6, n=10, lam=0.111803)
+    base, coef, eigv, bounds, _ = solver.solve(hl, 40, 16, ncycle, 10, 10)
+    return hl, base, coef, eigv, bounds
+
+
+@pytest.mark.gpu
+def test_cycle_gpu_matches_reference_near_convergence(ref, cuda_device):
+    """From a block the solver has brought near convergence, one GPU cycle and
+    one reference cycle on identical inputs: eigenvalues to 1e-7 relative,
+    vectors to 1 - |cos| <= 1e-7."""
+    from mlcp_gb300 import intertwine as IT
+    hl, base, coef, eigv, bounds = converged_block()
+    esh = IT.block_shift(eigv, bounds[1])
+    rb, rc, re, _ = ref.intertwine(base, coef, hl.nbas, 16, 40, hl, eigv, 10, 10, True, 1, esh)
+    gb, gc, ge = IT.intertwine(base, coef, hl.nbas, 16, 40, hl, eigv, 10, 10, True, 1, esh)
+    rel = np.abs(ge - re) / np.abs(re)
+    assert rel.max() <= CYCLE_EIG_RTOL, rel.max()
+    worst = min(cos_sim(gb[i * 16:(i + 1) * 16], gc[i * 16:(i + 1) * 16], rb[i * 16:(i + 1) * 16],
+                        rc[i * 16:(i + 1) * 16], hl.nbas) for i in range(40))
+    assert 1 - worst <= CYCLE_COS_TOL, worst
+
+
+@pytest.mark.gpu
+def test_solver_loop_tracks_reference(ref, cuda_device):
+    """The solver loop (block shift, one cycle, repeat) driven once through
+    the GPU cycle and once through the reference's, from the same
+    product-function guess, spectral bounds and starting quotients, five
+    cycles: the eigenvalue histories agree to 1e-7 relative every cycle."""
+    from mlcp_gb300 import hoplist as H
+    from mlcp_gb300 import intertwine as IT
+    from mlcp_gb300 import solver
+    hl = H.henon_heiles(D=6, n=10, lam=0.111803)
+    base, coef = solver.product_guess(hl.nbas, 40, 16)
+    sb, sc = oracle.spectral_start(hl.nbas, 16)
+    _, _, bounds = oracle.spectral_range(sb, sc, hl.nbas, 16, hl, 10, 5)
+    e0 = oracle.qhq_diag(base, coef, hl.nbas, 16, 40, hl)
+    gb, gc, ge = base.copy(), coef.copy(), e0.copy()
+    rb, rc, re = base.copy(), coef.copy(), e0.copy()
+    for cyc in range(5):
+        gb, gc, ge = IT.intertwine(gb, gc, hl.nbas, 16, 40, hl, ge, 10, 10, True, 1, IT.block_shift(ge, bounds[1]))
+        rb, rc, re, _ = ref.intertwine(rb, rc, hl.nbas, 16, 40, hl, re, 10, 10, True, 1,
+                                       IT.block_shift(re, bounds[1]))
+        rel = np.abs(ge - re) / np.abs(re)
+        assert rel.max() <= CYCLE_EIG_RTOL, (cyc, rel.max())

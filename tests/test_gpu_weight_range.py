@@ -4,9 +4,9 @@ src/intertw_mvp.cu:452-497, sweep loop :468-494).
 The reference applies (H - E) once per mode step and renormalises the CP
 weights only at the end of a sweep, so within a sweep the weights grow by
 about ||H - E|| per step.  In FP64 that is harmless; the GPU sweep carries
-the weights in double-word (FP32 exponent) and its right-hand sides in FP32,
-so it rescales them by a power of two after every step (the end-of-sweep
-renormalisation removes any common factor).
+the weights and right-hand sides in double-word arithmetic (FP32 exponent
+range), so it rescales the weights by a power of two after every step (the
+end-of-sweep renormalisation removes any common factor).
 
 Check: the same power cycle on H and on 2^40 H (shift scaled alike).  A
 power-of-two scale changes no rounding, so the two results agree to the last
@@ -29,13 +29,6 @@ CASES = [
     (lambda: H.henon_heiles(D=4, n=6), 6, 5, 3, 1, 6.0),
     (lambda: H.random_hoplist([6, 4, 5, 3], 9, seed=8, coupling=3), 4, 3, 2, -1, 1.5),
 ]
-
-
-@pytest.fixture(autouse=True)
-def cycle_penalties():
-    oracle.set_cycle_penalties(mvp=oracle.PEN_FP32, gs=oracle.PEN_FP64, upd=oracle.PEN_FP32)
-    yield
-    oracle.set_cycle_penalties()
 
 
 def scaled(hl, s):
