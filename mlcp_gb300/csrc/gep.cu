@@ -5,12 +5,19 @@
 //  * gep_inner_kernel: A(i,j) = <Q_j, (HQ)_i>, S(i,j) = <Q_j, Q_i> for j <= i,
 //    full CP inner products in FP64 (one CTA per pair).
 //  * gep_solve_kernel (one CTA): S = L L^T, C = L^-1 A L^-T in FP64;
-//    eigenvectors of C by parallel cyclic Jacobi in FP32 (round-robin
-//    ordering, disjoint rotations per round); eigenvalues as FP64 Rayleigh
-//    quotients of C at those vectors (error quadratic in the FP32 vector
-//    error); X = L^-T V with unit columns, so X^T S X = I to FP32 accuracy.
-//    Eigenpairs are returned in ascending order, each eigenvector with its
-//    largest-magnitude entry positive.
+//    eigenvectors of C by parallel cyclic Jacobi (round-robin ordering,
+//    disjoint rotations per round), first in FP32 in shared memory, then
+//    refined in FP64: the FP32 vectors V are orthonormalised (two
+//    Newton-Schulz steps), C' = V^T C V is formed and FP64 Jacobi sweeps
+//    diagonalise it (quadratic convergence from the FP32 start: two or three
+//    sweeps), the rotations accumulating into V.  Eigenvalues are the
+//    diagonal of C'.  The FP64 stage matters: the vector updates combine
+//    the block with the eigenvectors, and for nearly degenerate states (the
+//    benchmark block has relative gaps of 4e-5) FP32 eigenvectors are off
+//    by ~1e-7 / gap, which moved the updated vectors by 1e-5 against the
+//    reference's FP64 sygvd.  X = L^-T V with unit columns.  Eigenpairs are
+//    returned in ascending order, each eigenvector with its largest-magnitude
+//    entry positive.
 #include <cfloat>
 
 #include "common.cuh"
@@ -229,29 +236,138 @@ __global__ void __launch_bounds__(kSolveThreads) gep_solve_kernel(GepParams p) {
       __syncthreads();
     }
   }
-  // ---- FP64 Rayleigh quotients; unit eigenvector columns ----
-  for (int e = tid; e < B * B; e += nt) {  // W = C V (V read from FP32)
+  // ---- FP64 refinement of the eigenvectors ----
+  double* V = invd + B;              // [B][B] FP64 eigenvectors (columns)
+  double* C2 = V + (size_t)B * B;    // [B][B] V^T C V, diagonalised in place
+  for (int e = tid; e < B * B; e += nt) {
+    const int r = e % B, c = e / B;
+    V[e] = (double)Vf[r + (size_t)c * Bp];
+  }
+  __syncthreads();
+  for (int ns = 0; ns < 2; ++ns) {  // V <- V (3 I - V^T V) / 2
+    for (int e = tid; e < B * B; e += nt) {  // Wm = V^T V
+      const int r = e % B, c = e / B;
+      double acc = 0.0;
+      for (int k = 0; k < B; ++k) acc += V[k + (size_t)r * B] * V[k + (size_t)c * B];
+      Wm[e] = acc;
+    }
+    __syncthreads();
+    for (int e = tid; e < B * B; e += nt) {  // C2 = V (1.5 I - 0.5 Wm)
+      const int r = e % B, c = e / B;
+      double acc = 1.5 * V[r + (size_t)c * B];
+      for (int k = 0; k < B; ++k) acc -= 0.5 * V[r + (size_t)k * B] * Wm[k + (size_t)c * B];
+      C2[e] = acc;
+    }
+    __syncthreads();
+    for (int e = tid; e < B * B; e += nt) V[e] = C2[e];
+    __syncthreads();
+  }
+  for (int e = tid; e < B * B; e += nt) {  // Wm = C V
     const int r = e % B, c = e / B;
     double acc = 0.0;
-    for (int k = 0; k < B; ++k) acc += C[r + (size_t)k * B] * (double)Vf[k + (size_t)c * Bp];
+    for (int k = 0; k < B; ++k) acc += C[r + (size_t)k * B] * V[k + (size_t)c * B];
     Wm[e] = acc;
   }
   __syncthreads();
-  for (int c = tid; c < B; c += nt) {
-    double num = 0.0, den = 0.0;
+  for (int e = tid; e < B * B; e += nt) {  // C2 = V^T C V, symmetrised
+    const int r = e % B, c = e / B;
+    double a1 = 0.0, a2 = 0.0;
     for (int k = 0; k < B; ++k) {
-      const double v = Vf[k + (size_t)c * Bp];
-      num += v * Wm[k + (size_t)c * B];
-      den += v * v;
+      a1 += V[k + (size_t)r * B] * Wm[k + (size_t)c * B];
+      a2 += V[k + (size_t)c * B] * Wm[k + (size_t)r * B];
     }
-    lam[c] = num / den;
+    C2[e] = 0.5 * (a1 + a2);
+  }
+  __syncthreads();
+  const int npB = B / 2;  // pairs of the odd index padding are skipped below
+  for (int sweep = 0; sweep < 12; ++sweep) {
+    double off = 0.0, dia = 0.0;
+    for (int e = tid; e < B * B; e += nt) {
+      const double v = C2[e];
+      if (e % B == e / B) dia += v * v; else off += v * v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      dia += __shfl_xor_sync(0xffffffffu, dia, o);
+    }
+    __syncthreads();
+    if (tid % 32 == 0) red[tid / 32] = off;
+    __syncthreads();
+    double offt = 0.0;
+    for (int w = 0; w < nt / 32; ++w) offt += red[w];
+    __syncthreads();
+    if (tid % 32 == 0) red[tid / 32] = dia;
+    __syncthreads();
+    double diat = 0.0;
+    for (int w = 0; w < nt / 32; ++w) diat += red[w];
+    __syncthreads();
+    if (offt <= 1e-30 * diat || offt == 0.0) break;
+    (void)npB;
+    for (int round = 0; round < Bp - 1; ++round) {
+      double* rcd = Wm;           // [Bp/2] cosines (Wm is free until the back substitution)
+      double* rsd = Wm + Bp / 2;  // [Bp/2] sines
+      for (int k = tid; k < npairs; k += nt) {
+        int a, b;
+        if (k == 0) {
+          a = Bp - 1;
+          b = round;
+        } else {
+          a = (round + k) % (Bp - 1);
+          b = (round - k + (Bp - 1)) % (Bp - 1);
+        }
+        if (a > b) { const int t = a; a = b; b = t; }
+        pq[2 * k] = a;
+        pq[2 * k + 1] = b;
+        double c = 1.0, sn = 0.0;
+        if (b < B) {  // index Bp - 1 = B is padding when B is odd
+          const double app = C2[a + (size_t)a * B], aqq = C2[b + (size_t)b * B], apq = C2[a + (size_t)b * B];
+          if (apq != 0.0) {
+            const double theta = (aqq - app) / (2.0 * apq);
+            const double t = copysign(1.0, theta) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            c = 1.0 / sqrt(t * t + 1.0);
+            sn = t * c;
+          }
+        }
+        rcd[k] = c;
+        rsd[k] = sn;
+      }
+      __syncthreads();
+      for (int e = tid; e < npairs * B; e += nt) {  // rows: C2 <- J^T C2
+        const int k = e / B, col = e % B;
+        const int a = pq[2 * k], b = pq[2 * k + 1];
+        if (b >= B) continue;
+        const double c = rcd[k], sn = rsd[k];
+        const double xa = C2[a + (size_t)col * B], xb = C2[b + (size_t)col * B];
+        C2[a + (size_t)col * B] = c * xa - sn * xb;
+        C2[b + (size_t)col * B] = sn * xa + c * xb;
+      }
+      __syncthreads();
+      for (int e = tid; e < npairs * B; e += nt) {  // columns: C2 <- C2 J, V <- V J
+        const int k = e / B, row = e % B;
+        const int a = pq[2 * k], b = pq[2 * k + 1];
+        if (b >= B) continue;
+        const double c = rcd[k], sn = rsd[k];
+        const double xa = C2[row + (size_t)a * B], xb = C2[row + (size_t)b * B];
+        C2[row + (size_t)a * B] = c * xa - sn * xb;
+        C2[row + (size_t)b * B] = sn * xa + c * xb;
+        const double va = V[row + (size_t)a * B], vb = V[row + (size_t)b * B];
+        V[row + (size_t)a * B] = c * va - sn * vb;
+        V[row + (size_t)b * B] = sn * va + c * vb;
+      }
+      __syncthreads();
+    }
+  }
+  for (int c = tid; c < B; c += nt) {
+    double den = 0.0;
+    for (int k = 0; k < B; ++k) den += V[k + (size_t)c * B] * V[k + (size_t)c * B];
+    lam[c] = C2[c + (size_t)c * B];
     invd[c] = 1.0 / sqrt(den);  // reuse: column scale
   }
   __syncthreads();
   // X = L^-T V (back substitution per column, columns in parallel through rows)
   for (int e = tid; e < B * B; e += nt) {
     const int r = e % B, c = e / B;
-    Wm[e] = (double)Vf[r + (size_t)c * Bp] * invd[c];
+    Wm[e] = V[r + (size_t)c * B] * invd[c];
   }
   __syncthreads();
   for (int jr = B - 1; jr >= 0; --jr) {
@@ -289,7 +405,7 @@ __global__ void __launch_bounds__(kSolveThreads) gep_solve_kernel(GepParams p) {
   if (tid == 0 && info) atomicOr(p.status, 2);
 }
 
-size_t gep_work_doubles(int nbloc) { return (size_t)3 * nbloc * nbloc + 2 * nbloc; }
+size_t gep_work_doubles(int nbloc) { return (size_t)5 * nbloc * nbloc + 2 * nbloc; }
 
 int gep_launch(const GepParams& p, cudaStream_t st) {
   const int B = p.nbloc;

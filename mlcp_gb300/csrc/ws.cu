@@ -1,0 +1,204 @@
+// Learned ALS warm start: the data kernels around the MLP (mlp.cu).
+//
+// One feature row per (vector, mode): the mode's factors of the vector's
+// ntop largest-weight target terms, each scaled to unit norm with its
+// largest-magnitude entry positive (a factor's sign and scale are
+// arbitrary in CP format: the weight and the other modes absorb them),
+// followed by the terms' log-weights.  The training target of the same row
+// is the mode's factors of the converged reduction, terms ordered by
+// decreasing |weight|, normalised the same way.  A proposal turns the MLP's
+// output rows back into unit factors, with the largest target weights as
+// the starting weights (ALS overwrites the weights and the first mode's
+// factors in its first step; the weights matter only through the penalty).
+#include <cfloat>
+
+#include "common.cuh"
+#include "mlp.cuh"
+
+namespace mlcp {
+
+namespace {
+
+constexpr int kWsThreads = 256;
+
+// Indices of the k largest |coef| among n entries (ties: lower index first),
+// -1 past n; every thread returns with top[] filled.
+__device__ void top_terms(const double* coef, int n, int k, unsigned* taken, int* top, float* rv, int* ri) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int w = tid; w < (n + 31) / 32; w += kWsThreads) taken[w] = 0u;
+  __syncthreads();
+  for (int q = 0; q < k; ++q) {
+    float bv = -1.f;
+    int bi = 0x7fffffff;
+    for (int j = tid; j < n; j += kWsThreads) {
+      if (taken[j >> 5] & (1u << (j & 31))) continue;
+      const float a = (float)fabs(coef[j]);
+      if (a > bv || (a == bv && j < bi)) {
+        bv = a;
+        bi = j;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > bv || (ov == bv && oi < bi)) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      rv[warp] = bv;
+      ri[warp] = bi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      float v = rv[0];
+      int i = ri[0];
+      for (int w = 1; w < kWsThreads / 32; ++w)
+        if (rv[w] > v || (rv[w] == v && ri[w] < i)) {
+          v = rv[w];
+          i = ri[w];
+        }
+      const int pick = (v >= 0.f && i < n) ? i : -1;
+      top[q] = pick;
+      if (pick >= 0) taken[pick >> 5] |= 1u << (pick & 31);
+    }
+    __syncthreads();
+  }
+}
+
+// Scale of a factor: 1/||g|| with the sign of its largest-magnitude entry
+// (0 for a zero factor).
+__device__ __forceinline__ double canon_scale(const double* g, int n) {
+  double s2 = 0.0, big = 0.0;
+  for (int m = 0; m < n; ++m) {
+    s2 += g[m] * g[m];
+    if (fabs(g[m]) > fabs(big)) big = g[m];
+  }
+  if (!(s2 > 0.0)) return 0.0;
+  return (big < 0.0 ? -1.0 : 1.0) / sqrt(s2);
+}
+
+__global__ void __launch_bounds__(kWsThreads) ws_features_kernel(WsBatch b, __nv_bfloat16* X, int ldx) {
+  extern __shared__ unsigned ws_smem[];
+  __shared__ int top[64];
+  __shared__ float rv[kWsThreads / 32];
+  __shared__ int ri[kWsThreads / 32];
+  const int v = blockIdx.x, n = b.n, D = b.ndof, K = b.ntop;
+  const long long off = b.g_off[v];
+  top_terms(b.coef + off, b.g_rank[v], K, ws_smem, top, rv, ri);
+  for (int item = threadIdx.x; item < D * K; item += kWsThreads) {
+    const int d = item / K, k = item - d * K, j = top[k];
+    __nv_bfloat16* row = X + (size_t)(v * D + d) * ldx;
+    if (j < 0) {
+      for (int m = 0; m < n; ++m) row[k * n + m] = __float2bfloat16_rn(0.f);
+      row[K * n + k] = __float2bfloat16_rn(-1.f);
+      continue;
+    }
+    const double* g = b.base + (size_t)(off + j) * b.nD + (size_t)d * n;
+    const double s = canon_scale(g, n);
+    for (int m = 0; m < n; ++m) row[k * n + m] = __float2bfloat16_rn((float)(g[m] * s));
+    const double c0 = fabs(b.coef[off + top[0]]), ck = fabs(b.coef[off + j]);
+    const double lw = (c0 > 0.0 && ck > 0.0) ? log10(ck / c0) / 8.0 : -1.0;
+    row[K * n + k] = __float2bfloat16_rn((float)fmax(lw, -1.0));
+  }
+}
+
+__global__ void __launch_bounds__(kWsThreads) ws_targets_kernel(WsBatch b, float* T, int ldt) {
+  __shared__ int ord[64];
+  const int v = blockIdx.x, n = b.n, D = b.ndof, R = b.rank;
+  const long long off = b.f_off[v];
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < R; ++i) ord[i] = i;
+    for (int a = 0; a < R; ++a) {  // selection sort by decreasing |weight| (R <= 64)
+      int mx = a;
+      for (int c = a + 1; c < R; ++c)
+        if (fabs(b.coef[off + ord[c]]) > fabs(b.coef[off + ord[mx]])) mx = c;
+      const int t = ord[a];
+      ord[a] = ord[mx];
+      ord[mx] = t;
+    }
+  }
+  __syncthreads();
+  for (int item = threadIdx.x; item < D * R; item += kWsThreads) {
+    const int d = item / R, i = item - d * R;
+    const double* g = b.base + (size_t)(off + ord[i]) * b.nD + (size_t)d * n;
+    const double s = canon_scale(g, n);
+    float* row = T + (size_t)(v * D + d) * ldt;
+    for (int m = 0; m < n; ++m) row[i * n + m] = (float)(g[m] * s);
+  }
+}
+
+__global__ void __launch_bounds__(kWsThreads) ws_apply_kernel(WsBatch b, const float* Y, int ldy) {
+  extern __shared__ unsigned ws_smem[];
+  __shared__ int top[64];
+  __shared__ float rv[kWsThreads / 32];
+  __shared__ int ri[kWsThreads / 32];
+  const int v = blockIdx.x, n = b.n, D = b.ndof, R = b.rank;
+  const long long goff = b.g_off[v], foff = b.f_off[v];
+  top_terms(b.coef + goff, b.g_rank[v], R, ws_smem, top, rv, ri);
+  // weights first (f_coef may alias coef only at the F terms, which are not targets)
+  for (int i = threadIdx.x; i < R; i += kWsThreads) b.f_coef[foff + i] = top[i] >= 0 ? fabs(b.coef[goff + top[i]]) : 0.0;
+  for (int item = threadIdx.x; item < D * R; item += kWsThreads) {
+    const int d = item / R, i = item - d * R;
+    const float* y = Y + (size_t)(v * D + d) * ldy + (size_t)i * n;
+    double s2 = 0.0;
+    for (int m = 0; m < n; ++m) s2 += (double)y[m] * y[m];
+    double* f = b.f_base + (size_t)(foff + i) * b.nD + (size_t)d * n;
+    if (s2 > 0.0) {
+      const double inv = 1.0 / sqrt(s2);
+      for (int m = 0; m < n; ++m) f[m] = y[m] * inv;
+    } else {
+      for (int m = 0; m < n; ++m) f[m] = (m == i % n) ? 1.0 : 0.0;
+    }
+  }
+}
+
+size_t top_smem(const WsBatch& b, int rgmax) { return sizeof(unsigned) * (size_t)((rgmax + 31) / 32 + 1); }
+
+}  // namespace
+
+int ws_check(const WsBatch& b) {
+  if (b.ntop < 1 || b.ntop > 64 || b.rank < 1 || b.rank > 64 || b.n < 1 || b.nD != b.ndof * b.n) {
+    set_error("warm start: unsupported sizes (ntop=%d rank=%d n=%d ndof=%d nD=%d): modes of one basis size, "
+              "ntop and rank at most 64", b.ntop, b.rank, b.n, b.ndof, b.nD);
+    return kBadArgument;
+  }
+  return kOk;
+}
+
+int ws_features_launch(const WsBatch& b, __nv_bfloat16* X, int ldx, int rgmax, cudaStream_t st) {
+  int rc = ws_check(b);
+  if (rc) return rc;
+  const size_t smem = top_smem(b, rgmax);
+  if (smem > 48 * 1024) {
+    set_error("warm start: targets of %d terms exceed the selection bitmap", rgmax);
+    return kTooLarge;
+  }
+  ws_features_kernel<<<b.nvec, kWsThreads, smem, st>>>(b, X, ldx);
+  MLCP_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+int ws_targets_launch(const WsBatch& b, float* T, int ldt, cudaStream_t st) {
+  int rc = ws_check(b);
+  if (rc) return rc;
+  ws_targets_kernel<<<b.nvec, kWsThreads, 0, st>>>(b, T, ldt);
+  MLCP_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+int ws_apply_launch(const WsBatch& b, const float* Y, int ldy, int rgmax, cudaStream_t st) {
+  int rc = ws_check(b);
+  if (rc) return rc;
+  const size_t smem = top_smem(b, rgmax);
+  if (smem > 48 * 1024) {
+    set_error("warm start: targets of %d terms exceed the selection bitmap", rgmax);
+    return kTooLarge;
+  }
+  ws_apply_kernel<<<b.nvec, kWsThreads, smem, st>>>(b, Y, ldy);
+  MLCP_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+
+}  // namespace mlcp
