@@ -191,6 +191,55 @@ MLCP_API int mlcp_als_batched_host(int nvec, int ndof, const int *nbas, const in
 MLCP_API int mlcp_als_noalloc(int ndof, const int *nbas, int rF, int rG, double *d_coef, double *d_base, int nals,
                               int *d_status, void *stream);
 
+/* ---- Learned ALS warm start (no counterpart in the reference, whose GPU ALS
+ * starts from a random CP vector, GPU_ALS_AA in src/GPUIterate.f90:191-210).
+ * Device pointers; stream NULL: the library's stream; each returns a Status.
+ * BF16 matrices are row-major with the contracted dimension contiguous. */
+
+/* C[M x N] = A[M x K] B[N x K]^T on the tcgen05 tensor cores (BF16 operands,
+ * FP32 accumulation in tensor memory).  M a multiple of 128, N of 16, K of 64,
+ * lda/ldb multiples of 8.  Epilogue: x = acc + bias[col] (bias may be NULL);
+ * act 0 keeps x, 1 applies max(x, 0), 2 keeps x where mask[row][col] > 0
+ * (the ReLU derivative through the forward activations); rows >= valid_m
+ * become 0.  Optional outputs C (FP32 [M][ldc]), Cb (BF16 [M][ldcb]), Ct
+ * (BF16 transposed, [N][ldct]).  d_status (optional) receives bit 1 if an
+ * internal wait timed out (the result is then not valid). */
+MLCP_API int mlcp_mlp_gemm(const void *A, const void *B, int M, int N, int K, int lda, int ldb, const float *bias,
+                           int act, const void *mask, int ldm, float *C, int ldc, void *Cb, int ldcb, void *Ct,
+                           int ldct, int valid_m, int *d_status, void *stream);
+/* Mean squared error of Y against T over rows < m, cols < n (both FP32
+ * [rows_p][ld]); dY = 2 (Y - T) / (m n) as BF16 [rows_p][ld] and transposed
+ * [ld][rows_p] (zero outside the valid block); the loss is added to *loss. */
+MLCP_API int mlcp_mlp_loss(const float *Y, const float *T, int m, int n, int ld, int rows_p, void *dY, void *dYt,
+                           float *loss, void *stream);
+/* db[c] = sum over rows of G[r][c] (BF16 [rows][ld]), c < n. */
+MLCP_API int mlcp_mlp_colsum(const void *G, int rows, int n, int ld, float *db, void *stream);
+/* One Adam step (bias-corrected, step >= 1) on FP32 parameters w [rows][cols]
+ * with gradient g and moments m1, m2; writes the BF16 copy wb and, when wt is
+ * not NULL, the transposed BF16 copy [cols][rows]. */
+MLCP_API int mlcp_mlp_adam(float *w, const float *g, float *m1, float *m2, int rows, int cols, float lr, float b1,
+                           float b2, float eps, int step, void *wb, void *wt, void *stream);
+/* Feature rows of a batch of reduction targets (reference layout, every
+ * mode of basis size n): row v*ndof + d holds, for the ntop (<= 64)
+ * largest-|weight| target terms of vector v (terms d_g_off[v] ..
+ * + d_g_rank[v], at most rgmax of them considered), their mode-d factors
+ * scaled to unit norm with the largest-magnitude entry positive, then their
+ * log10(|c| / |c_max|) / 8.  X: BF16, ldx >= ntop (n + 1). */
+MLCP_API int mlcp_ws_features(int nvec, int ndof, int n, int ntop, const long long *d_g_off, const int *d_g_rank,
+                              int rgmax, const double *d_base, const double *d_coef, void *X, int ldx, void *stream);
+/* Training targets: row v*ndof + d holds the mode-d factors of the rank
+ * terms of vector v at d_f_off[v] (a converged reduction), ordered by
+ * decreasing |weight| and normalised like the features.  T: FP32,
+ * ldt >= rank n. */
+MLCP_API int mlcp_ws_targets(int nvec, int ndof, int n, int rank, const long long *d_f_off, const double *d_base,
+                             const double *d_coef, float *T, int ldt, void *stream);
+/* A proposal: the rank F terms of vector v (at d_f_off[v]) get the
+ * normalised rows of Y (row v*ndof + d, columns i*n ..) as mode-d factors
+ * and the rank largest |target weights| as weights. */
+MLCP_API int mlcp_ws_apply(int nvec, int ndof, int n, int rank, const long long *d_g_off, const int *d_g_rank,
+                           int rgmax, const long long *d_f_off, double *d_base, double *d_coef, const float *Y,
+                           int ldy, void *stream);
+
 /* Kernel timing (extension).  When enabled, the library records CUDA events
  * around its dominant kernel of each call on the call's stream;
  * mlcp_gb300_last_kernel_ms() synchronises on the end event and returns the

@@ -87,6 +87,22 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             L.mlcp_read_psi.restype = ctypes.c_int
             L.mlcp_read_psi.argtypes = [ctypes.c_char_p, _I, _D, ctypes.c_int, _D, _D, ctypes.c_int, _I,
                                         ctypes.c_int, _I, _D, _D, _I]
+        _F = ctypes.c_float
+        _i = ctypes.c_int
+        L.mlcp_mlp_gemm.restype = _i
+        L.mlcp_mlp_gemm.argtypes = [_V, _V, _i, _i, _i, _i, _i, _V, _i, _V, _i, _V, _i, _V, _i, _V, _i, _i, _V, _V]
+        L.mlcp_mlp_loss.restype = _i
+        L.mlcp_mlp_loss.argtypes = [_V, _V, _i, _i, _i, _i, _V, _V, _V, _V]
+        L.mlcp_mlp_colsum.restype = _i
+        L.mlcp_mlp_colsum.argtypes = [_V, _i, _i, _i, _V, _V]
+        L.mlcp_mlp_adam.restype = _i
+        L.mlcp_mlp_adam.argtypes = [_V, _V, _V, _V, _i, _i, _F, _F, _F, _F, _i, _V, _V, _V]
+        L.mlcp_ws_features.restype = _i
+        L.mlcp_ws_features.argtypes = [_i, _i, _i, _i, _V, _V, _i, _V, _V, _V, _i, _V]
+        L.mlcp_ws_targets.restype = _i
+        L.mlcp_ws_targets.argtypes = [_i, _i, _i, _i, _V, _V, _V, _V, _i, _V]
+        L.mlcp_ws_apply.restype = _i
+        L.mlcp_ws_apply.argtypes = [_i, _i, _i, _i, _V, _V, _i, _V, _V, _V, _V, _i, _V]
         if hasattr(L, "intwdevicemem_"):
             L.intwdevicemem_.restype = None
             L.intwdevicemem_.argtypes = [_I, _I, _I, _I, _I, _I, _I, ctypes.POINTER(ctypes.c_bool), _I]

@@ -45,6 +45,7 @@ struct WsBatch {
   int nvec, ndof, nD, n;     // n: the common basis size
   int ntop;                  // target terms per feature row (64)
   int rank;                  // rank of the proposal (F terms)
+  int rgmax;                 // the selection bitmap's capacity in target terms (g_rank is clamped to it)
   const long long* g_off;    // [nvec] first target term of each vector in base/coef
   const int* g_rank;         // [nvec] target terms of each vector
   const long long* f_off;    // [nvec] first F term

@@ -12,7 +12,9 @@
 // factors in its first step; the weights matter only through the penalty).
 #include <cfloat>
 
+#include "../../include/mlcp_gb300.h"
 #include "common.cuh"
+#include "context.cuh"
 #include "mlp.cuh"
 
 namespace mlcp {
@@ -86,7 +88,7 @@ __global__ void __launch_bounds__(kWsThreads) ws_features_kernel(WsBatch b, __nv
   __shared__ int ri[kWsThreads / 32];
   const int v = blockIdx.x, n = b.n, D = b.ndof, K = b.ntop;
   const long long off = b.g_off[v];
-  top_terms(b.coef + off, b.g_rank[v], K, ws_smem, top, rv, ri);
+  top_terms(b.coef + off, min(b.g_rank[v], b.rgmax), K, ws_smem, top, rv, ri);
   for (int item = threadIdx.x; item < D * K; item += kWsThreads) {
     const int d = item / K, k = item - d * K, j = top[k];
     __nv_bfloat16* row = X + (size_t)(v * D + d) * ldx;
@@ -136,7 +138,7 @@ __global__ void __launch_bounds__(kWsThreads) ws_apply_kernel(WsBatch b, const f
   __shared__ int ri[kWsThreads / 32];
   const int v = blockIdx.x, n = b.n, D = b.ndof, R = b.rank;
   const long long goff = b.g_off[v], foff = b.f_off[v];
-  top_terms(b.coef + goff, b.g_rank[v], R, ws_smem, top, rv, ri);
+  top_terms(b.coef + goff, min(b.g_rank[v], b.rgmax), R, ws_smem, top, rv, ri);
   // weights first (f_coef may alias coef only at the F terms, which are not targets)
   for (int i = threadIdx.x; i < R; i += kWsThreads) b.f_coef[foff + i] = top[i] >= 0 ? fabs(b.coef[goff + top[i]]) : 0.0;
   for (int item = threadIdx.x; item < D * R; item += kWsThreads) {
@@ -171,11 +173,13 @@ int ws_features_launch(const WsBatch& b, __nv_bfloat16* X, int ldx, int rgmax, c
   int rc = ws_check(b);
   if (rc) return rc;
   const size_t smem = top_smem(b, rgmax);
-  if (smem > 48 * 1024) {
-    set_error("warm start: targets of %d terms exceed the selection bitmap", rgmax);
+  if (smem > 48 * 1024 || rgmax < 1) {
+    set_error("warm start: targets of %d terms outside the selection bitmap", rgmax);
     return kTooLarge;
   }
-  ws_features_kernel<<<b.nvec, kWsThreads, smem, st>>>(b, X, ldx);
+  WsBatch bb = b;
+  bb.rgmax = rgmax;
+  ws_features_kernel<<<b.nvec, kWsThreads, smem, st>>>(bb, X, ldx);
   MLCP_CUDA_TRY(cudaGetLastError());
   return kOk;
 }
@@ -192,13 +196,129 @@ int ws_apply_launch(const WsBatch& b, const float* Y, int ldy, int rgmax, cudaSt
   int rc = ws_check(b);
   if (rc) return rc;
   const size_t smem = top_smem(b, rgmax);
-  if (smem > 48 * 1024) {
-    set_error("warm start: targets of %d terms exceed the selection bitmap", rgmax);
+  if (smem > 48 * 1024 || rgmax < 1) {
+    set_error("warm start: targets of %d terms outside the selection bitmap", rgmax);
     return kTooLarge;
   }
-  ws_apply_kernel<<<b.nvec, kWsThreads, smem, st>>>(b, Y, ldy);
+  WsBatch bb = b;
+  bb.rgmax = rgmax;
+  ws_apply_kernel<<<b.nvec, kWsThreads, smem, st>>>(bb, Y, ldy);
   MLCP_CUDA_TRY(cudaGetLastError());
   return kOk;
 }
 
 }  // namespace mlcp
+
+// ---------------------------------------------------------------------------
+// extern "C" layer (device pointers; stream NULL: the library's stream)
+// ---------------------------------------------------------------------------
+
+namespace mlcp {
+int finish_status(int status);
+}
+
+using namespace mlcp;
+
+namespace {
+cudaStream_t ws_stream(void* stream, int* rc) {
+  if (stream) return static_cast<cudaStream_t>(stream);
+  Context* ctx = get_context(rc);
+  return ctx ? ctx->stream : nullptr;
+}
+}  // namespace
+
+extern "C" int mlcp_mlp_gemm(const void* A, const void* B, int M, int N, int K, int lda, int ldb, const float* bias,
+                             int act, const void* mask, int ldm, float* C, int ldc, void* Cb, int ldcb, void* Ct,
+                             int ldct, int valid_m, int* d_status, void* stream) {
+  int rc = kOk;
+  cudaStream_t st = ws_stream(stream, &rc);
+  if (rc) return finish_status(rc);
+  if (!A || !B || (act == 2 && !mask) || act < 0 || act > 2) {
+    set_error("mlcp_mlp_gemm: bad arguments");
+    return finish_status(kBadArgument);
+  }
+  MlpGemm g;
+  g.A = static_cast<const __nv_bfloat16*>(A); g.B = static_cast<const __nv_bfloat16*>(B);
+  g.M = M; g.N = N; g.K = K; g.lda = lda; g.ldb = ldb; g.bias = bias; g.act = act;
+  g.mask = static_cast<const __nv_bfloat16*>(mask); g.ldm = ldm; g.C = C; g.ldc = ldc;
+  g.Cb = static_cast<__nv_bfloat16*>(Cb); g.ldcb = ldcb; g.Ct = static_cast<__nv_bfloat16*>(Ct); g.ldct = ldct;
+  g.valid_m = valid_m; g.status = d_status;
+  return finish_status(mlp_gemm_launch(g, st));
+}
+
+extern "C" int mlcp_mlp_loss(const float* Y, const float* T, int m, int n, int ld, int rows_p, void* dY, void* dYt,
+                             float* loss, void* stream) {
+  int rc = kOk;
+  cudaStream_t st = ws_stream(stream, &rc);
+  if (rc) return finish_status(rc);
+  return finish_status(mlp_loss_launch(Y, T, m, n, ld, rows_p, static_cast<__nv_bfloat16*>(dY),
+                                       static_cast<__nv_bfloat16*>(dYt), loss, st));
+}
+
+extern "C" int mlcp_mlp_colsum(const void* G, int rows, int n, int ld, float* db, void* stream) {
+  int rc = kOk;
+  cudaStream_t st = ws_stream(stream, &rc);
+  if (rc) return finish_status(rc);
+  return finish_status(mlp_colsum_launch(static_cast<const __nv_bfloat16*>(G), rows, n, ld, db, st));
+}
+
+extern "C" int mlcp_mlp_adam(float* w, const float* g, float* m1, float* m2, int rows, int cols, float lr, float b1,
+                             float b2, float eps, int step, void* wb, void* wt, void* stream) {
+  int rc = kOk;
+  cudaStream_t st = ws_stream(stream, &rc);
+  if (rc) return finish_status(rc);
+  return finish_status(mlp_adam_launch(w, g, m1, m2, rows, cols, lr, b1, b2, eps, step,
+                                       static_cast<__nv_bfloat16*>(wb), static_cast<__nv_bfloat16*>(wt), st));
+}
+
+namespace {
+WsBatch make_ws(int nvec, int ndof, int n, int ntop, int rank, const long long* g_off, const int* g_rank,
+                const long long* f_off, const double* base, const double* coef, double* f_base, double* f_coef) {
+  WsBatch b;
+  b.nvec = nvec; b.ndof = ndof; b.nD = ndof * n; b.n = n; b.ntop = ntop; b.rank = rank; b.rgmax = 0;
+  b.g_off = g_off; b.g_rank = g_rank; b.f_off = f_off; b.base = base; b.coef = coef;
+  b.f_base = f_base; b.f_coef = f_coef;
+  return b;
+}
+}  // namespace
+
+extern "C" int mlcp_ws_features(int nvec, int ndof, int n, int ntop, const long long* d_g_off, const int* d_g_rank,
+                                int rgmax, const double* d_base, const double* d_coef, void* X, int ldx,
+                                void* stream) {
+  int rc = kOk;
+  cudaStream_t st = ws_stream(stream, &rc);
+  if (rc) return finish_status(rc);
+  if (nvec < 1 || ldx < ntop * n + ntop) {
+    set_error("mlcp_ws_features: nvec = %d, ldx = %d below ntop (n + 1) = %d", nvec, ldx, ntop * (n + 1));
+    return finish_status(kBadArgument);
+  }
+  const WsBatch b = make_ws(nvec, ndof, n, ntop, 1, d_g_off, d_g_rank, nullptr, d_base, d_coef, nullptr, nullptr);
+  return finish_status(ws_features_launch(b, static_cast<__nv_bfloat16*>(X), ldx, rgmax, st));
+}
+
+extern "C" int mlcp_ws_targets(int nvec, int ndof, int n, int rank, const long long* d_f_off, const double* d_base,
+                               const double* d_coef, float* T, int ldt, void* stream) {
+  int rc = kOk;
+  cudaStream_t st = ws_stream(stream, &rc);
+  if (rc) return finish_status(rc);
+  if (nvec < 1 || ldt < rank * n) {
+    set_error("mlcp_ws_targets: nvec = %d, ldt = %d below rank n = %d", nvec, ldt, rank * n);
+    return finish_status(kBadArgument);
+  }
+  const WsBatch b = make_ws(nvec, ndof, n, 1, rank, nullptr, nullptr, d_f_off, d_base, d_coef, nullptr, nullptr);
+  return finish_status(ws_targets_launch(b, T, ldt, st));
+}
+
+extern "C" int mlcp_ws_apply(int nvec, int ndof, int n, int rank, const long long* d_g_off, const int* d_g_rank,
+                             int rgmax, const long long* d_f_off, double* d_base, double* d_coef, const float* Y,
+                             int ldy, void* stream) {
+  int rc = kOk;
+  cudaStream_t st = ws_stream(stream, &rc);
+  if (rc) return finish_status(rc);
+  if (nvec < 1 || ldy < rank * n) {
+    set_error("mlcp_ws_apply: nvec = %d, ldy = %d below rank n = %d", nvec, ldy, rank * n);
+    return finish_status(kBadArgument);
+  }
+  const WsBatch b = make_ws(nvec, ndof, n, 1, rank, d_g_off, d_g_rank, d_f_off, d_base, d_coef, d_base, d_coef);
+  return finish_status(ws_apply_launch(b, Y, ldy, rgmax, st));
+}

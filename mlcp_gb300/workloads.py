@@ -110,5 +110,59 @@ def main(argv=None) -> int:
     return 1 if bad else 0
 
 
+
+def apply_hamiltonian(hl, base: np.ndarray, coef: np.ndarray, shift: float = 0.0):
+    """(H - shift) F as an explicit CP vector: every term t of the operator
+    list applied to every term r of F (factors h_t^d F_r^d, weight alpha_t c_r),
+    then the shift's copy of F (weight -shift c_r); rank (T + 1) R.  This is
+    the unreduced vector that a power step reduces (reference PRODHV,
+    src/MODHVECML.f90:50-209)."""
+    from . import hoplist as H
+    D = hl.ndof
+    offs = np.concatenate([[0], np.cumsum(hl.nbas)])
+    cache = H.operator_cache(hl)
+    R = coef.size
+    T = hl.nterms
+    out_b = np.empty(((T + 1) * R, base.shape[1]))
+    out_c = np.empty((T + 1) * R)
+    for t in range(T):
+        blk = base.copy()
+        for d in range(D):
+            M = cache[t][d]
+            if M is not None:
+                blk[:, offs[d]:offs[d + 1]] = base[:, offs[d]:offs[d + 1]] @ M.T
+        out_b[t * R:(t + 1) * R] = blk
+        out_c[t * R:(t + 1) * R] = hl.coef[t] * coef
+    out_b[T * R:] = base
+    out_c[T * R:] = -shift * coef
+    return out_b, out_c
+
+
+def power_batch(hl, bases, coefs, rank: int, shift: float = 0.0) -> AlsBatch:
+    """A batch of power-step reductions: vector v reduces (H - shift) F_v
+    (normalised to unit weight sum of squares) to rank ``rank``; its F slots
+    hold the first ``rank`` target terms (to be replaced by a start)."""
+    tb, tc = [], []
+    for b, c in zip(bases, coefs):
+        gb, gc = apply_hamiltonian(hl, b, c, shift)
+        gc = gc / np.sqrt(np.sum(gc * gc))
+        tb.append(gb)
+        tc.append(gc)
+    rG = np.array([x.size for x in tc], dtype=np.int32)
+    rF = np.full(len(tc), rank, dtype=np.int32)
+    sizes = (rF + rG).astype(np.int64)
+    term_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    nD = int(np.sum(hl.nbas))
+    base = np.empty((int(sizes.sum()), nD))
+    coef = np.empty(int(sizes.sum()))
+    for v in range(len(tc)):
+        t0 = int(term_off[v])
+        base[t0:t0 + rank] = tb[v][:rank]
+        coef[t0:t0 + rank] = tc[v][:rank]
+        base[t0 + rank:t0 + rank + rG[v]] = tb[v]
+        coef[t0 + rank:t0 + rank + rG[v]] = tc[v]
+    return AlsBatch(nbas=np.asarray(hl.nbas, dtype=np.int32), rF=rF, rG=rG, term_off=term_off, coef=coef, base=base)
+
+
 if __name__ == "__main__":
     raise SystemExit(main())
