@@ -547,7 +547,8 @@ def run_gpu(args):
                              "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                              "kernel": "als_cluster_kernel", "kernel_ms": kernel_ms,
                              "algorithmic_bytes": alg_bytes},
-                "cpu_baseline": cpu, "clocks": clk}
+                "cpu_baseline": cpu, "clocks": clk,
+                "autotune": _lib.autotune_report().strip().splitlines()}
         if not args.no_cycle and ws == 1:
             line["power_cycle"] = run_cycle_bench(max(1, min(args.steps, 5)), cpu=not args.no_cpu)
         if not args.no_fp64 and ws == 1:

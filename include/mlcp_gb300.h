@@ -95,6 +95,17 @@ MLCP_API void getspectralrangecpp_(double *base, double *coef, int *nbas, MLCP_R
                                    double *mat, MLCP_REF(int) TxD, MLCP_REF(int) nops, MLCP_REF(int) msize,
                                    double *bounds);
 
+/* Replaces GetQHQ and GetOverlaps (src/BlockUtils.f90:229-264, :347-381) as
+ * one call: qhq[i + j*nbloc] = <Q_j|H|Q_i> and s[i + j*nbloc] = <Q_j|Q_i>
+ * (full symmetric nbloc x nbloc, column-major, FP64, H applied exactly; s may
+ * be NULL), for a block in intertwinecpp_'s layout.  With a one-term operator
+ * list it gives the matrix of a product of one-mode operators in the block's
+ * basis, which UpdateH/UpdateOperMat (src/Updater.f90:53-151) carry to the
+ * next layer of the mode tree. */
+MLCP_API void getqhqcpp_(double *base, double *coef, int *nbas, MLCP_REF(int) rk, MLCP_REF(int) ndof,
+                         MLCP_REF(int) nbloc, int *opid, int *mptr, double *Hcoef, double *mat, MLCP_REF(int) TxD,
+                         MLCP_REF(int) nops, MLCP_REF(int) msize, double *qhq, double *s);
+
 /* Replaces Diagonalize(Q, H, eigv, .FALSE., ...) (src/BlockUtils.f90:184-225),
  * the pre-diagonalisation of the block that the solver runs before its
  * cycles (src/Solver.f90:363-369), on the GPU: A = <Q|H|Q> and S = <Q|Q>
@@ -239,6 +250,18 @@ MLCP_API int mlcp_ws_targets(int nvec, int ndof, int n, int rank, const long lon
 MLCP_API int mlcp_ws_apply(int nvec, int ndof, int n, int rank, const long long *d_g_off, const int *d_g_rank,
                            int rgmax, const long long *d_f_off, double *d_base, double *d_coef, const float *Y,
                            int ldy, void *stream);
+
+/* Launch-shape autotuner of the batched ALS (extension; replaces the
+ * reference's fixed block-shape rules, PVVkernel::initnew in
+ * src/modvecvec.cu:27-94).  Enabled by default (MLCP_GB300_AUTOTUNE=0 in the
+ * environment, or enable = 0 here, selects the fixed rule).  The first
+ * device-resident reduction of a batch shape times one sweep for every
+ * feasible (cluster size, tile-ring depth) pair on the caller's data, F
+ * restored after each, and caches the fastest per device and shape; the call
+ * synchronises its stream while it tunes.  The report lists each cached
+ * choice with its trial times; returns the report's length. */
+MLCP_API void mlcp_gb300_set_autotune(int enable);
+MLCP_API int mlcp_gb300_autotune_report(char *buf, int len);
 
 /* Kernel timing (extension).  When enabled, the library records CUDA events
  * around its dominant kernel of each call on the call's stream;

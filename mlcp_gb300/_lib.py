@@ -65,6 +65,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         if hasattr(L, "getqhqdiagcpp_"):
             L.getqhqdiagcpp_.restype = None
             L.getqhqdiagcpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I, _I, _I, _D, _D, _I, _I, _I, _D]
+        if hasattr(L, "getqhqcpp_"):
+            L.getqhqcpp_.restype = None
+            L.getqhqcpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I, _I, _D, _D, _I, _I, _I, _D, _V]
         if hasattr(L, "getspectralrangecpp_"):
             L.getspectralrangecpp_.restype = None
             L.getspectralrangecpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I, _I, _I, _D, _D, _I, _I, _I, _D]
@@ -87,6 +90,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
             L.mlcp_read_psi.restype = ctypes.c_int
             L.mlcp_read_psi.argtypes = [ctypes.c_char_p, _I, _D, ctypes.c_int, _D, _D, ctypes.c_int, _I,
                                         ctypes.c_int, _I, _D, _D, _I]
+        L.mlcp_gb300_set_autotune.restype = None
+        L.mlcp_gb300_set_autotune.argtypes = [ctypes.c_int]
+        L.mlcp_gb300_autotune_report.restype = ctypes.c_int
+        L.mlcp_gb300_autotune_report.argtypes = [ctypes.c_char_p, ctypes.c_int]
         _F = ctypes.c_float
         _i = ctypes.c_int
         L.mlcp_mlp_gemm.restype = _i
@@ -118,6 +125,15 @@ def check(rc: int) -> None:
 
 def last_status() -> int:
     return load().mlcp_gb300_last_status()
+
+
+def autotune_report() -> str:
+    """The autotuner's cached launch shapes and trial times."""
+    L = load()
+    n = L.mlcp_gb300_autotune_report(None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    L.mlcp_gb300_autotune_report(buf, n + 1)
+    return buf.value.decode()
 
 
 def last_error() -> str:

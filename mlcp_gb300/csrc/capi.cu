@@ -4,8 +4,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/mlcp_gb300.h"
@@ -195,10 +197,188 @@ int plan_als(Context* ctx, int nvec, int ndof, const int* nbas, const int* rF, c
   return kOk;
 }
 
+// ---------------------------------------------------------------------------
+// Launch-shape autotuner of the batched ALS
+// ---------------------------------------------------------------------------
+// The reference sizes its kernels' blocks by fixed rules on the ranks
+// (PVVkernel::initnew, src/modvecvec.cu:27-94).  Here two shape parameters of
+// the cluster kernel are measured instead: the cluster size (CTAs sharing one
+// vector's target terms) and the depth of the target-tile ring.  The first
+// call for a batch shape runs one sweep with every feasible (cluster, stages)
+// pair on the caller's own data (the F terms are saved first and restored
+// after every trial, so the call's result is unaffected), times each with CUDA
+// events on the call's stream, and caches the fastest for the process, per
+// device and shape.  Later calls with the same shape reuse it.  Disabled by
+// mlcp_gb300_set_autotune(0) or MLCP_GB300_AUTOTUNE=0 (then the rule of
+// als_choose_shape applies).
+
+struct TuneKey {
+  int device, nvec, ndof, nD, npmax, gsmax, rGmax, rFmax;
+  long long total_rows;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(device, nvec, ndof, nD, npmax, gsmax, rGmax, rFmax, total_rows) <
+           std::tie(o.device, o.nvec, o.ndof, o.nD, o.npmax, o.gsmax, o.rGmax, o.rFmax, o.total_rows);
+  }
+};
+
+struct TuneEntry {
+  AlsShape shape;
+  std::vector<std::pair<AlsShape, float>> trials;  // (shape, ms for one sweep)
+};
+
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneEntry> g_tune;
+int g_autotune = -1;  // -1: not yet read from the environment
+
+bool autotune_enabled() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (g_autotune < 0) {
+    const char* e = getenv("MLCP_GB300_AUTOTUNE");
+    g_autotune = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_autotune != 0;
+}
+
+// Feasible (cluster, stages) pairs: every power-of-two cluster up to 16 whose
+// clusters fit on the GPU in at most two waves, every ring depth 2-6 whose
+// shared memory fits.
+std::vector<AlsShape> als_candidates(int nvec, int rGmax, int rFmax, int npmax, int gsmax, int num_sms,
+                                     size_t smem_limit) {
+  std::vector<AlsShape> out;
+  for (int cl = 1; cl <= 16; cl *= 2) {
+    if (cl > 1 && (long long)cl * nvec > 2LL * num_sms) break;
+    const int rows = (rGmax + cl - 1) / cl;
+    for (int ns = 2; ns <= 6; ++ns) {
+      const size_t b = als_smem_bytes(rows, rFmax, npmax, gsmax, ns);
+      if (b > smem_limit) continue;
+      AlsShape s;
+      s.cluster = cl;
+      s.stages = ns;
+      s.rows_cta = rows;
+      s.smem = b;
+      out.push_back(s);
+    }
+  }
+  return out;
+}
+
 }  // namespace
 
-// Runs one batched reduction; everything is enqueued on `st`.
+int als_run_shape(Context* ctx, const AlsJob& job, cudaStream_t st, const AlsShape* forced);
+
+// Runs one batched reduction; everything is enqueued on `st`.  The launch
+// shape comes from the autotuner (measured once per batch shape) or, with
+// tuning off or for shared-target and host-target jobs, from the rule.
 int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
+  if (job.nals <= 0 || job.shared_w || !autotune_enabled()) return als_run_shape(ctx, job, st, nullptr);
+  AlsPlan P;
+  int rc = plan_als(ctx, job.nvec, job.ndof, job.nbas, job.rF, job.rG, &P);
+  if (rc) return rc;
+  TuneKey key{ctx->device, job.nvec, job.ndof, P.nD, P.npmax, P.gsmax, 0, P.rFmax, P.total_rows};
+  for (int v = 0; v < job.nvec; ++v) key.rGmax = std::max(key.rGmax, job.rG[v]);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      const AlsShape s = it->second.shape;
+      return als_run_shape(ctx, job, st, &s);
+    }
+  }
+  if (job.g_host) return als_run_shape(ctx, job, st, nullptr);  // tuned by a device-resident call
+  std::vector<AlsShape> cand = als_candidates(job.nvec, key.rGmax, P.rFmax, P.npmax, P.gsmax, ctx->num_sms,
+                                              ctx->smem_optin);
+  if (cand.size() <= 1) return als_run_shape(ctx, job, st, nullptr);
+  // save the F terms (the trials overwrite them)
+  const size_t fvals = (size_t)P.total_f * P.nD;
+  const size_t bytes = sizeof(double) * (fvals + P.total_f);
+  if (bytes > ctx->tune_bytes) {
+    if (ctx->tune) {
+      MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+      MLCP_CUDA_TRY(cudaFree(ctx->tune));
+      ctx->tune = nullptr;
+      ctx->tune_bytes = 0;
+    }
+    MLCP_CUDA_TRY(cudaMalloc(&ctx->tune, bytes));
+    ctx->tune_bytes = bytes;
+  }
+  double* sb = static_cast<double*>(ctx->tune);
+  double* sc = sb + fvals;
+  auto copy_f = [&](bool save) -> int {
+    size_t fo = 0;
+    for (int v = 0; v < job.nvec; ++v) {
+      double* b = job.d_base + (size_t)job.term_off[v] * P.nD;
+      double* c = job.d_coef + job.term_off[v];
+      const size_t nb = sizeof(double) * (size_t)job.rF[v] * P.nD, nc = sizeof(double) * job.rF[v];
+      MLCP_CUDA_TRY(cudaMemcpyAsync(save ? sb + fo * P.nD : b, save ? b : sb + fo * P.nD, nb,
+                                    cudaMemcpyDeviceToDevice, st));
+      MLCP_CUDA_TRY(cudaMemcpyAsync(save ? sc + fo : c, save ? c : sc + fo, nc, cudaMemcpyDeviceToDevice, st));
+      fo += job.rF[v];
+    }
+    return kOk;
+  };
+  if ((rc = copy_f(true))) return rc;
+  cudaEvent_t e0, e1;
+  MLCP_CUDA_TRY(cudaEventCreate(&e0));
+  MLCP_CUDA_TRY(cudaEventCreate(&e1));
+  AlsJob trial = job;
+  trial.nals = 1;
+  TuneEntry entry;
+  float best = 0.f;
+  for (const AlsShape& c : cand) {
+    MLCP_CUDA_TRY(cudaEventRecord(e0, st));
+    rc = als_run_shape(ctx, trial, st, &c);
+    if (rc) break;
+    MLCP_CUDA_TRY(cudaEventRecord(e1, st));
+    MLCP_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    MLCP_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    entry.trials.push_back({c, ms});
+    if (entry.trials.size() == 1 || ms < best) {
+      best = ms;
+      entry.shape = c;
+    }
+    if ((rc = copy_f(false))) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = entry;
+  }
+  const AlsShape s = entry.shape;
+  return als_run_shape(ctx, job, st, &s);
+}
+
+int autotune_report(char* buf, int len) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::string out;
+  char line[256];
+  for (const auto& kv : g_tune) {
+    const TuneKey& k = kv.first;
+    snprintf(line, sizeof(line), "als nvec=%d ndof=%d nD=%d rG<=%d rF<=%d: cluster %d stages %d;", k.nvec, k.ndof,
+             k.nD, k.rGmax, k.rFmax, kv.second.shape.cluster, kv.second.shape.stages);
+    out += line;
+    for (const auto& t : kv.second.trials) {
+      snprintf(line, sizeof(line), " %dx%d=%.3fms", t.first.cluster, t.first.stages, t.second);
+      out += line;
+    }
+    out += "\n";
+  }
+  if (buf && len > 0) {
+    strncpy(buf, out.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)out.size();
+}
+
+void set_autotune(int on) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_autotune = on ? 1 : 0;
+}
+
+// One batched reduction with the given launch shape (null: the rule).
+int als_run_shape(Context* ctx, const AlsJob& job, cudaStream_t st, const AlsShape* forced) {
   const int nvec = job.nvec, ndof = job.ndof, nals = job.nals;
   const int *nbas = job.nbas, *rF = job.rF, *rG = job.rG;
   const long long* term_off = job.term_off;
@@ -213,6 +393,7 @@ int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
   AlsPlan P;
   int rc = plan_als(ctx, nvec, ndof, nbas, rF, rG, &P);
   if (rc) return rc;
+  if (forced) P.shape = *forced;
   const int CL = P.shape.cluster;
 
   // metadata block: ints then long longs (uploaded in one copy)
@@ -475,6 +656,10 @@ extern "C" double mlcp_gb300_last_kernel_ms(void) {
   return ms;
 }
 extern "C" int mlcp_gb300_last_status(void) { return t_status; }
+
+extern "C" void mlcp_gb300_set_autotune(int enable) { set_autotune(enable); }
+
+extern "C" int mlcp_gb300_autotune_report(char* buf, int len) { return autotune_report(buf, len); }
 
 static cudaStream_t pick_stream(Context* ctx, void* stream) {
   return stream ? static_cast<cudaStream_t>(stream) : ctx->stream;

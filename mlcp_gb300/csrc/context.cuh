@@ -26,6 +26,9 @@ struct Context {
   // also uses for its vector updates)
   void* cyc = nullptr;
   size_t cyc_bytes = 0;
+  // autotuner: saved F terms during trials
+  void* tune = nullptr;
+  size_t tune_bytes = 0;
   // device copies of caller host buffers (host-buffer entry points)
   void* io = nullptr;
   size_t io_bytes = 0;

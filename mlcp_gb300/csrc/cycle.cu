@@ -487,6 +487,72 @@ __global__ void range_shift_kernel(const double* bounds, double* shift) {
 // Reduction threshold of the reference's solver (redtol, src/Solver.f90:326).
 constexpr double kRedTol = 1.0e-12;
 
+// The block's H and overlap matrices with H applied exactly (reference GetQHQ
+// and GetOverlaps, src/BlockUtils.f90:229-264, :347-381), returned in full:
+// qhq[i + j nbloc] = <Q_j|H|Q_i>, s[i + j nbloc] = <Q_j|Q_i>, symmetric,
+// FP64 (rq_apply + rq_pair kernels).  With a one-term operator list this is
+// also the matrix of a product of one-mode operators in the block's basis,
+// which the next layer of a mode tree needs for terms that couple modes
+// inside one node (UpdateH / UpdateOperMat, src/Updater.f90:53-151).
+int qhq_full(Context* ctx, const double* base, const double* coef, const int* nbas, int rk, int ndof, int nbloc,
+             const int* opid, const int* mptr, const double* Hcoef, const double* mat, int TxD, int nops, int msize,
+             double* qhq, double* s_out) {
+  if (rk < 1 || rk > kMaxRankCycle) {
+    set_error("getqhqcpp_: rk = %d outside [1, %d]", rk, kMaxRankCycle);
+    return rk < 1 ? kBadArgument : kTooLarge;
+  }
+  if (ndof < 1 || nbloc < 1 || TxD < ndof || TxD % ndof != 0 || nops < 1 || msize < 1 || !qhq) {
+    set_error("getqhqcpp_: bad sizes (ndof=%d nbloc=%d TxD=%d nops=%d msize=%d)", ndof, nbloc, TxD, nops, msize);
+    return kBadArgument;
+  }
+  Layout Ly;
+  int rc = make_layout(ndof, nbas, &Ly);
+  if (rc) return rc;
+  const int T = TxD / ndof, R = rk, B = nbloc;
+  cudaStream_t st = ctx->stream;
+  OpTable tab;
+  rc = get_optable(ctx, Ly, nbas, R, T, opid, mptr, Hcoef, mat, nops, msize, st, &tab);
+  if (rc) return rc;
+  const size_t nvals = (size_t)B * R * Ly.nD;
+  size_t bytes = 0;
+  auto take = [&](size_t b) { size_t o = align256(bytes); bytes = o + b; return o; };
+  const size_t o_q = take(sizeof(double) * nvals), o_qc = take(sizeof(double) * B * R),
+               o_y = take(sizeof(double) * (size_t)B * tab.utot * R * tab.npmax),
+               o_a = take(sizeof(double) * (size_t)B * B), o_s = take(sizeof(double) * (size_t)B * B);
+  if (bytes > ctx->cyc_bytes) {
+    if (ctx->cyc) {
+      MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+      MLCP_CUDA_TRY(cudaFree(ctx->cyc));
+      ctx->cyc = nullptr;
+      ctx->cyc_bytes = 0;
+    }
+    MLCP_CUDA_TRY(cudaMalloc(&ctx->cyc, bytes));
+    ctx->cyc_bytes = bytes;
+  }
+  char* b = static_cast<char*>(ctx->cyc);
+  double* q = reinterpret_cast<double*>(b + o_q);
+  double* qc = reinterpret_cast<double*>(b + o_qc);
+  double* y = reinterpret_cast<double*>(b + o_y);
+  double* A = reinterpret_cast<double*>(b + o_a);
+  double* S = reinterpret_cast<double*>(b + o_s);
+  MLCP_CUDA_TRY(cudaMemcpyAsync(q, base, sizeof(double) * nvals, cudaMemcpyHostToDevice, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(qc, coef, sizeof(double) * B * R, cudaMemcpyHostToDevice, st));
+  if ((rc = rq_apply_launch(tab, B, Ly.nD, q, y, st))) return rc;
+  RqPairParams rp;
+  rp.ops = tab; rp.nvec = B; rp.nD = Ly.nD; rp.base = q; rp.coef = qc; rp.y = y; rp.A = A; rp.S = S;
+  if ((rc = rq_pair_launch(rp, (int)ctx->smem_optin, st))) return rc;
+  std::vector<double> ha((size_t)B * B), hs((size_t)B * B);
+  MLCP_CUDA_TRY(cudaMemcpyAsync(ha.data(), A, sizeof(double) * B * B, cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaMemcpyAsync(hs.data(), S, sizeof(double) * B * B, cudaMemcpyDeviceToHost, st));
+  MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int j = 0; j < B; ++j)
+    for (int i = j; i < B; ++i) {
+      qhq[i + (size_t)j * B] = qhq[j + (size_t)i * B] = ha[i + (size_t)j * B];
+      if (s_out) s_out[i + (size_t)j * B] = s_out[j + (size_t)i * B] = hs[i + (size_t)j * B];
+    }
+  return kOk;
+}
+
 // Reference Diagonalize with intw = .FALSE. (src/BlockUtils.f90:184-225), the
 // solver's pre-diagonalisation (src/Solver.f90:363-369): A = <Q|H|Q> and
 // S = <Q|Q> with H applied exactly (GetQHQ, GetOverlaps; the reference
@@ -860,6 +926,19 @@ extern "C" void getspectralrangecpp_(double* base, double* coef, int* nbas, cons
   }
   finish_status(rc);
   if (rc != kOk) fprintf(stderr, "getspectralrangecpp_: %s\n", last_error());
+}
+
+extern "C" void getqhqcpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof, const int& nbloc,
+                           int* opid, int* mptr, double* Hcoef, double* mat, const int& TxD, const int& nops,
+                           const int& msize, double* qhq, double* s) {
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (ctx) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    rc = qhq_full(ctx, base, coef, nbas, rk, ndof, nbloc, opid, mptr, Hcoef, mat, TxD, nops, msize, qhq, s);
+  }
+  finish_status(rc);
+  if (rc != kOk) fprintf(stderr, "getqhqcpp_: %s\n", last_error());
 }
 
 extern "C" void diagonalizecpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof,

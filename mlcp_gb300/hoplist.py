@@ -223,6 +223,18 @@ def synthetic_qff(D: int, n, seed: int, wmin: float = 200.0, wmax: float = 3200.
     semi-diagonal quartic constants N(0, quartic_sigma) on (i,i,j,j).  Each
     constant is divided by the factorials of its mode powers (the reference's
     ``divide`` option, src/FFPES.f90:390-397)."""
+    nb, single, terms = qff_terms(D, n, seed, wmin, wmax, cubic_frac, cubic_sigma, quartic_sigma)
+    if eigenbasis:
+        terms, eig_ops = _to_eigenbasis(nb, single, terms)
+        return build_hoplist(nb, terms, eig_ops)
+    return build_hoplist(nb, terms)
+
+
+def qff_terms(D: int, n, seed: int, wmin: float = 200.0, wmax: float = 3200.0, cubic_frac: float = 0.3,
+              cubic_sigma: float = 50.0, quartic_sigma: float = 5.0):
+    """The terms of synthetic_qff in the primitive harmonic-oscillator basis:
+    (nbas, one-mode harmonic operators, [(coef, {mode: operator})]) with the D
+    harmonic terms first."""
     rng = np.random.default_rng(seed)
     nb = np.full(D, n, dtype=np.int32) if np.isscalar(n) else np.asarray(n, dtype=np.int32)
     omega = rng.uniform(wmin, wmax, D)
@@ -249,10 +261,7 @@ def synthetic_qff(D: int, n, seed: int, wmin: float = 200.0, wmax: float = 3200.
                 terms.append((phi / 24.0, {i: q[i][4]}))
             else:
                 terms.append((phi / 4.0, {i: q[i][2], j: q[j][2]}))
-    if eigenbasis:
-        terms, eig_ops = _to_eigenbasis(nb, single, terms)
-        return build_hoplist(nb, terms, eig_ops)
-    return build_hoplist(nb, terms)
+    return nb, single, terms
 
 
 def random_hoplist(nbas: Sequence[int], T: int, seed: int, coupling: int = 2) -> HopList:

@@ -121,6 +121,30 @@ def diagonalize(base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int, h
     return base, coef, eigv
 
 
+def qhq(base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int, hl, overlaps: bool = False):
+    """Reference GetQHQ / GetOverlaps (src/BlockUtils.f90:229-264, :347-381)
+    through getqhqcpp_: the full nbloc x nbloc matrix <Q_j|H|Q_i> (FP64, H
+    applied exactly) and, with overlaps, <Q_j|Q_i>."""
+    base = np.ascontiguousarray(base, dtype=np.float64)
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32).copy()
+    opid = np.ascontiguousarray(hl.opid, dtype=np.int32).copy()
+    mptr = np.ascontiguousarray(hl.mptr, dtype=np.int32).copy()
+    hcoef = np.ascontiguousarray(hl.coef, dtype=np.float64).copy()
+    mat = np.ascontiguousarray(hl.mat, dtype=np.float64).copy()
+    A = np.zeros((nbloc, nbloc))
+    S = np.zeros((nbloc, nbloc)) if overlaps else None
+    ints = [ctypes.c_int(x) for x in (rk, nb.size, nbloc, opid.size, mptr.size, mat.size)]
+    L = _lib.load()
+    L.getqhqcpp_(base.ctypes.data_as(_D), coef.ctypes.data_as(_D), nb.ctypes.data_as(_I), ctypes.byref(ints[0]),
+                 ctypes.byref(ints[1]), ctypes.byref(ints[2]), opid.ctypes.data_as(_I), mptr.ctypes.data_as(_I),
+                 hcoef.ctypes.data_as(_D), mat.ctypes.data_as(_D), ctypes.byref(ints[3]), ctypes.byref(ints[4]),
+                 ctypes.byref(ints[5]), A.ctypes.data_as(_D), S.ctypes.data_as(_D) if S is not None else None)
+    if L.mlcp_gb300_last_status() != 0:
+        raise _lib.MlcpError(_lib.last_error())
+    return (A.T.copy(), S.T.copy()) if overlaps else A.T.copy()
+
+
 def update_opermat(imode: int, base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int,
                    xmats: np.ndarray) -> np.ndarray:
     """Reference UpdateOperMat (src/Updater.f90:110-151) through

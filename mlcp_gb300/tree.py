@@ -78,3 +78,95 @@ def hh_tree(D: int = 6, n: int = 10, lam: float = 0.111803, keep: int = 30, top_
     top = H.build_hoplist([keep] * npair, terms, eig_ops)
     _, _, eigv, _, hist = solver.solve(top, top_nev, rk, ncycle, npow, nals)
     return eigv, {"pairs": [{"eigv": p["eigv"], "last_rms": p["hist"][-1]} for p in pairs], "top_last_rms": hist[-1]}
+
+
+def _modes(ops) -> frozenset:
+    return frozenset(ops.keys())
+
+
+def mode_tree(single, terms, layers, keep, rk: int, ncycle: int, npow: int, nals: int, log=None):
+    """General multilayer walk (src/MLmain.f90:96-141) for a Hamiltonian given
+    as primitive-basis terms [(coef, {mode: operator})].
+
+    * Layer 1: each primitive mode's one-mode terms are diagonalised
+      (HamilSetup); every multi-mode term's factor on the mode is carried into
+      that eigenbasis.
+    * Each later layer groups the previous layer's nodes (``layers``: one
+      list of groups per layer, a group = child node indices; the last layer
+      has one group, the top).  A node's Hamiltonian is its children's
+      eigenvalues as diagonal operators plus every term whose modes lie in the
+      node but in no single child, as the product of its children's carried
+      factors.  The node is solved by the solver loop (spectral range, GPU
+      power cycles) for ``keep[layer]`` states at rank min(rk, smallest child
+      basis) when the node has two children (such a rank spans the node),
+      else rk.
+    * Terms reaching outside the node are carried into its basis: their
+      factor on the node is <Q_j| prod over its children of the children's
+      factors |Q_i> (UpdateH / UpdateOperMat, src/Updater.f90:53-151), one
+      getqhqcpp_ call per distinct product.
+
+    Returns (top eigenvalues, info)."""
+    D = len(single)
+    # layer 1
+    nodes = []
+    for m in range(D):
+        h = sum(c * ops[m] for c, ops in terms if _modes(ops) == {m})
+        w, V = np.linalg.eigh(h)
+        for j in range(V.shape[1]):
+            if V[np.argmax(np.abs(V[:, j])), j] < 0:
+                V[:, j] = -V[:, j]
+        fac = {t: V.T @ ops[m] @ V for t, (c, ops) in enumerate(terms) if m in ops and len(ops) > 1}
+        nodes.append({"prims": frozenset([m]), "evals": w, "factors": fac})
+    info = {"layers": []}
+    for li, groups in enumerate(layers):
+        nxt = []
+        linfo = []
+        for g in groups:
+            ch = [nodes[c] for c in g]
+            prims = frozenset().union(*[c["prims"] for c in ch])
+            sizes = [c["evals"].size for c in ch]
+            eig_ops = [np.diag(c["evals"]) for c in ch]
+            node_terms = [(1.0, {i: eig_ops[i]}) for i in range(len(ch))]
+            for t, (c, ops) in enumerate(terms):
+                mt = _modes(ops)
+                if not mt <= prims or any(mt <= cc["prims"] for cc in ch):
+                    continue
+                node_terms.append((c, {i: cc["factors"][t] for i, cc in enumerate(ch) if mt & cc["prims"]}))
+            hl = H.build_hoplist(sizes, node_terms, eig_ops)
+            nev = keep[li]
+            rank = min(rk, min(sizes)) if len(ch) == 2 else rk
+            base, coef, eigv, _, hist = solver.solve(hl, nev, rank, ncycle, npow, nals)
+            node = {"prims": prims, "evals": eigv, "factors": {}}
+            if li < len(layers) - 1:
+                cache = {}
+                for t, (c, ops) in enumerate(terms):
+                    mt = _modes(ops)
+                    if not (mt & prims) or mt <= prims:
+                        continue
+                    parts = {i: cc["factors"][t] for i, cc in enumerate(ch) if mt & cc["prims"]}
+                    key = tuple((i, parts[i].tobytes()) for i in sorted(parts))
+                    if key not in cache:
+                        one = H.build_hoplist(sizes, [(1.0, parts)])
+                        cache[key] = IT.qhq(base, coef, sizes, rank, nev, one)
+                    node["factors"][t] = cache[key]
+            nxt.append(node)
+            linfo.append({"modes": sorted(prims), "terms": len(node_terms), "last_rms": hist[-1] if hist else None,
+                          "carried": len(node["factors"]), "lowest": float(eigv[0])})
+            if log:
+                log(f"layer {li + 2} node {sorted(prims)}: {len(node_terms)} terms, E0 {eigv[0]:.6f}")
+        nodes = nxt
+        info["layers"].append(linfo)
+    return nodes[0]["evals"], info
+
+
+def qff_tree(D: int = 24, n: int = 8, seed: int = 3, keep_pair: int = 24, keep_group: int = 48, top_nev: int = 100,
+             rk: int = 30, ncycle: int = 10, npow: int = 15, nals: int = 15, log=None):
+    """The benchmark's three-layer tree for a synthetic quartic force field
+    (hoplist.qff_terms): modes in pairs (0 1)(2 3)..., pairs of pairs, one top
+    node over all groups of four."""
+    if D % 4:
+        raise ValueError("the three-layer tree groups modes in fours: D must be a multiple of 4")
+    _, single, terms = H.qff_terms(D, n, seed)
+    layers = [[[2 * i, 2 * i + 1] for i in range(D // 2)], [[2 * i, 2 * i + 1] for i in range(D // 4)],
+              [list(range(D // 4))]]
+    return mode_tree(single, terms, layers, [keep_pair, keep_group, top_nev], rk, ncycle, npow, nals, log=log)

@@ -91,7 +91,7 @@ class WarmStart:
         losses = []
         for _ in range(epochs):
             self.net.forward(Xp, rows)
-            losses.append(self.net.backward(Xp, rows, Tp))
+            losses.append(self.net.backward(Xp, rows, Tp).clone())
             self.net.adam(lr=lr)
         self.net.check_status()
         self.trained_on = rows
@@ -99,7 +99,6 @@ class WarmStart:
 
     def propose(self, batch, coef, base):
         """Overwrite the F terms of the device batch with the MLP's proposal."""
-        t = self.torch
         X = self.features(batch, coef, base)
         Xp, rows = self.net.pad_inputs(X)
         Y = self.net.forward(Xp, rows)
@@ -109,7 +108,6 @@ class WarmStart:
                                    rgmax, f_off.data_ptr(), base.data_ptr(), coef.data_ptr(), Y.data_ptr(),
                                    self.net.out_p, torch_stream()))
         self.net.check_status()
-        del t
 
     # -- the judged reduction --
     def reduce(self, batch, fixed_sweeps: int, max_sweeps: int, seed: int = 0):
@@ -147,13 +145,11 @@ class WarmStart:
             need = (reach[0] + 1) if reach.size else max_sweeps
             saved.append(need - fixed_sweeps)
         # per vector: the accepted proposal's terms, else the random start's
-        keep = t.as_tensor(~accept, device=self.dev)
         out_c, out_b = c_m.clone(), b_m.clone()
         for v in np.nonzero(~accept)[0]:
             t0, f = int(batch.term_off[v]), int(batch.rF[v])
             out_c[t0:t0 + f] = c_fix[t0:t0 + f]
             out_b[t0:t0 + f] = b_fix[t0:t0 + f]
-        del keep
         stats = {"accept_rate": float(accept.mean()), "sweeps_saved": float(np.mean(saved)) if saved else 0.0,
                  "fixed_sweeps": fixed_sweeps, "residual_mlp": r_mlp, "residual_random": r_plain,
                  "random_history": hist}

@@ -61,11 +61,12 @@ def test_warm_start_saves_sweeps(cuda_device):
     from mlcp_gb300.warmstart import WarmStart
     ws = WarmStart(ndof=NDOF, n=NB, rank=RANK, seed=1, device=cuda_device)
     losses, stats = run_cycles(ws, cuda_device)
-    assert losses[-1] < 0.2 * losses[0], (losses[0], losses[-1])
+    print(f"training loss {losses[0]:.4e} -> {losses[-1]:.4e}")
     for s in stats:
         print(f"cycle {s['cycle']}: accept rate {s['accept_rate']:.2f}, sweeps saved {s['sweeps_saved']:.2f}, "
               f"median residual {np.median(s['residual_mlp']):.3e} (proposal) "
               f"{np.median(s['residual_random']):.3e} (random start)")
+    assert losses[-1] < 0.2 * losses[0], (losses[0], losses[-1])
     acc = np.mean([s["accept_rate"] for s in stats])
     saved = np.mean([s["sweeps_saved"] for s in stats])
     assert acc >= 0.5, acc
