@@ -59,6 +59,18 @@ MLCP_API void intertwinecpp_(double *base, double *coef, int *nbas, MLCP_REF(int
                     MLCP_REF(int) ncpu, MLCP_REF(int) nals, MLCP_REF(bool) update, MLCP_REF(int) ishift,
                     MLCP_REF(double) Eshift);
 
+/* Extension beside intertwinecpp_ (no counterpart: the reference requires equal
+ * ranks in a block, src/GPUIterate.f90:152-158): the same cycle for a block
+ * whose vector v has rank ranks[v] <= rk.  Every vector is stored with rk
+ * terms (the layout of intertwinecpp_); terms at or beyond ranks[v] are
+ * padding, given zero weight on entry and kept at zero weight, and vector v
+ * is fitted as a rank-ranks[v] vector in every stage. */
+MLCP_API void intertwineraggedcpp_(double *base, double *coef, int *nbas, MLCP_REF(int) rk, const int *ranks,
+                                   MLCP_REF(int) ndof, MLCP_REF(int) nbloc, int *opid, int *mptr, double *Hcoef,
+                                   double *mat, MLCP_REF(int) TxD, MLCP_REF(int) nops, MLCP_REF(int) msize,
+                                   double *eigv, MLCP_REF(int) npow, MLCP_REF(int) ncpu, MLCP_REF(int) nals,
+                                   MLCP_REF(bool) update, MLCP_REF(int) ishift, MLCP_REF(double) Eshift);
+
 /* Replaces src/intertwining.cu:180 (alscpp_): nals ALS sweeps reducing the
  * rank-rG target G (terms rF..rF+rG-1 of coef/base) to the rank-rF vector F
  * (terms 0..rF-1, also the starting guess).  Overwrites terms 0..rF-1. */
@@ -238,15 +250,17 @@ MLCP_API int mlcp_mlp_adam(float *w, const float *g, float *m1, float *m2, int r
  * log10(|c| / |c_max|) / 8.  X: BF16, ldx >= ntop (n + 1). */
 MLCP_API int mlcp_ws_features(int nvec, int ndof, int n, int ntop, const long long *d_g_off, const int *d_g_rank,
                               int rgmax, const double *d_base, const double *d_coef, void *X, int ldx, void *stream);
-/* Training targets: row v*ndof + d holds the mode-d factors of the rank
- * terms of vector v at d_f_off[v] (a converged reduction), ordered by
- * decreasing |weight| and normalised like the features.  T: FP32,
- * ldt >= rank n. */
-MLCP_API int mlcp_ws_targets(int nvec, int ndof, int n, int rank, const long long *d_f_off, const double *d_base,
-                             const double *d_coef, float *T, int ldt, void *stream);
-/* A proposal: the rank F terms of vector v (at d_f_off[v]) get the
- * normalised rows of Y (row v*ndof + d, columns i*n ..) as mode-d factors
- * and the rank largest |target weights| as weights. */
+/* Training targets: row v*ndof + d holds, in slot j < rank, the mode-d factor
+ * of the term of vector v's reduction (rank terms at d_f_off[v]) that the
+ * j-th largest-|weight| target term turned into (greedy matching by the
+ * product over modes of the normalised overlaps), unit, with the sign that
+ * aligns it with that target term's feature factor.  T: FP32, ldt >= rank n. */
+MLCP_API int mlcp_ws_targets(int nvec, int ndof, int n, int rank, const long long *d_g_off, const int *d_g_rank,
+                             int rgmax, const long long *d_f_off, const double *d_base, const double *d_coef,
+                             float *T, int ldt, void *stream);
+/* A proposal: F term j of vector v (at d_f_off[v] + j) gets the normalised
+ * slot j of Y's row v*ndof + d (columns j*n ..) as its mode-d factor and the
+ * j-th largest |target weight| as its weight. */
 MLCP_API int mlcp_ws_apply(int nvec, int ndof, int n, int rank, const long long *d_g_off, const int *d_g_rank,
                            int rgmax, const long long *d_f_off, double *d_base, double *d_coef, const float *Y,
                            int ldy, void *stream);

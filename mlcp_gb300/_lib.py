@@ -65,6 +65,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         if hasattr(L, "getqhqdiagcpp_"):
             L.getqhqdiagcpp_.restype = None
             L.getqhqdiagcpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I, _I, _I, _D, _D, _I, _I, _I, _D]
+        if hasattr(L, "intertwineraggedcpp_"):
+            L.intertwineraggedcpp_.restype = None
+            L.intertwineraggedcpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I, _I, _I, _D, _D, _I, _I, _I, _D, _I, _I, _I,
+                                               ctypes.POINTER(ctypes.c_bool), _I, _D]
         if hasattr(L, "getqhqcpp_"):
             L.getqhqcpp_.restype = None
             L.getqhqcpp_.argtypes = [_D, _D, _I, _I, _I, _I, _I, _I, _D, _D, _I, _I, _I, _D, _V]
@@ -107,7 +111,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mlcp_ws_features.restype = _i
         L.mlcp_ws_features.argtypes = [_i, _i, _i, _i, _V, _V, _i, _V, _V, _V, _i, _V]
         L.mlcp_ws_targets.restype = _i
-        L.mlcp_ws_targets.argtypes = [_i, _i, _i, _i, _V, _V, _V, _V, _i, _V]
+        L.mlcp_ws_targets.argtypes = [_i, _i, _i, _i, _V, _V, _i, _V, _V, _V, _V, _i, _V]
         L.mlcp_ws_apply.restype = _i
         L.mlcp_ws_apply.argtypes = [_i, _i, _i, _i, _V, _V, _i, _V, _V, _V, _V, _i, _V]
         if hasattr(L, "intwdevicemem_"):

@@ -272,7 +272,7 @@ size_t plan_cycle(const Layout& Ly, const OpTable& t, int R, int B, CycleBuffers
   cb->wts = (double*)take(sizeof(double) * (size_t)B * B * R);
   cb->uwork = (dw*)take(sizeof(dw) * upd_work_dw(B, R, Ly.D));
   cb->qdw = (dw*)take(sizeof(dw) * upd_qdw_dw(B, R, Ly.nD));
-  cb->meta = (int*)take(sizeof(int) * 3 * (Ly.D + 1));
+  cb->meta = (int*)take(sizeof(int) * (3 * (Ly.D + 1) + B));
   cb->status = (int*)take(sizeof(int) * (B + 4));
   return bytes;
 }
@@ -280,8 +280,9 @@ size_t plan_cycle(const Layout& Ly, const OpTable& t, int R, int B, CycleBuffers
 // New block: vector i fits sum_k U(k,i) Q_k (cb.U from the Rayleigh-Ritz
 // solve), nals sweeps from Q_i, into cb.qn / cb.qnc.
 int run_updates(Context* ctx, const Layout& Ly, const CycleBuffers& cb, const int* d_nbas, const int* d_off, int R,
-                int B, int nals, cudaStream_t st) {
-  UpdParams u;
+                int B, int nals, cudaStream_t st, const int* d_rank = nullptr) {
+  UpdParams u{};
+  u.rank_v = d_rank;
   u.D = Ly.D; u.R = R; u.B = B; u.nD = Ly.nD; u.npmax = Ly.npmax; u.nals = nals; u.tile = 0;
   u.nbas = d_nbas; u.off = d_off; u.q = cb.q; u.qc = cb.qc; u.U = cb.U; u.qn = cb.qn; u.qnc = cb.qnc;
   u.qdw = cb.qdw; u.work = cb.uwork; u.pen_factor = kPen; u.status = cb.status;
@@ -293,7 +294,8 @@ int run_updates(Context* ctx, const Layout& Ly, const CycleBuffers& cb, const in
 // Full cycle; host buffers in, host buffers out.  Returns a Status.
 int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, int rk, int ndof, int nbloc,
                      const int* opid, const int* mptr, const double* Hcoef, const double* mat, int TxD, int nops,
-                     int msize, double* eigv, int npow, int nals, bool update, int ishift, double Eshift) {
+                     int msize, double* eigv, int npow, int nals, bool update, int ishift, double Eshift,
+                     const int* ranks = nullptr) {
   if (rk < 1 || rk > kMaxRankCycle) {
     set_error("intertwinecpp_: rk = %d outside [1, %d]", rk, kMaxRankCycle);
     return rk < 1 ? kBadArgument : kTooLarge;
@@ -314,6 +316,12 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
   int rc = make_layout(ndof, nbas, &Ly);
   if (rc) return rc;
   const int T = TxD / ndof, R = rk, B = nbloc;
+  if (ranks)
+    for (int v = 0; v < B; ++v)
+      if (ranks[v] < 1 || ranks[v] > R) {
+        set_error("intertwineraggedcpp_: ranks[%d] = %d outside [1, rk = %d]", v, ranks[v], R);
+        return kBadArgument;
+      }
   cudaStream_t st = ctx->stream;
   OpTable tab;
   rc = get_optable(ctx, Ly, nbas, R, T, opid, mptr, Hcoef, mat, nops, msize, st, &tab);
@@ -341,47 +349,58 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
   plan_cycle(Ly, tab, R, B, &cb, static_cast<char*>(ctx->cyc));
   const size_t nvals = (size_t)B * R * Ly.nD;
   MLCP_CUDA_TRY(cudaMemcpyAsync(cb.q, base, sizeof(double) * nvals, cudaMemcpyHostToDevice, st));
-  MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qc, coef, sizeof(double) * B * R, cudaMemcpyHostToDevice, st));
+  std::vector<double> qc_host;
+  if (ranks) {  // ragged: terms beyond a vector's rank carry zero weight
+    qc_host.assign(coef, coef + (size_t)B * R);
+    for (int v = 0; v < B; ++v)
+      for (int r = ranks[v]; r < R; ++r) qc_host[(size_t)v * R + r] = 0.0;
+  }
+  MLCP_CUDA_TRY(cudaMemcpyAsync(cb.qc, ranks ? qc_host.data() : coef, sizeof(double) * B * R,
+                                cudaMemcpyHostToDevice, st));
   {
-    std::vector<int> meta(3 * (ndof + 1), 0);
+    std::vector<int> meta(3 * (ndof + 1) + B, 0);
     std::memcpy(meta.data(), nbas, sizeof(int) * ndof);
     std::memcpy(meta.data() + (ndof + 1), Ly.off.data(), sizeof(int) * (ndof + 1));
     std::memcpy(meta.data() + 2 * (ndof + 1), Ly.offp.data(), sizeof(int) * (ndof + 1));
+    if (ranks) std::memcpy(meta.data() + 3 * (ndof + 1), ranks, sizeof(int) * B);
     MLCP_CUDA_TRY(cudaMemcpyAsync(cb.meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, st));
-    MLCP_CUDA_TRY(cudaStreamSynchronize(st));  // meta lives on the host stack
+    MLCP_CUDA_TRY(cudaStreamSynchronize(st));  // meta and the weights live on the host stack
   }
   const int* d_nbas = cb.meta;
   const int* d_off = cb.meta + (ndof + 1);
   const int* d_offp = cb.meta + 2 * (ndof + 1);
+  const int* d_rank = ranks ? cb.meta + 3 * (ndof + 1) : nullptr;
   MLCP_CUDA_TRY(cudaMemsetAsync(cb.status, 0, sizeof(int) * (B + 4), st));
 
   // --- matrix-vector products: POW_ALS on every vector ---
   if (npow > 0) {
-    OpAlsParams p;
+    OpAlsParams p{};
     p.eshift_v = nullptr;
     p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 0; p.nsweeps = npow; p.ishift = ishift; p.eshift = Eshift;
     p.pen_factor = kPen;
     p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.q; p.f_coef = cb.qc;
     p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
+    p.rank_v = d_rank;
     if ((rc = opals_launch(p, st))) return rc;
   }
   // --- Gram-Schmidt ---
   if (nals > 0) {
-    GsParams g;
+    GsParams g{};
     g.D = ndof; g.R = R; g.nbloc = B; g.nD = Ly.nD; g.nDp = Ly.nDp; g.npmax = Ly.npmax; g.nals = nals;
     g.nbas = d_nbas; g.off = d_off; g.offp = d_offp; g.base = cb.q; g.coef = cb.qc;
-    g.work = cb.gsw; g.status = cb.status + B;
+    g.work = cb.gsw; g.status = cb.status + B; g.rank_v = d_rank;
     if ((rc = gs_launch(g, st))) return rc;
   }
   if (update) {
     // --- <Q|H|Q>, <Q|Q>, generalised eigenproblem ---
     if (nals > 0) {
-      OpAlsParams p;
+      OpAlsParams p{};
       p.eshift_v = nullptr;
       p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 1; p.nsweeps = nals; p.ishift = 0; p.eshift = 0.0;
       p.pen_factor = kPen;
       p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.hq; p.f_coef = cb.hqc;
       p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
+      p.rank_v = d_rank;
       if ((rc = opals_launch(p, st))) return rc;
     } else {
       MLCP_CUDA_TRY(cudaMemsetAsync(cb.hq, 0, sizeof(double) * nvals, st));
@@ -394,7 +413,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
     if ((rc = gep_launch(gp, st))) return rc;
     // --- vector updates: new Q_i fits sum_k U(k,i) Q_k, starting from Q_i ---
     if (nals > 0) {
-      if ((rc = run_updates(ctx, Ly, cb, d_nbas, d_off, R, B, nals, st))) return rc;
+      if ((rc = run_updates(ctx, Ly, cb, d_nbas, d_off, R, B, nals, st, d_rank))) return rc;
       std::swap(cb.q, cb.qn);
       std::swap(cb.qc, cb.qnc);
     }
@@ -817,7 +836,7 @@ int spectral_range(Context* ctx, double* base, double* coef, const int* nbas, in
     range_shift_kernel<<<1, 1, 0, st>>>(rq, shift);
     MLCP_CUDA_TRY(cudaGetLastError());
     if (npow > 0) {
-      OpAlsParams p;
+      OpAlsParams p{};
       p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 0; p.nsweeps = npow; p.ishift = 1; p.eshift = 0.0;
       p.eshift_v = shift;
       p.pen_factor = kPen;
@@ -899,6 +918,28 @@ extern "C" void intertwinecpp_(double* base, double* coef, int* nbas, const int&
   }
   finish_status(rc);
   if (rc != kOk) fprintf(stderr, "intertwinecpp_: %s\n", last_error());
+}
+
+extern "C" void intertwineraggedcpp_(double* base, double* coef, int* nbas, const int& rk, const int* ranks,
+                                     const int& ndof, const int& nbloc, int* opid, int* mptr, double* Hcoef,
+                                     double* mat, const int& TxD, const int& nops, const int& msize, double* eigv,
+                                     const int& npow, const int& ncpu, const int& nals, const bool& update,
+                                     const int& ishift, const double& Eshift) {
+  (void)ncpu;
+  int rc = kOk;
+  Context* ctx = get_context(&rc);
+  if (ctx) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!ranks) {
+      set_error("intertwineraggedcpp_: ranks is null");
+      rc = kBadArgument;
+    } else {
+      rc = intertwine_cycle(ctx, base, coef, nbas, rk, ndof, nbloc, opid, mptr, Hcoef, mat, TxD, nops, msize, eigv,
+                            npow, nals, update, ishift, Eshift, ranks);
+    }
+  }
+  finish_status(rc);
+  if (rc != kOk) fprintf(stderr, "intertwineraggedcpp_: %s\n", last_error());
 }
 
 extern "C" void getqhqdiagcpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof,

@@ -163,7 +163,14 @@ __device__ dw block_sum_ready(dw v, dw* red) {
 struct Gs {
   GsArrays a;
   int R, RR, RRp, D, nD, npm, CL, rank, tid;
+  int rv;  // rank of the vector being fitted (ragged blocks; R otherwise)
 };
+
+// Ragged ranks: rows and columns >= rv of the normal equations are the
+// identity, so the padded terms stay decoupled from the fit.
+__device__ __forceinline__ dw mask_bb(const Gs& c, int i, int i2, dw v) {
+  return (i >= c.rv || i2 >= c.rv) ? dw_make(i == i2 ? 1.f : 0.f) : v;
+}
 
 // The vector iv as the working copy: factors, weights, penalty.
 __device__ void load_vector(const Gs& c, const GsParams& p, int iv) {
@@ -285,7 +292,7 @@ __device__ void step_products(const Gs& c, int j, int nk, bool pre, int t0, dw q
       for (int d = 0; d < D; ++d)
         if (d != j) prod = dw_mul(prod, c.a.g[(size_t)d * RR + ee]);
       c.a.Gp[ee] = prod;
-      c.a.BB[ee] = (ee % R == ee / R) ? dw_add(prod, pen) : prod;
+      c.a.BB[ee] = mask_bb(c, ee % R, ee / R, (ee % R == ee / R) ? dw_add(prod, pen) : prod);
     } else {
       const int ee = e - ngp, r = ee % R, m = ee / R;
       c.a.wf[ee] = dw_mul(dw_mul(c.a.fcs[r], qinv), c.a.fb[(size_t)r * c.nD + offj + m]);
@@ -363,7 +370,7 @@ __device__ void step_gather(const Gs& c, int j, dw* bp, int nown) {
     acc_add(acc, c.a.part[(size_t)Rn + e]);
 #pragma unroll
     for (int r = 0; r < 16; ++r) acc_add(acc, v[r]);
-    c.a.b0[e] = acc_value(acc);
+    c.a.b0[e] = (e % c.R >= c.rv) ? dw_make(e / c.R == 0 ? 1.f : 0.f) : acc_value(acc);  // ragged padding
   }
   __syncthreads();
 }
@@ -432,7 +439,7 @@ __device__ dw step_update(const Gs& c, int j, int jn, int nk, bool pre) {
         const dw gn = dw_mul(gp, s);
         c.a.Gp[ee] = gn;
         c.a.Gp[et] = gn;
-        c.a.BB[ee] = (i == i2) ? dw_add(gn, pen) : gn;
+        c.a.BB[ee] = mask_bb(c, i, i2, (i == i2) ? dw_add(gn, pen) : gn);
         c.a.BB[et] = c.a.BB[ee];
       }
     } else {
@@ -471,6 +478,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
   c.nD = p.nD;
   c.npm = p.npmax;
   c.tid = threadIdx.x;
+  c.rv = p.R;
   const GsDims dims{p.R, p.D, p.nD, p.npmax, p.nkmax, kResident ? 0 : p.gmask};
   gs_carve(dims, &c.a, smem_raw, reinterpret_cast<dw*>(p.work) + (size_t)c.rank * p.work_stride, nullptr);
   for (int d = c.tid; d <= c.D; d += kGsThreads) {
@@ -487,6 +495,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
 
   int step = 0;
   for (int iv = 1; iv < p.nbloc && p.nals > 0; ++iv) {
+    c.rv = p.rank_v ? p.rank_v[iv] : c.R;
     load_vector(c, p, iv);
     all_grams(c);
     const int nk = (iv - c.rank + c.CL - 1) / c.CL;  // owned k = rank, rank + CL, ... < iv
@@ -553,6 +562,10 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
         }
         if (!pre_done) {
           step_preproducts(c, j, jn, nk, c.tid, kGsThreads);
+          __syncthreads();
+        }
+        if (c.rv < c.R) {  // ragged: the padded terms keep zero weight
+          for (int i = c.rv + c.tid; i < c.R; i += kGsThreads) c.a.fcs[i] = dw_make(0.f);
           __syncthreads();
         }
         qinv = step_update(c, j, jn, nk, more);

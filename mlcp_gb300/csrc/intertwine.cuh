@@ -30,6 +30,14 @@ struct OpTable {
   const int* gstart;        // [D][umax+1] group starts in order[j]
 };
 
+// Ragged ranks (an extension; the reference requires equal ranks in a block,
+// src/GPUIterate.f90:152-158): a vector of rank r <= R is stored with R terms,
+// those beyond r at zero weight.  The fitting kernels keep it a rank-r fit:
+// rows and columns >= r of its normal equations are the identity, the same
+// rows of its right-hand side the first unit vector (so the solve leaves them
+// decoupled and finite), and their weights are set back to zero after every
+// solve, so they contribute nothing to any product, overlap or norm.
+
 // Per-vector sweep of ALS-fitted operator applications.
 struct OpAlsParams {
   OpTable ops;
@@ -50,6 +58,7 @@ struct OpAlsParams {
   dw* zscr;               // [nvec][umax][R][npmax] h Fo_j
   double* g64;            // [nvec][D][R][R] FP64 Grams of F
   int* status;            // [nvec]
+  const int* rank_v;      // [nvec] ranks <= R (terms beyond carry zero weight), or null: all R
 };
 
 int opals_launch(const OpAlsParams& p, cudaStream_t st);
@@ -65,6 +74,7 @@ struct GsParams {
   double* coef;
   double* work;   // per-CTA scratch for the arrays that do not fit in shared memory (gs_work_doubles)
   int* status;
+  const int* rank_v;  // [nbloc] ranks <= R (terms beyond carry zero weight), or null: all R
   // set by gs_launch
   int nkmax;             // earlier vectors owned by one CTA, at most
   int gmask;             // array groups placed in global scratch
@@ -92,6 +102,7 @@ struct UpdParams {
   dw* work;               // upd_work_dw(B, R, D): per-vector overlaps, Grams, target weights
   double pen_factor;      // penalty = pen_factor * max(weights of Q_i)
   int* status;            // [B] bit 0: non-positive pivot
+  const int* rank_v;      // [B] ranks <= R (terms beyond carry zero weight), or null: all R
 };
 int upd_launch(UpdParams p, int smem_optin, cudaStream_t st);
 size_t upd_work_dw(int B, int R, int D);

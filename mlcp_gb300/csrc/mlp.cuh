@@ -59,9 +59,10 @@ struct WsBatch {
 // ntop largest-magnitude target weights of vector v; BF16, leading dim ldx.
 // rgmax: the largest g_rank (sizes the selection bitmap).
 int ws_features_launch(const WsBatch& b, __nv_bfloat16* X, int ldx, int rgmax, cudaStream_t st);
-// T[(v ndof + d)][i n + m] = F_i^d(m) normalised likewise, F's terms ordered
-// by decreasing |weight| (rank terms at f_off); FP32, leading dim ldt.
-int ws_targets_launch(const WsBatch& b, float* T, int ldt, cudaStream_t st);
+// T[(v ndof + d)][j n + m] = the mode-d factor of the reduction's term (rank
+// terms at f_off) matched to the j-th largest-weight target term, unit, its
+// sign aligned with that term's canonical factor; FP32, leading dim ldt.
+int ws_targets_launch(const WsBatch& b, float* T, int ldt, int rgmax, cudaStream_t st);
 // Proposal: F_i^d = Y[(v ndof + d)][i n + ..] normalised, F weights = the
 // rank largest |target weights|; written at f_off into f_base / f_coef.
 int ws_apply_launch(const WsBatch& b, const float* Y, int ldy, int rgmax, cudaStream_t st);

@@ -249,6 +249,7 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
   for (int d = 0; d < D; ++d) f_gram_from64(t, d, fb, nD, G + (size_t)d * R * R);
   __syncthreads();
   const dw pen = s.misc[0];
+  const int rv = p.rank_v ? p.rank_v[v] : R;  // ragged: this vector's rank
   for (int d = 0; d < D; ++d)
     for (int u = 0; u < t.uoff[d + 1] - t.uoff[d]; ++u)
       operator_gram(t, hmat, d, t.uoff[d] + u, s, M + (size_t)(t.uoff[d] + u) * R * R);
@@ -267,6 +268,7 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
         for (int d = 0; d < D; ++d)
           if (d != j) bb = dw_mul(bb, G[(size_t)d * RR + e]);
         if (e % R == e / R) bb = dw_add(bb, pen);
+        if (e % R >= rv || e / R >= rv) bb = dw_make(e % R == e / R ? 1.f : 0.f);  // ragged: decoupled padding
         s.BB[e] = bb;
       }
       __syncthreads();
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
             for (int r = 0; r < R; ++r)
               acc_fma(acc, dw_mul(W[(size_t)u * RR + r * R + i], cg[r]), Z[(size_t)u * R * npm + r * npm + m]);
           const dw b = acc_value(acc);
-          s.b0[i + m * R] = p.ishift < 0 ? dw_neg(b) : b;
+          s.b0[i + m * R] = i >= rv ? dw_make(m == 0 ? 1.f : 0.f) : (p.ishift < 0 ? dw_neg(b) : b);
         }
       }
       __syncthreads();
@@ -381,6 +383,8 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
       //    rescales the POW weights first; no other thread reads them before
       //    the next barrier) --
       if (threadIdx.x < 32) {
+        for (int i = rv + threadIdx.x; i < R; i += 32) s.cf[i] = dw_make(0.f);  // ragged: padding stays weightless
+        __syncwarp();
         if (pow_mode) rescale_weights_warp(s.cf, R);
         for (int i = threadIdx.x; i < R; i += 32) fc[i] = dw_to_double(s.cf[i]);
       }

@@ -156,6 +156,7 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
   }
   __syncthreads();
   const dw pen = s.misc[0];
+  const int rv = p.rank_v ? p.rank_v[i] : R;  // ragged: this vector's rank
 
   for (int sw = 0; sw < p.nals; ++sw) {
     for (int k = 0; k < D; ++k) {
@@ -167,6 +168,7 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
         for (int d = 0; d < D; ++d)
           if (d != k) bb = dw_mul(bb, fg[(size_t)d * RR + e]);
         if (e % R == e / R) bb = dw_add(bb, pen);
+        if (e % R >= rv || e / R >= rv) bb = dw_make(e % R == e / R ? 1.f : 0.f);  // ragged: decoupled padding
         s.BB[e] = bb;
       }
       __syncthreads();
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
           dw b = s.bacc[o];
           for (int sl = 1; sl < nsl; ++sl) b = dw_add(b, s.bacc[sl * nout + o]);
           const int ip = o % R, m = o / R;
-          s.b0[ip + m * R] = b;
+          s.b0[ip + m * R] = ip >= rv ? dw_make(m == 0 ? 1.f : 0.f) : b;
         }
       }
       __syncthreads();
@@ -249,6 +251,7 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
         }
         __syncthreads();
       }
+      for (int r = rv + threadIdx.x; r < R; r += kThreads) s.cf[r] = dw_make(0.f);  // ragged: weightless padding
       // -- the new factor: FP64 output, its Gram, the block overlaps of mode k --
       for (int e = threadIdx.x; e < R * nk; e += kThreads) {
         const int ip = e / nk, m = e % nk;

@@ -5,10 +5,10 @@
 // largest-magnitude entry positive (a factor's sign and scale are
 // arbitrary in CP format: the weight and the other modes absorb them),
 // followed by the terms' log-weights.  The training target of the same row
-// is the mode's factors of the converged reduction, terms ordered by
-// decreasing |weight|, normalised the same way.  A proposal turns the MLP's
-// output rows back into unit factors, with the largest target weights as
-// the starting weights (ALS overwrites the weights and the first mode's
+// holds, in slot j, the mode's factor of the converged reduction's term that
+// the j-th input term turned into (ws_targets_kernel).  A proposal turns the
+// MLP's output slots back into unit factors, with the largest target weights
+// as the starting weights (ALS overwrites the weights and the first mode's
 // factors in its first step; the weights matter only through the penalty).
 #include <cfloat>
 
@@ -106,28 +106,81 @@ __global__ void __launch_bounds__(kWsThreads) ws_features_kernel(WsBatch b, __nv
   }
 }
 
+// Targets aligned with the inputs: output slot j (j < rank) stands for the
+// j-th largest-weight target term, and its target is the reduction's term
+// that term turned into -- the pairs (F term i, slot j) are matched greedily
+// by the largest prod_d |<F_i^d, G_j^d>| / (|F_i^d| |G_j^d|), and each
+// target factor takes the sign that makes its overlap with the slot's input
+// factor (as canonicalised in the features) non-negative.  Ordering the
+// reduction's terms by weight instead made the slots of nearly equal weights
+// swap between samples, and the network learned their average.
 __global__ void __launch_bounds__(kWsThreads) ws_targets_kernel(WsBatch b, float* T, int ldt) {
-  __shared__ int ord[64];
+  extern __shared__ unsigned ws_smem[];
+  __shared__ int top[64];
+  __shared__ int slot_of[64];  // F term assigned to slot j
+  __shared__ float ov[64 * 64];
+  __shared__ float rv[kWsThreads / 32];
+  __shared__ int ri[kWsThreads / 32];
   const int v = blockIdx.x, n = b.n, D = b.ndof, R = b.rank;
-  const long long off = b.f_off[v];
+  const long long foff = b.f_off[v], goff = b.g_off[v];
+  top_terms(b.coef + goff, min(b.g_rank[v], b.rgmax), R, ws_smem, top, rv, ri);
+  for (int e = threadIdx.x; e < R * R; e += kWsThreads) {
+    const int i = e / R, j = e - i * R;
+    float o = 0.f;
+    if (top[j] >= 0) {
+      double prod = 1.0;
+      for (int d = 0; d < D; ++d) {
+        const double* f = b.base + (size_t)(foff + i) * b.nD + (size_t)d * n;
+        const double* g = b.base + (size_t)(goff + top[j]) * b.nD + (size_t)d * n;
+        double fg = 0.0, ff = 0.0, gg = 0.0;
+        for (int m = 0; m < n; ++m) {
+          fg += f[m] * g[m];
+          ff += f[m] * f[m];
+          gg += g[m] * g[m];
+        }
+        prod *= (ff > 0.0 && gg > 0.0) ? fabs(fg) / sqrt(ff * gg) : 0.0;
+      }
+      o = (float)prod;
+    }
+    ov[e] = o;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    for (int i = 0; i < R; ++i) ord[i] = i;
-    for (int a = 0; a < R; ++a) {  // selection sort by decreasing |weight| (R <= 64)
-      int mx = a;
-      for (int c = a + 1; c < R; ++c)
-        if (fabs(b.coef[off + ord[c]]) > fabs(b.coef[off + ord[mx]])) mx = c;
-      const int t = ord[a];
-      ord[a] = ord[mx];
-      ord[mx] = t;
+    unsigned long long used_i = 0ull, used_j = 0ull;
+    for (int q = 0; q < R; ++q) slot_of[q] = q;
+    for (int q = 0; q < R; ++q) {  // greedy: the best remaining (F term, slot) pair
+      float best = -1.f;
+      int bi = -1, bj = -1;
+      for (int i = 0; i < R; ++i) {
+        if (used_i >> i & 1ull) continue;
+        for (int j = 0; j < R; ++j) {
+          if (used_j >> j & 1ull) continue;
+          if (ov[i * R + j] > best) {
+            best = ov[i * R + j];
+            bi = i;
+            bj = j;
+          }
+        }
+      }
+      slot_of[bj] = bi;
+      used_i |= 1ull << bi;
+      used_j |= 1ull << bj;
     }
   }
   __syncthreads();
   for (int item = threadIdx.x; item < D * R; item += kWsThreads) {
-    const int d = item / R, i = item - d * R;
-    const double* g = b.base + (size_t)(off + ord[i]) * b.nD + (size_t)d * n;
-    const double s = canon_scale(g, n);
+    const int d = item / R, j = item - d * R;
+    const double* f = b.base + (size_t)(foff + slot_of[j]) * b.nD + (size_t)d * n;
+    double s2 = 0.0, dot = 0.0;
+    if (top[j] >= 0) {
+      const double* g = b.base + (size_t)(goff + top[j]) * b.nD + (size_t)d * n;
+      const double gs = canon_scale(g, n);
+      for (int m = 0; m < n; ++m) dot += f[m] * g[m] * gs;
+    }
+    for (int m = 0; m < n; ++m) s2 += f[m] * f[m];
+    const double s = (s2 > 0.0) ? ((dot < 0.0) ? -1.0 : 1.0) / sqrt(s2) : 0.0;
     float* row = T + (size_t)(v * D + d) * ldt;
-    for (int m = 0; m < n; ++m) row[i * n + m] = (float)(g[m] * s);
+    for (int m = 0; m < n; ++m) row[j * n + m] = (float)(f[m] * s);
   }
 }
 
@@ -184,10 +237,17 @@ int ws_features_launch(const WsBatch& b, __nv_bfloat16* X, int ldx, int rgmax, c
   return kOk;
 }
 
-int ws_targets_launch(const WsBatch& b, float* T, int ldt, cudaStream_t st) {
+int ws_targets_launch(const WsBatch& b, float* T, int ldt, int rgmax, cudaStream_t st) {
   int rc = ws_check(b);
   if (rc) return rc;
-  ws_targets_kernel<<<b.nvec, kWsThreads, 0, st>>>(b, T, ldt);
+  const size_t smem = top_smem(b, rgmax);
+  if (smem > 24 * 1024 || rgmax < 1) {
+    set_error("warm start: targets of %d terms outside the selection bitmap", rgmax);
+    return kTooLarge;
+  }
+  WsBatch bb = b;
+  bb.rgmax = rgmax;
+  ws_targets_kernel<<<b.nvec, kWsThreads, smem, st>>>(bb, T, ldt);
   MLCP_CUDA_TRY(cudaGetLastError());
   return kOk;
 }
@@ -296,8 +356,9 @@ extern "C" int mlcp_ws_features(int nvec, int ndof, int n, int ntop, const long 
   return finish_status(ws_features_launch(b, static_cast<__nv_bfloat16*>(X), ldx, rgmax, st));
 }
 
-extern "C" int mlcp_ws_targets(int nvec, int ndof, int n, int rank, const long long* d_f_off, const double* d_base,
-                               const double* d_coef, float* T, int ldt, void* stream) {
+extern "C" int mlcp_ws_targets(int nvec, int ndof, int n, int rank, const long long* d_g_off, const int* d_g_rank,
+                               int rgmax, const long long* d_f_off, const double* d_base, const double* d_coef, float* T,
+                               int ldt, void* stream) {
   int rc = kOk;
   cudaStream_t st = ws_stream(stream, &rc);
   if (rc) return finish_status(rc);
@@ -305,8 +366,8 @@ extern "C" int mlcp_ws_targets(int nvec, int ndof, int n, int rank, const long l
     set_error("mlcp_ws_targets: nvec = %d, ldt = %d below rank n = %d", nvec, ldt, rank * n);
     return finish_status(kBadArgument);
   }
-  const WsBatch b = make_ws(nvec, ndof, n, 1, rank, nullptr, nullptr, d_f_off, d_base, d_coef, nullptr, nullptr);
-  return finish_status(ws_targets_launch(b, T, ldt, st));
+  const WsBatch b = make_ws(nvec, ndof, n, 1, rank, d_g_off, d_g_rank, d_f_off, d_base, d_coef, nullptr, nullptr);
+  return finish_status(ws_targets_launch(b, T, ldt, rgmax, st));
 }
 
 extern "C" int mlcp_ws_apply(int nvec, int ndof, int n, int rank, const long long* d_g_off, const int* d_g_rank,

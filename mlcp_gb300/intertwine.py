@@ -20,9 +20,12 @@ _I = ctypes.POINTER(ctypes.c_int)
 
 
 def intertwine(base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int, hl, eigv: np.ndarray, npow: int,
-               nals: int, update: bool = True, ishift: int = 1, Eshift: float = 0.0, ncpu: int = 1):
+               nals: int, update: bool = True, ishift: int = 1, Eshift: float = 0.0, ncpu: int = 1, ranks=None):
     """Run one cycle on copies of (base, coef, eigv) and return the new
-    (base, coef, eigv).  base is (nbloc*rk, nD) with row = term."""
+    (base, coef, eigv).  base is (nbloc*rk, nD) with row = term.  With
+    ``ranks`` (one per vector, each <= rk) the block is ragged and the cycle
+    goes through intertwineraggedcpp_: vector v's terms at or beyond
+    ranks[v] are zero-weight padding."""
     base = np.ascontiguousarray(base, dtype=np.float64).copy()
     coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
     eig = np.ascontiguousarray(eigv, dtype=np.float64).copy()
@@ -36,6 +39,20 @@ def intertwine(base: np.ndarray, coef: np.ndarray, nbas, rk: int, nbloc: int, hl
     upd = ctypes.c_bool(bool(update))
     esh = ctypes.c_double(float(Eshift))
     L = _lib.load()
+    if ranks is not None:
+        rv = np.ascontiguousarray(ranks, dtype=np.int32).copy()
+        if rv.size != nbloc:
+            raise ValueError(f"ranks has {rv.size} entries for a block of {nbloc}")
+        L.intertwineraggedcpp_(base.ctypes.data_as(_D), coef.ctypes.data_as(_D), nb.ctypes.data_as(_I),
+                               ctypes.byref(ints[0]), rv.ctypes.data_as(_I), ctypes.byref(ints[1]),
+                               ctypes.byref(ints[2]), opid.ctypes.data_as(_I), mptr.ctypes.data_as(_I),
+                               hcoef.ctypes.data_as(_D), mat.ctypes.data_as(_D), ctypes.byref(ints[3]),
+                               ctypes.byref(ints[4]), ctypes.byref(ints[5]), eig.ctypes.data_as(_D),
+                               ctypes.byref(ints[6]), ctypes.byref(ints[7]), ctypes.byref(ints[8]), ctypes.byref(upd),
+                               ctypes.byref(ints[9]), ctypes.byref(esh))
+        if L.mlcp_gb300_last_status() != 0:
+            raise _lib.MlcpError(_lib.last_error())
+        return base, coef, eig
     L.intertwinecpp_(base.ctypes.data_as(_D), coef.ctypes.data_as(_D), nb.ctypes.data_as(_I),
                      ctypes.byref(ints[0]), ctypes.byref(ints[1]), ctypes.byref(ints[2]),
                      opid.ctypes.data_as(_I), mptr.ctypes.data_as(_I), hcoef.ctypes.data_as(_D),

@@ -10,10 +10,11 @@ proposes the starting factors instead, from the unreduced vector itself:
   largest-weight target terms (unit, largest entry positive) and their
   log-weights (``mlcp_ws_features``);
 * output: the mode's factors of the rank-R reduction (``mlcp_ws_apply``),
-  one network shared by all modes of the same basis size;
+  one slot per input term among the R largest, one network shared by all
+  modes of the same basis size;
 * training pairs: (unreduced vector, converged reduction) from reductions
-  the solver has already run (``collect``: the targets of ``mlcp_ws_targets``
-  order the reduction's terms by weight);
+  the solver has already run (``collect``: ``mlcp_ws_targets`` matches each
+  slot's input term with the reduction term it turned into);
 * the judge: both starts run the same fixed number of sweeps, and the
   proposal is accepted, vector by vector, when its relative residual
   ||F - G|| / ||G|| is no larger than the random start's; otherwise the
@@ -72,11 +73,12 @@ class WarmStart:
         its targets (the device arrays after a full reduction)."""
         t = self.torch
         X = self.features(batch, coef, base)
-        _, _, f_off, _ = self._meta(batch)
+        g_off, g_rank, f_off, rgmax = self._meta(batch)
         T = t.zeros((batch.nvec * self.ndof, self.out_dim), dtype=t.float32, device=self.dev)
         L = _lib.load()
-        _lib.check(L.mlcp_ws_targets(batch.nvec, self.ndof, self.n, self.rank, f_off.data_ptr(), base.data_ptr(),
-                                     coef.data_ptr(), T.data_ptr(), self.out_dim, torch_stream()))
+        _lib.check(L.mlcp_ws_targets(batch.nvec, self.ndof, self.n, self.rank, g_off.data_ptr(), g_rank.data_ptr(),
+                                     rgmax, f_off.data_ptr(), base.data_ptr(), coef.data_ptr(), T.data_ptr(),
+                                     self.out_dim, torch_stream()))
         self.X.append(X)
         self.T.append(T)
 

@@ -1,0 +1,74 @@
+"""Ragged ranks inside the power cycle (intertwineraggedcpp_; the reference
+requires equal ranks in a block, src/GPUIterate.f90:152-158).
+
+* Equivalence: a block whose vectors all have rank 5 but are stored with 8
+  terms (3 padding terms of random factors) gives, through the ragged entry,
+  the same eigenvalues (1e-9 relative) and vectors (1 - |cos| <= 1e-9) as the
+  same block stored at rank 5 through intertwinecpp_, in every stage
+  (power sweep, Gram-Schmidt, Rayleigh-Ritz, updates).
+* Mixed ranks 2..8 in one block: padding weights stay exactly zero, every
+  Ritz value lies above the corresponding exact eigenvalue of the small
+  Hamiltonian (dense diagonalisation) -- the Rayleigh-Ritz bound of an
+  S-orthonormal block -- and four cycles lower their sum below the first
+  cycle's.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from mlcp_gb300 import hoplist as H
+from mlcp_gb300 import intertwine as IT
+
+
+def cos_sim(ab, ac, bb, bc, nbas):
+    aa = oracle.cp_dot(ab, ac, ab, ac, nbas)
+    b2 = oracle.cp_dot(bb, bc, bb, bc, nbas)
+    x = oracle.cp_dot(ab, ac, bb, bc, nbas)
+    return abs(x) / np.sqrt(aa * b2)
+
+
+@pytest.mark.gpu
+def test_padded_block_equals_unpadded(cuda_device):
+    hl = H.random_hoplist([5, 4, 6], 6, seed=31)
+    nb = hl.nbas
+    nD = int(np.sum(nb))
+    B, r, R = 6, 5, 8
+    rng = np.random.default_rng(4)
+    Q = rng.uniform(-0.5, 0.5, size=(B * r, nD))
+    qc = rng.uniform(0.5, 1.0, B * r)
+    eig0 = np.arange(B, dtype=float)
+    ub, uc, ue = IT.intertwine(Q, qc, nb, r, B, hl, eig0, 3, 4, True, 1, 2.0)
+    Qp = rng.uniform(-0.5, 0.5, size=(B * R, nD))
+    qcp = np.zeros(B * R)
+    for v in range(B):
+        Qp[v * R:v * R + r] = Q[v * r:(v + 1) * r]
+        qcp[v * R:v * R + r] = qc[v * r:(v + 1) * r]
+    pb, pc, pe = IT.intertwine(Qp, qcp, nb, R, B, hl, eig0, 3, 4, True, 1, 2.0, ranks=[r] * B)
+    np.testing.assert_allclose(pe, ue, rtol=1e-9)
+    for v in range(B):
+        assert np.all(pc[v * R + r:(v + 1) * R] == 0.0)
+        c = cos_sim(pb[v * R:v * R + r], pc[v * R:v * R + r], ub[v * r:(v + 1) * r], uc[v * r:(v + 1) * r], nb)
+        assert 1 - c <= 1e-9, (v, c)
+
+
+@pytest.mark.gpu
+def test_mixed_ranks_stay_ragged_and_variational(cuda_device):
+    hl = H.coupled_oscillators(3, 6)
+    nb = hl.nbas
+    nD = int(np.sum(nb))
+    B, R = 7, 8
+    ranks = [2, 8, 3, 5, 8, 4, 6]
+    rng = np.random.default_rng(5)
+    Q = rng.uniform(-0.5, 0.5, size=(B * R, nD))
+    qc = np.ones(B * R)
+    exact = np.sort(np.linalg.eigvalsh(H.dense_hamiltonian(hl)))[:B]
+    eig = np.arange(B, dtype=float) + 1.0
+    sums = []
+    for cyc in range(4):
+        Q, qc, eig = IT.intertwine(Q, qc, nb, R, B, hl, eig, 4, 4, True, 1, 6.0, ranks=ranks)
+        for v in range(B):
+            assert np.all(qc[v * R + ranks[v]:(v + 1) * R] == 0.0)
+        assert np.all(np.isfinite(eig))
+        assert np.all(eig >= exact - 1e-9 * np.abs(exact)), (eig, exact)
+        sums.append(float(np.sum(eig)))
+    assert sums[-1] < sums[0], sums
