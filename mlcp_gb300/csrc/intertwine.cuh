@@ -59,9 +59,11 @@ struct OpAlsParams {
   double* g64;            // [nvec][D][R][R] FP64 Grams of F
   int* status;            // [nvec]
   const int* rank_v;      // [nvec] ranks <= R (terms beyond carry zero weight), or null: all R
+  int tabulate;           // set by opals_launch: term/operator tables copied to shared memory
 };
 
 int opals_launch(const OpAlsParams& p, cudaStream_t st);
+// Smallest shared-memory footprint of the kernel (no resident operators, no tables).
 size_t opals_smem_bytes(const OpTable& t);
 
 // ALS-guided Gram-Schmidt over a block (reference src/intertw_lcv.cu:131).

@@ -73,8 +73,11 @@ struct OpSmem {
 constexpr int kMoffMax = 8192;
 
 // Carves the shared memory (null base: sizes only); returns the bytes.
+// tabulate: copy the term tables (Gram offsets, operator groups, term
+// coefficients) into shared memory when T D <= kMoffMax; without them the
+// kernel reads the same tables from the global operator table.
 __host__ __device__ inline size_t carve(OpSmem& s, unsigned char* base, const OpTable& t, bool separate_fo,
-                                        bool resident) {
+                                        bool resident, bool tabulate) {
   size_t o = 0;
   auto take = [&](size_t bytes) -> unsigned char* {
     const size_t r = o;
@@ -100,7 +103,7 @@ __host__ __device__ inline size_t carve(OpSmem& s, unsigned char* base, const Op
   s.cs.conv = (float*)take(sizeof(float) * 64);
   s.cs.rmax = (float*)take(sizeof(float) * 16 * 32);
   s.cs.rsum = (dw*)take(sizeof(dw) * 16 * 32);
-  const bool tab = t.T * t.D <= kMoffMax;
+  const bool tab = tabulate && t.T * t.D <= kMoffMax;
   s.moff = tab ? (int*)take(sizeof(int) * t.T * t.D) : nullptr;
   s.ord = tab ? (int*)take(sizeof(int) * t.T * t.D) : nullptr;
   s.gst = tab ? (int*)take(sizeof(int) * t.D * (t.umax + 1)) : nullptr;
@@ -196,7 +199,7 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
   const bool pow_mode = (p.mode == 0);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   OpSmem s;
-  carve(s, smem_raw, t, !pow_mode, kResident);
+  carve(s, smem_raw, t, !pow_mode, kResident, p.tabulate != 0);
 
   const double* fob = p.fo_base + (size_t)v * R * nD;
   const double* foc = p.fo_coef + (size_t)v * R;
@@ -455,22 +458,36 @@ __global__ void __launch_bounds__(kThreads, 1) opals_kernel(OpAlsParams p) {
 
 size_t opals_smem_bytes(const OpTable& t) {
   OpSmem s;
-  return carve(s, nullptr, t, true, false);
+  return carve(s, nullptr, t, true, false, false);
 }
 
-int opals_launch(const OpAlsParams& p, cudaStream_t st) {
+// Largest layout that fits: operators and Grams resident with the tables,
+// then the tables alone, then neither (wide top-layer vectors, e.g. rank 30
+// over 6 x 48 basis functions, where F and Fo take 138 KB).
+int opals_launch(const OpAlsParams& p0, cudaStream_t st) {
   int dev = 0, limit = 0;
   MLCP_CUDA_TRY(cudaGetDevice(&dev));
   MLCP_CUDA_TRY(cudaDeviceGetAttribute(&limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  OpAlsParams p = p0;
   OpSmem s;
-  const size_t res = carve(s, nullptr, p.ops, p.mode != 0, true);
+  p.tabulate = 1;
+  const size_t res = carve(s, nullptr, p.ops, p.mode != 0, true, true);
   if (res <= (size_t)limit) {
     MLCP_CUDA_TRY(cudaFuncSetAttribute(opals_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)res));
     opals_kernel<true><<<p.nvec, kThreads, res, st>>>(p);
     MLCP_CUDA_TRY(cudaGetLastError());
     return kOk;
   }
-  const size_t smem = carve(s, nullptr, p.ops, p.mode != 0, false);
+  size_t smem = carve(s, nullptr, p.ops, p.mode != 0, false, true);
+  if (smem > (size_t)limit) {
+    p.tabulate = 0;
+    smem = carve(s, nullptr, p.ops, p.mode != 0, false, false);
+  }
+  if (smem > (size_t)limit) {
+    set_error("ALS-fitted products: rank %d over %d padded basis functions needs %zu bytes of shared memory (limit %d)",
+              p.ops.R, p.ops.nDp, smem, limit);
+    return kTooLarge;
+  }
   MLCP_CUDA_TRY(cudaFuncSetAttribute(opals_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   opals_kernel<false><<<p.nvec, kThreads, smem, st>>>(p);
   MLCP_CUDA_TRY(cudaGetLastError());

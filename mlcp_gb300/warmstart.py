@@ -182,3 +182,60 @@ def residuals(batch, coef, base) -> np.ndarray:
     als.cp_dot_batched(coef, base, batch.nbas, xo, batch.rF, yo, batch.rG, out[2])
     ff, gg, fg = out.cpu().numpy()
     return np.sqrt(np.maximum(ff + gg - 2 * fg, 0.0) / gg)
+
+
+def power_steps(ws: WarmStart, hl, nvec: int, shift: float, ncycle: int = 8, train_cycles: int = 5,
+                train_sweeps: int = 20, epochs: int = 600, fixed_sweeps: int = 3, max_sweeps: int = 20, seed: int = 0,
+                device=None):
+    """The warm start inside a power iteration: each cycle reduces
+    (H - shift) F_v / ||.|| back to rank ws.rank for nvec vectors (the
+    unreduced vectors of power steps, workloads.power_batch).  Cycles
+    1..train_cycles are the solver's own reductions -- each started from the
+    vector's previous iterate (a random start in cycle 1), train_sweeps sweeps
+    -- and their pairs train the MLP; later cycles are judged reductions
+    (WarmStart.reduce) whose result feeds the next cycle.  Returns
+    (training losses, per judged cycle stats, seconds spent training)."""
+    import time
+
+    import torch
+
+    from . import hoplist as H  # noqa: F401
+    dev = device or ws.dev
+    rank = ws.rank
+    nD = int(np.sum(hl.nbas))
+    rng = np.random.default_rng(seed)
+    F = [(rng.uniform(-0.5, 0.5, size=(rank, nD)), np.ones(rank)) for _ in range(nvec)]
+    losses, stats, t_train = None, [], 0.0
+    for c in range(ncycle):
+        batch = workloads.power_batch(hl, [f[0] for f in F], [f[1] for f in F], rank, shift=shift)
+        if c < train_cycles:
+            if c == 0:
+                start = random_start(batch, seed=100)
+            else:
+                cb, bb = batch.coef.copy(), batch.base.copy()
+                for v in range(nvec):
+                    t0 = int(batch.term_off[v])
+                    bb[t0:t0 + rank] = F[v][0]
+                    cb[t0:t0 + rank] = F[v][1]
+                start = workloads.AlsBatch(nbas=batch.nbas, rF=batch.rF, rG=batch.rG, term_off=batch.term_off,
+                                           coef=cb, base=bb)
+            coef = torch.from_numpy(start.coef).to(dev)
+            base = torch.from_numpy(start.base).to(dev)
+            st = torch.zeros(nvec, dtype=torch.int32, device=dev)
+            als.reduce_batched(coef, base, batch.nbas, batch.rF, batch.rG, batch.term_off, train_sweeps, status=st)
+            if bool(st.any()):
+                raise _lib.MlcpError("warm start: a training reduction reported a non-positive pivot")
+            ws.collect(batch, coef, base)
+            if c == train_cycles - 1:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                losses = ws.train(epochs=epochs)
+                t_train = time.perf_counter() - t0
+        else:
+            coef, base, s = ws.reduce(batch, fixed_sweeps=fixed_sweeps, max_sweeps=max_sweeps, seed=100 + c)
+            s["cycle"] = c + 1
+            stats.append(s)
+        cn, bn = coef.cpu().numpy(), base.cpu().numpy()
+        F = [(bn[int(batch.term_off[v]):int(batch.term_off[v]) + rank].copy(),
+              cn[int(batch.term_off[v]):int(batch.term_off[v]) + rank].copy()) for v in range(nvec)]
+    return losses, stats, t_train

@@ -6,8 +6,14 @@ library under ``mlcp_gb300/`` never calls it.
 
 The C code in ``mlcp_oracle.c`` restates the reference's CUDA algorithm
 (src/intertwining.cu, src/als.cu, src/intertw_mvp.cu, src/intertw_lcv.cu)
-in FP64.  Parity is unpinned: the reference holds no golden vectors for this
-path and cannot be run here; mathematical known answers stand in.
+in FP64.  The reference holds no golden vectors for this path, so the
+restatement is pinned against the reference itself: ``ref_build.py``
+compiles the reference's own FP64 CUDA library from its sources (where
+they are staged) and ``Reference`` runs it in a child process, and the GPU
+tests compare this oracle, the reference library and the GB300 library on
+the same inputs (ALS: 1e-12; one power cycle: 1e-10).  Mathematical known
+answers (dense diagonalisation, FP64 Lanczos fixtures under
+``tests/golden/``) cover the host loops.
 """
 from __future__ import annotations
 

@@ -6,14 +6,18 @@ requires equal ranks in a block, src/GPUIterate.f90:152-158).
   the same eigenvalues (1e-9 relative) and vectors (1 - |cos| <= 1e-9) as the
   same block stored at rank 5 through intertwinecpp_, in every stage
   (power sweep, Gram-Schmidt, Rayleigh-Ritz, updates).
-* Mixed ranks 2..8 in one block: padding weights stay exactly zero, every
-  Ritz value lies above the corresponding exact eigenvalue of the small
-  Hamiltonian (dense diagonalisation) -- the Rayleigh-Ritz bound of an
-  S-orthonormal block -- and four cycles lower their sum below the first
-  cycle's.
+* Mixed ranks 2..8 in one block: padding weights stay exactly zero, and
+  the exact Rayleigh-Ritz values of each returned block (dense H and S of
+  the CP vectors) lie above the exact eigenvalues of the small Hamiltonian
+  and fall, as a sum, over four cycles.  The cycle's own eigenvalues are
+  not a variational bound: the reference builds QHQ(i, j) from
+  <Q_j | (H Q_i) reduced to the vector's rank by ALS>
+  (src/intertw_mvp.cu:621-630), so a rank-2 vector's Ritz value can fall
+  slightly below the exact level; they are only checked to be finite.
 """
 import numpy as np
 import pytest
+import scipy.linalg
 
 import oracle
 from mlcp_gb300 import hoplist as H
@@ -61,14 +65,25 @@ def test_mixed_ranks_stay_ragged_and_variational(cuda_device):
     rng = np.random.default_rng(5)
     Q = rng.uniform(-0.5, 0.5, size=(B * R, nD))
     qc = np.ones(B * R)
-    exact = np.sort(np.linalg.eigvalsh(H.dense_hamiltonian(hl)))[:B]
+    Hd = H.dense_hamiltonian(hl)
+    spectrum = np.sort(np.linalg.eigvalsh(Hd))
+    exact = spectrum[:B]
+
+    def ritz(Q, qc):
+        # exact Rayleigh-Ritz values of the block, each vector at its own rank
+        Qd = np.array([oracle.cp_dense(Q[v * R:v * R + ranks[v]], qc[v * R:v * R + ranks[v]], nb)
+                       for v in range(B)])
+        return scipy.linalg.eigh(Qd @ Hd @ Qd.T, Qd @ Qd.T, eigvals_only=True)
+
     eig = np.arange(B, dtype=float) + 1.0
     sums = []
     for cyc in range(4):
-        Q, qc, eig = IT.intertwine(Q, qc, nb, R, B, hl, eig, 4, 4, True, 1, 6.0, ranks=ranks)
+        esh = IT.block_shift(eig, spectrum[-1])  # GetBlockShift: the power steps favour the lowest states
+        Q, qc, eig = IT.intertwine(Q, qc, nb, R, B, hl, eig, 4, 4, True, 1, esh, ranks=ranks)
         for v in range(B):
             assert np.all(qc[v * R + ranks[v]:(v + 1) * R] == 0.0)
         assert np.all(np.isfinite(eig))
-        assert np.all(eig >= exact - 1e-9 * np.abs(exact)), (eig, exact)
-        sums.append(float(np.sum(eig)))
+        lam = ritz(Q, qc)
+        assert np.all(lam >= exact - 1e-9 * np.abs(exact)), (lam, exact)
+        sums.append(float(np.sum(lam)))
     assert sums[-1] < sums[0], sums

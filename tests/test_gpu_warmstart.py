@@ -1,67 +1,31 @@
-"""The learned ALS warm start (mlcp_gb300/warmstart.py) on power-step
-reductions of a synthetic quartic force field (6 modes of 8 functions, 39
-terms): each cycle reduces (H F_v) / ||.|| (rank 40 x 30 = 1200) back to
-rank 30 for a block of 24 vectors.  Cycles 1-5 reduce from the reference's
-random start (GetRandomCPvec) with 12 sweeps and their (unreduced vector,
-reduction) pairs train the MLP; from cycle 6 on the MLP proposes the starts.
+"""The learned ALS warm start (mlcp_gb300/warmstart.py) inside a power
+iteration of a synthetic quartic force field (6 modes of 8 functions, 39
+terms): each cycle reduces (H - 30000) F_v / ||.|| (rank 40 x 30 = 1200) back
+to rank 30 for a block of 24 vectors.  Cycles 1-5 are the solver's own
+reductions (each from the vector's previous iterate, 20 sweeps) and their
+(unreduced vector, reduction) pairs train the MLP (600 full-batch Adam
+steps); from cycle 6 on the MLP proposes the starts and the reference's
+random start (GetRandomCPvec) runs beside it as the fallback and the judge.
 
-Checks: training lowers the loss at least fivefold; on cycles 6-8 the
+Checks: training lowers the loss at least fivefold; over cycles 6-8 the
 proposal, after the same 3 fixed sweeps as the random start, is accepted
-(residual no larger) for at least half of the vectors, and for the accepted
-ones the random start needs at least one more sweep on average to reach the
-accepted residual.  The measured accept rate and sweeps saved are printed.
+(residual no larger) for at least 75 % of the vectors, and for the accepted
+ones the random start needs on average at least 1.5 more sweeps to reach the
+accepted residual (measured on the GB300: accept rates 0.92-1.0, 2.0-3.4
+sweeps saved).  The measured values are printed.
 """
 import numpy as np
 import pytest
 
-NVEC, RANK, NDOF, NB = 24, 30, 6, 8
-
-
-def f_terms(batch, coef, base):
-    """Each vector's F terms (base, coef) from a reduced batch."""
-    out = []
-    for v in range(batch.nvec):
-        t0 = int(batch.term_off[v])
-        out.append((base[t0:t0 + RANK].copy(), coef[t0:t0 + RANK].copy()))
-    return out
-
-
-def run_cycles(ws, cuda_device, ncyc=8, train_cycles=5, fixed=3, max_sweeps=12):
-    import torch
-    from mlcp_gb300 import als
-    from mlcp_gb300 import hoplist as H
-    from mlcp_gb300 import workloads as W
-    from mlcp_gb300.warmstart import random_start
-    hl = H.synthetic_qff(NDOF, NB, seed=2)
-    rng = np.random.default_rng(0)
-    F = [(rng.uniform(-0.5, 0.5, size=(RANK, NDOF * NB)), np.ones(RANK)) for _ in range(NVEC)]
-    stats, losses = [], None
-    for c in range(ncyc):
-        batch = W.power_batch(hl, [f[0] for f in F], [f[1] for f in F], RANK)
-        if c < train_cycles:
-            rb = random_start(batch, seed=100 + c)
-            coef = torch.from_numpy(rb.coef).to(cuda_device)
-            base = torch.from_numpy(rb.base).to(cuda_device)
-            st = torch.zeros(batch.nvec, dtype=torch.int32, device=cuda_device)
-            als.reduce_batched(coef, base, batch.nbas, batch.rF, batch.rG, batch.term_off, max_sweeps, status=st)
-            assert not st.any()
-            ws.collect(batch, coef, base)
-            if c == train_cycles - 1:
-                losses = ws.train(epochs=300)
-        else:
-            coef, base, s = ws.reduce(batch, fixed_sweeps=fixed, max_sweeps=max_sweeps, seed=100 + c)
-            s["cycle"] = c + 1
-            stats.append(s)
-        F = f_terms(batch, coef.cpu().numpy(), base.cpu().numpy())
-    return losses, stats
-
 
 @pytest.mark.gpu
 def test_warm_start_saves_sweeps(cuda_device):
-    from mlcp_gb300.warmstart import WarmStart
-    ws = WarmStart(ndof=NDOF, n=NB, rank=RANK, seed=1, device=cuda_device)
-    losses, stats = run_cycles(ws, cuda_device)
-    print(f"training loss {losses[0]:.4e} -> {losses[-1]:.4e}")
+    from mlcp_gb300 import hoplist as H
+    from mlcp_gb300.warmstart import WarmStart, power_steps
+    ws = WarmStart(ndof=6, n=8, rank=30, seed=1, device=cuda_device)
+    hl = H.synthetic_qff(6, 8, seed=2)
+    losses, stats, t_train = power_steps(ws, hl, nvec=24, shift=30000.0)
+    print(f"training loss {losses[0]:.4e} -> {losses[-1]:.4e} in {t_train:.2f} s")
     for s in stats:
         print(f"cycle {s['cycle']}: accept rate {s['accept_rate']:.2f}, sweeps saved {s['sweeps_saved']:.2f}, "
               f"median residual {np.median(s['residual_mlp']):.3e} (proposal) "
@@ -69,5 +33,5 @@ def test_warm_start_saves_sweeps(cuda_device):
     assert losses[-1] < 0.2 * losses[0], (losses[0], losses[-1])
     acc = np.mean([s["accept_rate"] for s in stats])
     saved = np.mean([s["sweeps_saved"] for s in stats])
-    assert acc >= 0.5, acc
-    assert saved >= 1.0, saved
+    assert acc >= 0.75, acc
+    assert saved >= 1.5, saved
