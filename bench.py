@@ -20,6 +20,12 @@ also give the GPU's residual errors on the headline workload), and the
 reference's own FP64 CUDA library (fp64_gpu_baseline: oracle/ref_build.py,
 run in a child process on the same GPU) on a smaller sample and on one power
 cycle, with the GPU's errors against it.
+
+Further legs after the timed regions (N=1 only): the power cycle and its
+neighbours (power_cycle), the learned ALS warm start inside a power
+iteration (warm_start: accept rate, sweeps saved, training time), and the
+24-mode three-layer quartic-force-field tree solved node by node on the GPU
+(tree_qff24).
 """
 from __future__ import annotations
 
@@ -418,6 +424,46 @@ def run_cycle_bench(steps: int, cpu: bool):
     return out
 
 
+# Learned warm start inside a power iteration: a 6-mode quartic force field
+# of 8 functions per mode, 24 vectors of rank 30, (H - 30000) F reduced back
+# to rank 30 each cycle; cycles 1-5 train, 6-8 are judged.
+WS_D, WS_N, WS_RANK, WS_NVEC, WS_SHIFT = 6, 8, 30, 24, 30000.0
+
+
+def run_warm_start_bench(dev):
+    """Accept rate and sweeps saved by the MLP's proposals against the
+    reference's random start (the judge), and the on-GPU training time."""
+    from mlcp_gb300 import hoplist as H
+    from mlcp_gb300.warmstart import WarmStart, power_steps
+    ws = WarmStart(ndof=WS_D, n=WS_N, rank=WS_RANK, seed=1, device=dev)
+    hl = H.synthetic_qff(WS_D, WS_N, seed=2)
+    t0 = time.perf_counter()
+    losses, stats, t_train = power_steps(ws, hl, nvec=WS_NVEC, shift=WS_SHIFT)
+    return {"workload": f"synthetic QFF D={WS_D} n={WS_N}: {WS_NVEC} vectors, (H - {WS_SHIFT:g}) F of rank "
+                        f"{WS_RANK} x {hl.nterms} reduced to rank {WS_RANK}; cycles 1-5 train, 6-8 judged",
+            "network": "3 layers, width 256, BF16 weights, FP32 accumulation (tcgen05)",
+            "train_seconds": t_train, "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
+            "accept_rate": float(np.mean([s["accept_rate"] for s in stats])),
+            "sweeps_saved": float(np.mean([s["sweeps_saved"] for s in stats])),
+            "per_cycle": [{"cycle": s["cycle"], "accept_rate": float(s["accept_rate"]),
+                           "sweeps_saved": float(s["sweeps_saved"])} for s in stats],
+            "seconds": time.perf_counter() - t0}
+
+
+def run_tree3_bench():
+    """The three-layer tree of the 24-mode quartic force field (pairs, groups
+    of four, top node), every node solved by the GPU solver loop."""
+    from mlcp_gb300 import tree
+    t0 = time.perf_counter()
+    eig, info = tree.qff_tree(D=24, n=8, seed=3, keep_pair=24, keep_group=48, top_nev=100, rk=30, ncycle=10,
+                              npow=15, nals=15)
+    top = info["layers"][-1][0]
+    return {"workload": "synthetic QFF D=24, n=8: pairs (24 states) -> groups of four (48 states) -> top "
+                        "(100 states), rank 30, ncycle=10, npow=nals=15",
+            "seconds": time.perf_counter() - t0, "top_terms": top["terms"], "lowest": [float(x) for x in eig[:5]],
+            "top_last_rms": top["last_rms"]}
+
+
 def run_gpu(args):
     import torch
     from mlcp_gb300 import _lib, als, workloads
@@ -551,6 +597,10 @@ def run_gpu(args):
                 "autotune": _lib.autotune_report().strip().splitlines()}
         if not args.no_cycle and ws == 1:
             line["power_cycle"] = run_cycle_bench(max(1, min(args.steps, 5)), cpu=not args.no_cpu)
+        if not args.no_warm_start and ws == 1:
+            line["warm_start"] = run_warm_start_bench(dev)
+        if not args.no_tree3 and ws == 1:
+            line["tree_qff24"] = run_tree3_bench()
         if not args.no_fp64 and ws == 1:
             cyc_ms = line["power_cycle"]["gpu_ms_per_cycle"] if "power_cycle" in line else None
             line["fp64_gpu_baseline"] = fp64_gpu_baseline(batch, gcoef, gbase, e2e_value, cyc_ms)
@@ -570,6 +620,8 @@ def main():
     ap.add_argument("--no-cycle", action="store_true", help="skip the power-cycle measurement")
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the reference FP64 GPU library's timing (fp64_gpu_baseline)")
+    ap.add_argument("--no-warm-start", action="store_true", help="skip the learned warm-start measurement")
+    ap.add_argument("--no-tree3", action="store_true", help="skip the 24-mode three-layer tree")
     ap.add_argument("--cycle-only", action="store_true",
                     help="time only the power cycle (--steps cycles after one warm-up) and print its JSON")
     args = ap.parse_args()
