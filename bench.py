@@ -572,10 +572,10 @@ def run_gpu(args):
         rate, dt, fp64 = cpu_sample_rate(batch, sample, threads, keep=True)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{sample} of the {NVEC} vectors (full 10 sweeps each) in {dt:.1f} s"}
-        rerr, dist = als_errors(batch, gcoef, gbase, fp64)
+        rerr, vdist = als_errors(batch, gcoef, gbase, fp64)
         accuracy = {"against": "FP64 oracle (the reference's algorithm; pinned to the reference library by "
                                "tests/test_gpu_reference.py)", "sample": f"vectors 0-{sample - 1}",
-                    "als_residual_rel_err_max": rerr, "als_vec_rel_dist_max": dist}
+                    "als_residual_rel_err_max": rerr, "als_vec_rel_dist_max": vdist}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,

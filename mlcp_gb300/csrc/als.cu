@@ -233,9 +233,9 @@ constexpr int kWaitLimit = 1 << 20;
 // ---------------------------------------------------------------------------
 
 struct AlsSmem {
-  int rFp, ldP, stage_floats;
+  int rFp, ldP, stage_floats, kp, nf;
   size_t bar, done, issued, fillno, flags, ring, P, cw, fa, fb, bred, bpart, BB, X, L, sk, dinv, u, nrm, misc, gi, b0, res,
-      red, total;
+      red, cb, fp, tcbar, tbase, total;
 };
 
 __host__ __device__ inline size_t carve(size_t* cursor, size_t bytes, size_t align) {
@@ -244,11 +244,14 @@ __host__ __device__ inline size_t carve(size_t* cursor, size_t bytes, size_t ali
   return o;
 }
 
-__host__ __device__ inline AlsSmem als_smem_layout(int rows_cta, int rF, int npmax, int gsmax, int stages) {
+__host__ __device__ inline AlsSmem als_smem_layout(int rows_cta, int rF, int npmax, int gsmax, int stages,
+                                                    int tc = 0) {
   AlsSmem s;
   s.rFp = round_up(rF, 4);
   s.ldP = round_up(rows_cta > 0 ? rows_cta : 1, 32);
   s.stage_floats = kAlsTileRows * 2 * gsmax;
+  s.kp = als_tc_kp(npmax);
+  s.nf = als_tc_nf(rF);
   size_t o = 0;
   s.bar = carve(&o, 8 * (size_t)stages, 16);
   s.done = carve(&o, 4 * (size_t)stages, 16);
@@ -256,7 +259,7 @@ __host__ __device__ inline AlsSmem als_smem_layout(int rows_cta, int rF, int npm
   s.fillno = carve(&o, 4 * (size_t)stages, 16);
   s.flags = carve(&o, 4 * 8, 16);
   s.ring = carve(&o, sizeof(float) * (size_t)stages * s.stage_floats, 128);
-  s.P = carve(&o, sizeof(float) * (size_t)s.rFp * s.ldP, 16);
+  s.P = carve(&o, tc ? 0 : sizeof(float) * (size_t)s.rFp * s.ldP, 16);  // tensor memory in the tensor-core form
   s.cw = carve(&o, sizeof(float) * (size_t)s.ldP, 16);
   s.fa = carve(&o, sizeof(float) * (size_t)s.rFp * gsmax, 16);
   s.fb = carve(&o, sizeof(float) * (size_t)s.rFp * gsmax, 16);
@@ -274,6 +277,12 @@ __host__ __device__ inline AlsSmem als_smem_layout(int rows_cta, int rF, int npm
   s.b0 = carve(&o, sizeof(dw) * (size_t)rF * npmax, 16);
   s.res = carve(&o, sizeof(dw) * (size_t)rF * npmax, 16);
   s.red = carve(&o, sizeof(float) * 4, 16);
+  // tensor-core form: two tiles' BF16 operand pieces (hi, mid, lo), the
+  // factor's pieces, the MMA completion barriers, the tensor-memory base
+  s.cb = carve(&o, tc ? (size_t)2 * 3 * kAlsTileRows * s.kp * 2 : 0, 128);
+  s.fp = carve(&o, tc ? (size_t)3 * s.nf * s.kp * 2 : 0, 128);
+  s.tcbar = carve(&o, 8 * 2, 16);
+  s.tbase = carve(&o, 4, 16);
   s.total = o;
   return s;
 }
@@ -1055,8 +1064,8 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
   }
 }
 
-size_t als_smem_bytes(int rows_cta, int rF, int npmax, int gsmax, int stages) {
-  return als_smem_layout(rows_cta, rF, npmax, gsmax, stages).total;
+size_t als_smem_bytes(int rows_cta, int rF, int npmax, int gsmax, int stages, int tc) {
+  return als_smem_layout(rows_cta, rF, npmax, gsmax, stages, tc).total;
 }
 
 bool als_choose_shape(int nvec, int rGmax, int rFmax, int npmax, int gsmax, int num_sms, size_t smem_limit,

@@ -22,6 +22,24 @@ constexpr int kAlsWarps = kAlsThreads / 32;
 constexpr int kAlsSolverWarps = 4;     // warps 0-3 run the double-word solves
 constexpr int kAlsTileRows = 128;      // target terms per staged tile (4 per lane)
 
+// Tensor-core form (AlsParams::tc): the per-mode dot products <G_j^d, F_i^d>
+// of a tile are one tcgen05 MMA (M = 128 target terms, N = rF padded to 16,
+// K = the basis size padded to 16) on BF16 three-way splits of both
+// operands, accumulated in FP32 in tensor memory, and the running products
+// live in tensor memory instead of shared memory.
+constexpr int kAlsTcMaxRank = 32;      // largest rF of the tensor-core form
+constexpr int kAlsTcCols = 512;        // tensor-memory columns taken per CTA
+__host__ __device__ inline int als_tc_kp(int npmax) { return (npmax + 15) / 16 * 16; }
+__host__ __device__ inline int als_tc_nf(int rF) { return (rF + 15) / 16 * 16; }
+// Whether a CTA owning rows_cta target terms fits the tensor-core form:
+// two MMA result buffers plus the running products of every tile (rF
+// columns each) plus 16 columns of read slack within the allocation.
+__host__ __device__ inline bool als_tc_fits(int rows_cta, int rF, int npmax) {
+  if (rF < 1 || rF > kAlsTcMaxRank || npmax > 64) return false;
+  const int ntiles = (rows_cta + kAlsTileRows - 1) / kAlsTileRows;
+  return 2 * als_tc_nf(rF) + ntiles * rF + 16 <= kAlsTcCols;
+}
+
 // All arrays are device pointers unless marked otherwise.
 struct AlsParams {
   int nvec;          // vectors in the batch
@@ -36,6 +54,7 @@ struct AlsParams {
   double pen_factor; // penalty = pen_factor * max(F weights) (1e-10 FP64 rule, 1e-5 FP32 rule)
   int cluster;       // CTAs per vector
   int stages;        // bulk-copy ring stages
+  int tc;            // 1: the tensor-core form of the product passes (als_tc_fits must hold)
   int rows_cta_max;  // max target terms owned by one CTA
   long long total_rows;     // sum of rG
   long long total_f_terms;  // sum of rF
@@ -71,13 +90,20 @@ struct AlsParams {
 };
 
 // Shared memory of the cluster kernel.
-size_t als_smem_bytes(int rows_cta, int rF, int npmax, int gsmax, int stages);
+size_t als_smem_bytes(int rows_cta, int rF, int npmax, int gsmax, int stages, int tc = 0);
 
-// Launch shape chosen for a batch: cluster size, ring stages, shared memory.
+// Launch shape chosen for a batch: cluster size, ring stages, engine, shared memory.
 struct AlsShape {
   int cluster = 0, stages = 0, rows_cta = 0;
+  int tc = 0;  // 1: tensor-core form
   size_t smem = 0;
 };
+
+// Product-pass engine: 0 automatic (the autotuner measures both forms; the
+// rule without it takes the CUDA-core form), 1 CUDA cores only, 2 tensor
+// cores wherever they fit.
+int als_engine();
+void set_als_engine(int e);
 // Returns false (shape untouched) when no shape fits smem_limit.
 bool als_choose_shape(int nvec, int rGmax, int rFmax, int npmax, int gsmax, int num_sms, size_t smem_limit,
                       AlsShape* out);
