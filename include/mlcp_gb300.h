@@ -277,6 +277,19 @@ MLCP_API int mlcp_ws_apply(int nvec, int ndof, int n, int rank, const long long 
 MLCP_API void mlcp_gb300_set_autotune(int enable);
 MLCP_API int mlcp_gb300_autotune_report(char *buf, int len);
 
+/* Product-pass engine of the batched ALS (extension).  The per-mode dot
+ * products of a tile of target terms run either on the CUDA cores (FP32
+ * FMAs) or on the tensor cores (one tcgen05 MMA per tile on BF16 three-way
+ * splits of both operands, FP32 accumulation; running products held in
+ * tensor memory).  0: automatic (the autotuner times both forms among its
+ * candidates; without the autotuner the CUDA-core rule applies), 1: CUDA
+ * cores only, 2: tensor cores wherever the shape fits (rF <= 32 and the
+ * running products of a CTA's terms within 512 tensor-memory columns).
+ * MLCP_GB300_ALS_ENGINE=1 or 2 in the environment sets the initial value.
+ * Changing it re-tunes shapes on their next call. */
+MLCP_API void mlcp_gb300_set_als_engine(int engine);
+MLCP_API int mlcp_gb300_als_engine(void);
+
 /* Kernel timing (extension).  When enabled, the library records CUDA events
  * around its dominant kernel of each call on the call's stream;
  * mlcp_gb300_last_kernel_ms() synchronises on the end event and returns the

@@ -96,6 +96,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
                                         ctypes.c_int, _I, _D, _D, _I]
         L.mlcp_gb300_set_autotune.restype = None
         L.mlcp_gb300_set_autotune.argtypes = [ctypes.c_int]
+        L.mlcp_gb300_set_als_engine.restype = None
+        L.mlcp_gb300_set_als_engine.argtypes = [ctypes.c_int]
+        L.mlcp_gb300_als_engine.restype = ctypes.c_int
+        L.mlcp_gb300_als_engine.argtypes = []
         L.mlcp_gb300_autotune_report.restype = ctypes.c_int
         L.mlcp_gb300_autotune_report.argtypes = [ctypes.c_char_p, ctypes.c_int]
         _F = ctypes.c_float
@@ -138,6 +142,16 @@ def autotune_report() -> str:
     buf = ctypes.create_string_buffer(n + 1)
     L.mlcp_gb300_autotune_report(buf, n + 1)
     return buf.value.decode()
+
+
+def set_als_engine(engine: int) -> None:
+    """Product-pass engine of the batched ALS: 0 automatic (autotuned), 1 CUDA
+    cores, 2 tensor cores where the shape fits."""
+    load().mlcp_gb300_set_als_engine(int(engine))
+
+
+def als_engine() -> int:
+    return int(load().mlcp_gb300_als_engine())
 
 
 def last_error() -> str:

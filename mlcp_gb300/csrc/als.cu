@@ -35,6 +35,7 @@
 // One launch covers all sweeps; the host is not involved between steps.
 
 #include <cooperative_groups.h>
+#include <cuda_bf16.h>
 #include <cfloat>
 #include <cstdint>
 
@@ -314,6 +315,12 @@ struct Cta {
   float* fcta;      // this CTA's FP32 factor copy [rF][nDp]
   dw* gram;         // this CTA's Grams [D][rF][rF]
   dw* suf;          // this CTA's suffix products [D][rF][rF]
+  // tensor-core form
+  int tc, kp, nf;         // engine; K and N of the MMA (basis and rF padded to 16)
+  unsigned char* cb;      // [2][3][128 x kp] BF16 pieces of two target tiles (canonical K-major)
+  unsigned char* fp;      // [3][nf x kp] BF16 pieces of the factor
+  uint64_t* tcbar;        // [2] MMA completion of the two result buffers
+  uint32_t tmem;          // tensor-memory base: results at columns [0, 2 nf), running products after
 };
 
 // Tile source: one or two mode slabs of the CTA's target terms.
@@ -616,7 +623,7 @@ __device__ __forceinline__ void item_bm(const Cta& c, const float* tk, int gsk, 
 // i-quad count) and rF <= 32: it then inverts the step's normal equations in
 // registers during the first round.
 __device__ __forceinline__ bool phase_b_inverts(const Cta& c) {
-  return c.rF <= 32 && (kAlsWarps / c.nIq) * c.nIq < kAlsWarps;
+  return !c.tc && c.rF <= 32 && (kAlsWarps / c.nIq) * c.nIq < kAlsWarps;
 }
 
 // Sums the 4 MW accumulators of each lane over the warp into out[cc MW + m]
@@ -722,6 +729,497 @@ __device__ unsigned phase_b(const Cta& c, const AlsParams& p, unsigned seq, int 
     used += (unsigned)c.ntiles;
   }
   return used;
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core form of the product passes (AlsParams::tc)
+// ---------------------------------------------------------------------------
+// For a tile of 128 target terms j and mode d the dot products
+// D(j, i) = <G_j^d, F_i^d> of every F term i are one MMA on the 5th-generation
+// tensor cores: A = the tile (128 x kp, K = the basis padded to 16), B = the
+// factor (nf x kp), D in tensor memory (lane j, column i).  Both operands are
+// split into three BF16 pieces, x = h + m + l (each the BF16 rounding of what
+// the previous pieces leave, so the split is exact to 2^-27 of x), and six
+// products mm + hl + lh + hm + mh + hh (smallest first) are accumulated in
+// FP32: the dropped ml, lm, ll terms are below 2^-26 of the product, so the
+// dots carry the accuracy of FP32 dots.  The same instructions on the same
+// operands give bit-identical results, so a factor divided out of a running
+// product is exactly the one multiplied in earlier, as in the CUDA-core form.
+//
+// The running products P(j, i) live in tensor memory (columns 2 nf + T rF + i
+// for tile T), so a tile's update is tcgen05.ld of D and P, the product or
+// quotient in registers, tcgen05.st of P: warp w reaches lanes 32 (w % 4) ..
+// +31 (its rows of every tile) and the warps sharing a lane quarter split the
+// F terms.  Tiles are pipelined two deep: while the warps update tile T from
+// result buffer T % 2, the operand pieces of tile T + 1 are converted and its
+// MMAs run into the other buffer.
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor, no swizzle, K-major canonical layout:
+// 8-row x 16-byte core matrices, 128 B apart along K and sbo apart along
+// M/N; descriptor version 1.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t sbo) {
+  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)(128u >> 4) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor of kind::f16: BF16 A and B (K-major), FP32 D, M = 128, N = n.
+__device__ __forceinline__ uint32_t tc_idesc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+// LW consecutive FP32 columns of this warp's 32 lanes, waited for inside the
+// same statement (so no use of the values can be scheduled before the wait).
+template <int LW>
+__device__ __forceinline__ void tm_ld(uint32_t taddr, float (&v)[LW]);
+
+template <>
+__device__ __forceinline__ void tm_ld<8>(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int q = 0; q < 8; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+template <>
+__device__ __forceinline__ void tm_ld<16>(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+// One FP32 column of this warp's 32 lanes.
+__device__ __forceinline__ void tm_st1(uint32_t taddr, float v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x1.b32 [%0], {%1};" ::"r"(taddr), "r"(__float_as_uint(v)) : "memory");
+}
+__device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// Tensor-memory address of column col in the lane quarter of this warp.
+__device__ __forceinline__ uint32_t tm_addr(const Cta& c, int col) {
+  return c.tmem + ((uint32_t)(32 * (c.warp & 3)) << 16) + (uint32_t)col;
+}
+__device__ __forceinline__ int tc_pcol(const Cta& c, int T) { return 2 * c.nf + T * c.rF; }
+__device__ __forceinline__ unsigned char* tc_cbuf(const Cta& c, unsigned s) {
+  return c.cb + (size_t)(s & 1u) * 3 * kAlsTileRows * c.kp * 2;
+}
+
+// BF16 three-way split of eight floats, packed per piece.
+__device__ __forceinline__ void split3(const float (&x)[8], uint4& h, uint4& m, uint4& l) {
+  uint32_t hw[4], mw[4], lw[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    uint32_t ph = 0, pm = 0, pl = 0;
+#pragma unroll
+    for (int z = 0; z < 2; ++z) {
+      const float v = x[2 * u + z];
+      const __nv_bfloat16 bh = __float2bfloat16_rn(v);
+      const float r1 = v - __bfloat162float(bh);
+      const __nv_bfloat16 bm = __float2bfloat16_rn(r1);
+      const float r2 = r1 - __bfloat162float(bm);
+      const __nv_bfloat16 bl = __float2bfloat16_rn(r2);
+      ph |= (uint32_t)__bfloat16_as_ushort(bh) << (16 * z);
+      pm |= (uint32_t)__bfloat16_as_ushort(bm) << (16 * z);
+      pl |= (uint32_t)__bfloat16_as_ushort(bl) << (16 * z);
+    }
+    hw[u] = ph;
+    mw[u] = pm;
+    lw[u] = pl;
+  }
+  h = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+  m = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+  l = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+}
+
+// Rows [0, rows) of a matrix (row stride ld floats, n valid entries per
+// row, entries [n, round_up(n, 4)) readable) as three BF16 pieces of a
+// rows x kp operand in the canonical K-major layout: 16-byte chunk (r, kc)
+// at ((r / 8) (kp / 8) + kc) 128 + (r % 8) 16 bytes; piece stride `piece`
+// bytes.  Rows >= valid are written as zeros.  Threads t of nt.
+__device__ __forceinline__ void tc_split_rows(const float* src, int ld, int n, int valid, int rows, int kp,
+                                              unsigned char* dst, size_t piece, int t, int nt) {
+  const int kc8 = kp / 8;
+  for (int e = t; e < rows * kc8; e += nt) {
+    const int r = e / kc8, kc = e - r * kc8, q0 = kc * 8;
+    float x[8];
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+    if (r < valid) {
+      if (q0 < n) a = *reinterpret_cast<const float4*>(src + (size_t)r * ld + q0);
+      if (q0 + 4 < n) b = *reinterpret_cast<const float4*>(src + (size_t)r * ld + q0 + 4);
+    }
+    x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+    x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      if (q0 + u >= n) x[u] = 0.f;
+    uint4 h, m, l;
+    split3(x, h, m, l);
+    const size_t off = ((size_t)(r >> 3) * kc8 + kc) * 128 + (size_t)(r & 7) * 16;
+    *reinterpret_cast<uint4*>(dst + off) = h;
+    *reinterpret_cast<uint4*>(dst + piece + off) = m;
+    *reinterpret_cast<uint4*>(dst + 2 * piece + off) = l;
+  }
+}
+
+// The six MMAs of one tile (one thread): D[dcol..] = sum over K of A B^T.
+__device__ __forceinline__ void tc_issue(const Cta& c, unsigned s) {
+  tc_fence_after();
+  const uint32_t a0 = smem_addr(tc_cbuf(c, s)), b0 = smem_addr(c.fp);
+  const uint32_t pa = (uint32_t)kAlsTileRows * c.kp * 2, pb = (uint32_t)c.nf * c.kp * 2;
+  const uint32_t sbo = (uint32_t)(c.kp / 8) * 128;
+  const uint32_t idesc = tc_idesc(c.nf);
+  const uint32_t dt = c.tmem + (uint32_t)((s & 1u) * c.nf);
+  // pieces 0 = hi, 1 = mid, 2 = lo; (A, B) pairs smallest first
+  const int ap[6] = {1, 0, 2, 0, 1, 0}, bq[6] = {1, 2, 0, 1, 0, 0};
+  uint32_t acc = 0;
+  for (int ks = 0; ks < c.kp / 16; ++ks)
+#pragma unroll
+    for (int u = 0; u < 6; ++u) {
+      tc_mma(dt, tc_desc(a0 + ap[u] * pa + ks * 256, sbo), tc_desc(b0 + bq[u] * pb + ks * 256, sbo), idesc, acc);
+      acc = 1;
+    }
+  tc_commit(&c.tcbar[s & 1u]);
+}
+
+// Bounded wait (whole warp) for the MMAs of tile sequence number s.
+__device__ bool tc_wait(const Cta& c, unsigned s) {
+  uint64_t* bar = &c.tcbar[s & 1u];
+  const uint32_t par = (s >> 1) & 1u;
+  for (int it = 0; it < kWaitLimit; ++it) {
+    const bool ready = mbar_try_wait(bar, par);
+    if (__all_sync(0xffffffffu, ready)) return true;
+  }
+  atomicExch(c.flags, 1);
+  return false;
+}
+
+// Barrier of the warps taking part in a pass: all 16, or warps 4-15 (named
+// barrier 2, the phase-A warps).
+__device__ __forceinline__ void tc_part_sync(int nw) {
+  if (nw == kAlsWarps) __syncthreads();
+  else asm volatile("bar.sync 2, %0;" ::"r"(nw * 32) : "memory");
+}
+
+// One pipelined pass over the CTA's tiles of a slab (row stride gs, n
+// entries): each tile's dot products with the factor whose pieces are in
+// c.fp, one MMA batch per tile (sequence numbers tcseq, tcseq + 1, ...),
+// then consume(T, ok) by the warps [w0, w0 + nw) (nw = 12 or 16).  The ring
+// stage of a tile is released after its consumption.
+// The ring stage of tile g (index T) is free: refill it with tile T + stages.
+// One thread, after a barrier that follows every use of the stage.  The
+// refill of tile T + 1 happens in the iteration before its conversion, so
+// the tensor-core form needs at least three stages.
+__device__ __forceinline__ void tc_release(const Cta& c, unsigned g, int T, const TileSrc& s) {
+  if (T + c.stages < c.ntiles && !*(volatile int*)c.flags) issue_tile(c, g + c.stages, T + c.stages, s);
+}
+
+template <class Consume>
+__device__ void tc_pass(const Cta& c, unsigned seq, unsigned tcseq, const TileSrc& src, int gs, int n, int w0,
+                        int nw, Consume&& consume) {
+  const int t = c.tid - 32 * w0, nt = 32 * nw;
+  const size_t piece = (size_t)kAlsTileRows * c.kp * 2;
+  auto convert = [&](int T) {
+    const unsigned g = seq + (unsigned)T;
+    const bool got = wait_tile(c, g);
+    const float* tile = c.ring + (size_t)(g % (unsigned)c.stages) * c.stage_floats;
+    const int rows = min(kAlsTileRows, c.nrows - T * kAlsTileRows);
+    tc_split_rows(tile, gs, n, got ? rows : 0, kAlsTileRows, c.kp, tc_cbuf(c, tcseq + (unsigned)T), piece, t, nt);
+  };
+  // one barrier per tile: tile T + 1 is converted and its MMAs issued before
+  // tile T is consumed, so they run while the warps wait for and use tile T.
+  // Reuse is safe: MMA T + 1 writes the result buffer of tile T - 1, consumed
+  // before this barrier, and convert T + 1 overwrites the operands of MMA
+  // T - 1, which every thread waited for in the previous iteration.
+  // The ring stage of tile T - 1 is released once, by the issuing thread,
+  // after the barrier that follows every warp's use of it.
+  if (c.ntiles > 0) convert(0);
+  fence_async_shared();
+  tc_part_sync(nw);
+  if (t == 0 && c.ntiles > 0) tc_issue(c, tcseq);
+  for (int T = 0; T < c.ntiles; ++T) {
+    if (T + 1 < c.ntiles) {
+      convert(T + 1);
+      fence_async_shared();
+      tc_fence_before();
+      tc_part_sync(nw);
+      if (t == 0) {
+        tc_issue(c, tcseq + (unsigned)(T + 1));
+        if (T > 0) tc_release(c, seq + (unsigned)(T - 1), T - 1, src);
+      }
+    }
+    const bool ok = tc_wait(c, tcseq + (unsigned)T);
+    tc_fence_after();
+    consume(T, ok);
+    tm_wait_st();
+    tc_fence_before();
+  }
+  tc_part_sync(nw);
+  if (t == 0 && c.ntiles > 0) {
+    if (c.ntiles >= 2) tc_release(c, seq + (unsigned)(c.ntiles - 2), c.ntiles - 2, src);
+    tc_release(c, seq + (unsigned)(c.ntiles - 1), c.ntiles - 1, src);
+  }
+}
+
+// The F terms [i0, i0 + cnt) of this warp when nw warps share the rF terms
+// four lane quarters at a time.
+__device__ __forceinline__ void tc_cols(const Cta& c, int w0, int nw, int& i0, int& cnt, int& ci) {
+  const int ng = nw >> 2, grp = (c.warp - w0) >> 2;
+  ci = (c.rF + ng - 1) / ng;
+  i0 = min(c.rF, grp * ci);
+  cnt = min(c.rF, i0 + ci) - i0;
+}
+
+// Product pass of mode d (tensor-core form), warps [w0, w0 + nw):
+//   kDivide = false: P(j,i) *= <G_j^d, F_i^d>            (prologue)
+//   kDivide = true:  P(j,i) /= <G_j^d, F_i^d>, rebuilding prod_{d' not in
+//                    {ex, d}} when the division is unsafe  (phase A)
+// fa holds F^d.  One thread of the group must call start_phase first.
+template <int LW, bool kDivide>
+__device__ void tc_product_pass(const Cta& c, const AlsParams& p, unsigned seq, unsigned tcseq, int d, int ex,
+                                int w0, int nw) {
+  const int n = p.nbas[d], gs = als_gstride(n);
+  const TileSrc src{c.gm + (long long)p.offg[d] * c.rG, gs, nullptr, 0};
+  tc_split_rows(c.fa, c.gsmax, n, c.rF, c.nf, c.kp, c.fp, (size_t)c.nf * c.kp * 2, c.tid - 32 * w0, 32 * nw);
+  int i0, cnt, ci;
+  tc_cols(c, w0, nw, i0, cnt, ci);
+  const int q = c.warp & 3;
+  tc_pass(c, seq, tcseq, src, gs, n, w0, nw, [&](int T, bool ok) {
+    if (cnt <= 0) return;
+    const int j = T * kAlsTileRows + 32 * q + c.lane;
+    const bool live = ok && j < c.nrows;
+    float dv[LW], pv[LW];
+    tm_ld<LW>(tm_addr(c, (int)((tcseq + (unsigned)T) & 1u) * c.nf + i0), dv);
+    tm_ld<LW>(tm_addr(c, tc_pcol(c, T) + i0), pv);
+    if (!kDivide) {
+#pragma unroll
+      for (int u = 0; u < LW; ++u)
+        if (u < cnt) pv[u] *= dv[u];
+    } else {
+      unsigned rebuild = 0u;
+#pragma unroll
+      for (int u = 0; u < LW; ++u) {
+        if (u >= cnt) continue;
+        const float x = pv[u];
+        const float qv = div_nr(x, dv[u]);
+        const bool good = fabsf(x) >= FLT_MIN && fabsf(qv) <= FLT_MAX;  // also catches a zero divisor
+        if (!good && live) rebuild |= 1u << u;
+        pv[u] = qv;
+      }
+      for (unsigned pending = __ballot_sync(0xffffffffu, rebuild != 0u); pending;
+           pending = __ballot_sync(0xffffffffu, rebuild != 0u)) {
+        const int L = __ffs(pending) - 1;
+        const int bit = __ffs(__shfl_sync(0xffffffffu, rebuild, L)) - 1;
+        const float qv = rebuild_product(c, p, T * kAlsTileRows + 32 * q + L, i0 + bit, ex, d);
+        if (c.lane == L) {
+          rebuild &= rebuild - 1;
+#pragma unroll
+          for (int u = 0; u < LW; ++u)
+            if (u == bit) pv[u] = qv;
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < LW; ++u)
+      if (u < cnt) tm_st1(tm_addr(c, tc_pcol(c, T) + i0 + u), pv[u]);
+  });
+}
+
+// Sums NV values of each lane over the warp into out[0 .. NV) by recursive
+// halving (as warp_sum_values).
+template <int NV>
+__device__ __forceinline__ void warp_sum_flat(const float (&a)[NV], int lane, float* out) {
+  constexpr int P2 = NV <= 16 ? 16 : (NV <= 32 ? 32 : 64);
+  static_assert(NV <= 64, "at most 64 values per lane");
+  float v[P2];
+#pragma unroll
+  for (int q = 0; q < P2; ++q) v[q] = q < NV ? a[q] : 0.f;
+  int base = 0;
+  int n = P2;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool up = (lane & o) != 0;
+    if (n > 1) {
+      const int h = n / 2;
+#pragma unroll
+      for (int q = 0; q < P2 / 2; ++q) {
+        if (q >= h) break;
+        const float send = up ? v[q] : v[h + q];
+        const float keep = up ? v[h + q] : v[q];
+        v[q] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+      if (up) base += h;
+      n = h;
+    } else {
+      v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+    if (q < n && base + q < NV && (P2 >= 32 || (lane & 1) == 0)) out[base + q] = v[q];
+}
+
+// One round of phase B (tensor-core form, all 16 warps) for right-hand-side
+// columns [m0, m0 + MW): round 0 multiplies <G_j^kp, Fnew_i^kp> into P (one
+// MMA batch per tile, factor pieces from fb); every round accumulates
+// acc(i, m) += cG_j P(j,i) G_j^k(m0 + m) for the warp's F terms and lane
+// rows, and ends with the CTA's partial right-hand side columns in bout.
+template <int LW, int CI, int MW>
+__device__ void tc_phase_b_round(const Cta& c, const AlsParams& p, unsigned seq, unsigned tcseq, int round, int m0,
+                                 int k, int kp, float* bout) {
+  const int gsk = als_gstride(p.nbas[k]);
+  const int np_ = p.nbas[kp], gsp = als_gstride(np_);
+  const float* slab_k = c.gm + (long long)p.offg[k] * c.rG;
+  const float* slab_p = c.gm + (long long)p.offg[kp] * c.rG;
+  const TileSrc src = (round == 0) ? TileSrc{slab_p, gsp, slab_k, gsk} : TileSrc{slab_k, gsk, nullptr, 0};
+  const int koff = (round == 0) ? kAlsTileRows * gsp : 0;  // the k slab's place in a stage
+  int i0, cnt, ci;
+  tc_cols(c, 0, kAlsWarps, i0, cnt, ci);
+  const int q = c.warp & 3, jj = 32 * q + c.lane;
+  float acc[CI][MW];
+#pragma unroll
+  for (int u = 0; u < CI; ++u)
+#pragma unroll
+    for (int m = 0; m < MW; ++m) acc[u][m] = 0.f;
+  auto accumulate = [&](int T, const float* stage, const float (&pv)[LW], bool live) {
+    // rows beyond the CTA's terms hold arbitrary running products (0/0 after
+    // a division): select them away, never multiply them by a zero weight
+    const float cwj = live ? c.cw[T * kAlsTileRows + jj] : 0.f;
+    float w[CI];
+#pragma unroll
+    for (int u = 0; u < CI; ++u) w[u] = (live && u < cnt) ? pv[u] * cwj : 0.f;
+    const float* tk = stage + koff + jj * gsk + m0;
+    float4 g4[MW / 4];
+#pragma unroll
+    for (int m4 = 0; m4 < MW / 4; ++m4) g4[m4] = *reinterpret_cast<const float4*>(tk + 4 * m4);
+#pragma unroll
+    for (int u = 0; u < CI; ++u)
+#pragma unroll
+      for (int m4 = 0; m4 < MW / 4; ++m4) {
+        acc[u][4 * m4 + 0] = fmaf(w[u], g4[m4].x, acc[u][4 * m4 + 0]);
+        acc[u][4 * m4 + 1] = fmaf(w[u], g4[m4].y, acc[u][4 * m4 + 1]);
+        acc[u][4 * m4 + 2] = fmaf(w[u], g4[m4].z, acc[u][4 * m4 + 2]);
+        acc[u][4 * m4 + 3] = fmaf(w[u], g4[m4].w, acc[u][4 * m4 + 3]);
+      }
+  };
+  if (round == 0) {
+    if (c.tid == 0) start_phase(c, seq, src);
+    tc_split_rows(c.fb, c.gsmax, np_, c.rF, c.nf, c.kp, c.fp, (size_t)c.nf * c.kp * 2, c.tid, kAlsThreads);
+    tc_pass(c, seq, tcseq, src, gsp, np_, 0, kAlsWarps, [&](int T, bool ok) {
+      if (cnt <= 0) return;
+      const unsigned g = seq + (unsigned)T;
+      const float* stage = c.ring + (size_t)(g % (unsigned)c.stages) * c.stage_floats;
+      const bool live = ok && T * kAlsTileRows + jj < c.nrows;
+      float dv[LW], pv[LW];
+      tm_ld<LW>(tm_addr(c, (int)((tcseq + (unsigned)T) & 1u) * c.nf + i0), dv);
+      tm_ld<LW>(tm_addr(c, tc_pcol(c, T) + i0), pv);
+#pragma unroll
+      for (int u = 0; u < LW; ++u)
+        if (u < cnt) pv[u] *= dv[u];
+#pragma unroll
+      for (int u = 0; u < LW; ++u)
+        if (u < cnt) tm_st1(tm_addr(c, tc_pcol(c, T) + i0 + u), pv[u]);
+      accumulate(T, stage, pv, live);
+    });
+  } else {
+    __syncthreads();  // the ring is idle (every tile of the previous round released)
+    if (c.tid == 0) start_phase(c, seq, src);
+    for (int T = 0; T < c.ntiles; ++T) {
+      const unsigned g = seq + (unsigned)T;
+      const bool ok = wait_tile(c, g);
+      if (cnt > 0) {
+        const float* stage = c.ring + (size_t)(g % (unsigned)c.stages) * c.stage_floats;
+        float pv[LW];
+        tm_ld<LW>(tm_addr(c, tc_pcol(c, T) + i0), pv);
+        accumulate(T, stage, pv, ok && T * kAlsTileRows + jj < c.nrows);
+      }
+      release_tile(c, g, T, kAlsWarps, src);
+    }
+  }
+  {
+    float flat[CI * MW];
+#pragma unroll
+    for (int u = 0; u < CI; ++u)
+#pragma unroll
+      for (int m = 0; m < MW; ++m) flat[u * MW + m] = acc[u][m];
+    warp_sum_flat<CI * MW>(flat, c.lane, c.bred + c.warp * 64);
+  }
+  __syncthreads();
+  // sum over the four lane quarters of each F term (fixed order)
+  for (int e = c.tid; e < c.rF * MW; e += kAlsThreads) {
+    const int i = e / MW, m = e - i * MW, grp = i / ci, u = i - grp * ci;
+    float s = 0.f;
+#pragma unroll
+    for (int qq = 0; qq < 4; ++qq) s += c.bred[(qq + 4 * grp) * 64 + u * MW + m];
+    bout[i * c.npmax + m0 + m] = s;
+  }
+  __syncthreads();
+}
+
+template <int LW, int CI, int RW>
+__device__ unsigned tc_phase_b_rounds(const Cta& c, const AlsParams& p, unsigned seq, unsigned tcseq, int k, int kp,
+                                      float* bout) {
+  const int npk = round_up(p.nbas[k], 4);
+  unsigned used = 0;
+  for (int round = 0, m0 = 0; m0 < npk; ++round, m0 += RW) {
+    const int mw = min(RW, npk - m0);
+    if (mw >= RW) tc_phase_b_round<LW, CI, RW>(c, p, seq + used, tcseq, round, m0, k, kp, bout);
+    else if (mw == 12) tc_phase_b_round<LW, CI, (RW > 12 ? 12 : RW)>(c, p, seq + used, tcseq, round, m0, k, kp, bout);
+    else if (mw == 8) tc_phase_b_round<LW, CI, (RW > 8 ? 8 : RW)>(c, p, seq + used, tcseq, round, m0, k, kp, bout);
+    else tc_phase_b_round<LW, CI, 4>(c, p, seq + used, tcseq, round, m0, k, kp, bout);
+    used += (unsigned)c.ntiles;
+  }
+  return used;
+}
+
+// All rounds of phase B for mode k (tensor-core form); returns tiles used.
+// Round widths keep CI x MW accumulators per lane within 64 registers.
+__device__ unsigned tc_phase_b(const Cta& c, const AlsParams& p, unsigned seq, unsigned tcseq, int k, int kp,
+                               float* bout) {
+  const int cib = (c.rF + 3) / 4;
+  if (cib <= 4) return tc_phase_b_rounds<8, 4, 16>(c, p, seq, tcseq, k, kp, bout);
+  if (cib == 5) return tc_phase_b_rounds<8, 5, 12>(c, p, seq, tcseq, k, kp, bout);
+  if (cib == 6) return tc_phase_b_rounds<8, 6, 8>(c, p, seq, tcseq, k, kp, bout);
+  return tc_phase_b_rounds<8, 8, 8>(c, p, seq, tcseq, k, kp, bout);
+}
+
+// Running products of every tile set to 1 (tensor-core form, all warps).
+__device__ void tc_init_products(const Cta& c) {
+  int i0, cnt, ci;
+  tc_cols(c, 0, kAlsWarps, i0, cnt, ci);
+  for (int T = 0; T < c.ntiles; ++T)
+    for (int u = 0; u < cnt; ++u) tm_st1(tm_addr(c, tc_pcol(c, T) + i0 + u), 1.f);
+  tm_wait_st();
 }
 
 // The double-word solver team (threads 0-127, named barrier 1).
@@ -888,6 +1386,9 @@ __device__ void solve_step(const Cta& c, const AlsParams& p, cg::cluster_group& 
 // finish within the solve; the solver's dependent chains compete with its
 // warps for issue slots, so fewer of them can shorten the step.
 constexpr int kDivideWarps = 12;
+// Tensor-core form: phase A on warps 4-15 (three per lane quarter).
+constexpr int kSolverWarpsAls = kAlsSolverWarps;
+constexpr int kTcDivideWarps = kAlsWarps - kAlsSolverWarps;
 
 // Barrier among the phase-A warps only (named barrier 2).
 __device__ __forceinline__ void worker_sync() {
@@ -900,6 +1401,9 @@ __device__ __forceinline__ void worker_sync() {
 // Persistent cluster kernel
 // ---------------------------------------------------------------------------
 
+// kTc: the tensor-core form (its own instantiation, so that neither form's
+// register allocation carries the other's).
+template <bool kTc>
 __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p) {
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -922,7 +1426,7 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
     c.nrows = min(c.rG, c.row0 + rows_per) - c.row0;
   }
   c.ntiles = (c.nrows + kAlsTileRows - 1) / kAlsTileRows;
-  const AlsSmem lay = als_smem_layout(p.rows_cta_max, p.rf_max, p.npmax, p.gsmax, p.stages);
+  const AlsSmem lay = als_smem_layout(p.rows_cta_max, p.rf_max, p.npmax, p.gsmax, p.stages, p.tc);
   c.ldP = lay.ldP;
   c.gsmax = p.gsmax;
   c.npmax = p.npmax;
@@ -953,6 +1457,20 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
   c.b0 = reinterpret_cast<dw*>(smem_raw + lay.b0);
   c.res = reinterpret_cast<dw*>(smem_raw + lay.res);
   c.red = reinterpret_cast<float*>(smem_raw + lay.red);
+  c.tc = kTc ? 1 : 0;
+  c.kp = lay.kp;
+  c.nf = lay.nf;
+  c.cb = smem_raw + lay.cb;
+  c.fp = smem_raw + lay.fp;
+  c.tcbar = reinterpret_cast<uint64_t*>(smem_raw + lay.tcbar);
+  uint32_t* tbase = reinterpret_cast<uint32_t*>(smem_raw + lay.tbase);
+  c.tmem = 0;
+  if (kTc && c.warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tbase)),
+                 "r"(kAlsTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
   c.gm = p.gm + p.gm_off[c.v];
   c.fcta = p.fcta + (p.f_row_off[c.v] * c.CL + (long long)c.rank * c.rF) * p.nDp;
   {
@@ -964,7 +1482,8 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
 
   // ---- prologue ----
   for (int e = c.tid; e < c.stages * c.stage_floats; e += kAlsThreads) c.ring[e] = 0.f;  // stale reads stay finite
-  for (int e = c.tid; e < lay.rFp * c.ldP; e += kAlsThreads) c.P[e] = (e / c.ldP < rF) ? 1.f : 0.f;
+  if (!kTc)
+    for (int e = c.tid; e < lay.rFp * c.ldP; e += kAlsThreads) c.P[e] = (e / c.ldP < rF) ? 1.f : 0.f;
   for (int j = c.tid; j < c.ldP; j += kAlsThreads) c.cw[j] = (j < c.nrows) ? p.gc[p.g_row_off[c.v] + c.row0 + j] : 0.f;
   for (int e = c.tid; e < 2 * lay.rFp * c.npmax; e += kAlsThreads) c.bpart[e] = 0.f;
   if (c.tid < c.stages) {
@@ -975,20 +1494,37 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
   if (c.tid < 8) c.flags[c.tid] = 0;
   if (c.tid == 0) {
     for (int s = 0; s < c.stages; ++s) mbar_init(&c.bar[s], 1);
+    mbar_init(&c.tcbar[0], 1);
+    mbar_init(&c.tcbar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   const float* f32v = p.f32 + p.f_row_off[c.v] * p.nDp;
   const float* f32lo_v = p.f32lo + p.f_row_off[c.v] * p.nDp;
   for (int e = c.tid; e < rF * p.nDp; e += kAlsThreads) c.fcta[e] = f32v[e];
+  tc_fence_before();
   __syncthreads();
+  tc_fence_after();
+  if (kTc) {
+    c.tmem = *tbase;
+    tc_init_products(c);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+  }
 
   // running products without modes 0 and D-1 (the state phase B of step 0 expects)
   unsigned seq = 0;
+  unsigned tcseq = 0;  // MMA batches issued so far (tensor-core form; the same count in every thread)
   for (int d = 1; d <= D - 2; ++d) {
     load_factor(c, p, d, c.fa, 0, kAlsThreads);
     __syncthreads();
     if (c.tid == 0) start_phase(c, seq, TileSrc{c.gm + (long long)p.offg[d] * c.rG, als_gstride(p.nbas[d]), nullptr, 0});
-    product_pass(c, p, seq, d, false, -1, 0, kAlsWarps);
+    if (kTc) {
+      tc_product_pass<8, false>(c, p, seq, tcseq, d, -1, 0, kAlsWarps);
+      tcseq += (unsigned)c.ntiles;
+    } else {
+      product_pass(c, p, seq, d, false, -1, 0, kAlsWarps);
+    }
     seq += (unsigned)c.ntiles;
     __syncthreads();
   }
@@ -1029,7 +1565,12 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
   const int nsteps = p.nals * D;
   for (int t = 0; t < nsteps; ++t) {
     const int k = t % D, kp = (k + D - 1) % D, kn = (k + 1) % D;
-    seq += phase_b(c, p, seq, k, kp, c.bpart + (size_t)(t & 1) * c.rFp * c.npmax);
+    if (kTc) {
+      seq += tc_phase_b(c, p, seq, tcseq, k, kp, c.bpart + (size_t)(t & 1) * c.rFp * c.npmax);
+      tcseq += (unsigned)c.ntiles;
+    } else {
+      seq += phase_b(c, p, seq, k, kp, c.bpart + (size_t)(t & 1) * c.rFp * c.npmax);
+    }
     cluster_arrive();
     if (c.warp < kAlsSolverWarps) {
       cluster_wait();
@@ -1040,13 +1581,22 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
         worker_sync();
         if (c.tid == kSolverThreads)
           start_phase(c, seq, TileSrc{c.gm + (long long)p.offg[kn] * c.rG, als_gstride(p.nbas[kn]), nullptr, 0});
-        if (c.warp >= kAlsWarps - kDivideWarps)
+        if (kTc) {
+          if ((rF + 2) / 3 <= 8) tc_product_pass<8, true>(c, p, seq, tcseq, kn, k, kSolverWarpsAls, kTcDivideWarps);
+          else tc_product_pass<16, true>(c, p, seq, tcseq, kn, k, kSolverWarpsAls, kTcDivideWarps);
+        } else if (c.warp >= kAlsWarps - kDivideWarps) {
           product_pass(c, p, seq, kn, true, k, kAlsWarps - kDivideWarps, kDivideWarps);
+        }
       }
       cluster_wait();
     }
-    if (t + 1 < nsteps) seq += (unsigned)c.ntiles;
+    if (t + 1 < nsteps) {
+      seq += (unsigned)c.ntiles;
+      if (kTc) tcseq += (unsigned)c.ntiles;
+    }
+    tc_fence_before();
     __syncthreads();
+    tc_fence_after();
   }
   // every CTA of the cluster has gathered before any shared memory goes away
   cluster_arrive();
@@ -1062,6 +1612,14 @@ __global__ void __launch_bounds__(kAlsThreads, 1) als_cluster_kernel(AlsParams p
     if (c.flags[0]) atomicOr(&p.status[c.v], 2);
     if (c.flags[1]) atomicOr(&p.status[c.v], 1);
   }
+  if (kTc) {
+    // every MMA batch was waited for by its consumers; free the tensor memory
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (c.warp == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(c.tmem), "r"(kAlsTcCols) : "memory");
+  }
 }
 
 size_t als_smem_bytes(int rows_cta, int rF, int npmax, int gsmax, int stages, int tc) {
@@ -1074,20 +1632,25 @@ bool als_choose_shape(int nvec, int rGmax, int rFmax, int npmax, int gsmax, int 
   // whole batch still fit on the SMs at one CTA per SM; larger when the
   // running products of a CTA's term range need more shared memory.  Ring
   // depth: as many stages (2-6) as fit.
+  // With the tensor-core engine forced (als_engine() == 2) the same walk
+  // takes the tensor-core form wherever it fits.
+  const bool want_tc = als_engine() == 2;
   int cl = 1;
   while (cl < 16 && cl * 2 * nvec <= num_sms) cl *= 2;
   for (;;) {
     const int rows = (rGmax + cl - 1) / cl;
-    for (int ns = 6; ns >= 2; --ns) {
-      const size_t b = als_smem_bytes(rows, rFmax, npmax, gsmax, ns);
-      if (b <= smem_limit) {
-        out->cluster = cl;
-        out->stages = ns;
-        out->rows_cta = rows;
-        out->smem = b;
-        return true;
+    for (int tc = (want_tc && als_tc_fits(rows, rFmax, npmax)) ? 1 : 0; tc >= 0; --tc)
+      for (int ns = 6; ns >= (tc ? 3 : 2); --ns) {
+        const size_t b = als_smem_bytes(rows, rFmax, npmax, gsmax, ns, tc);
+        if (b <= smem_limit) {
+          out->cluster = cl;
+          out->stages = ns;
+          out->rows_cta = rows;
+          out->tc = tc;
+          out->smem = b;
+          return true;
+        }
       }
-    }
     if (cl >= 16) return false;
     cl *= 2;
   }
@@ -1173,7 +1736,7 @@ int als_launch(const AlsParams& p, size_t smem, cudaStream_t st, cudaEvent_t t0,
   als_prep_kernel<<<(int)blocks, 256, 0, st>>>(p);
   MLCP_CUDA_TRY(cudaGetLastError());
   if (t0) MLCP_CUDA_TRY(cudaEventRecord(t0, st));
-  auto fn = als_cluster_kernel;
+  auto fn = p.tc ? als_cluster_kernel<true> : als_cluster_kernel<false>;
   MLCP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (p.cluster > 8) MLCP_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};

@@ -215,9 +215,10 @@ int plan_als(Context* ctx, int nvec, int ndof, const int* nbas, const int* rF, c
 struct TuneKey {
   int device, nvec, ndof, nD, npmax, gsmax, rGmax, rFmax;
   long long total_rows;
+  int engine;
   bool operator<(const TuneKey& o) const {
-    return std::tie(device, nvec, ndof, nD, npmax, gsmax, rGmax, rFmax, total_rows) <
-           std::tie(o.device, o.nvec, o.ndof, o.nD, o.npmax, o.gsmax, o.rGmax, o.rFmax, o.total_rows);
+    return std::tie(device, nvec, ndof, nD, npmax, gsmax, rGmax, rFmax, total_rows, engine) <
+           std::tie(o.device, o.nvec, o.ndof, o.nD, o.npmax, o.gsmax, o.rGmax, o.rFmax, o.total_rows, o.engine);
   }
 };
 
@@ -230,6 +231,26 @@ std::mutex g_tune_mu;
 std::map<TuneKey, TuneEntry> g_tune;
 int g_autotune = -1;  // -1: not yet read from the environment
 
+int g_als_engine = -1;  // -1: not yet read from the environment
+
+}  // namespace
+
+int als_engine() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (g_als_engine < 0) {
+    const char* e = getenv("MLCP_GB300_ALS_ENGINE");
+    g_als_engine = (e && (e[0] == '1' || e[0] == '2')) ? e[0] - '0' : 0;
+  }
+  return g_als_engine;
+}
+
+void set_als_engine(int e) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_als_engine = (e == 1 || e == 2) ? e : 0;
+}
+
+namespace {
+
 bool autotune_enabled() {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   if (g_autotune < 0) {
@@ -239,25 +260,38 @@ bool autotune_enabled() {
   return g_autotune != 0;
 }
 
-// Feasible (cluster, stages) pairs: every power-of-two cluster up to 16 whose
-// clusters fit on the GPU in at most two waves, every ring depth 2-6 whose
-// shared memory fits.
+// Feasible (cluster, stages, engine) triples: every power-of-two cluster up
+// to 16 whose clusters fit on the GPU in at most two waves, every ring depth
+// 2-6 whose shared memory fits, in the CUDA-core form and, where it fits
+// (als_tc_fits), the tensor-core form, as the engine setting allows.
 std::vector<AlsShape> als_candidates(int nvec, int rGmax, int rFmax, int npmax, int gsmax, int num_sms,
                                      size_t smem_limit) {
   std::vector<AlsShape> out;
+  const int engine = als_engine();
   for (int cl = 1; cl <= 16; cl *= 2) {
     if (cl > 1 && (long long)cl * nvec > 2LL * num_sms) break;
     const int rows = (rGmax + cl - 1) / cl;
-    for (int ns = 2; ns <= 6; ++ns) {
-      const size_t b = als_smem_bytes(rows, rFmax, npmax, gsmax, ns);
-      if (b > smem_limit) continue;
-      AlsShape s;
-      s.cluster = cl;
-      s.stages = ns;
-      s.rows_cta = rows;
-      s.smem = b;
-      out.push_back(s);
+    for (int tc = 1; tc >= 0; --tc) {
+      if (tc == 1 && (engine == 1 || !als_tc_fits(rows, rFmax, npmax))) continue;
+      for (int ns = tc ? 3 : 2; ns <= 6; ++ns) {  // the tensor-core form refills one tile ahead
+        const size_t b = als_smem_bytes(rows, rFmax, npmax, gsmax, ns, tc);
+        if (b > smem_limit) continue;
+        AlsShape s;
+        s.cluster = cl;
+        s.stages = ns;
+        s.rows_cta = rows;
+        s.tc = tc;
+        s.smem = b;
+        out.push_back(s);
+      }
     }
+  }
+  // forced tensor cores: only the tensor-core shapes, unless none fits
+  if (engine == 2) {
+    std::vector<AlsShape> t;
+    for (const AlsShape& s : out)
+      if (s.tc) t.push_back(s);
+    if (!t.empty()) out.swap(t);
   }
   return out;
 }
@@ -274,15 +308,20 @@ int als_run(Context* ctx, const AlsJob& job, cudaStream_t st) {
   AlsPlan P;
   int rc = plan_als(ctx, job.nvec, job.ndof, job.nbas, job.rF, job.rG, &P);
   if (rc) return rc;
-  TuneKey key{ctx->device, job.nvec, job.ndof, P.nD, P.npmax, P.gsmax, 0, P.rFmax, P.total_rows};
+  TuneKey key{ctx->device, job.nvec, job.ndof, P.nD, P.npmax, P.gsmax, 0, P.rFmax, P.total_rows, als_engine()};
   for (int v = 0; v < job.nvec; ++v) key.rGmax = std::max(key.rGmax, job.rG[v]);
   {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    auto it = g_tune.find(key);
-    if (it != g_tune.end()) {
-      const AlsShape s = it->second.shape;
-      return als_run_shape(ctx, job, st, &s);
+    AlsShape cached;
+    bool hit = false;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) {
+        cached = it->second.shape;
+        hit = true;
+      }
     }
+    if (hit) return als_run_shape(ctx, job, st, &cached);  // (outside the lock: the run reads the engine setting)
   }
   if (job.g_host) return als_run_shape(ctx, job, st, nullptr);  // tuned by a device-resident call
   std::vector<AlsShape> cand = als_candidates(job.nvec, key.rGmax, P.rFmax, P.npmax, P.gsmax, ctx->num_sms,
@@ -356,11 +395,13 @@ int autotune_report(char* buf, int len) {
   char line[256];
   for (const auto& kv : g_tune) {
     const TuneKey& k = kv.first;
-    snprintf(line, sizeof(line), "als nvec=%d ndof=%d nD=%d rG<=%d rF<=%d: cluster %d stages %d;", k.nvec, k.ndof,
-             k.nD, k.rGmax, k.rFmax, kv.second.shape.cluster, kv.second.shape.stages);
+    snprintf(line, sizeof(line), "als nvec=%d ndof=%d nD=%d rG<=%d rF<=%d engine=%d: cluster %d stages %d %s;",
+             k.nvec, k.ndof, k.nD, k.rGmax, k.rFmax, k.engine, kv.second.shape.cluster, kv.second.shape.stages,
+             kv.second.shape.tc ? "tensor" : "cuda");
     out += line;
     for (const auto& t : kv.second.trials) {
-      snprintf(line, sizeof(line), " %dx%d=%.3fms", t.first.cluster, t.first.stages, t.second);
+      snprintf(line, sizeof(line), " %dx%d%s=%.3fms", t.first.cluster, t.first.stages, t.first.tc ? "t" : "c",
+               t.second);
       out += line;
     }
     out += "\n";
@@ -470,6 +511,7 @@ int als_run_shape(Context* ctx, const AlsJob& job, cudaStream_t st, const AlsSha
   prm.pen_factor = job.pen_factor;
   prm.cluster = CL;
   prm.stages = P.shape.stages;
+  prm.tc = P.shape.tc;
   prm.rows_cta_max = P.shape.rows_cta;
   prm.total_rows = P.total_rows;
   prm.total_f_terms = P.total_f;
@@ -658,6 +700,10 @@ extern "C" double mlcp_gb300_last_kernel_ms(void) {
 extern "C" int mlcp_gb300_last_status(void) { return t_status; }
 
 extern "C" void mlcp_gb300_set_autotune(int enable) { set_autotune(enable); }
+
+extern "C" void mlcp_gb300_set_als_engine(int engine) { set_als_engine(engine); }
+
+extern "C" int mlcp_gb300_als_engine(void) { return als_engine(); }
 
 extern "C" int mlcp_gb300_autotune_report(char* buf, int len) { return autotune_report(buf, len); }
 

@@ -172,6 +172,7 @@ int run(int ndof, const int* nbas, int rF, int rG, double* d_coef, double* d_bas
   prm.pen_factor = 1.0e-10;
   prm.cluster = CL;
   prm.stages = shape.stages;
+  prm.tc = shape.tc;
   prm.rows_cta_max = shape.rows_cta;
   prm.total_rows = rG;
   prm.total_f_terms = rF;
