@@ -290,6 +290,16 @@ MLCP_API int mlcp_gb300_autotune_report(char *buf, int len);
 MLCP_API void mlcp_gb300_set_als_engine(int engine);
 MLCP_API int mlcp_gb300_als_engine(void);
 
+/* CUDA-graph replay of the power cycle (extension).  intertwinecpp_ and
+ * intertwineraggedcpp_ capture the device part of a cycle (POW_ALS,
+ * Gram-Schmidt, PRODHV_ALS, Rayleigh-Ritz, vector updates) as a CUDA graph
+ * the first time a shape is seen and replay it for later cycles of the same
+ * shape (block, ranks, operator table, npow, nals, update, ishift); only the
+ * host copies in and out stay outside the graph.  Enabled by default;
+ * enable = 0 here, or MLCP_GB300_CYCLE_GRAPH=0, launches the kernels one by
+ * one instead.  Results are identical either way. */
+MLCP_API void mlcp_gb300_set_cycle_graph(int enable);
+
 /* Kernel timing (extension).  When enabled, the library records CUDA events
  * around its dominant kernel of each call on the call's stream;
  * mlcp_gb300_last_kernel_ms() synchronises on the end event and returns the

@@ -100,6 +100,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.mlcp_gb300_set_als_engine.argtypes = [ctypes.c_int]
         L.mlcp_gb300_als_engine.restype = ctypes.c_int
         L.mlcp_gb300_als_engine.argtypes = []
+        L.mlcp_gb300_set_cycle_graph.restype = None
+        L.mlcp_gb300_set_cycle_graph.argtypes = [ctypes.c_int]
         L.mlcp_gb300_autotune_report.restype = ctypes.c_int
         L.mlcp_gb300_autotune_report.argtypes = [ctypes.c_char_p, ctypes.c_int]
         _F = ctypes.c_float

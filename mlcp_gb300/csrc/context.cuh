@@ -32,6 +32,11 @@ struct Context {
   // device copies of caller host buffers (host-buffer entry points)
   void* io = nullptr;
   size_t io_bytes = 0;
+  // the power cycle's launch sequence captured as a CUDA graph, with the
+  // key (shape, buffers, operator table) it was captured for
+  cudaGraph_t cyc_graph = nullptr;
+  cudaGraphExec_t cyc_exec = nullptr;
+  unsigned long long cyc_key[16] = {};
   // optional timing of the dominant kernel of the latest call
   bool timing = false;
   bool timed = false;

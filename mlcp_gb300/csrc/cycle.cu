@@ -243,7 +243,7 @@ __global__ void update_weights_kernel(int B, int R, const double* qcoef, const d
 }
 
 struct CycleBuffers {
-  double *q, *qc, *hq, *hqc, *qn, *qnc;
+  double *q, *qc, *hq, *hqc, *qn, *qnc, *shift;
   dw *mscr, *wscr, *zscr, *uwork, *qdw;
   double *g64, *gsw, *A, *S, *U, *eigv, *gwork, *wts;
   int *meta, *status;
@@ -272,9 +272,32 @@ size_t plan_cycle(const Layout& Ly, const OpTable& t, int R, int B, CycleBuffers
   cb->wts = (double*)take(sizeof(double) * (size_t)B * B * R);
   cb->uwork = (dw*)take(sizeof(dw) * upd_work_dw(B, R, Ly.D));
   cb->qdw = (dw*)take(sizeof(dw) * upd_qdw_dw(B, R, Ly.nD));
+  cb->shift = (double*)take(sizeof(double) * B);
   cb->meta = (int*)take(sizeof(int) * (3 * (Ly.D + 1) + B));
   cb->status = (int*)take(sizeof(int) * (B + 4));
   return bytes;
+}
+
+// CUDA-graph replay of the cycle's launch sequence (on unless
+// MLCP_GB300_CYCLE_GRAPH=0 or mlcp_gb300_set_cycle_graph(0)).
+std::mutex g_graph_mu;
+int g_cycle_graph = -1;
+
+bool cycle_graph_enabled() {
+  std::lock_guard<std::mutex> lk(g_graph_mu);
+  if (g_cycle_graph < 0) {
+    const char* e = getenv("MLCP_GB300_CYCLE_GRAPH");
+    g_cycle_graph = (e && e[0] == '0') ? 0 : 1;
+  }
+  return g_cycle_graph != 0;
+}
+
+void drop_cycle_graph(Context* ctx) {
+  if (ctx->cyc_exec) cudaGraphExecDestroy(ctx->cyc_exec);
+  if (ctx->cyc_graph) cudaGraphDestroy(ctx->cyc_graph);
+  ctx->cyc_exec = nullptr;
+  ctx->cyc_graph = nullptr;
+  for (auto& k : ctx->cyc_key) k = 0;
 }
 
 // New block: vector i fits sum_k U(k,i) Q_k (cb.U from the Rayleigh-Ritz
@@ -339,6 +362,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
   if (bytes > ctx->cyc_bytes) {
     if (ctx->cyc) {
       MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+      drop_cycle_graph(ctx);  // it refers to the old workspace
       MLCP_CUDA_TRY(cudaFree(ctx->cyc));
       ctx->cyc = nullptr;
       ctx->cyc_bytes = 0;
@@ -348,6 +372,11 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
   }
   plan_cycle(Ly, tab, R, B, &cb, static_cast<char*>(ctx->cyc));
   const size_t nvals = (size_t)B * R * Ly.nD;
+  {
+    const std::vector<double> sh(B, Eshift);  // per-vector shifts: a device input of the graph
+    MLCP_CUDA_TRY(cudaMemcpyAsync(cb.shift, sh.data(), sizeof(double) * B, cudaMemcpyHostToDevice, st));
+    MLCP_CUDA_TRY(cudaStreamSynchronize(st));
+  }
   MLCP_CUDA_TRY(cudaMemcpyAsync(cb.q, base, sizeof(double) * nvals, cudaMemcpyHostToDevice, st));
   std::vector<double> qc_host;
   if (ranks) {  // ragged: terms beyond a vector's rank carry zero weight
@@ -370,53 +399,103 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
   const int* d_off = cb.meta + (ndof + 1);
   const int* d_offp = cb.meta + 2 * (ndof + 1);
   const int* d_rank = ranks ? cb.meta + 3 * (ndof + 1) : nullptr;
-  MLCP_CUDA_TRY(cudaMemsetAsync(cb.status, 0, sizeof(int) * (B + 4), st));
-
-  // --- matrix-vector products: POW_ALS on every vector ---
-  if (npow > 0) {
-    OpAlsParams p{};
-    p.eshift_v = nullptr;
-    p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 0; p.nsweeps = npow; p.ishift = ishift; p.eshift = Eshift;
-    p.pen_factor = kPen;
-    p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.q; p.f_coef = cb.qc;
-    p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
-    p.rank_v = d_rank;
-    if ((rc = opals_launch(p, st))) return rc;
-  }
-  // --- Gram-Schmidt ---
-  if (nals > 0) {
-    GsParams g{};
-    g.D = ndof; g.R = R; g.nbloc = B; g.nD = Ly.nD; g.nDp = Ly.nDp; g.npmax = Ly.npmax; g.nals = nals;
-    g.nbas = d_nbas; g.off = d_off; g.offp = d_offp; g.base = cb.q; g.coef = cb.qc;
-    g.work = cb.gsw; g.status = cb.status + B; g.rank_v = d_rank;
-    if ((rc = gs_launch(g, st))) return rc;
-  }
-  if (update) {
-    // --- <Q|H|Q>, <Q|Q>, generalised eigenproblem ---
-    if (nals > 0) {
+  // The device part of the cycle: status reset, POW_ALS, Gram-Schmidt,
+  // PRODHV_ALS, Rayleigh-Ritz and the vector updates.  Every input it reads
+  // (block, weights, shifts, ranks, operator table) sits in device buffers
+  // whose addresses depend only on the shape, so the sequence is captured
+  // once as a CUDA graph and replayed by later cycles of the same shape.
+  auto enqueue = [&]() -> int {
+    MLCP_CUDA_TRY(cudaMemsetAsync(cb.status, 0, sizeof(int) * (B + 4), st));
+    // --- matrix-vector products: POW_ALS on every vector ---
+    if (npow > 0) {
       OpAlsParams p{};
-      p.eshift_v = nullptr;
-      p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 1; p.nsweeps = nals; p.ishift = 0; p.eshift = 0.0;
+      p.eshift_v = cb.shift;
+      p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 0; p.nsweeps = npow; p.ishift = ishift; p.eshift = Eshift;
       p.pen_factor = kPen;
-      p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.hq; p.f_coef = cb.hqc;
+      p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.q; p.f_coef = cb.qc;
       p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
       p.rank_v = d_rank;
-      if ((rc = opals_launch(p, st))) return rc;
-    } else {
-      MLCP_CUDA_TRY(cudaMemsetAsync(cb.hq, 0, sizeof(double) * nvals, st));
-      MLCP_CUDA_TRY(cudaMemsetAsync(cb.hqc, 0, sizeof(double) * B * R, st));
+      if (int r = opals_launch(p, st)) return r;
     }
-    GepParams gp;
-    gp.D = ndof; gp.R = R; gp.nbloc = B; gp.nD = Ly.nD; gp.nbas = d_nbas;
-    gp.q_base = cb.q; gp.q_coef = cb.qc; gp.hq_base = cb.hq; gp.hq_coef = cb.hqc;
-    gp.A = cb.A; gp.S = cb.S; gp.eigv = cb.eigv; gp.U = cb.U; gp.work = cb.gwork; gp.status = cb.status + B + 1;
-    if ((rc = gep_launch(gp, st))) return rc;
-    // --- vector updates: new Q_i fits sum_k U(k,i) Q_k, starting from Q_i ---
+    // --- Gram-Schmidt ---
     if (nals > 0) {
-      if ((rc = run_updates(ctx, Ly, cb, d_nbas, d_off, R, B, nals, st, d_rank))) return rc;
-      std::swap(cb.q, cb.qn);
-      std::swap(cb.qc, cb.qnc);
+      GsParams g{};
+      g.D = ndof; g.R = R; g.nbloc = B; g.nD = Ly.nD; g.nDp = Ly.nDp; g.npmax = Ly.npmax; g.nals = nals;
+      g.nbas = d_nbas; g.off = d_off; g.offp = d_offp; g.base = cb.q; g.coef = cb.qc;
+      g.work = cb.gsw; g.status = cb.status + B; g.rank_v = d_rank;
+      if (int r = gs_launch(g, st)) return r;
     }
+    if (update) {
+      // --- <Q|H|Q>, <Q|Q>, generalised eigenproblem ---
+      if (nals > 0) {
+        OpAlsParams p{};
+        p.eshift_v = nullptr;
+        p.ops = tab; p.nvec = B; p.nD = Ly.nD; p.mode = 1; p.nsweeps = nals; p.ishift = 0; p.eshift = 0.0;
+        p.pen_factor = kPen;
+        p.fo_base = cb.q; p.fo_coef = cb.qc; p.f_base = cb.hq; p.f_coef = cb.hqc;
+        p.mscr = cb.mscr; p.wscr = cb.wscr; p.zscr = cb.zscr; p.g64 = cb.g64; p.status = cb.status;
+        p.rank_v = d_rank;
+        if (int r = opals_launch(p, st)) return r;
+      } else {
+        MLCP_CUDA_TRY(cudaMemsetAsync(cb.hq, 0, sizeof(double) * nvals, st));
+        MLCP_CUDA_TRY(cudaMemsetAsync(cb.hqc, 0, sizeof(double) * B * R, st));
+      }
+      GepParams gp;
+      gp.D = ndof; gp.R = R; gp.nbloc = B; gp.nD = Ly.nD; gp.nbas = d_nbas;
+      gp.q_base = cb.q; gp.q_coef = cb.qc; gp.hq_base = cb.hq; gp.hq_coef = cb.hqc;
+      gp.A = cb.A; gp.S = cb.S; gp.eigv = cb.eigv; gp.U = cb.U; gp.work = cb.gwork; gp.status = cb.status + B + 1;
+      if (int r = gep_launch(gp, st)) return r;
+      // --- vector updates: new Q_i fits sum_k U(k,i) Q_k, starting from Q_i ---
+      if (nals > 0)
+        if (int r = run_updates(ctx, Ly, cb, d_nbas, d_off, R, B, nals, st, d_rank)) return r;
+    }
+    return kOk;
+  };
+  if (cycle_graph_enabled()) {
+    const unsigned long long key[16] = {(unsigned long long)(uintptr_t)ctx->cyc, bytes,
+                                        (unsigned long long)(uintptr_t)tab.hdw,
+                                        (unsigned long long)(uintptr_t)tab.alpha, (unsigned long long)ndof,
+                                        (unsigned long long)R, (unsigned long long)B, (unsigned long long)T,
+                                        (unsigned long long)npow, (unsigned long long)nals,
+                                        (unsigned long long)update, (unsigned long long)(ishift + 8),
+                                        (unsigned long long)(ranks != nullptr), (unsigned long long)Ly.nD,
+                                        (unsigned long long)Ly.nDp,
+                                        ((unsigned long long)tab.utot << 40) | ((unsigned long long)tab.umax << 20) |
+                                            (unsigned long long)tab.npmax};
+    if (!ctx->cyc_exec || std::memcmp(key, ctx->cyc_key, sizeof(key)) != 0) {
+      drop_cycle_graph(ctx);
+      MLCP_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+      const int erc = enqueue();
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+      if (erc != kOk || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (erc != kOk) return erc;
+        set_error("intertwinecpp_: capture of the cycle failed: %s", cudaGetErrorString(ce));
+        return kCudaError;
+      }
+      cudaGraphExec_t exec = nullptr;
+      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+      if (ie != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        cudaGetLastError();
+        set_error("intertwinecpp_: instantiation of the cycle graph failed: %s", cudaGetErrorString(ie));
+        return kCudaError;
+      }
+      ctx->cyc_graph = graph;
+      ctx->cyc_exec = exec;
+      std::memcpy(ctx->cyc_key, key, sizeof(key));
+    }
+    MLCP_CUDA_TRY(cudaGraphLaunch(ctx->cyc_exec, st));
+  } else {
+    if ((rc = enqueue())) return rc;
+  }
+  if (update && nals > 0) {  // the updated block is in qn
+    std::swap(cb.q, cb.qn);
+    std::swap(cb.qc, cb.qnc);
+  }
+  if (update) {
     MLCP_CUDA_TRY(cudaMemcpyAsync(eigv, cb.eigv, sizeof(double) * B, cudaMemcpyDeviceToHost, st));
   }
   MLCP_CUDA_TRY(cudaMemcpyAsync(base, cb.q, sizeof(double) * nvals, cudaMemcpyDeviceToHost, st));
@@ -903,6 +982,11 @@ size_t cycle_bytes_estimate(int rk, int ndof, int nbloc, const int* nbas, int T,
 }  // namespace mlcp
 
 using namespace mlcp;
+
+extern "C" void mlcp_gb300_set_cycle_graph(int enable) {
+  std::lock_guard<std::mutex> lk(mlcp::g_graph_mu);
+  mlcp::g_cycle_graph = enable ? 1 : 0;
+}
 
 extern "C" void intertwinecpp_(double* base, double* coef, int* nbas, const int& rk, const int& ndof,
                                const int& nbloc, int* opid, int* mptr, double* Hcoef, double* mat, const int& TxD,

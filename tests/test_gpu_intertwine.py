@@ -293,3 +293,34 @@ def test_diagonalize_three_modes_matches_oracle(nals, cuda_device):
         np.testing.assert_array_equal(gc, coef)
     else:
         compare_blocks(gb, gc, ob, oc, nbas, rk, B)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [1, 3, 7])
+def test_cycle_graph_replay_matches_eager_launches(case, cuda_device):
+    """The cycle replayed from its captured CUDA graph gives bit-identical
+    blocks and eigenvalues to the same cycle launched kernel by kernel, over
+    three cycles that change the shift (a device input of the graph) and
+    interleave another shape (which recaptures)."""
+    from mlcp_gb300 import _lib
+    L = _lib.load()
+    make, rk, nbloc, npow, nals, update, ishift, esh = CASES[case]
+    hl = make()
+    other = H.random_hoplist([4, 5, 3], 6, seed=3)
+    Q0, qc0 = start_block(hl.nbas, rk, nbloc, seed=40 + case)
+    Qo, qco = start_block(other.nbas, 3, 4, seed=99)
+    outs = {}
+    for graph in (0, 1):
+        L.mlcp_gb300_set_cycle_graph(graph)
+        Q, qc, eig = Q0.copy(), qc0.copy(), np.arange(nbloc, dtype=float)
+        res = []
+        for cyc in range(3):
+            Q, qc, eig = IT.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, eig, npow, nals, update, ishift,
+                                       esh + 0.5 * cyc)
+            IT.intertwine(Qo, qco, other.nbas, 3, 4, other, np.arange(4.0), 2, 2, True, 1, 2.0)
+            res.append((Q.copy(), qc.copy(), eig.copy()))
+        outs[graph] = res
+    L.mlcp_gb300_set_cycle_graph(1)
+    for (a, b) in zip(outs[0], outs[1]):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
