@@ -93,6 +93,8 @@ size_t gs_work_doubles(int nbloc, int R, int nD, int D, int npm);
 struct UpdParams {
   int D, R, B, nD, npmax, nals;
   int tile;               // block terms per shared-memory tile (set by upd_launch)
+  int cl;                 // CTAs per output vector (a cluster; set by upd_launch)
+  int resident;           // 1: the block overlaps of a CTA's terms in shared memory (set by upd_launch)
   const int* nbas;        // [D] (device)
   const int* off;         // [D+1] reference-layout offsets (device)
   const double* q;        // old block (reference layout)

@@ -15,27 +15,40 @@
 // are the Grams and the solve; FP32 right-hand sides are not accurate enough
 // for that rule.
 //
-// GB300 layout: one CTA per output vector (the updates are independent: the
-// reference writes each new vector to the host and keeps fitting the old
-// block).  The block's factors are converted once to a double-word,
-// mode-major copy shared by all CTAs (the mode-k slice of all B R terms is
-// one contiguous run, L2-resident); each CTA keeps in global scratch the
-// per-mode overlaps Gram_d(i', lr) = <Q_lr^d, F_i'^d> of every block term lr
-// with its own terms i' (only mode k changes per step) and its F Grams.  The
-// right-hand side streams the block terms through shared memory in tiles:
-// the products w_lr prod_{d!=k} Gram_d(i', lr) of a tile first, then the
-// contraction with the tile's mode-k factors, while warp 0 inverts BB in
-// registers (the refinement's preconditioner).
+// GB300 layout: a cluster of cl CTAs per output vector (the updates are
+// independent: the reference writes each new vector to the host and keeps
+// fitting the old block); cl is the largest of 1-4 that keeps the whole
+// block's clusters on the SMs at once.  The block's factors are converted
+// once to a double-word, mode-major copy shared by all CTAs (the mode-k
+// slice of all B R terms is one contiguous run, L2-resident).  CTA `rank`
+// of a cluster owns a contiguous range of the B R block terms lr and keeps
+// the per-mode overlaps Gram_d(i', lr) = <Q_lr^d, F_i'^d> of its terms with
+// the fitted vector's terms i' (only mode k changes per step), in shared
+// memory when they fit, else in global scratch; every CTA keeps the same F
+// Grams.  The right-hand side streams the CTA's block terms through shared
+// memory in tiles: the products w_lr prod_{d!=k} Gram_d(i', lr) of a tile
+// first, then the contraction with the tile's mode-k factors, while warp 0
+// inverts BB in registers (the refinement's preconditioner).  The partial
+// right-hand sides meet through distributed shared memory, summed in rank
+// order, so every CTA solves the identical system and holds the identical
+// new factor; one cluster barrier per mode step.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
 #include "common.cuh"
 #include "dword.cuh"
 #include "dwsolve.cuh"
 #include "intertwine.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace mlcp {
 
 namespace {
 
 constexpr int kThreads = 512;
+constexpr int kMaxCl = 4;
 constexpr int kWarps = kThreads / 32;
 
 struct UpdSmem {
@@ -54,10 +67,14 @@ struct UpdSmem {
   dw* P;      // [R][TL] products of one tile of block terms
   dw* Qt;     // [TL][npmax] mode-k factors of the tile
   dw* bacc;   // [max(nw, R*npmax)] partial right-hand sides
+  dw* bpart;  // [2][R*npmax] this CTA's partial right-hand side (read by the cluster)
+  dw* gram;   // [D][R][nlr] block overlaps of the CTA's terms (resident form only)
   int* flags; // [4]
 };
 
-__host__ __device__ inline size_t upd_carve(UpdSmem& s, unsigned char* base, int R, int npm, int TL) {
+// Shared memory; D and nlr (block terms per CTA) only matter for the resident form.
+__host__ __device__ inline size_t upd_carve(UpdSmem& s, unsigned char* base, int R, int npm, int TL, int D = 0,
+                                            int nlr = 0, bool resident = false) {
   size_t o = 0;
   auto take = [&](size_t bytes) -> unsigned char* {
     const size_t r = o;
@@ -82,8 +99,22 @@ __host__ __device__ inline size_t upd_carve(UpdSmem& s, unsigned char* base, int
   s.P = (dw*)take(sizeof(dw) * (size_t)R * TL);
   s.Qt = (dw*)take(sizeof(dw) * (size_t)TL * npm);
   s.bacc = (dw*)take(sizeof(dw) * (Rn > (size_t)kThreads ? Rn : (size_t)kThreads));
+  s.bpart = (dw*)take(sizeof(dw) * 2 * Rn);
+  s.gram = resident ? (dw*)take(sizeof(dw) * (size_t)D * R * nlr) : nullptr;
   s.flags = (int*)take(sizeof(int) * 4);
   return o;
+}
+
+__device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+// Block terms per CTA when cl CTAs share a vector's B R terms.
+__host__ __device__ inline int upd_per(int BR, int cl) { return (BR + cl - 1) / cl; }
+
+// Global scratch (dw) of one CTA: overlaps (non-resident form), F Grams, target weights.
+__host__ __device__ inline size_t upd_cta_dw(int BR, int R, int D, int cl) {
+  const size_t per = (size_t)upd_per(BR, cl);
+  return (size_t)D * R * per + (size_t)D * R * R + per;
 }
 
 // Block factors to the double-word mode-major copy: mode d of block term lr
@@ -114,23 +145,29 @@ __device__ dw block_sum(dw v, dw* red) {
 }
 
 __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
-  const int i = blockIdx.x;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CL = p.cl, rank = CL > 1 ? (int)cluster.block_rank() : 0;
+  const int i = blockIdx.x / CL;
   const int R = p.R, B = p.B, D = p.D, nD = p.nD, npm = p.npmax, RR = R * R, BR = B * R, TL = p.tile;
+  const int per = upd_per(BR, CL), lr0 = min(BR, rank * per), nlr = min(BR, lr0 + per) - lr0;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   UpdSmem s;
-  upd_carve(s, smem_raw, R, npm, TL);
-  const size_t cta_stride = (size_t)D * R * BR + (size_t)D * RR + (size_t)BR;
-  dw* gram = p.work + (size_t)i * cta_stride;   // [D][R][BR]: <Q_lr^d, F_i'^d>, lr fastest
-  dw* fg = gram + (size_t)D * R * BR;           // [D][R][R] F Grams
-  dw* w = fg + (size_t)D * RR;                  // [BR] target weights U(l,i) c_lr
+  upd_carve(s, smem_raw, R, npm, TL, D, per, p.resident != 0);
+  dw* scr = p.work + (size_t)(i * CL + rank) * upd_cta_dw(BR, R, D, CL);
+  dw* gram = p.resident ? s.gram : scr;          // [D][R][nlr]: <Q_lr^d, F_i'^d>, own terms lr0.., lr fastest
+  dw* fg = scr + (size_t)D * R * per;            // [D][R][R] F Grams (the same in every CTA of the cluster)
+  dw* w = fg + (size_t)D * RR;                   // [nlr] target weights U(l,i) c_lr of the own terms
   double* fb = p.qn + (size_t)i * R * nD;
   double* fc = p.qnc + (size_t)i * R;
   const double* qi = p.q + (size_t)i * R * nD;
 
   // ---- set-up: F = Q_i, target weights, penalty, Grams ----
-  for (int e = threadIdx.x; e < R * nD; e += kThreads) fb[e] = qi[e];
-  for (int lr = threadIdx.x; lr < BR; lr += kThreads)
-    w[lr] = dw_from_double(p.U[lr / R + (size_t)i * B] * p.qc[lr]);
+  if (rank == 0)
+    for (int e = threadIdx.x; e < R * nD; e += kThreads) fb[e] = qi[e];
+  for (int c = threadIdx.x; c < nlr; c += kThreads) {
+    const int lr = lr0 + c;
+    w[c] = dw_from_double(p.U[lr / R + (size_t)i * B] * p.qc[lr]);
+  }
   if (threadIdx.x == 0) {
     double pen = p.qc[(size_t)i * R];
     for (int r = 1; r < R; ++r) pen = p.qc[(size_t)i * R + r] > pen ? p.qc[(size_t)i * R + r] : pen;
@@ -141,11 +178,11 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
     const int nd = p.nbas[d], od = p.off[d];
     const dw* qd = p.qdw + (size_t)od * BR;
     const dw* fd = p.qdw + (size_t)od * BR + (size_t)i * R * nd;  // F = Q_i: its own terms in the copy
-    for (int e = threadIdx.x; e < R * BR; e += kThreads) {
-      const int ip = e / BR, lr = e - ip * BR;
+    for (int e = threadIdx.x; e < R * nlr; e += kThreads) {
+      const int ip = e / nlr, c = e - ip * nlr;
       dw_acc acc = acc_zero();
-      for (int m = 0; m < nd; ++m) acc_fma(acc, qd[(size_t)lr * nd + m], fd[(size_t)ip * nd + m]);
-      gram[(size_t)d * R * BR + e] = acc_value(acc);
+      for (int m = 0; m < nd; ++m) acc_fma(acc, qd[(size_t)(lr0 + c) * nd + m], fd[(size_t)ip * nd + m]);
+      gram[(size_t)d * R * nlr + e] = acc_value(acc);
     }
     for (int e = threadIdx.x; e < RR; e += kThreads) {
       const int a = e % R, c = e / R;
@@ -158,10 +195,12 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
   const dw pen = s.misc[0];
   const int rv = p.rank_v ? p.rank_v[i] : R;  // ragged: this vector's rank
 
+  int step = 0;
   for (int sw = 0; sw < p.nals; ++sw) {
-    for (int k = 0; k < D; ++k) {
+    for (int k = 0; k < D; ++k, ++step) {
       const int nk = p.nbas[k], ok = p.off[k];
       const dw* qk = p.qdw + (size_t)ok * BR;
+      dw* bp = s.bpart + (size_t)(step & 1) * R * npm;
       // -- normal equations --
       for (int e = threadIdx.x; e < RR; e += kThreads) {
         dw bb = dw_make(1.f);
@@ -189,29 +228,29 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
           }
         }
       } else {
-        // -- right-hand side, tile by tile over the block terms --
+        // -- this CTA's part of the right-hand side, tile by tile over its block terms --
         const int wt = threadIdx.x - w0, nw = kThreads - w0;
         const int nout = R * nk;
         const int nsl = nout >= nw ? 1 : nw / nout;  // slices of a tile per output
         const int items = nout * nsl;
         for (int it = wt; it < items; it += nw) s.bacc[it] = dw_make(0.f);
-        for (int l0 = 0; l0 < BR; l0 += TL) {
-          const int tl = min(TL, BR - l0);
+        for (int c0 = 0; c0 < nlr; c0 += TL) {
+          const int tl = min(TL, nlr - c0);
           for (int e = wt; e < R * tl; e += nw) {
-            const int ip = e / tl, c = e - ip * tl, lr = l0 + c;
-            dw pr = w[lr];
+            const int ip = e / tl, c = e - ip * tl;
+            dw pr = w[c0 + c];
             for (int d = 0; d < D; ++d)
-              if (d != k) pr = dw_mul(pr, gram[(size_t)d * R * BR + (size_t)ip * BR + lr]);
+              if (d != k) pr = dw_mul(pr, gram[(size_t)d * R * nlr + (size_t)ip * nlr + c0 + c]);
             s.P[ip * TL + c] = pr;
           }
-          for (int e = wt; e < tl * nk; e += nw) s.Qt[e] = qk[(size_t)l0 * nk + e];
+          for (int e = wt; e < tl * nk; e += nw) s.Qt[e] = qk[(size_t)(lr0 + c0) * nk + e];
           asm volatile("bar.sync 2, %0;" ::"r"(nw) : "memory");
           for (int it = wt; it < items; it += nw) {
             const int o = it % nout, sl = it / nout;
             const int ip = o % R, m = o / R;
-            const int c0 = sl * tl / nsl, c1 = (sl + 1) * tl / nsl;
+            const int a0 = sl * tl / nsl, a1 = (sl + 1) * tl / nsl;
             dw_acc acc = acc_zero();
-            for (int c = c0; c < c1; ++c) acc_fma(acc, s.P[ip * TL + c], s.Qt[c * nk + m]);
+            for (int c = a0; c < a1; ++c) acc_fma(acc, s.P[ip * TL + c], s.Qt[c * nk + m]);
             s.bacc[it] = dw_add(s.bacc[it], acc_value(acc));
           }
           asm volatile("bar.sync 2, %0;" ::"r"(nw) : "memory");
@@ -220,8 +259,42 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
           dw b = s.bacc[o];
           for (int sl = 1; sl < nsl; ++sl) b = dw_add(b, s.bacc[sl * nout + o]);
           const int ip = o % R, m = o / R;
-          s.b0[ip + m * R] = ip >= rv ? dw_make(m == 0 ? 1.f : 0.f) : b;
+          bp[ip + m * R] = b;
         }
+      }
+      // -- the cluster's partial right-hand sides, summed in rank order (a
+      // peer's part of step s is rewritten at step s + 2, after every CTA has
+      // passed the barrier of step s + 1 and so finished its gather of s) --
+      if (CL > 1) {
+        cl_arrive();
+        cl_wait();
+      } else {
+        __syncthreads();
+      }
+      for (int e = threadIdx.x; e < R * nk; e += kThreads) {
+        const int ip = e % R, m = e / R;
+        dw b;
+        if (CL > 1) {
+          const uint32_t local = (uint32_t)__cvta_generic_to_shared(bp + e);
+          dw v[kMaxCl];
+#pragma unroll
+          for (int r = 0; r < kMaxCl; ++r) {
+            v[r] = dw_make(0.f);
+            if (r < CL) {
+              uint32_t remote;
+              asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(r));
+              asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v[r].hi), "=f"(v[r].lo) : "r"(remote)
+                           : "memory");
+            }
+          }
+          b = v[0];
+#pragma unroll
+          for (int r = 1; r < kMaxCl; ++r)
+            if (r < CL) b = dw_add(b, v[r]);
+        } else {
+          b = bp[e];
+        }
+        s.b0[e] = ip >= rv ? dw_make(m == 0 ? 1.f : 0.f) : b;
       }
       __syncthreads();
       // -- solve (as in the power sweep) --
@@ -252,11 +325,12 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
         __syncthreads();
       }
       for (int r = rv + threadIdx.x; r < R; r += kThreads) s.cf[r] = dw_make(0.f);  // ragged: weightless padding
-      // -- the new factor: FP64 output, its Gram, the block overlaps of mode k --
-      for (int e = threadIdx.x; e < R * nk; e += kThreads) {
-        const int ip = e / nk, m = e % nk;
-        fb[(size_t)ip * nD + ok + m] = dw_to_double(s.X[ip + m * R]);
-      }
+      // -- the new factor: FP64 output (rank 0), its Gram, the own block overlaps of mode k --
+      if (rank == 0)
+        for (int e = threadIdx.x; e < R * nk; e += kThreads) {
+          const int ip = e / nk, m = e % nk;
+          fb[(size_t)ip * nD + ok + m] = dw_to_double(s.X[ip + m * R]);
+        }
       for (int e = threadIdx.x; e < RR; e += kThreads) {
         const int a = e % R, c = e / R;
         if (a > c) continue;
@@ -266,11 +340,11 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
         fg[(size_t)k * RR + a + c * R] = g;
         fg[(size_t)k * RR + c + a * R] = g;
       }
-      for (int e = threadIdx.x; e < R * BR; e += kThreads) {
-        const int ip = e / BR, lr = e - ip * BR;
+      for (int e = threadIdx.x; e < R * nlr; e += kThreads) {
+        const int ip = e / nlr, c = e - ip * nlr;
         dw_acc acc = acc_zero();
-        for (int m = 0; m < nk; ++m) acc_fma(acc, qk[(size_t)lr * nk + m], s.X[ip + m * R]);
-        gram[(size_t)k * R * BR + e] = acc_value(acc);
+        for (int m = 0; m < nk; ++m) acc_fma(acc, qk[(size_t)(lr0 + c) * nk + m], s.X[ip + m * R]);
+        gram[(size_t)k * R * nlr + e] = acc_value(acc);
       }
       __syncthreads();
     }
@@ -287,45 +361,75 @@ __global__ void __launch_bounds__(kThreads, 1) upd_kernel(UpdParams p) {
     if (threadIdx.x == 0) s.misc[1] = dw_sqrt(dw_abs(tot));
     __syncthreads();
     const dw q = s.misc[1];
-    for (int r = threadIdx.x; r < R; r += kThreads) fc[r] = dw_to_double(dw_div(s.cf[r], q));
-  } else {
+    if (rank == 0)
+      for (int r = threadIdx.x; r < R; r += kThreads) fc[r] = dw_to_double(dw_div(s.cf[r], q));
+  } else if (rank == 0) {
     for (int r = threadIdx.x; r < R; r += kThreads) fc[r] = p.qc[(size_t)i * R + r];
   }
-  if (threadIdx.x == 0 && s.flags[1]) atomicOr(&p.status[i], 1);
+  if (threadIdx.x == 0 && rank == 0 && s.flags[1]) atomicOr(&p.status[i], 1);
+  // no CTA leaves while a peer may still read its shared memory
+  if (CL > 1) {
+    cl_arrive();
+    cl_wait();
+  }
 }
 
 }  // namespace
 
 size_t upd_work_dw(int B, int R, int D) {
-  const size_t BR = (size_t)B * R;
-  return (size_t)B * ((size_t)D * R * BR + (size_t)D * R * R + BR);
+  size_t most = 0;
+  for (int cl = 1; cl <= kMaxCl; ++cl) most = std::max(most, (size_t)B * cl * upd_cta_dw(B * R, R, D, cl));
+  return most;
 }
 
 size_t upd_qdw_dw(int B, int R, int nD) { return (size_t)B * R * nD; }
 
 int upd_launch(UpdParams p, int smem_optin, cudaStream_t st) {
-  int tile = 0;
+  int dev = 0, nsm = 0;
+  MLCP_CUDA_TRY(cudaGetDevice(&dev));
+  MLCP_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  // CTAs per vector: the most (up to 4) that keeps every cluster of the block
+  // on the SMs at once; the block overlaps resident when they fit
+  int cl = kMaxCl;
+  while (cl > 1 && p.B * cl > nsm) --cl;
+  const int BR = p.B * p.R, per = upd_per(BR, cl);
+  int tile = 0, resident = 0;
   size_t smem = 0;
-  for (int tl = 128; tl >= 16; tl /= 2) {
-    UpdSmem s;
-    smem = upd_carve(s, nullptr, p.R, p.npmax, tl);
-    if (smem <= (size_t)smem_optin) {
-      tile = tl;
-      break;
+  for (int res = 1; res >= 0 && !tile; --res)
+    for (int tl = 128; tl >= 16; tl /= 2) {
+      UpdSmem s;
+      smem = upd_carve(s, nullptr, p.R, p.npmax, tl, p.D, per, res != 0);
+      if (smem <= (size_t)smem_optin) {
+        tile = tl;
+        resident = res;
+        break;
+      }
     }
-  }
   if (!tile) {
     set_error("vector updates: rank %d with %d basis functions needs more shared memory than %d bytes", p.R,
               p.npmax, smem_optin);
     return kTooLarge;
   }
   p.tile = tile;
+  p.cl = cl;
+  p.resident = resident;
   const long long n = (long long)p.B * p.R * p.nD;
   upd_prep_kernel<<<(int)std::min<long long>((n + 255) / 256, 4096), 256, 0, st>>>(p);
   MLCP_CUDA_TRY(cudaGetLastError());
   MLCP_CUDA_TRY(cudaFuncSetAttribute(upd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  upd_kernel<<<p.B, kThreads, smem, st>>>(p);
-  MLCP_CUDA_TRY(cudaGetLastError());
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(p.B * cl);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MLCP_CUDA_TRY(cudaLaunchKernelEx(&cfg, upd_kernel, p));
   return kOk;
 }
 

@@ -79,6 +79,12 @@ def lib() -> ctypes.CDLL:
                                          _D, _D, ctypes.c_int, _D]
         L.orc_qhq_diag.argtypes = [_D, _D, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, _I, _D,
                                    _D, ctypes.c_int, _D, ctypes.c_int]
+        L.orc_reduc_als.restype = ctypes.c_int
+        L.orc_reduc_als.argtypes = [_D, _D, ctypes.c_int, _D, _D, ctypes.c_int, _I, ctypes.c_int, ctypes.c_int]
+        L.orc_reduc_als_batched.restype = ctypes.c_int
+        L.orc_reduc_als_batched.argtypes = [ctypes.c_int, ctypes.POINTER(_D), ctypes.POINTER(_D), _I,
+                                            ctypes.POINTER(_D), ctypes.POINTER(_D), _I, _I, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_int]
     return _lib
 
 
@@ -104,6 +110,35 @@ def als(coef: np.ndarray, base: np.ndarray, nbas, rF: int, rG: int, nals: int):
     nb = np.ascontiguousarray(nbas, dtype=np.int32)
     lib().orc_alscpp(_dp(coef), _dp(base), _ip(nb), len(nb), rF, rG, nals)
     return coef[:rF].copy(), base[:rF].copy()
+
+
+def reduc_als(gcoef, gbase, fcoef, fbase, nbas, nitn: int):
+    """The Fortran host's CPU ALS reduction reduc_ALS (src/REDUCTIONML.f90:
+    593-731): F fitted to G by nitn sweeps, penalty 1e-15 max c_G.  Returns
+    the new (coef, base) of F; raises when a weight comes out NaN."""
+    gc = np.ascontiguousarray(gcoef, dtype=np.float64)
+    gb = np.ascontiguousarray(gbase, dtype=np.float64)
+    fc = np.ascontiguousarray(fcoef, dtype=np.float64).copy()
+    fb = np.ascontiguousarray(fbase, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    if lib().orc_reduc_als(_dp(gc), _dp(gb), gc.size, _dp(fc), _dp(fb), fc.size, _ip(nb), len(nb), nitn):
+        raise FloatingPointError("reduc_ALS: NaN weight (the reference restarts from a random vector)")
+    return fc, fb
+
+
+def reduc_als_batched(gcoefs, gbases, fcoefs, fbases, nbas, nitn: int, nthreads: int = 0) -> int:
+    """reduc_ALS on independent vectors, OpenMP over vectors; F in place.
+    Returns the number of vectors that hit a NaN weight."""
+    n = len(gcoefs)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    gcp = (_D * n)(*[_dp(c) for c in gcoefs])
+    gbp = (_D * n)(*[_dp(b) for b in gbases])
+    fcp = (_D * n)(*[_dp(c) for c in fcoefs])
+    fbp = (_D * n)(*[_dp(b) for b in fbases])
+    rg = np.ascontiguousarray([c.size for c in gcoefs], dtype=np.int32)
+    rf = np.ascontiguousarray([c.size for c in fcoefs], dtype=np.int32)
+    return int(lib().orc_reduc_als_batched(n, gcp, gbp, _ip(rg), fcp, fbp, _ip(rf), _ip(nb), len(nb), nitn,
+                                           nthreads))
 
 
 def pad_target(coef: np.ndarray, base: np.ndarray, rF: int, rG: int, seed: int = 0):

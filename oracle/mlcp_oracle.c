@@ -2,9 +2,12 @@
  * CPU oracle for the MLCP GPU power-iteration hot path (TEST INFRASTRUCTURE).
  *
  * Only tests/, the smoke entry and bench.py's CPU-baseline leg call this code,
- * as the checker.  It restates the reference's CUDA algorithm in FP64 C; each
- * function names the reference file:line it follows.  Parity is unpinned
- * (the reference has no golden data for this path); see mlcp_oracle.h.
+ * as the checker.  It restates the reference's CUDA algorithm in FP64 C, and
+ * the Fortran host's CPU ALS reduction (reduc_ALS); each function names the
+ * reference file:line it follows.  The reference has no golden data for this
+ * path; the restatement is pinned against the reference's own FP64 CUDA
+ * library, built from its sources and run on the GPU (ALS to 1e-12, one
+ * power cycle to 1e-8 relative).
  *
  * Built with -ffp-contract=off so that x86 and Arm hosts give identical bits.
  */
@@ -404,6 +407,164 @@ void orc_als_batched(int nvec, double *const *coef, double *const *base, const i
 #endif
   for (int v = 0; v < nvec; ++v) orc_alscpp(coef[v], base[v], nbas, ndof, rF[v], rG[v], nals);
   (void)nthreads;
+}
+
+/* ------------------------------------------------------------------ */
+/* The Fortran host's CPU ALS reduction (src/REDUCTIONML.f90:593-731)   */
+/* ------------------------------------------------------------------ */
+
+/* PRODND (src/MODVECVECML.f90:432-461): prod over modes d != kskip of
+ * <a^d, b^d>, modes in increasing order, each dot summed in basis order.
+ * kskip < 0 includes every mode. */
+static double prodnd(const double *a, const double *b, const int *nbas, int ndof, int kskip) {
+  double prod = 1.0;
+  int gi = 0;
+  for (int d = 0; d < ndof; ++d) {
+    if (d != kskip) {
+      double s = 0.0;
+      for (int j = 0; j < nbas[d]; ++j) s += a[gi + j] * b[gi + j];
+      prod *= s;
+    }
+    gi += nbas[d];
+  }
+  return prod;
+}
+
+/* UpdateBB / UpdatePS (src/MODVECVECML.f90:622-708): multiply (divide = 0)
+ * or divide (divide = 1) the running products by the mode-k dots. */
+static void update_bb(const double *fb, int rF, int nD, int gi, int n, double *BB, int divide) {
+  for (int i = 0; i < rF; ++i)
+    for (int j = i; j < rF; ++j) {
+      double p = 0.0;
+      for (int r = 0; r < n; ++r) p += fb[(size_t)i * nD + gi + r] * fb[(size_t)j * nD + gi + r];
+      if (divide) p = 1.0 / p;
+      BB[i + (size_t)j * rF] *= p;
+    }
+  for (int i = 1; i < rF; ++i)
+    for (int j = 0; j < i; ++j) BB[i + (size_t)j * rF] = BB[j + (size_t)i * rF];
+}
+
+static void update_ps(const double *fb, int rF, const double *gb, int rG, int nD, int gi, int n, double *PS,
+                      int divide) {
+  for (int i = 0; i < rG; ++i)
+    for (int j = 0; j < rF; ++j) {
+      double p = 0.0;
+      for (int r = 0; r < n; ++r) p += gb[(size_t)i * nD + gi + r] * fb[(size_t)j * nD + gi + r];
+      if (divide) p = 1.0 / p;
+      PS[i + (size_t)j * rG] *= p;
+    }
+}
+
+/* CONSTBBTOT / CONSTPSTOT (src/MODVECVECML.f90:465-528), skipping mode kskip. */
+static void const_bb(const double *fb, int rF, const int *nbas, int ndof, int nD, int kskip, double *BB) {
+  for (int i = 0; i < rF; ++i)
+    for (int j = i; j < rF; ++j)
+      BB[i + (size_t)j * rF] = prodnd(fb + (size_t)j * nD, fb + (size_t)i * nD, nbas, ndof, kskip);
+  for (int i = 1; i < rF; ++i)
+    for (int j = 0; j < i; ++j) BB[i + (size_t)j * rF] = BB[j + (size_t)i * rF];
+}
+
+static void const_ps(const double *fb, int rF, const double *gb, int rG, const int *nbas, int ndof, int nD,
+                     int kskip, double *PS) {
+  for (int i = 0; i < rG; ++i)
+    for (int j = 0; j < rF; ++j)
+      PS[i + (size_t)j * rG] = prodnd(fb + (size_t)j * nD, gb + (size_t)i * nD, nbas, ndof, kskip);
+}
+
+/* reduc_ALS: F (rF terms, updated in place) fitted to G (rG terms) by nitn
+ * ALS sweeps over the modes.  Penalty 1e-15 max c_G on the diagonal.  With
+ * more than three modes BB and PS are kept by division and multiplication
+ * of one mode's dots; otherwise rebuilt at every mode step.  LU solve
+ * (dgetrf/dgetrs), then each row of the solution normalised into its
+ * weight.  Returns 0, or 1 when a weight came out NaN (the reference then
+ * restarts from GetRandomCPvec's random vector, whose generator is not
+ * restated; the caller sees the flag instead). */
+int orc_reduc_als(const double *gcoef, const double *gbase, int rG, double *fcoef, double *fbase, int rF,
+                  const int *nbas, int ndof, int nitn) {
+  if (nitn <= 0) return 0;
+  int nD = 0, nmax = 0;
+  for (int d = 0; d < ndof; ++d) {
+    nD += nbas[d];
+    nmax = nbas[d] > nmax ? nbas[d] : nmax;
+  }
+  const int update = ndof > 3;
+  double *BB = (double *)malloc(sizeof(double) * rF * rF);
+  double *BBmem = (double *)malloc(sizeof(double) * rF * rF);
+  double *PS = (double *)malloc(sizeof(double) * (size_t)rG * rF);
+  double *bjk = (double *)malloc(sizeof(double) * (size_t)rF * nmax);
+  int *ipiv = (int *)malloc(sizeof(int) * rF);
+  double gmax = gcoef[0];
+  for (int j = 1; j < rG; ++j) gmax = gcoef[j] > gmax ? gcoef[j] : gmax;
+  const double valpen = gmax * 1.0e-15;
+  int bad = 0;
+  if (update) {
+    const_bb(fbase, rF, nbas, ndof, nD, 0, BBmem);
+    const_ps(fbase, rF, gbase, rG, nbas, ndof, nD, 0, PS);
+  }
+  int kp = -1;
+  for (int itn = 0; itn < nitn && !bad; ++itn) {
+    int gst = 0;
+    for (int k = 0; k < ndof; ++k) {
+      const int n = nbas[k];
+      if (update) {
+        if (kp >= 0) {
+          update_bb(fbase, rF, nD, gst, n, BBmem, 1);
+          update_ps(fbase, rF, gbase, rG, nD, gst, n, PS, 1);
+        }
+        memcpy(BB, BBmem, sizeof(double) * rF * rF);
+      } else {
+        const_bb(fbase, rF, nbas, ndof, nD, k, BB);
+        const_ps(fbase, rF, gbase, rG, nbas, ndof, nD, k, PS);
+      }
+      for (int i = 0; i < rF; ++i) BB[i + (size_t)i * rF] += valpen;
+      /* b_j_k(l', nr), bjk column-major [rF][n] (Beylkin eq. 3.4) */
+      for (int e = 0; e < rF * n; ++e) bjk[e] = 0.0;
+      for (int ir = 0; ir < n; ++ir)
+        for (int j = 0; j < rG; ++j) {
+          const double gtmp = gcoef[j] * gbase[(size_t)j * nD + gst + ir];
+          for (int i = 0; i < rF; ++i) bjk[i + (size_t)ir * rF] += gtmp * PS[j + (size_t)i * rG];
+        }
+      lu_solve(BB, bjk, rF, n, ipiv);
+      for (int i = 0; i < rF; ++i) {
+        double s = 0.0;
+        for (int ir = 0; ir < n; ++ir) s += bjk[i + (size_t)ir * rF] * bjk[i + (size_t)ir * rF];
+        const double rnorm = sqrt(fabs(s));
+        fcoef[i] = rnorm;
+        for (int ir = 0; ir < n; ++ir) fbase[(size_t)i * nD + gst + ir] = bjk[i + (size_t)ir * rF] / rnorm;
+      }
+      for (int i = 0; i < rF; ++i)
+        if (fcoef[i] != fcoef[i]) bad = 1;
+      if (bad) break;
+      if (update && (itn < nitn - 1 || k < ndof - 1)) {
+        update_bb(fbase, rF, nD, gst, n, BBmem, 0);
+        update_ps(fbase, rF, gbase, rG, nD, gst, n, PS, 0);
+      }
+      gst += n;
+      kp = k;
+    }
+  }
+  free(BB);
+  free(BBmem);
+  free(PS);
+  free(bjk);
+  free(ipiv);
+  return bad;
+}
+
+/* reduc_ALS over a batch of independent reductions, OpenMP over vectors (as
+ * the Fortran host runs its per-vector reductions). */
+int orc_reduc_als_batched(int nvec, const double *const *gcoef, const double *const *gbase, const int *rG,
+                          double *const *fcoef, double *const *fbase, const int *rF, const int *nbas, int ndof,
+                          int nitn, int nthreads) {
+  int bad = 0;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : bad)
+#endif
+  for (int v = 0; v < nvec; ++v)
+    bad += orc_reduc_als(gcoef[v], gbase[v], rG[v], fcoef[v], fbase[v], rF[v], nbas, ndof, nitn);
+  (void)nthreads;
+  return bad;
 }
 
 /* ------------------------------------------------------------------ */

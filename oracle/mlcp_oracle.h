@@ -13,12 +13,18 @@
  * (dgetrf/dgetrs with partial pivoting; dsygvd is replaced by a Cholesky
  * reduction followed by cyclic Jacobi, which yields the same eigenpairs).
  *
- * Parity unpinned: the reference ships no tests, golden vectors or
- * fixtures for this path, its Fortran host cannot be compiled without a
- * Fortran compiler, and its CUDA library cannot be built for the Arm GPU
- * host from here.  Known-answer tests derived from mathematics (exactly
+ * It also restates the Fortran host's CPU ALS reduction, reduc_ALS
+ * (src/REDUCTIONML.f90:593-731), the reference's own CPU implementation of
+ * the rank reduction, which the benchmark times as the reference CPU path.
+ *
+ * Pinning: the reference ships no tests, golden vectors or fixtures for
+ * this path, and its Fortran host cannot be compiled without a Fortran
+ * compiler.  Its CUDA library is built from its own sources on the GPU host
+ * (oracle/ref_build.py) and run beside this oracle on the same inputs
+ * (tests/test_gpu_reference.py: ALS residuals to 1e-12, one power cycle to
+ * 1e-8 relative).  Known-answer tests derived from mathematics (exactly
  * representable reductions, analytically solvable Hamiltonians, a Lanczos
- * reference on the full direct-product basis) stand in.
+ * reference on the full direct-product basis) cover the host loops.
  *
  * Layout (reference src/cpvector.cu:407-414): a CP vector of rank R over D
  * modes with basis sizes nbas[d] stores term r, mode d, index i at
@@ -103,6 +109,17 @@ void orc_set_rhs_fp32(int on);
  * column-major A, B used).  Eigenvalues ascending; X column-major with
  * X^T B X = I and the largest-magnitude entry of each column positive. */
 int orc_sygv(int n, const double *A, const double *B, double *w, double *X);
+
+/* reduc_ALS (src/REDUCTIONML.f90:593-731): F (rF terms, in place) fitted to
+ * G (rG terms) by nitn sweeps; penalty 1e-15 max c_G; returns 1 when a
+ * weight came out NaN (the reference restarts from a random vector). */
+int orc_reduc_als(const double *gcoef, const double *gbase, int rG, double *fcoef, double *fbase, int rF,
+                  const int *nbas, int ndof, int nitn);
+/* The same over independent vectors, OpenMP over vectors (nthreads < 1: all);
+ * returns the number of vectors that hit a NaN weight. */
+int orc_reduc_als_batched(int nvec, const double *const *gcoef, const double *const *gbase, const int *rG,
+                          double *const *fcoef, double *const *fbase, const int *rF, const int *nbas, int ndof,
+                          int nitn, int nthreads);
 
 #ifdef __cplusplus
 }
