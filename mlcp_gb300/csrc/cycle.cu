@@ -468,26 +468,23 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
       const int erc = enqueue();
       cudaGraph_t graph = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(st, &graph);
-      if (erc != kOk || ce != cudaSuccess) {
+      cudaGraphExec_t exec = nullptr;
+      cudaError_t ie = cudaErrorUnknown;
+      if (erc == kOk && ce == cudaSuccess) ie = cudaGraphInstantiate(&exec, graph, 0);
+      if (ie != cudaSuccess) {
+        // a launch the runtime cannot record (or instantiate): run this
+        // cycle kernel by kernel instead (a real launch error shows there)
         if (graph) cudaGraphDestroy(graph);
         cudaGetLastError();
-        if (erc != kOk) return erc;
-        set_error("intertwinecpp_: capture of the cycle failed: %s", cudaGetErrorString(ce));
-        return kCudaError;
+        if ((rc = enqueue())) return rc;
+      } else {
+        ctx->cyc_graph = graph;
+        ctx->cyc_exec = exec;
+        std::memcpy(ctx->cyc_key, key, sizeof(key));
       }
-      cudaGraphExec_t exec = nullptr;
-      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-      if (ie != cudaSuccess) {
-        cudaGraphDestroy(graph);
-        cudaGetLastError();
-        set_error("intertwinecpp_: instantiation of the cycle graph failed: %s", cudaGetErrorString(ie));
-        return kCudaError;
-      }
-      ctx->cyc_graph = graph;
-      ctx->cyc_exec = exec;
-      std::memcpy(ctx->cyc_key, key, sizeof(key));
     }
-    MLCP_CUDA_TRY(cudaGraphLaunch(ctx->cyc_exec, st));
+    if (ctx->cyc_exec && std::memcmp(key, ctx->cyc_key, sizeof(key)) == 0)
+      MLCP_CUDA_TRY(cudaGraphLaunch(ctx->cyc_exec, st));
   } else {
     if ((rc = enqueue())) return rc;
   }

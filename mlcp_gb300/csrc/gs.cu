@@ -163,6 +163,7 @@ __device__ dw block_sum_ready(dw v, dw* red) {
 struct Gs {
   GsArrays a;
   int R, RR, RRp, D, nD, npm, CL, rank, tid;
+  int G, cid, gr, NC;  // clusters, this CTA's cluster, its index over all CTAs, all CTAs
   int rv;  // rank of the vector being fitted (ragged blocks; R otherwise)
 };
 
@@ -231,18 +232,18 @@ __device__ void normalize_weights(const Gs& c) {
   __syncthreads();
 }
 
-// The finished vector: FP64 output (rank 0), and the owner's resident copy
-// when later vectors use it.
+// The finished vector: FP64 output (CTA 0 of the grid), and the owner's
+// resident copy when later vectors use it.
 __device__ void finish_vector(const Gs& c, const GsParams& p, int iv, bool factors) {
   const int R = c.R, nD = c.nD;
-  if (c.rank == 0) {
+  if (c.gr == 0) {
     double* fb = p.base + (size_t)iv * R * nD;
     if (factors)
       for (int e = c.tid; e < R * nD; e += kGsThreads) fb[e] = dw_to_double(c.a.fb[e]);
     for (int i = c.tid; i < R; i += kGsThreads) p.coef[(size_t)iv * R + i] = dw_to_double(c.a.fcs[i]);
   }
-  if (iv < p.nbloc - 1 && iv % c.CL == c.rank) {
-    const int kl = iv / c.CL;
+  if (iv < p.nbloc - 1 && iv % c.NC == c.gr) {
+    const int kl = iv / c.NC;
     dw* qf = c.a.qf + (size_t)kl * R * nD;
     dw* qw = c.a.qw + (size_t)kl * R * nD;
     for (int e = c.tid; e < R * nD; e += kGsThreads) {
@@ -349,9 +350,11 @@ __device__ void step_rhs_part(const Gs& c, int j, int nk, dw* bp, int w0) {
 
 // Step phase 4 (after the cluster barrier): the self term plus the partial
 // right-hand sides of the cluster, summed as a fixed tree over ranks so that
-// every CTA forms the identical system.
+// every CTA forms the identical system.  With several clusters (xout set)
+// the cluster's sum alone goes to xout (by rank 0) and the grid-wide step
+// below completes b0.
 // (ranks >= nown own no earlier vector yet; their parts are exact zeros)
-__device__ void step_gather(const Gs& c, int j, dw* bp, int nown) {
+__device__ void step_gather(const Gs& c, int j, dw* bp, int nown, dw* xout = nullptr) {
   const int Rn = c.R * c.a.nb[j];
   for (int e = c.tid; e < Rn; e += kGsThreads) {
     const uint32_t local = (uint32_t)__cvta_generic_to_shared(bp + e);
@@ -366,10 +369,55 @@ __device__ void step_gather(const Gs& c, int j, dw* bp, int nown) {
       }
     }
     dw_acc acc = acc_zero();
+    if (xout) {
+#pragma unroll
+      for (int r = 0; r < 16; ++r) acc_add(acc, v[r]);
+      if (c.rank == 0) xout[e] = acc_value(acc);
+      continue;
+    }
     acc_add(acc, c.a.part[e]);
     acc_add(acc, c.a.part[(size_t)Rn + e]);
 #pragma unroll
     for (int r = 0; r < 16; ++r) acc_add(acc, v[r]);
+    c.a.b0[e] = (e % c.R >= c.rv) ? dw_make(e / c.R == 0 ? 1.f : 0.f) : acc_value(acc);  // ragged padding
+  }
+  __syncthreads();
+}
+
+// Iterations of the bounded wait for the other clusters' partial sums.
+constexpr int kGridWaitLimit = 1 << 22;
+
+// Grid-wide step (several clusters): once every cluster leader has posted
+// its cluster sum for this step (counter >= G (step + 1)), every CTA forms
+// b0 = self term + the cluster sums in cluster order -- the identical system
+// everywhere.  The wait is bounded: on expiry status bit 2 is set and the
+// step goes on with whatever has arrived (the result is then flagged invalid).
+__device__ void step_grid_sum(const Gs& c, const GsParams& p, int j, int step, const dw* xs) {
+  const int Rn = c.R * c.a.nb[j];
+  if (c.tid == 0) {
+    if (c.rank == 0) {
+      __threadfence();
+      atomicAdd(p.xctr, 1u);
+    }
+    const unsigned target = (unsigned)c.G * (unsigned)(step + 1);
+    int it = 0;
+    while (*(volatile unsigned*)p.xctr < target && it < kGridWaitLimit) {
+      __nanosleep(32);
+      ++it;
+    }
+    if (it >= kGridWaitLimit) atomicOr(p.status, 2);
+    __threadfence();
+  }
+  __syncthreads();
+  const size_t stride = (size_t)c.R * c.npm;
+  for (int e = c.tid; e < Rn; e += kGsThreads) {
+    dw_acc acc = acc_zero();
+    acc_add(acc, c.a.part[e]);
+    acc_add(acc, c.a.part[(size_t)Rn + e]);
+    for (int g = 0; g < c.G; ++g) {
+      const dw* x = xs + (size_t)g * stride + e;
+      acc_add(acc, dw_make(__ldcg(&x->hi), __ldcg(&x->lo)));
+    }
     c.a.b0[e] = (e % c.R >= c.rv) ? dw_make(e / c.R == 0 ? 1.f : 0.f) : acc_value(acc);  // ragged padding
   }
   __syncthreads();
@@ -471,6 +519,10 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
   Gs c;
   c.CL = (int)cluster.num_blocks();
   c.rank = (int)cluster.block_rank();
+  c.G = p.ngrp;
+  c.cid = blockIdx.x / c.CL;
+  c.gr = c.cid * c.CL + c.rank;
+  c.NC = c.G * c.CL;
   c.R = p.R;
   c.RR = p.R * p.R;
   c.RRp = gs_rrp(p.R);
@@ -480,7 +532,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
   c.tid = threadIdx.x;
   c.rv = p.R;
   const GsDims dims{p.R, p.D, p.nD, p.npmax, p.nkmax, kResident ? 0 : p.gmask};
-  gs_carve(dims, &c.a, smem_raw, reinterpret_cast<dw*>(p.work) + (size_t)c.rank * p.work_stride, nullptr);
+  gs_carve(dims, &c.a, smem_raw, reinterpret_cast<dw*>(p.work) + (size_t)c.gr * p.work_stride, nullptr);
   for (int d = c.tid; d <= c.D; d += kGsThreads) {
     c.a.nb[d] = d < c.D ? p.nbas[d] : 0;
     c.a.off[d] = p.off[d];
@@ -498,7 +550,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
     c.rv = p.rank_v ? p.rank_v[iv] : c.R;
     load_vector(c, p, iv);
     all_grams(c);
-    const int nk = (iv - c.rank + c.CL - 1) / c.CL;  // owned k = rank, rank + CL, ... < iv
+    const int nk = (iv - c.gr + c.NC - 1) / c.NC;  // owned k = gr, gr + NC, ... < iv
     all_overlaps(c, nk);
     bool pre = false;
     dw qinv = dw_make(1.f);  // 1 / |F| not yet applied to the weights (see step_update)
@@ -532,7 +584,17 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
         // CTA has passed the barrier of step s + 1 (and so its gather of s)
         cl_arrive();
         cl_wait();
-        step_gather(c, j, bp, iv < c.CL ? iv : c.CL);
+        {
+          // ranks of this cluster that own an earlier vector (the others' parts are zero)
+          const int nown = min(c.CL, max(0, iv - c.cid * c.CL));
+          if (c.G == 1) {
+            step_gather(c, j, bp, nown);
+          } else {
+            dw* xs = p.xpart + (size_t)(step & 1) * c.G * c.R * c.npm;
+            step_gather(c, j, bp, nown, xs + (size_t)c.cid * c.R * c.npm);
+            step_grid_sum(c, p, j, step, xs);
+          }
+        }
         if (c.R <= 32) gj_ok = c.a.flags[2] != 0;
         // the solve: refinement in registers (warps 0..nsw-1, one or two
         // right-hand-side columns each), or the solver warps' refinement /
@@ -576,7 +638,7 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
     __syncthreads();
     finish_vector(c, p, iv, true);
   }
-  if (c.rank == 0 && c.tid == 0 && c.a.flags[1]) atomicOr(p.status, 1);
+  if (c.gr == 0 && c.tid == 0 && c.a.flags[1]) atomicOr(p.status, 1);
   // no CTA leaves while a peer may still read its shared memory
   cl_arrive();
   cl_wait();
@@ -586,63 +648,109 @@ int gs_cluster_size(int nbloc) { return nbloc > 16 ? 16 : (nbloc > 1 ? nbloc - 1
 
 namespace {
 
-int gs_nkmax(int nbloc) {
-  const int cl = gs_cluster_size(nbloc);
-  return std::max(1, (nbloc - 1 + cl - 1) / cl);
+// Most clusters a grid may hold (the GB300's 152 SMs at one 16-CTA cluster
+// per 16 SMs); the scratch is sized for it.
+constexpr int kMaxGroups = 9;
+
+int gs_nkmax(int nbloc, int ngrp) {
+  const int nc = gs_cluster_size(nbloc) * ngrp;
+  return std::max(1, (nbloc - 1 + nc - 1) / nc);
 }
 
 // Global scratch entries (dw) of one CTA with every movable group there.
-size_t gs_cta_work(int nbloc, int R, int nD, int D, int npm) {
+size_t gs_cta_work(int nbloc, int R, int nD, int D, int npm, int ngrp) {
   GsArrays a;
   size_t gw = 0;
-  gs_carve(GsDims{R, D, nD, npm, gs_nkmax(nbloc), kGroupAll}, &a, nullptr, nullptr, &gw);
+  gs_carve(GsDims{R, D, nD, npm, gs_nkmax(nbloc, ngrp), kGroupAll}, &a, nullptr, nullptr, &gw);
   return gw;
+}
+
+// Shared-memory layout: keep as much resident as fits (the owned vectors
+// move out first, then their overlaps, then the working vector).
+bool gs_fit(const GsParams& p, int ngrp, int smem_max, int* gmask, size_t* smem) {
+  static const int masks[4] = {0, kGroupQ, kGroupQ | kGroupP, kGroupAll};
+  for (int q = 0; q < 4; ++q) {
+    GsArrays a;
+    const size_t b = gs_carve(GsDims{p.R, p.D, p.nD, p.npmax, gs_nkmax(p.nbloc, ngrp), masks[q]}, &a, nullptr,
+                              nullptr, nullptr);
+    if (b <= (size_t)smem_max) {
+      *gmask = masks[q];
+      *smem = b;
+      return true;
+    }
+  }
+  return false;
 }
 
 }  // namespace
 
 size_t gs_work_doubles(int nbloc, int R, int nD, int D, int npm) {
-  return (size_t)gs_cluster_size(nbloc) * gs_cta_work(nbloc, R, nD, D, npm);
+  // the per-CTA scratch of the largest grid (one cluster owns the most per
+  // CTA, so size the scratch for every CTA of kMaxGroups clusters at the
+  // one-cluster share), then the cluster partials and the arrival counter
+  const size_t per = gs_cta_work(nbloc, R, nD, D, npm, 1);
+  return (size_t)gs_cluster_size(nbloc) * kMaxGroups * per + (size_t)2 * kMaxGroups * R * npm + 2;
+}
+
+// Clusters for a block: one when everything fits in shared memory (small
+// blocks are bound by the latency of each mode step, and a grid-wide step
+// would only add to it); otherwise as many as the SMs hold at one CTA each,
+// up to one owned vector per CTA, so that the owned arrays' work spreads
+// over more SMs.
+int gs_groups(const GsParams& p, int num_sms, int smem_max) {
+  int gmask = 0;
+  size_t smem = 0;
+  if (gs_fit(p, 1, smem_max, &gmask, &smem) && gmask == 0) return 1;
+  const int cl = gs_cluster_size(p.nbloc);
+  int g = std::min(kMaxGroups, num_sms / cl);
+  g = std::min(g, (p.nbloc - 1 + cl - 1) / cl);
+  return std::max(1, g);
 }
 
 int gs_launch(const GsParams& prm, cudaStream_t st) {
   GsParams p = prm;
   const int cl = gs_cluster_size(p.nbloc);
-  p.nkmax = gs_nkmax(p.nbloc);
-  p.work_stride = (long long)gs_cta_work(p.nbloc, p.R, p.nD, p.D, p.npmax);
-  int dev = 0, smem_max = 0;
+  int dev = 0, smem_max = 0, nsm = 0;
   MLCP_CUDA_TRY(cudaGetDevice(&dev));
   MLCP_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  // keep as much resident as fits: the owned vectors move out first, then
-  // their overlaps, then the working vector
-  static const int masks[4] = {0, kGroupQ, kGroupQ | kGroupP, kGroupAll};
+  MLCP_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const char* env = getenv("MLCP_GB300_GS_GROUPS");  // a fixed cluster count (tests)
+  int ngrp = env ? std::max(1, std::min(kMaxGroups, atoi(env))) : gs_groups(p, nsm, smem_max);
+  if (ngrp * cl > nsm) ngrp = std::max(1, nsm / cl);
+  p.ngrp = ngrp;
+  p.nkmax = gs_nkmax(p.nbloc, ngrp);
+  p.work_stride = (long long)gs_cta_work(p.nbloc, p.R, p.nD, p.D, p.npmax, ngrp);
   size_t smem = 0;
-  int q = 0;
-  for (; q < 4; ++q) {
-    GsArrays a;
-    smem = gs_carve(GsDims{p.R, p.D, p.nD, p.npmax, p.nkmax, masks[q]}, &a, nullptr, nullptr, nullptr);
-    if (smem <= (size_t)smem_max) break;
-  }
-  if (q == 4) {
-    set_error("intertwinecpp_: Gram-Schmidt needs %zu bytes of shared memory (rank %d)", smem, p.R);
+  int gmask = 0;
+  if (!gs_fit(p, ngrp, smem_max, &gmask, &smem)) {
+    set_error("intertwinecpp_: Gram-Schmidt needs more shared memory than %d bytes (rank %d)", smem_max, p.R);
     return kTooLarge;
   }
-  p.gmask = masks[q];
+  p.gmask = gmask;
+  // the cluster partials and the arrival counter follow the per-CTA scratch
+  dw* after = reinterpret_cast<dw*>(p.work) + (size_t)cl * ngrp * p.work_stride;
+  p.xpart = after;
+  p.xctr = reinterpret_cast<unsigned*>(after + (size_t)2 * kMaxGroups * p.R * p.npmax);
+  if (ngrp > 1) MLCP_CUDA_TRY(cudaMemsetAsync(p.xctr, 0, sizeof(unsigned), st));
   void (*kern)(GsParams) = p.gmask == 0 ? gs_kernel<true> : gs_kernel<false>;
   MLCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (cl > 8) MLCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(cl);
+  cfg.gridDim = dim3(cl * ngrp);
   cfg.blockDim = dim3(kGsThreads);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = cl;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
+  // several clusters wait on one another each step: all of them must be
+  // resident together, which a cooperative launch guarantees (or refuses)
+  attr[1].id = cudaLaunchAttributeCooperative;
+  attr[1].val.cooperative = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = ngrp > 1 ? 2 : 1;
   MLCP_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, p));
   return kOk;
 }

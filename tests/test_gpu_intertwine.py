@@ -324,3 +324,33 @@ def test_cycle_graph_replay_matches_eager_launches(case, cuda_device):
     for (a, b) in zip(outs[0], outs[1]):
         for x, y in zip(a, b):
             np.testing.assert_array_equal(x, y)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [5, 6])
+@pytest.mark.parametrize("groups", [2, 3])
+def test_gram_schmidt_over_several_clusters(case, groups, cuda_device, monkeypatch):
+    """The Gram-Schmidt spread over several 16-CTA clusters (a cooperative
+    launch whose cluster leaders exchange their partial right-hand sides
+    through global memory each mode step; the library picks it for blocks
+    whose arrays do not fit in shared memory) against one cluster and the
+    oracle: the same cycle to the oracle tolerances, and to 1e-9 of the
+    one-cluster result (only the order of the partial sums differs)."""
+    from mlcp_gb300 import _lib
+    L = _lib.load()
+    L.mlcp_gb300_set_cycle_graph(0)  # the cluster count is read at launch time
+    try:
+        make, rk, nbloc, npow, nals, update, ishift, esh = CASES[case]
+        hl = make()
+        Q, qc = start_block(hl.nbas, rk, nbloc, seed=case)
+        eig0 = np.arange(nbloc, dtype=float)
+        res = {}
+        for g in (1, groups):
+            monkeypatch.setenv("MLCP_GB300_GS_GROUPS", str(g))
+            res[g] = IT.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, eig0, npow, nals, update, ishift, esh)
+        ob, oc, oe = oracle.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, eig0, npow, nals, update, ishift, esh)
+        gb, gc, ge = res[groups]
+        compare_blocks(gb, gc, ob, oc, hl.nbas, rk, nbloc)
+        compare_blocks(gb, gc, res[1][0], res[1][1], hl.nbas, rk, nbloc, tol=1e-9)
+    finally:
+        L.mlcp_gb300_set_cycle_graph(1)
