@@ -384,14 +384,18 @@ __device__ void step_gather(const Gs& c, int j, dw* bp, int nown, dw* xout = nul
   __syncthreads();
 }
 
-// Iterations of the bounded wait for the other clusters' partial sums.
-constexpr int kGridWaitLimit = 1 << 22;
+// Iterations of the bounded wait for the other clusters' partial sums (each
+// a global load and a short sleep: about a tenth of a second in all, far
+// above the imbalance of one mode step).
+constexpr int kGridWaitLimit = 1 << 17;
 
 // Grid-wide step (several clusters): once every cluster leader has posted
-// its cluster sum for this step (counter >= G (step + 1)), every CTA forms
+// its cluster sum for this step (xctr[0] >= G (step + 1)), every CTA forms
 // b0 = self term + the cluster sums in cluster order -- the identical system
-// everywhere.  The wait is bounded: on expiry status bit 2 is set and the
-// step goes on with whatever has arrived (the result is then flagged invalid).
+// everywhere.  The wait is bounded: the first CTA whose wait runs out sets
+// status bit 2 and the abort word xctr[1], after which no CTA waits again;
+// the kernel then runs to its end on whatever has arrived, and the result
+// is flagged invalid.
 __device__ void step_grid_sum(const Gs& c, const GsParams& p, int j, int step, const dw* xs) {
   const int Rn = c.R * c.a.nb[j];
   if (c.tid == 0) {
@@ -400,12 +404,15 @@ __device__ void step_grid_sum(const Gs& c, const GsParams& p, int j, int step, c
       atomicAdd(p.xctr, 1u);
     }
     const unsigned target = (unsigned)c.G * (unsigned)(step + 1);
-    int it = 0;
-    while (*(volatile unsigned*)p.xctr < target && it < kGridWaitLimit) {
-      __nanosleep(32);
-      ++it;
+    volatile unsigned* ctr = p.xctr;
+    for (int it = 0; ctr[0] < target && ctr[1] == 0u; ++it) {
+      if (it >= kGridWaitLimit) {
+        atomicExch(p.xctr + 1, 1u);
+        atomicOr(p.status, 2);
+        break;
+      }
+      __nanosleep(64);
     }
-    if (it >= kGridWaitLimit) atomicOr(p.status, 2);
     __threadfence();
   }
   __syncthreads();
@@ -731,7 +738,7 @@ int gs_launch(const GsParams& prm, cudaStream_t st) {
   dw* after = reinterpret_cast<dw*>(p.work) + (size_t)cl * ngrp * p.work_stride;
   p.xpart = after;
   p.xctr = reinterpret_cast<unsigned*>(after + (size_t)2 * kMaxGroups * p.R * p.npmax);
-  if (ngrp > 1) MLCP_CUDA_TRY(cudaMemsetAsync(p.xctr, 0, sizeof(unsigned), st));
+  if (ngrp > 1) MLCP_CUDA_TRY(cudaMemsetAsync(p.xctr, 0, 2 * sizeof(unsigned), st));  // arrivals, abort word
   void (*kern)(GsParams) = p.gmask == 0 ? gs_kernel<true> : gs_kernel<false>;
   MLCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (cl > 8) MLCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));

@@ -83,7 +83,7 @@ struct GsParams {
   long long work_stride; // scratch entries of one CTA
   int ngrp;              // clusters sharing the block (1: one cluster, no grid-wide step)
   dw* xpart;             // [2][ngrp][R * npmax] cluster partial right-hand sides (ngrp > 1)
-  unsigned* xctr;        // arrivals of the cluster leaders, zeroed before the launch (ngrp > 1)
+  unsigned* xctr;        // [0] arrivals of the cluster leaders, [1] abort word; zeroed before the launch (ngrp > 1)
 };
 int gs_launch(const GsParams& p, cudaStream_t st);
 // Doubles of GsParams::work needed for a block of nbloc vectors (npm: the
