@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -452,7 +453,10 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
     return kOk;
   };
   if (cycle_graph_enabled()) {
-    const unsigned long long key[16] = {(unsigned long long)(uintptr_t)ctx->cyc, bytes,
+    // a fixed Gram-Schmidt cluster count changes the captured launch
+    const char* gsg = getenv("MLCP_GB300_GS_GROUPS");
+    const unsigned long long gsg_v = gsg ? (unsigned long long)atoi(gsg) + 1 : 0ull;
+    const unsigned long long key[16] = {(unsigned long long)(uintptr_t)ctx->cyc ^ (gsg_v << 56), bytes,
                                         (unsigned long long)(uintptr_t)tab.hdw,
                                         (unsigned long long)(uintptr_t)tab.alpha, (unsigned long long)ndof,
                                         (unsigned long long)R, (unsigned long long)B, (unsigned long long)T,

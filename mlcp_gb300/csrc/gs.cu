@@ -31,6 +31,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "common.cuh"
 #include "dword.cuh"
@@ -651,7 +652,13 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
   cl_wait();
 }
 
-int gs_cluster_size(int nbloc) { return nbloc > 16 ? 16 : (nbloc > 1 ? nbloc - 1 : 1); }
+// CTAs per cluster: 16 (the non-portable maximum) unless the block is
+// smaller; MLCP_GB300_GS_CLUSTER fixes a smaller size (measurements).
+int gs_cluster_size(int nbloc) {
+  int cl = 16;
+  if (const char* e = getenv("MLCP_GB300_GS_CLUSTER")) cl = std::max(2, std::min(16, atoi(e)));
+  return nbloc > cl ? cl : (nbloc > 1 ? nbloc - 1 : 1);
+}
 
 namespace {
 
