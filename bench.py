@@ -23,7 +23,9 @@ run in a child process on the same GPU) on a smaller sample and on one power
 cycle, with the GPU's errors against it.
 
 Further legs after the timed regions (N=1 only): the power cycle and its
-neighbours (power_cycle), the learned ALS warm start inside a power
+neighbours (power_cycle; on the host cores the oracle of the GPU
+algorithm, cpu_ms_per_cycle, and the Fortran host's own CPU solver
+restated, pals_cpu_ms_per_cycle), the learned ALS warm start inside a power
 iteration (warm_start: accept rate, sweeps saved, training time), and the
 24-mode three-layer quartic-force-field tree solved node by node on the GPU
 (tree_qff24).
@@ -426,6 +428,12 @@ def run_cycle_bench(steps: int, cpu: bool):
         t0 = time.perf_counter()
         oracle.intertwine(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
         out["cpu_ms_per_cycle"] = 1e3 * (time.perf_counter() - t0)
+        # the Fortran host's own CPU solver (solver pals, lowmem 4: ALS_POW3,
+        # ALS_ORTHO_2, PRODHV_ALS2, ALS_SUMLCVEC_2) restated, OpenMP as there
+        t0 = time.perf_counter()
+        oracle.pals_cycle(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
+        out["pals_cpu_ms_per_cycle"] = 1e3 * (time.perf_counter() - t0)
+        out["cpu_threads"] = os.cpu_count()
         t0 = time.perf_counter()
         oracle.qhq_diag(gb, gc, hl.nbas, CYC_R, CYC_B, hl)
         out["qhq_diag_cpu_ms"] = 1e3 * (time.perf_counter() - t0)

@@ -14,6 +14,12 @@ tests compare this oracle, the reference library and the GB300 library on
 the same inputs (ALS: 1e-12; one power cycle: 1e-10).  Mathematical known
 answers (dense diagonalisation, FP64 Lanczos fixtures under
 ``tests/golden/``) cover the host loops.
+
+The Fortran host's own CPU routines are restated beside it: reduc_ALS
+(``reduc_als``) and the CPU power solver, solver pals at lowmem 4
+(``pals_pow3``, ``pals_ortho2``, ``pals_prodhv2``, ``pals_sumlcvec2``,
+``pals_diagonalize``, ``pals_cycle``), which agree with the CUDA-algorithm
+restatement stage by stage to rounding (``tests/test_oracle_pals.py``).
 """
 from __future__ import annotations
 
@@ -85,6 +91,17 @@ def lib() -> ctypes.CDLL:
         L.orc_reduc_als_batched.argtypes = [ctypes.c_int, ctypes.POINTER(_D), ctypes.POINTER(_D), _I,
                                             ctypes.POINTER(_D), ctypes.POINTER(_D), _I, _I, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_int]
+        c_i, c_d = ctypes.c_int, ctypes.c_double
+        for name in ("orc_pals_pow3", "orc_pals_ortho2", "orc_pals_prodhv2", "orc_pals_sumlcvec2",
+                     "orc_pals_diagonalize", "orc_pals_cycle"):
+            getattr(L, name).restype = c_i
+        L.orc_pals_pow3.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, _I, _I, _D, _D, c_i, c_i, c_i, c_d, c_i]
+        L.orc_pals_ortho2.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, c_i]
+        L.orc_pals_prodhv2.argtypes = [_D, _D, _D, _D, _I, c_i, c_i, _I, _I, _D, _D, c_i, c_i, c_d, c_i]
+        L.orc_pals_sumlcvec2.argtypes = [_D, _D, _I, c_i, c_i, _I, _D, c_i, c_i]
+        L.orc_pals_diagonalize.argtypes = [_D, _D, _I, c_i, c_i, _I, _I, _I, _D, _D, c_i, c_i, _D, _D, c_i]
+        L.orc_pals_cycle.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, _I, _I, _D, _D, c_i, c_i, c_i, c_i, c_i, c_d,
+                                     _D, c_i]
     return _lib
 
 
@@ -561,6 +578,91 @@ def sygv(A: np.ndarray, B: np.ndarray):
     X = np.zeros(n * n)
     info = lib().orc_sygv(n, _dp(Acm), _dp(Bcm), _dp(w), _dp(X))
     return w, X.reshape(n, n).T.copy(), info
+
+
+# --- the Fortran host's CPU solver (solver pals, src/Solver.f90:508-538, lowmem 4) ---
+# A block is the terms of vector 0, then vector 1, ...; ``ranks`` gives each
+# vector's number of terms (default: rk for all).  Every routine works on
+# copies and raises on a NaN weight, where the reference aborts.
+
+def _block(base, coef, nbloc, rk, ranks):
+    base = np.ascontiguousarray(base, dtype=np.float64).copy()
+    coef = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    rv = np.full(nbloc, rk, dtype=np.int32) if ranks is None else np.ascontiguousarray(ranks, dtype=np.int32)
+    if rv.size != nbloc or int(rv.sum()) != coef.size:
+        raise ValueError(f"ranks {rv.tolist()} do not cover {coef.size} terms")
+    return base, coef, rv
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise FloatingPointError(f"{what}: {'eigensolve failed' if rc < 0 else 'NaN weight'}")
+
+
+def pals_pow3(base, coef, nbas, rk, nbloc, hl, npow, ishift=1, Eshift=0.0, nconv=0, ranks=None, nthreads=0):
+    """ALS_POW3 (src/ALSPow.f90:569-660) on vectors nconv..nbloc-1."""
+    base, coef, rv = _block(base, coef, nbloc, rk, ranks)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    _check(lib().orc_pals_pow3(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), nconv, _ip(hl.opid),
+                               _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, npow, ishift, float(Eshift),
+                               nthreads), "ALS_POW3")
+    return base, coef
+
+
+def pals_ortho2(base, coef, nbas, rk, nbloc, nitn, ranks=None, nthreads=0):
+    """ALS_ORTHO_2 (src/ALSUtils.f90:156-377)."""
+    base, coef, rv = _block(base, coef, nbloc, rk, ranks)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    _check(lib().orc_pals_ortho2(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), nitn, nthreads),
+           "ALS_ORTHO_2")
+    return base, coef
+
+
+def pals_prodhv2(base, coef, nbas, hl, nitn, ishift=0, Eshift=0.0):
+    """PRODHV_ALS2 (src/ALSPow.f90:664-780): ALS fit of (H - Eshift) F, F's rank."""
+    fb = np.ascontiguousarray(base, dtype=np.float64)
+    fc = np.ascontiguousarray(coef, dtype=np.float64)
+    ob, oc = np.zeros_like(fb), np.zeros_like(fc)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    _check(lib().orc_pals_prodhv2(_dp(fb), _dp(fc), _dp(ob), _dp(oc), _ip(nb), len(nb), fc.size, _ip(hl.opid),
+                                  _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, ishift, float(Eshift), nitn),
+           "PRODHV_ALS2")
+    return ob, oc
+
+
+def pals_sumlcvec2(base, coef, nbas, rk, nbloc, U, nitn, ranks=None, nthreads=0):
+    """UpdateVecs2 with ALS_SUMLCVEC_2: vector i <- fit of sum_l U[l, i] Q_l."""
+    base, coef, rv = _block(base, coef, nbloc, rk, ranks)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    Ucm = np.ascontiguousarray(np.asarray(U, dtype=np.float64).T)
+    _check(lib().orc_pals_sumlcvec2(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), _dp(Ucm), nitn,
+                                    nthreads), "ALS_SUMLCVEC_2")
+    return base, coef
+
+
+def pals_diagonalize(base, coef, nbas, rk, nbloc, hl, nitn, ranks=None, nthreads=0):
+    """Diagonalize with intertwining (src/BlockUtils.f90:184-225); returns
+    (base, coef, eigenvalues, U with U[:, i] = eigenvector i)."""
+    base, coef, rv = _block(base, coef, nbloc, rk, ranks)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    eig = np.zeros(nbloc)
+    U = np.zeros(nbloc * nbloc)
+    _check(lib().orc_pals_diagonalize(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), _ip(hl.opid),
+                                      _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, nitn, _dp(eig), _dp(U),
+                                      nthreads), "Diagonalize")
+    return base, coef, eig, U.reshape(nbloc, nbloc).T.copy()
+
+
+def pals_cycle(base, coef, nbas, rk, nbloc, hl, eigv, npow, nals, update=True, ishift=1, Eshift=0.0, nconv=0,
+               ranks=None, nthreads=0):
+    """One cycle of the Fortran host's CPU solver; returns (base, coef, eigv)."""
+    base, coef, rv = _block(base, coef, nbloc, rk, ranks)
+    eig = np.ascontiguousarray(eigv, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    _check(lib().orc_pals_cycle(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), nconv, _ip(hl.opid),
+                                _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, npow, nals, int(bool(update)),
+                                ishift, float(Eshift), _dp(eig), nthreads), "pals cycle")
+    return base, coef, eig
 
 
 # --- the reference's own FP64 CUDA library (oracle/ref_build.py, oracle/ref_run.py) ---

@@ -2,12 +2,15 @@
  * CPU oracle for the MLCP GPU power-iteration hot path (TEST INFRASTRUCTURE).
  *
  * Only tests/, the smoke entry and bench.py's CPU-baseline leg call this code,
- * as the checker.  It restates the reference's CUDA algorithm in FP64 C, and
- * the Fortran host's CPU ALS reduction (reduc_ALS); each function names the
- * reference file:line it follows.  The reference has no golden data for this
- * path; the restatement is pinned against the reference's own FP64 CUDA
- * library, built from its sources and run on the GPU (ALS to 1e-12, one
- * power cycle to 1e-8 relative).
+ * as the checker.  It restates the reference's CUDA algorithm in FP64 C, the
+ * Fortran host's CPU ALS reduction (reduc_ALS) and the Fortran host's CPU
+ * power solver (solver pals: ALS_POW3, ALS_ORTHO_2, PRODHV_ALS2,
+ * ALS_SUMLCVEC_2); each function names the reference file:line it follows.
+ * The reference has no golden data for this path; the restatement of the
+ * CUDA algorithm is pinned against the reference's own FP64 CUDA library,
+ * built from its sources and run on the GPU (ALS to 1e-12, one power cycle
+ * to 1e-8 relative), and the Fortran twins agree with it stage by stage to
+ * rounding where the two algorithms coincide.
  *
  * Built with -ffp-contract=off so that x86 and Arm hosts give identical bits.
  */
@@ -1011,4 +1014,629 @@ double orc_cp_dot(const double *vb, const double *vc, int rv, const double *wb, 
   free(col);
   free(off);
   return total;
+}
+
+/* ------------------------------------------------------------------ */
+/* The Fortran host's CPU power cycle (solver pals, src/Solver.f90:508-538) */
+/* ------------------------------------------------------------------ */
+/*
+ * Iterate's CPU branch for the ALS power solver (styp = -1) runs, per cycle:
+ * ALS_POW_alg on vectors nconv.. (OpenMP over vectors), ALS_ORTHO_alg, and
+ * with update = T Diagonalize(intw = T): GetQHQ3 (PRODHV_ALS_alg, then
+ * PRODVV), GetOverlaps, SolveGenEigval (DSYGV 'U'), UpdateVecs2
+ * (ALS_SUMLCVEC_alg).  The routines restated here are the ones that run at
+ * lowmem = 4, the value of the reference's sample input: ALS_POW3,
+ * ALS_ORTHO_2, PRODHV_ALS2 and ALS_SUMLCVEC_2 (the dispatchers fall back to
+ * the _2 forms for lowmem 4, src/ALSUtils.f90:112-121, :141-150,
+ * src/ALSPow.f90:131-140).  Unlike the reference's GPU path, vectors of a
+ * block may have different ranks (the `ranks` table of ALS_ORTHO_2): the
+ * terms of vector v are terms toff[v] .. toff[v] + ranks[v] - 1 of the block.
+ * Every penalty is 1e-10 times the largest weight of the vector being fitted,
+ * as these routines hard-code it.
+ */
+
+typedef struct {
+  double *BB, *BBmem, *PS, *bjk, *T, *psk;
+  int *ipiv;
+} pals_ws;
+
+static pals_ws pals_ws_alloc(int rF, int rG, int nmax) {
+  pals_ws w;
+  w.BB = (double *)malloc(sizeof(double) * rF * rF);
+  w.BBmem = (double *)malloc(sizeof(double) * rF * rF);
+  w.PS = (double *)malloc(sizeof(double) * (size_t)rG * rF);
+  w.psk = (double *)malloc(sizeof(double) * (size_t)rG * rF);
+  w.bjk = (double *)malloc(sizeof(double) * (size_t)rF * nmax);
+  w.T = (double *)malloc(sizeof(double) * nmax);
+  w.ipiv = (int *)malloc(sizeof(int) * rF);
+  return w;
+}
+
+static void pals_ws_free(pals_ws *w) {
+  free(w->BB); free(w->BBmem); free(w->PS); free(w->psk); free(w->bjk); free(w->T); free(w->ipiv);
+}
+
+static double dot_n(const double *a, const double *b, int n) {
+  double s = 0.0;
+  for (int j = 0; j < n; ++j) s += a[j] * b[j];
+  return s;
+}
+
+static double maxval(const double *c, int n) {
+  double m = c[0];
+  for (int i = 1; i < n; ++i) m = c[i] > m ? c[i] : m;
+  return m;
+}
+
+/* HVBaseProd (src/MODHVECML.f90:170-209): y = fac h_{t,d} x, fac = opcoef(t)
+ * on the first mode and 1 elsewhere, h packed upper-triangular (dspmv 'U');
+ * the identity is stored as an explicit operator in the hoplist. */
+static void hv_base_prod(const hoplist *H, int t, int d, const double *x, double *y, int n) {
+  const double *h = H->mat + H->mptr[H->opid[t * H->ndof + d] - 1] - 1;
+  const double fac = (d == 0) ? H->coef[t] : 1.0;
+  for (int ib = 0; ib < n; ++ib) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const int ir = i < ib ? i : ib, ic = i < ib ? ib : i;
+      s += h[ir + ic * (ic + 1) / 2] * x[i];
+    }
+    y[ib] = fac * s;
+  }
+}
+
+/* PRODVV_AA (src/MODVECVECML.f90:356-392): <F,F> from the upper triangle
+ * doubled plus the diagonal. */
+static double prodvv_aa(const double *coef, const double *base, int r, const int *nbas, int ndof, int nD) {
+  double s = 0.0;
+  for (int i = 0; i < r - 1; ++i)
+    for (int j = i + 1; j < r; ++j)
+      s += coef[i] * coef[j] * prodnd(base + (size_t)i * nD, base + (size_t)j * nD, nbas, ndof, -1);
+  s = 2 * s;
+  for (int i = 0; i < r; ++i)
+    s += coef[i] * coef[i] * prodnd(base + (size_t)i * nD, base + (size_t)i * nD, nbas, ndof, -1);
+  return s;
+}
+
+/* PRODVV_AB (src/MODVECVECML.f90:394-430): <F,G>. */
+static double prodvv_ab(const double *fc, const double *fb, int rF, const double *gc, const double *gb, int rG,
+                        const int *nbas, int ndof, int nD) {
+  double s = 0.0;
+  for (int i = 0; i < rF; ++i)
+    for (int j = 0; j < rG; ++j)
+      s += fc[i] * gc[j] * prodnd(fb + (size_t)i * nD, gb + (size_t)j * nD, nbas, ndof, -1);
+  return s;
+}
+
+/* NORMBASE + NORMCOEF (src/MODVECVECML.f90:295-352): every factor scaled to
+ * unit 2-norm with the norms moved into the weight, then the weights scaled
+ * so that <F,F> = 1. */
+static void normcoef(double *coef, double *base, int r, const int *nbas, const int *off, int ndof) {
+  const int nD = off[ndof];
+  for (int i = 0; i < r; ++i) {
+    double nd = 1.0;
+    for (int d = 0; d < ndof; ++d) {
+      double *x = base + (size_t)i * nD + off[d];
+      const double n1 = sqrt(dot_n(x, x, nbas[d]));
+      for (int j = 0; j < nbas[d]; ++j) x[j] = x[j] / n1;
+      nd = nd * n1;
+    }
+    coef[i] = coef[i] * nd;
+  }
+  const double s = 1 / sqrt(fabs(prodvv_aa(coef, base, r, nbas, ndof, nD)));
+  for (int i = 0; i < r; ++i) coef[i] = coef[i] * s;
+}
+
+/* "Construct improved F" (e.g. src/ALSPow.f90:622-627): weight i = the
+ * 2-norm of row i of the solution, mode factor = the row over it.  Returns 1
+ * when a weight is NaN (the reference aborts there). */
+static int rows_to_mode(double *coef, double *base, int rF, int nD, int gst, const double *bjk, int n) {
+  int bad = 0;
+  for (int i = 0; i < rF; ++i) {
+    double s = 0.0;
+    for (int ir = 0; ir < n; ++ir) s += bjk[i + (size_t)ir * rF] * bjk[i + (size_t)ir * rF];
+    const double rnorm = sqrt(fabs(s));
+    coef[i] = rnorm;
+    for (int ir = 0; ir < n; ++ir) base[(size_t)i * nD + gst + ir] = bjk[i + (size_t)ir * rF] / rnorm;
+  }
+  for (int i = 0; i < rF; ++i)
+    if (coef[i] != coef[i]) bad = 1;
+  return bad;
+}
+
+/* BuildbjkDirectX (src/ALSPow.f90:1154-1310) with recalcB = F: for mode k,
+ *   BB(i,l)  = prod_{m != k} <F_l^m, Fo_i^m>,
+ *   bjk(l,:) = sum_t sum_i co_i [prod_{m != k} <F_l^m, h_{t,m} Fo_i^m>] h_{t,k} Fo_i^k
+ *              - E sum_i co_i BB(i,l) Fo_i^k            (ishift != 0),
+ * negated at k = 0 when ishift < 0.  The other modes are visited in the
+ * order k+1, ..., D-1, 0, ..., k-1; T holds one applied factor. */
+static void buildbjk_direct(const hoplist *H, const double *focoef, const double *fobase, const double *fbase, int rF,
+                            const int *nbas, const int *off, int ndof, int k, int ishift, double Eshift, double *BB,
+                            double *bjk, double *T) {
+  const int nD = off[ndof], n = nbas[k];
+  for (int e = 0; e < rF * n; ++e) bjk[e] = 0.0;
+  for (int t = 0; t < H->T; ++t)
+    for (int i = 0; i < rF; ++i) {
+      for (int l = 0; l < rF; ++l) BB[i + (size_t)l * rF] = 1.0;
+      for (int m = 1; m < ndof; ++m) {
+        const int mm = (k + m) % ndof;
+        hv_base_prod(H, t, mm, fobase + (size_t)i * nD + off[mm], T, nbas[mm]);
+        for (int l = 0; l < rF; ++l)
+          BB[i + (size_t)l * rF] *= dot_n(fbase + (size_t)l * nD + off[mm], T, nbas[mm]);
+      }
+      hv_base_prod(H, t, k, fobase + (size_t)i * nD + off[k], T, n);
+      for (int l = 0; l < rF; ++l) {
+        const double tmp = focoef[i] * BB[i + (size_t)l * rF];
+        for (int j = 0; j < n; ++j) bjk[l + (size_t)j * rF] += tmp * T[j];
+      }
+    }
+  for (int i = 0; i < rF; ++i) {
+    for (int l = 0; l < rF; ++l) BB[i + (size_t)l * rF] = 1.0;
+    const double tmp = -Eshift * focoef[i];
+    for (int m = 1; m < ndof; ++m) {
+      const int mm = (k + m) % ndof;
+      const double *x = fobase + (size_t)i * nD + off[mm];
+      for (int l = 0; l < rF; ++l) BB[i + (size_t)l * rF] *= dot_n(fbase + (size_t)l * nD + off[mm], x, nbas[mm]);
+    }
+    if (ishift != 0) {
+      const double *x = fobase + (size_t)i * nD + off[k];
+      for (int l = 0; l < rF; ++l) {
+        const double tmp2 = tmp * BB[i + (size_t)l * rF];
+        for (int j = 0; j < n; ++j) bjk[l + (size_t)j * rF] += tmp2 * x[j];
+      }
+    }
+  }
+  if (k == 0 && ishift < 0)
+    for (int e = 0; e < rF * n; ++e) bjk[e] = -bjk[e];
+}
+
+/* ALS_POW3 (src/ALSPow.f90:569-660): nitn in-place sweeps of F <- ALS fit of
+ * (H - E)F; each mode step builds BB and bjk from F itself
+ * (BuildbjkDirectX(F, F, ...)), adds 1e-10 max c (taken once), solves by LU
+ * and moves the row norms into the weights; after the last mode the weights
+ * are scaled to <F,F> = 1.  Returns 1 on a NaN weight. */
+static int pals_pow3(const hoplist *H, double *coef, double *base, int rF, const int *nbas, const int *off, int ndof,
+                     int nitn, int ishift, double Eshift, pals_ws *w) {
+  if (nitn == 0) return 0;
+  const int nD = off[ndof];
+  const double valpen = maxval(coef, rF) * 1.0e-10;
+  for (int itn = 0; itn < nitn; ++itn)
+    for (int k = 0; k < ndof; ++k) {
+      const int n = nbas[k];
+      buildbjk_direct(H, coef, base, base, rF, nbas, off, ndof, k, ishift, Eshift, w->BB, w->bjk, w->T);
+      for (int i = 0; i < rF; ++i) w->BB[i + (size_t)i * rF] += valpen;
+      lu_solve(w->BB, w->bjk, rF, n, w->ipiv);
+      if (rows_to_mode(coef, base, rF, nD, off[k], w->bjk, n)) return 1;
+      if (k == ndof - 1) {
+        const double s = 1 / sqrt(fabs(prodvv_aa(coef, base, rF, nbas, ndof, nD)));
+        for (int i = 0; i < rF; ++i) coef[i] = coef[i] * s;
+      }
+    }
+  return 0;
+}
+
+/* UpdateXPS (src/ALSPow.f90:937-1032), divide = 0, and the PS half of
+ * DowndateXPS (:1034-1150), divide = 1: row ik = t rF + i of the
+ * rG x rF matrix PS (rG = T rF, plus rF rows for the shift) is multiplied
+ * or divided by <F_l^k, h_{t,k} Fo_i^k>; the shift rows by <F_l^k, Fo_i^k>,
+ * negated on mode 0.  With divide set, bjk(l,:) += co_i PS(ik,l) h Fo_i^k
+ * (and + E co_i PS(ik,l) (+-Fo_i^k) for the shift rows).  On mode 0 with
+ * ishift < 0 PS (and bjk) change sign. */
+static void xps_step(const hoplist *H, const double *focoef, const double *fobase, const double *fbase, int rF,
+                     const int *nbas, const int *off, int ndof, int k, int ishift, double Eshift, double *PS,
+                     double *bjk, double *T, int divide) {
+  const int nD = off[ndof], n = nbas[k];
+  const int rG = rF * H->T + (ishift != 0 ? rF : 0);
+  if (divide)
+    for (int e = 0; e < rF * n; ++e) bjk[e] = 0.0;
+  int ik = 0;
+  for (int t = 0; t < H->T; ++t)
+    for (int i = 0; i < rF; ++i, ++ik) {
+      hv_base_prod(H, t, k, fobase + (size_t)i * nD + off[k], T, n);
+      for (int l = 0; l < rF; ++l) {
+        const double prod = dot_n(fbase + (size_t)l * nD + off[k], T, n);
+        if (!divide) {
+          PS[ik + (size_t)l * rG] = PS[ik + (size_t)l * rG] * prod;
+        } else {
+          PS[ik + (size_t)l * rG] = PS[ik + (size_t)l * rG] / prod;
+          const double tmp = focoef[i] * PS[ik + (size_t)l * rG];
+          for (int j = 0; j < n; ++j) bjk[l + (size_t)j * rF] += tmp * T[j];
+        }
+      }
+    }
+  if (ishift != 0) {
+    for (int i = 0; i < rF; ++i, ++ik) {
+      const double tmp = Eshift * focoef[i];
+      for (int j = 0; j < n; ++j) T[j] = fobase[(size_t)i * nD + off[k] + j];
+      if (k == 0)
+        for (int j = 0; j < n; ++j) T[j] = -T[j];
+      for (int l = 0; l < rF; ++l) {
+        const double prod = dot_n(fbase + (size_t)l * nD + off[k], T, n);
+        if (!divide) {
+          PS[ik + (size_t)l * rG] = PS[ik + (size_t)l * rG] * prod;
+        } else {
+          PS[ik + (size_t)l * rG] = PS[ik + (size_t)l * rG] / prod;
+          const double tmp2 = tmp * PS[ik + (size_t)l * rG];
+          for (int j = 0; j < n; ++j) bjk[l + (size_t)j * rF] += tmp2 * T[j];
+        }
+      }
+    }
+    if (k == 0 && ishift < 0) {
+      for (size_t e = 0; e < (size_t)rG * rF; ++e) PS[e] = -PS[e];
+      if (divide)
+        for (int e = 0; e < rF * n; ++e) bjk[e] = -bjk[e];
+    }
+  }
+}
+
+/* PRODHV_ALS2 (src/ALSPow.f90:664-780): F <- ALS fit of (H - E)Fo, starting
+ * from F = Fo, by nitn sweeps.  BB = <F,F> without mode 0 at the start
+ * (CONSTBBTOT), then kept by UpdateBB division / multiplication; PS starts
+ * at 1 and takes every mode by UpdateXPS; each mode step divides its mode
+ * out of PS while building bjk (DowndateXPS), adds 1e-10 max c_Fo, solves by
+ * LU and moves the row norms into the weights, then multiplies the new mode
+ * back into BB and PS (except after the very last step).  No final
+ * normalisation.  Returns 1 on a NaN weight. */
+static int pals_prodhv2(const hoplist *H, const double *focoef, const double *fobase, double *coef, double *base,
+                        int rF, const int *nbas, const int *off, int ndof, int ishift, double Eshift, int nitn,
+                        pals_ws *w) {
+  if (nitn == 0) return 0;
+  const int nD = off[ndof];
+  const int rG = rF * H->T + (ishift != 0 ? rF : 0);
+  memcpy(coef, focoef, sizeof(double) * rF);
+  memcpy(base, fobase, sizeof(double) * (size_t)rF * nD);
+  const double valpen = maxval(coef, rF) * 1.0e-10;
+  const_bb(base, rF, nbas, ndof, nD, 0, w->BBmem);
+  for (size_t e = 0; e < (size_t)rG * rF; ++e) w->PS[e] = 1.0;
+  for (int k = 0; k < ndof; ++k)
+    xps_step(H, focoef, fobase, base, rF, nbas, off, ndof, k, ishift, Eshift, w->PS, NULL, w->T, 0);
+  int kp = -1;
+  for (int itn = 0; itn < nitn; ++itn)
+    for (int k = 0; k < ndof; ++k) {
+      const int n = nbas[k];
+      if (kp >= 0) update_bb(base, rF, nD, off[k], n, w->BBmem, 1);
+      memcpy(w->BB, w->BBmem, sizeof(double) * rF * rF);
+      for (int i = 0; i < rF; ++i) w->BB[i + (size_t)i * rF] += valpen;
+      xps_step(H, focoef, fobase, base, rF, nbas, off, ndof, k, ishift, Eshift, w->PS, w->bjk, w->T, 1);
+      lu_solve(w->BB, w->bjk, rF, n, w->ipiv);
+      if (rows_to_mode(coef, base, rF, nD, off[k], w->bjk, n)) return 1;
+      if (itn < nitn - 1 || k < ndof - 1) {
+        update_bb(base, rF, nD, off[k], n, w->BBmem, 0);
+        xps_step(H, focoef, fobase, base, rF, nbas, off, ndof, k, ishift, Eshift, w->PS, NULL, w->T, 0);
+      }
+      kp = k;
+    }
+  return 0;
+}
+
+/* CONSTPSk (src/MODVECVECML.f90:532-569) for one block of PS: P(j,i) =
+ * <G_j^k, F_i^k>, leading dimension ld. */
+static void const_psk(const double *fb, int rF, const double *gb, int rT, int nD, int gi, int n, double *P, int ld) {
+  for (int j = 0; j < rT; ++j)
+    for (int i = 0; i < rF; ++i) P[j + (size_t)i * ld] = dot_n(gb + (size_t)j * nD + gi, fb + (size_t)i * nD + gi, n);
+}
+
+/* ALS_ORTHO_2 (src/ALSUtils.f90:156-377): ALS-guided Gram-Schmidt.  Q_0 is
+ * normalised (NORMCOEF).  Each later Q_v is refitted, nitn sweeps, to
+ *   Q_v + sum_{l<v} coefs_l Q_l,   coefs_l = -<Q_l, Q_v> (from the full PS,
+ * recomputed at every mode step);
+ * PS (rows: the terms of Q_0..Q_v, columns: the terms of Q_v) starts as the
+ * full products (CONSTPSTOT), and each mode step divides mode k out of it,
+ * takes BB from the Q_v rows plus 1e-10 max c_v (taken once per vector),
+ * builds bjk from the coefs-weighted terms, solves by LU, moves the row
+ * norms into the weights, multiplies the new mode k back into PS and scales
+ * the weights of Q_v to unit norm with the Q_v block of PS.  The loops over
+ * l and over the entries of bjk are OpenMP-parallel, as in the reference.
+ * Returns 1 on a NaN weight. */
+static int pals_ortho2(double *coef, double *base, const int *ranks, const int *toff, int nbloc, const int *nbas,
+                       const int *off, int ndof, int nitn, int nthreads) {
+  if (nitn == 0) return 0;
+  const int nD = off[ndof];
+  int nmax = 0, rmax = 0;
+  for (int d = 0; d < ndof; ++d) nmax = nbas[d] > nmax ? nbas[d] : nmax;
+  for (int v = 0; v < nbloc; ++v) rmax = ranks[v] > rmax ? ranks[v] : rmax;
+  const int rtot = toff[nbloc - 1] + ranks[nbloc - 1];
+  double *coefs = (double *)malloc(sizeof(double) * nbloc);
+  double *PS = (double *)malloc(sizeof(double) * (size_t)rtot * rmax);
+  double *P2 = (double *)malloc(sizeof(double) * (size_t)rtot * rmax);
+  double *BB = (double *)malloc(sizeof(double) * rmax * rmax);
+  double *bjk = (double *)malloc(sizeof(double) * (size_t)rmax * nmax);
+  int *ipiv = (int *)malloc(sizeof(int) * rmax);
+  int bad = 0;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#endif
+  (void)nthreads;
+  normcoef(coef, base, ranks[0], nbas, off, ndof);
+  for (int iv = 1; iv < nbloc && !bad; ++iv) {
+    double *fc = coef + toff[iv], *fb = base + (size_t)toff[iv] * nD;
+    const int rF = ranks[iv], rG = toff[iv] + rF, s = toff[iv];
+    const double valpen = maxval(fc, rF) * 1.0e-10;
+    coefs[iv] = 1.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+    for (int l = 0; l <= iv; ++l) {
+      const double *gb = base + (size_t)toff[l] * nD;
+      for (int j = 0; j < ranks[l]; ++j)
+        for (int i = 0; i < rF; ++i)
+          PS[toff[l] + j + (size_t)i * rG] = prodnd(fb + (size_t)i * nD, gb + (size_t)j * nD, nbas, ndof, -1);
+    }
+    for (int itn = 0; itn < nitn && !bad; ++itn)
+      for (int k = 0; k < ndof; ++k) {
+        const int n = nbas[k], gst = off[k];
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+        for (int l = 0; l < iv; ++l) {
+          double c = 0.0;
+          for (int i = 0; i < rF; ++i)
+            for (int j = 0; j < ranks[l]; ++j) c = c - PS[toff[l] + j + (size_t)i * rG] * fc[i] * coef[toff[l] + j];
+          coefs[l] = c;
+        }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+        for (int l = 0; l <= iv; ++l) {
+          const_psk(fb, rF, base + (size_t)toff[l] * nD, ranks[l], nD, gst, n, P2 + toff[l], rG);
+          for (int j = 0; j < ranks[l]; ++j)
+            for (int i = 0; i < rF; ++i)
+              PS[toff[l] + j + (size_t)i * rG] = PS[toff[l] + j + (size_t)i * rG] / P2[toff[l] + j + (size_t)i * rG];
+        }
+        for (int i = 0; i < rF; ++i)
+          for (int j = 0; j < rF; ++j) BB[j + (size_t)i * rF] = PS[s + j + (size_t)i * rG];
+        for (int i = 0; i < rF; ++i) BB[i + (size_t)i * rF] += valpen;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+        for (int m = 0; m < n * rF; ++m) {
+          const int i = m / n, ir = m % n;
+          double b = 0.0;
+          for (int l = 0; l <= iv; ++l)
+            for (int j = 0; j < ranks[l]; ++j)
+              b = b + coefs[l] * coef[toff[l] + j] * base[(size_t)(toff[l] + j) * nD + gst + ir] *
+                          PS[toff[l] + j + (size_t)i * rG];
+          bjk[i + (size_t)ir * rF] = b;
+        }
+        lu_solve(BB, bjk, rF, n, ipiv);
+        if (rows_to_mode(fc, fb, rF, nD, gst, bjk, n)) { bad = 1; break; }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+        for (int l = 0; l <= iv; ++l) {
+          const_psk(fb, rF, base + (size_t)toff[l] * nD, ranks[l], nD, gst, n, P2 + toff[l], rG);
+          for (int j = 0; j < ranks[l]; ++j)
+            for (int i = 0; i < rF; ++i)
+              PS[toff[l] + j + (size_t)i * rG] = PS[toff[l] + j + (size_t)i * rG] * P2[toff[l] + j + (size_t)i * rG];
+        }
+        double rn = 0.0;
+        for (int i = 0; i < rF; ++i) {
+          rn = rn + PS[s + i + (size_t)i * rG] * fc[i] * fc[i];
+          for (int j = 0; j < i; ++j) rn = rn + 2 * PS[s + j + (size_t)i * rG] * fc[i] * fc[j];
+        }
+        rn = 1 / sqrt(fabs(rn));
+        for (int i = 0; i < rF; ++i) fc[i] = rn * fc[i];
+      }
+  }
+  free(coefs); free(PS); free(P2); free(BB); free(bjk); free(ipiv);
+  return bad;
+}
+
+/* ALS_SUMLCVEC_2 (src/ALSUtils.f90:731-891): F (rF terms, starting guess in
+ * place) <- ALS fit of sum_l w_l Q_l by nitn sweeps.  PS (rows: the terms of
+ * every Q_l, columns: the terms of F) and BB = <F,F> start as the full
+ * products and are kept by dividing mode k out before its step and
+ * multiplying the new mode k back after it (PS not after the very last
+ * step); penalty 1e-10 max c_F (taken once); at the end the weights are
+ * scaled to unit norm with BB.  Returns 1 on a NaN weight. */
+static int pals_sumlcvec2(double *fcoef, double *fbase, int rF, const double *qcoef, const double *qbase,
+                          const int *ranks, const int *toff, int nbloc, const double *w, const int *nbas,
+                          const int *off, int ndof, int nitn, pals_ws *ws) {
+  if (nitn == 0) return 0;
+  const int nD = off[ndof], rG = toff[nbloc - 1] + ranks[nbloc - 1];
+  double *PS = ws->PS, *P2 = ws->psk, *BBmem = ws->BBmem, *BB = ws->BB, *bjk = ws->bjk;
+  const double valpen = maxval(fcoef, rF) * 1.0e-10;
+  for (int l = 0; l < nbloc; ++l)
+    for (int j = 0; j < ranks[l]; ++j)
+      for (int i = 0; i < rF; ++i)
+        PS[toff[l] + j + (size_t)i * rG] =
+            prodnd(fbase + (size_t)i * nD, qbase + (size_t)(toff[l] + j) * nD, nbas, ndof, -1);
+  const_bb(fbase, rF, nbas, ndof, nD, -1, BBmem);
+  for (int itn = 0; itn < nitn; ++itn)
+    for (int k = 0; k < ndof; ++k) {
+      const int n = nbas[k], gst = off[k];
+      for (int l = 0; l < nbloc; ++l) {
+        const_psk(fbase, rF, qbase + (size_t)toff[l] * nD, ranks[l], nD, gst, n, P2 + toff[l], rG);
+        for (int j = 0; j < ranks[l]; ++j)
+          for (int i = 0; i < rF; ++i)
+            PS[toff[l] + j + (size_t)i * rG] = PS[toff[l] + j + (size_t)i * rG] / P2[toff[l] + j + (size_t)i * rG];
+      }
+      update_bb(fbase, rF, nD, gst, n, BBmem, 1);
+      memcpy(BB, BBmem, sizeof(double) * rF * rF);
+      for (int i = 0; i < rF; ++i) BB[i + (size_t)i * rF] += valpen;
+      for (int e = 0; e < rF * n; ++e) bjk[e] = 0.0;
+      for (int ir = 0; ir < n; ++ir)
+        for (int l = 0; l < nbloc; ++l)
+          for (int j = 0; j < ranks[l]; ++j) {
+            const double gtmp = w[l] * qcoef[toff[l] + j] * qbase[(size_t)(toff[l] + j) * nD + gst + ir];
+            for (int i = 0; i < rF; ++i) bjk[i + (size_t)ir * rF] += gtmp * PS[toff[l] + j + (size_t)i * rG];
+          }
+      lu_solve(BB, bjk, rF, n, ws->ipiv);
+      if (rows_to_mode(fcoef, fbase, rF, nD, gst, bjk, n)) return 1;
+      if (itn < nitn - 1 || k < ndof - 1)
+        for (int l = 0; l < nbloc; ++l) {
+          const_psk(fbase, rF, qbase + (size_t)toff[l] * nD, ranks[l], nD, gst, n, P2 + toff[l], rG);
+          for (int j = 0; j < ranks[l]; ++j)
+            for (int i = 0; i < rF; ++i)
+              PS[toff[l] + j + (size_t)i * rG] = PS[toff[l] + j + (size_t)i * rG] * P2[toff[l] + j + (size_t)i * rG];
+        }
+      update_bb(fbase, rF, nD, gst, n, BBmem, 0);
+    }
+  double rn = 0.0;
+  for (int i = 0; i < rF; ++i) {
+    rn = rn + BBmem[i + (size_t)i * rF] * (fcoef[i] * fcoef[i]);
+    for (int j = 0; j < i; ++j) rn = rn + 2 * BBmem[i + (size_t)j * rF] * fcoef[i] * fcoef[j];
+  }
+  rn = 1 / sqrt(fabs(rn));
+  for (int i = 0; i < rF; ++i) fcoef[i] = rn * fcoef[i];
+  return 0;
+}
+
+static int *rank_offsets(const int *ranks, int nbloc) {
+  int *toff = (int *)malloc(sizeof(int) * (nbloc + 1));
+  toff[0] = 0;
+  for (int v = 0; v < nbloc; ++v) toff[v + 1] = toff[v] + ranks[v];
+  return toff;
+}
+
+int orc_pals_pow3(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
+                  const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
+                  int ishift, double Eshift, int nthreads) {
+  int *off = make_offsets(nbas, ndof), *toff = rank_offsets(ranks, nbloc);
+  const int nD = off[ndof], nmax = max_nbas(nbas, ndof);
+  hoplist H = {T, ndof, opid, mptr, Hcoef, mat};
+  int bad = 0;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : bad)
+#endif
+  for (int v = nconv < 0 ? 0 : nconv; v < nbloc; ++v) {
+    pals_ws w = pals_ws_alloc(ranks[v], 1, nmax);
+    bad += pals_pow3(&H, coef + toff[v], base + (size_t)toff[v] * nD, ranks[v], nbas, off, ndof, npow, ishift,
+                     Eshift, &w);
+    pals_ws_free(&w);
+  }
+  (void)nthreads;
+  free(off); free(toff);
+  return bad;
+}
+
+int orc_pals_ortho2(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nitn,
+                    int nthreads) {
+  int *off = make_offsets(nbas, ndof), *toff = rank_offsets(ranks, nbloc);
+  const int bad = pals_ortho2(coef, base, ranks, toff, nbloc, nbas, off, ndof, nitn, nthreads);
+  free(off); free(toff);
+  return bad;
+}
+
+int orc_pals_prodhv2(const double *fobase, const double *focoef, double *base, double *coef, const int *nbas,
+                     int ndof, int rF, const int *opid, const int *mptr, const double *Hcoef, const double *mat,
+                     int T, int ishift, double Eshift, int nitn) {
+  int *off = make_offsets(nbas, ndof);
+  hoplist H = {T, ndof, opid, mptr, Hcoef, mat};
+  pals_ws w = pals_ws_alloc(rF, rF * T + rF, max_nbas(nbas, ndof));
+  const int bad = pals_prodhv2(&H, focoef, fobase, coef, base, rF, nbas, off, ndof, ishift, Eshift, nitn, &w);
+  pals_ws_free(&w);
+  free(off);
+  return bad;
+}
+
+int orc_pals_sumlcvec2(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
+                       const double *U, int nitn, int nthreads) {
+  int *off = make_offsets(nbas, ndof), *toff = rank_offsets(ranks, nbloc);
+  const int nD = off[ndof], nmax = max_nbas(nbas, ndof), rtot = toff[nbloc];
+  double *qb = (double *)malloc(sizeof(double) * (size_t)rtot * nD);
+  double *qc = (double *)malloc(sizeof(double) * rtot);
+  memcpy(qb, base, sizeof(double) * (size_t)rtot * nD);
+  memcpy(qc, coef, sizeof(double) * rtot);
+  int bad = 0;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : bad)
+#endif
+  for (int v = 0; v < nbloc; ++v) {
+    pals_ws w = pals_ws_alloc(ranks[v], rtot, nmax);
+    bad += pals_sumlcvec2(coef + toff[v], base + (size_t)toff[v] * nD, ranks[v], qc, qb, ranks, toff, nbloc,
+                          U + (size_t)v * nbloc, nbas, off, ndof, nitn, &w);
+    pals_ws_free(&w);
+  }
+  (void)nthreads;
+  free(qb); free(qc); free(off); free(toff);
+  return bad;
+}
+
+/* Diagonalize with intertwining (src/BlockUtils.f90:184-225): GetQHQ3
+ * (:309-345: H Q_i by PRODHV_ALS2 with nitn sweeps and no shift, then
+ * QHQ(i,j) = <Q_j, H Q_i> for j >= i, OpenMP over i), GetOverlaps (:347-381:
+ * S(i,j) = <Q_j, Q_i>, j >= i), SolveGenEigval (src/LinAlg.f90:380-428,
+ * DSYGV itype 1 on the upper triangles), then UpdateVecs2 (:479-516):
+ * vector i <- ALS_SUMLCVEC_2 fit of sum_l U(l,i) Q_l starting from Q_i.
+ * eigv receives the eigenvalues (ascending); U (column-major, column i =
+ * eigenvector i, largest-magnitude entry positive) when not NULL.
+ * Requires nitn >= 1 (PRODHV_ALS2 returns an undefined H Q_i otherwise).
+ * Returns the number of NaN events, or -1 on a failed eigensolve. */
+int orc_pals_diagonalize(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
+                         const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int nitn,
+                         double *eigv, double *Uout, int nthreads) {
+  if (nitn < 1) return -1;
+  int *off = make_offsets(nbas, ndof), *toff = rank_offsets(ranks, nbloc);
+  const int nD = off[ndof], nmax = max_nbas(nbas, ndof);
+  hoplist H = {T, ndof, opid, mptr, Hcoef, mat};
+  double *QHQ = (double *)calloc((size_t)nbloc * nbloc, sizeof(double));
+  double *S = (double *)calloc((size_t)nbloc * nbloc, sizeof(double));
+  double *U = (double *)malloc(sizeof(double) * (size_t)nbloc * nbloc);
+  int bad = 0;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : bad)
+#endif
+  for (int i = 0; i < nbloc; ++i) {
+    const int rF = ranks[i];
+    pals_ws w = pals_ws_alloc(rF, rF * T, nmax);
+    double *hc = (double *)malloc(sizeof(double) * rF);
+    double *hb = (double *)malloc(sizeof(double) * (size_t)rF * nD);
+    bad += pals_prodhv2(&H, coef + toff[i], base + (size_t)toff[i] * nD, hc, hb, rF, nbas, off, ndof, 0, 0.0, nitn,
+                        &w);
+    for (int j = i; j < nbloc; ++j)
+      QHQ[i + (size_t)j * nbloc] =
+          prodvv_ab(coef + toff[j], base + (size_t)toff[j] * nD, ranks[j], hc, hb, rF, nbas, ndof, nD);
+    free(hc); free(hb);
+    pals_ws_free(&w);
+  }
+  const int nij = nbloc * (nbloc + 1) / 2;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
+#endif
+  for (int ij = 0; ij < nij; ++ij) {
+    int i = 0, rem = ij;
+    while (rem >= nbloc - i) { rem -= nbloc - i; ++i; }
+    const int j = i + rem;
+    S[i + (size_t)j * nbloc] = prodvv_ab(coef + toff[j], base + (size_t)toff[j] * nD, ranks[j], coef + toff[i],
+                                         base + (size_t)toff[i] * nD, ranks[i], nbas, ndof, nD);
+  }
+  (void)nthreads;
+  /* DSYGV 'U' reads the upper triangles; the eigensolver here reads lower. */
+  for (int j = 0; j < nbloc; ++j)
+    for (int i = j + 1; i < nbloc; ++i) {
+      QHQ[i + (size_t)j * nbloc] = QHQ[j + (size_t)i * nbloc];
+      S[i + (size_t)j * nbloc] = S[j + (size_t)i * nbloc];
+    }
+  if (orc_sygv(nbloc, QHQ, S, eigv, U) != 0) {
+    bad = -1;
+  } else {
+    if (Uout) memcpy(Uout, U, sizeof(double) * (size_t)nbloc * nbloc);
+    bad += orc_pals_sumlcvec2(base, coef, nbas, ndof, nbloc, ranks, U, nitn, nthreads);
+  }
+  free(QHQ); free(S); free(U); free(off); free(toff);
+  return bad;
+}
+
+/* One cycle of Iterate's CPU branch for solver pals (src/Solver.f90:508-538)
+ * at lowmem = 4: ALS_POW3 (npow sweeps of H - Eshift, ishift) on vectors
+ * nconv..nbloc-1, OpenMP over vectors; ALS_ORTHO_2 (nals sweeps); with
+ * update, Diagonalize with intertwining (nals sweeps), which fills eigv.
+ * Without update the reference goes on to GetQHQdiag and SortVecs, which
+ * the caller applies.  Returns the number of NaN events (the reference
+ * aborts on one), or -1 on a failed eigensolve. */
+int orc_pals_cycle(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
+                   const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
+                   int nals, int update, int ishift, double Eshift, double *eigv, int nthreads) {
+  int bad = orc_pals_pow3(base, coef, nbas, ndof, nbloc, ranks, nconv, opid, mptr, Hcoef, mat, T, npow, ishift,
+                          Eshift, nthreads);
+  if (bad) return bad;
+  bad = orc_pals_ortho2(base, coef, nbas, ndof, nbloc, ranks, nals, nthreads);
+  if (bad) return bad;
+  if (update)
+    bad = orc_pals_diagonalize(base, coef, nbas, ndof, nbloc, ranks, opid, mptr, Hcoef, mat, T, nals, eigv, NULL,
+                               nthreads);
+  return bad;
 }

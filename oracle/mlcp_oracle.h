@@ -15,7 +15,10 @@
  *
  * It also restates the Fortran host's CPU ALS reduction, reduc_ALS
  * (src/REDUCTIONML.f90:593-731), the reference's own CPU implementation of
- * the rank reduction, which the benchmark times as the reference CPU path.
+ * the rank reduction, which the benchmark times as the reference CPU path,
+ * and the Fortran host's CPU power solver (solver pals at lowmem 4:
+ * ALS_POW3, ALS_ORTHO_2, PRODHV_ALS2, ALS_SUMLCVEC_2), the CPU twin of the
+ * GPU power cycle.
  *
  * Pinning: the reference ships no tests, golden vectors or fixtures for
  * this path, and its Fortran host cannot be compiled without a Fortran
@@ -120,6 +123,39 @@ int orc_reduc_als(const double *gcoef, const double *gbase, int rG, double *fcoe
 int orc_reduc_als_batched(int nvec, const double *const *gcoef, const double *const *gbase, const int *rG,
                           double *const *fcoef, double *const *fbase, const int *rF, const int *nbas, int ndof,
                           int nitn, int nthreads);
+
+/* The Fortran host's CPU power cycle, solver pals at lowmem 4
+ * (src/Solver.f90:508-538).  A block holds nbloc vectors; vector v has
+ * ranks[v] terms, stored after the terms of vectors 0..v-1 (ragged blocks
+ * are allowed, as in ALS_ORTHO_2's ranks table).  Each call returns the
+ * number of NaN weights met (the reference aborts on one); the
+ * diagonalisation and the cycle return -1 when the eigensolve fails. */
+/* ALS_POW3 (src/ALSPow.f90:569-660) on vectors nconv..nbloc-1, OpenMP over vectors. */
+int orc_pals_pow3(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
+                  const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
+                  int ishift, double Eshift, int nthreads);
+/* ALS_ORTHO_2 (src/ALSUtils.f90:156-377). */
+int orc_pals_ortho2(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nitn,
+                    int nthreads);
+/* PRODHV_ALS2 (src/ALSPow.f90:664-780): (base, coef) <- ALS fit of
+ * (H - Eshift) Fo, rF terms, starting from Fo. */
+int orc_pals_prodhv2(const double *fobase, const double *focoef, double *base, double *coef, const int *nbas,
+                     int ndof, int rF, const int *opid, const int *mptr, const double *Hcoef, const double *mat,
+                     int T, int ishift, double Eshift, int nitn);
+/* UpdateVecs2 (src/BlockUtils.f90:479-516) with ALS_SUMLCVEC_2
+ * (src/ALSUtils.f90:731-891): vector v <- fit of sum_l U[v*nbloc + l] Q_l. */
+int orc_pals_sumlcvec2(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
+                       const double *U, int nitn, int nthreads);
+/* Diagonalize with intertwining (src/BlockUtils.f90:184-225): GetQHQ3,
+ * GetOverlaps, SolveGenEigval (upper triangles), UpdateVecs2.  U (optional)
+ * receives the eigenvectors, column-major. */
+int orc_pals_diagonalize(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
+                         const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int nitn,
+                         double *eigv, double *U, int nthreads);
+/* One cycle: ALS_POW3, ALS_ORTHO_2 and, with update, the diagonalisation. */
+int orc_pals_cycle(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
+                   const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
+                   int nals, int update, int ishift, double Eshift, double *eigv, int nthreads);
 
 #ifdef __cplusplus
 }

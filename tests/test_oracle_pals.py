@@ -1,0 +1,212 @@
+"""The restated Fortran CPU solver (solver pals at lowmem 4: ALS_POW3,
+ALS_ORTHO_2, PRODHV_ALS2, Diagonalize with intertwining, ALS_SUMLCVEC_2).
+
+The reference's GPU path mirrors these routines (src/ALSPow.f90:569 is the
+algorithm of POW_ALS, src/ALSUtils.f90:156 of GramSchmidt, :731 of
+UPDATES_ALS).  So the two restatements must agree to rounding stage by stage
+where the algorithms coincide: the power sweep, the Gram-Schmidt and the
+vector updates.  They differ in one place only: the Fortran Rayleigh-Ritz
+step reads the upper triangle of the ALS-reduced QHQ (DSYGV 'U') and the GPU
+path the lower one.  Known answers cover the rest: exactly representable
+products, a numpy eigensolve of the upper triangle, and convergence to exact
+spectra.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from mlcp_gb300 import hoplist as H
+
+
+def dense_block(base, coef, nbas, ranks):
+    out, s = [], 0
+    for r in ranks:
+        out.append(oracle.cp_dense(base[s:s + r], coef[s:s + r], nbas).ravel())
+        s += r
+    return np.array(out)
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def start_block(nbas, rk, nbloc, seed):
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-0.5, 0.5, size=(rk * nbloc, int(np.sum(nbas)))), np.ones(rk * nbloc)
+
+
+@pytest.mark.parametrize("D,npow", [(4, 3), (3, 2)])
+@pytest.mark.parametrize("ishift,esh", [(1, 9.0), (0, 0.0), (-1, 4.0)])
+def test_pow3_matches_gpu_algorithm_sweep(ishift, esh, D, npow):
+    """With ishift < 0 the GPU path changes the sign of bjk at every mode
+    (src/intertw_mvp.cu:437-440), ALS_POW3 at the first mode only
+    (src/ALSPow.f90:1265-1269): a mode's factor takes the sign of its own
+    step, so each sweep leaves the two vectors (-1)^(D-1) apart.  The
+    cycles use ishift = 1."""
+    hl = H.henon_heiles(D=D, n=5, lam=0.111803)
+    nb, rk, nbloc = hl.nbas, 4, 3
+    Q, qc = start_block(nb, rk, nbloc, 1)
+    a_b, a_c = oracle.pow_als_block(Q, qc, nb, rk, nbloc, hl, npow, ishift, esh)
+    b_b, b_c = oracle.pals_pow3(Q, qc, nb, rk, nbloc, hl, npow, ishift, esh)
+    sign = (-1) ** ((D - 1) * npow) if ishift < 0 else 1
+    assert rel(dense_block(b_b, b_c, nb, [rk] * nbloc), sign * dense_block(a_b, a_c, nb, [rk] * nbloc)) < 1e-10
+
+
+def test_pow3_skips_converged_vectors():
+    hl = H.random_hoplist([4, 3, 5], 5, seed=4)
+    Q, qc = start_block(hl.nbas, 3, 4, 2)
+    b, c = oracle.pals_pow3(Q, qc, hl.nbas, 3, 4, hl, 2, 1, 1.0, nconv=2)
+    np.testing.assert_array_equal(b[:6], Q[:6])
+    np.testing.assert_array_equal(c[:6], qc[:6])
+    assert not np.array_equal(c[6:], qc[6:])
+    # each swept vector leaves unit norm (the weights are scaled after the last mode)
+    for v in (2, 3):
+        s = slice(3 * v, 3 * v + 3)
+        assert abs(oracle.cp_dot(b[s], c[s], b[s], c[s], hl.nbas) - 1) < 1e-12
+
+
+def test_ortho2_matches_gpu_algorithm_gram_schmidt():
+    hl = H.henon_heiles(D=4, n=5, lam=0.111803)
+    nb, rk, nbloc = hl.nbas, 4, 5
+    Q, qc = start_block(nb, rk, nbloc, 3)
+    Q, qc = oracle.pow_als_block(Q, qc, nb, rk, nbloc, hl, 2, 1, 9.0)
+    a_b, a_c = oracle.gram_schmidt(Q, qc, nb, rk, nbloc, 4)
+    b_b, b_c = oracle.pals_ortho2(Q, qc, nb, rk, nbloc, 4)
+    assert rel(dense_block(b_b, b_c, nb, [rk] * nbloc), dense_block(a_b, a_c, nb, [rk] * nbloc)) < 1e-10
+
+
+def test_ortho2_ragged_block():
+    """ALS_ORTHO_2 keeps a ranks table, so a block may mix ranks: every
+    vector leaves with unit norm and the overlaps drop."""
+    hl = H.coupled_oscillators(3, 5)
+    nb, ranks = hl.nbas, [2, 6, 3, 5]
+    rng = np.random.default_rng(7)
+    Q = rng.uniform(-0.5, 0.5, size=(sum(ranks), int(nb.sum())))
+    qc = np.ones(sum(ranks))
+    # a common component makes the start far from orthogonal
+    Q[:, :5] += 0.8
+    D0 = dense_block(Q, qc, nb, ranks)
+    b, c = oracle.pals_ortho2(Q, qc, nb, 0, len(ranks), 12, ranks=ranks)
+    D1 = dense_block(b, c, nb, ranks)
+    np.testing.assert_allclose(np.einsum("ij,ij->i", D1, D1), 1.0, atol=1e-10)
+    off0 = np.abs(np.triu((D0 / np.linalg.norm(D0, axis=1)[:, None]) @ (D0 / np.linalg.norm(D0, axis=1)[:, None]).T,
+                          1)).max()
+    off1 = np.abs(np.triu(D1 @ D1.T, 1)).max()
+    assert off1 < 0.1 * off0
+
+
+def test_prodhv2_exact_for_one_product_term():
+    """With one term acting on one mode, H F has F's rank and the fit
+    converges to it."""
+    hl = H.random_hoplist([4, 5, 3, 4], 1, seed=9, coupling=1)
+    rng = np.random.default_rng(2)
+    F = rng.normal(size=(3, int(hl.nbas.sum())))
+    fc = rng.uniform(0.5, 1.5, 3)
+    b, c = oracle.pals_prodhv2(F, fc, hl.nbas, hl, 200)
+    want = H.dense_hamiltonian(hl) @ oracle.cp_dense(F, fc, hl.nbas).ravel()
+    got = oracle.cp_dense(b, c, hl.nbas).ravel()
+    assert np.linalg.norm(got - want) < 1e-8 * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("nitn", [1, 4])
+def test_prodhv2_matches_explicit_target_reduction(nitn):
+    """PRODHV_ALS2 never forms H F; reduc_ALS on the explicit rT-term H F,
+    from the same start, runs the same sweeps with the same update and
+    downdate of BB and PS.  Only the penalties differ (1e-10 max c_F against
+    1e-15 max c_G)."""
+    hl = H.random_hoplist([4, 5, 3, 4], 4, seed=3, coupling=2)
+    nb = hl.nbas
+    off = np.concatenate([[0], np.cumsum(nb)])
+    rng = np.random.default_rng(5)
+    F = rng.normal(size=(3, int(nb.sum())))
+    fc = rng.uniform(0.5, 1.5, 3)
+    gb, gc = [], []
+    for t in range(hl.nterms):
+        for i in range(3):
+            row = np.concatenate([hl.operator(t, d) @ F[i, off[d]:off[d + 1]] for d in range(len(nb))])
+            row[:nb[0]] *= hl.coef[t]
+            gb.append(row)
+            gc.append(fc[i])
+    rc, rb = oracle.reduc_als(np.array(gc), np.array(gb), fc, F, nb, nitn)
+    b, c = oracle.pals_prodhv2(F, fc, nb, hl, nitn)
+    assert rel(oracle.cp_dense(b, c, nb), oracle.cp_dense(rb, rc, nb)) < 1e-8
+
+
+@pytest.mark.parametrize("ishift", [1, -1])
+def test_prodhv2_shift_on_identity_hamiltonian(ishift):
+    """H = c I: (H - E) F = (c - E) F exactly, (E - H) F with ishift < 0."""
+    nb = [3, 4, 5]
+    hl = H.build_hoplist(nb, [(2.5, {})])
+    rng = np.random.default_rng(4)
+    F = rng.normal(size=(2, sum(nb)))
+    fc = np.array([1.0, 0.7])
+    E = 4.0
+    b, c = oracle.pals_prodhv2(F, fc, nb, hl, 2, ishift=ishift, Eshift=E)
+    want = ishift * (2.5 - E) * oracle.cp_dense(F, fc, nb)
+    assert rel(oracle.cp_dense(b, c, nb), want) < 1e-9
+
+
+def test_sumlcvec2_matches_gpu_algorithm_updates():
+    hl = H.henon_heiles(D=4, n=5, lam=0.111803)
+    nb, rk, nbloc = hl.nbas, 4, 4
+    Q, qc = start_block(nb, rk, nbloc, 5)
+    Q, qc = oracle.pals_ortho2(Q, qc, nb, rk, nbloc, 3)
+    rng = np.random.default_rng(6)
+    U = np.linalg.qr(rng.normal(size=(nbloc, nbloc)))[0]
+    a_b, a_c = oracle.vector_updates(Q, qc, nb, rk, nbloc, U, 4)
+    b_b, b_c = oracle.pals_sumlcvec2(Q, qc, nb, rk, nbloc, U, 4)
+    assert rel(dense_block(b_b, b_c, nb, [rk] * nbloc), dense_block(a_b, a_c, nb, [rk] * nbloc)) < 1e-10
+
+
+def test_diagonalize_reads_upper_triangle():
+    """GetQHQ3 + GetOverlaps + DSYGV('U'): the eigenpairs of the matrices
+    whose upper triangles hold <Q_j, H Q_i> (H Q_i from PRODHV_ALS2) and
+    <Q_j, Q_i>, j >= i."""
+    import scipy.linalg
+    hl = H.henon_heiles(D=3, n=5, lam=0.111803)
+    nb, rk, nbloc, nitn = hl.nbas, 3, 4, 3
+    Q, qc = start_block(nb, rk, nbloc, 8)
+    Q, qc = oracle.pals_ortho2(Q, qc, nb, rk, nbloc, 4)
+    A = np.zeros((nbloc, nbloc))
+    S = np.zeros((nbloc, nbloc))
+    for i in range(nbloc):
+        si = slice(i * rk, (i + 1) * rk)
+        hb, hc = oracle.pals_prodhv2(Q[si], qc[si], nb, hl, nitn)
+        for j in range(i, nbloc):
+            sj = slice(j * rk, (j + 1) * rk)
+            A[i, j] = A[j, i] = oracle.cp_dot(Q[sj], qc[sj], hb, hc, nb)
+            S[i, j] = S[j, i] = oracle.cp_dot(Q[sj], qc[sj], Q[si], qc[si], nb)
+    lam, X = scipy.linalg.eigh(A, S)
+    _, _, eig, U = oracle.pals_diagonalize(Q, qc, nb, rk, nbloc, hl, nitn)
+    np.testing.assert_allclose(eig, lam, rtol=1e-11, atol=1e-11)
+    for m in range(nbloc):
+        x = X[:, m] * np.sign(X[np.argmax(np.abs(X[:, m])), m])
+        np.testing.assert_allclose(U[:, m], x, atol=1e-9)
+
+
+def _run(cycle, hl, rk, nbloc, ncyc, npow, nals, seed):
+    Q, qc = start_block(hl.nbas, rk, nbloc, seed)
+    ex = np.linalg.eigvalsh(H.dense_hamiltonian(hl))
+    est = ex[:nbloc] + 0.3
+    eig = np.zeros(nbloc)
+    for _ in range(ncyc):
+        Esh = 0.5 * (2 * est[-1] - est[-2] + ex[-1])
+        Q, qc, eig = cycle(Q, qc, hl.nbas, rk, nbloc, hl, eig, npow, nals, True, 1, Esh)
+        est = eig
+    return eig, ex[:nbloc]
+
+
+def test_pals_cycle_converges_henon_heiles():
+    hl = H.henon_heiles(D=3, n=6, lam=0.111803)
+    eig, ex = _run(oracle.pals_cycle, hl, 8, 4, 20, 5, 5, seed=1)
+    np.testing.assert_allclose(eig, ex, rtol=1e-5)
+
+
+def test_pals_cycle_tracks_gpu_algorithm_cycle():
+    """Same start, same cycles: the two solvers differ only by the triangle
+    of the ALS-reduced QHQ, so their Ritz values stay within the ALS error."""
+    hl = H.coupled_oscillators(3, 6)
+    e_pals, ex = _run(oracle.pals_cycle, hl, 6, 4, 15, 5, 5, seed=0)
+    e_gpu, _ = _run(oracle.intertwine, hl, 6, 4, 15, 5, 5, seed=0)
+    np.testing.assert_allclose(e_pals[:-1], ex[:-1], rtol=2e-5)
+    np.testing.assert_allclose(e_pals, e_gpu, rtol=1e-3)
