@@ -102,6 +102,11 @@ def lib() -> ctypes.CDLL:
         L.orc_pals_diagonalize.argtypes = [_D, _D, _I, c_i, c_i, _I, _I, _I, _D, _D, c_i, c_i, _D, _D, c_i]
         L.orc_pals_cycle.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, _I, _I, _D, _D, c_i, c_i, c_i, c_i, c_i, c_d,
                                      _D, c_i]
+        L.orc_prodhv.argtypes = [_D, _D, _I, c_i, c_i, _I, _I, _D, _D, c_i, c_i, c_d, _D, _D]
+        L.orc_powr_recurse.restype = c_i
+        L.orc_powr_recurse.argtypes = [_D, _D, _I, c_i, c_i, _I, _I, _D, _D, c_i, c_i, c_d, c_i]
+        L.orc_gramortho.restype = c_i
+        L.orc_gramortho.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, c_i, c_i]
     return _lib
 
 
@@ -663,6 +668,40 @@ def pals_cycle(base, coef, nbas, rk, nbloc, hl, eigv, npow, nals, update=True, i
                                 _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, npow, nals, int(bool(update)),
                                 ishift, float(Eshift), _dp(eig), nthreads), "pals cycle")
     return base, coef, eig
+
+
+# --- the Fortran host's plain power solver (solver powr), reduc = reduc_ALS ---
+
+def prodhv(base, coef, nbas, hl, ishift=0, Eshift=0.0):
+    """PRODHV (src/MODHVECML.f90:50-110): the explicit (H - Eshift) F."""
+    fb = np.ascontiguousarray(base, dtype=np.float64)
+    fc = np.ascontiguousarray(coef, dtype=np.float64)
+    rG = fc.size * (hl.nterms + (1 if ishift else 0))
+    gb = np.zeros((rG, fb.shape[-1]))
+    gc = np.zeros(rG)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    lib().orc_prodhv(_dp(fb), _dp(fc), _ip(nb), len(nb), fc.size, _ip(hl.opid), _ip(hl.mptr), _dp(hl.coef),
+                     _dp(hl.mat), hl.nterms, ishift, float(Eshift), _dp(gb), _dp(gc))
+    return gb, gc
+
+
+def powr_recurse(base, coef, nbas, hl, npow, Eshift, nloop):
+    """PowrRecurse (src/BlockPower.f90:49-73) on one vector (copies)."""
+    fb = np.ascontiguousarray(base, dtype=np.float64).copy()
+    fc = np.ascontiguousarray(coef, dtype=np.float64).copy()
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    _check(lib().orc_powr_recurse(_dp(fb), _dp(fc), _ip(nb), len(nb), fc.size, _ip(hl.opid), _ip(hl.mptr),
+                                  _dp(hl.coef), _dp(hl.mat), hl.nterms, npow, float(Eshift), nloop), "PowrRecurse")
+    return fb, fc
+
+
+def gramortho(base, coef, nbas, rk, nbloc, nloop, k=0, ranks=None, nthreads=0):
+    """GRAMORTHO (k = 0) / pGRAMORTHO (src/BlockUtils.f90:22-123)."""
+    base, coef, rv = _block(base, coef, nbloc, rk, ranks)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    _check(lib().orc_gramortho(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), k, nloop, nthreads),
+           "GRAMORTHO")
+    return base, coef
 
 
 # --- the reference's own FP64 CUDA library (oracle/ref_build.py, oracle/ref_run.py) ---

@@ -1640,3 +1640,113 @@ int orc_pals_cycle(double *base, double *coef, const int *nbas, int ndof, int nb
                                nthreads);
   return bad;
 }
+
+/* ------------------------------------------------------------------ */
+/* The Fortran host's plain power solver (solver powr): PowrRecurse,    */
+/* GRAMORTHO / pGRAMORTHO, with reduc = reduc_ALS                       */
+/* ------------------------------------------------------------------ */
+
+/* PRODHV (src/MODHVECML.f90:50-110): the explicit product (H - E)F of
+ * rF (T + [ishift != 0]) terms, term t rF + i = c_i (x) h_{t,m} F_i^m with
+ * opcoef(t) in the first mode's factor (HVBaseProd); the shift terms are
+ * |E| c_i (x) F_i^m with the sign of -E (ishift > 0) in the first mode's
+ * factor (VecScalarMult, VecSignChange, src/MODVECVECML.f90:66-100); with
+ * ishift < 0 the H terms change sign instead. */
+static void prodhv_explicit(const hoplist *H, const double *fc, const double *fb, int rF, const int *nbas,
+                            const int *off, int ndof, int ishift, double E, double *gc, double *gb) {
+  const int nD = off[ndof], rFH = rF * H->T, n0 = nbas[0];
+  int ik = 0;
+  for (int t = 0; t < H->T; ++t)
+    for (int i = 0; i < rF; ++i, ++ik) {
+      gc[ik] = fc[i];
+      for (int d = 0; d < ndof; ++d)
+        hv_base_prod(H, t, d, fb + (size_t)i * nD + off[d], gb + (size_t)ik * nD + off[d], nbas[d]);
+    }
+  if (ishift == 0) return;
+  for (int i = 0; i < rF; ++i, ++ik) {
+    gc[ik] = fabs(E) * fc[i];
+    memcpy(gb + (size_t)ik * nD, fb + (size_t)i * nD, sizeof(double) * nD);
+    if (E < 0.0)
+      for (int q = 0; q < n0; ++q) gb[(size_t)ik * nD + q] = -gb[(size_t)ik * nD + q];
+  }
+  const int s0 = ishift > 0 ? rFH : 0, s1 = ishift > 0 ? rFH + rF : rFH;
+  for (int r = s0; r < s1; ++r)
+    for (int q = 0; q < n0; ++q) gb[(size_t)r * nD + q] = -gb[(size_t)r * nD + q];
+}
+
+void orc_prodhv(const double *base, const double *coef, const int *nbas, int ndof, int rF, const int *opid,
+                const int *mptr, const double *Hcoef, const double *mat, int T, int ishift, double Eshift,
+                double *gbase, double *gcoef) {
+  int *off = make_offsets(nbas, ndof);
+  hoplist H = {T, ndof, opid, mptr, Hcoef, mat};
+  prodhv_explicit(&H, coef, base, rF, nbas, off, ndof, ishift, Eshift, gcoef, gbase);
+  free(off);
+}
+
+/* PowrRecurse (src/BlockPower.f90:49-73) for more than two modes (redND =
+ * ALS): npow times, w = PRODHV(v, ishift 1, E), v <- reduc_ALS of w from v
+ * (nloop sweeps; reduc_AB keeps v as the starting guess, its rank being the
+ * target rank), NORMCOEF(v).  Returns 1 on a NaN weight. */
+int orc_powr_recurse(double *base, double *coef, const int *nbas, int ndof, int rF, const int *opid, const int *mptr,
+                     const double *Hcoef, const double *mat, int T, int npow, double Eshift, int nloop) {
+  int *off = make_offsets(nbas, ndof);
+  const int nD = off[ndof], rG = rF * (T + 1);
+  hoplist H = {T, ndof, opid, mptr, Hcoef, mat};
+  double *gc = (double *)malloc(sizeof(double) * rG);
+  double *gb = (double *)malloc(sizeof(double) * (size_t)rG * nD);
+  int bad = 0;
+  for (int i = 0; i < npow && !bad; ++i) {
+    prodhv_explicit(&H, coef, base, rF, nbas, off, ndof, 1, Eshift, gc, gb);
+    bad = orc_reduc_als(gc, gb, rG, coef, base, rF, nbas, ndof, nloop);
+    if (!bad) normcoef(coef, base, rF, nbas, off, ndof);
+  }
+  free(gc); free(gb); free(off);
+  return bad;
+}
+
+/* GRAMORTHO (src/BlockUtils.f90:22-68, k = 0) and pGRAMORTHO (:72-123,
+ * vectors 0..k-1 already orthonormal): for each later vector i, NORMCOEF(Q_i),
+ * w_l = -<Q_i, Q_l> (l < i; OpenMP over l), v = Q_i + sum_l w_l Q_l built
+ * explicitly (SUMLCVEC: |w_l| in the weights, the sign in the first mode's
+ * factor), Q_i <- reduc_ALS of v from Q_i (nloop sweeps), NORMCOEF(Q_i).
+ * GRAMORTHO first normalises Q_0.  Returns the number of NaN events. */
+int orc_gramortho(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int k,
+                  int nloop, int nthreads) {
+  int *off = make_offsets(nbas, ndof), *toff = rank_offsets(ranks, nbloc);
+  const int nD = off[ndof], n0 = nbas[0], rtot = toff[nbloc];
+  double *w = (double *)malloc(sizeof(double) * nbloc);
+  double *vc = (double *)malloc(sizeof(double) * rtot);
+  double *vb = (double *)malloc(sizeof(double) * (size_t)rtot * nD);
+  int bad = 0;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#endif
+  (void)nthreads;
+  if (k <= 0) {
+    normcoef(coef, base, ranks[0], nbas, off, ndof);
+    k = 1;
+  }
+  for (int i = k; i < nbloc && !bad; ++i) {
+    double *qc = coef + toff[i], *qb = base + (size_t)toff[i] * nD;
+    normcoef(qc, qb, ranks[i], nbas, off, ndof);
+    w[i] = 1.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+    for (int l = 0; l < i; ++l)
+      w[l] = -prodvv_ab(qc, qb, ranks[i], coef + toff[l], base + (size_t)toff[l] * nD, ranks[l], nbas, ndof, nD);
+    const int rv = toff[i] + ranks[i];
+    for (int l = 0; l <= i; ++l)
+      for (int j = 0; j < ranks[l]; ++j) {
+        const int r = toff[l] + j;
+        vc[r] = fabs(w[l]) * coef[r];
+        memcpy(vb + (size_t)r * nD, base + (size_t)r * nD, sizeof(double) * nD);
+        if (w[l] < 0.0)
+          for (int q = 0; q < n0; ++q) vb[(size_t)r * nD + q] = -vb[(size_t)r * nD + q];
+      }
+    if (rv > ranks[i]) bad += orc_reduc_als(vc, vb, rv, qc, qb, ranks[i], nbas, ndof, nloop);
+    if (!bad) normcoef(qc, qb, ranks[i], nbas, off, ndof);
+  }
+  free(w); free(vc); free(vb); free(off); free(toff);
+  return bad;
+}

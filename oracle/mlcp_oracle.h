@@ -157,6 +157,21 @@ int orc_pals_cycle(double *base, double *coef, const int *nbas, int ndof, int nb
                    const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
                    int nals, int update, int ishift, double Eshift, double *eigv, int nthreads);
 
+/* PRODHV (src/MODHVECML.f90:50-110): the explicit (H - Eshift) F, rF T
+ * terms (plus rF with a shift) into gbase/gcoef. */
+void orc_prodhv(const double *base, const double *coef, const int *nbas, int ndof, int rF, const int *opid,
+                const int *mptr, const double *Hcoef, const double *mat, int T, int ishift, double Eshift,
+                double *gbase, double *gcoef);
+/* The plain power solver (solver powr), reductions by reduc_ALS (more than
+ * two modes).  PowrRecurse (src/BlockPower.f90:49-73) on one vector of rF
+ * terms. */
+int orc_powr_recurse(double *base, double *coef, const int *nbas, int ndof, int rF, const int *opid, const int *mptr,
+                     const double *Hcoef, const double *mat, int T, int npow, double Eshift, int nloop);
+/* GRAMORTHO (src/BlockUtils.f90:22-68) for k = 0, pGRAMORTHO (:72-123)
+ * with vectors 0..k-1 already orthonormal. */
+int orc_gramortho(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int k,
+                  int nloop, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

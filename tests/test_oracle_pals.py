@@ -9,7 +9,9 @@ vector updates.  They differ in one place only: the Fortran Rayleigh-Ritz
 step reads the upper triangle of the ALS-reduced QHQ (DSYGV 'U') and the GPU
 path the lower one.  Known answers cover the rest: exactly representable
 products, a numpy eigensolve of the upper triangle, and convergence to exact
-spectra.
+spectra.  The plain power solver's routines (solver powr: PRODHV,
+PowrRecurse, GRAMORTHO, reductions by reduc_ALS) are checked against dense
+products and exactly representable projections.
 """
 import numpy as np
 import pytest
@@ -210,3 +212,77 @@ def test_pals_cycle_tracks_gpu_algorithm_cycle():
     e_gpu, _ = _run(oracle.intertwine, hl, 6, 4, 15, 5, 5, seed=0)
     np.testing.assert_allclose(e_pals[:-1], ex[:-1], rtol=2e-5)
     np.testing.assert_allclose(e_pals, e_gpu, rtol=1e-3)
+
+
+# --- the plain power solver (solver powr): PRODHV, PowrRecurse, GRAMORTHO ---
+
+@pytest.mark.parametrize("ishift,E", [(0, 0.0), (1, 3.5), (1, -2.0), (-1, 3.5)])
+def test_prodhv_explicit_matches_dense(ishift, E):
+    hl = H.random_hoplist([3, 4, 3], 5, seed=12)
+    rng = np.random.default_rng(3)
+    F = rng.normal(size=(2, int(hl.nbas.sum())))
+    fc = rng.uniform(0.5, 1.5, 2)
+    gb, gc = oracle.prodhv(F, fc, hl.nbas, hl, ishift, E)
+    assert gc.size == 2 * (hl.nterms + (1 if ishift else 0)) and np.all(gc >= 0)
+    Hd = H.dense_hamiltonian(hl)
+    op = Hd if ishift == 0 else (Hd - E * np.eye(Hd.shape[0])) * (1 if ishift > 0 else -1)
+    want = op @ oracle.cp_dense(F, fc, hl.nbas).ravel()
+    assert rel(oracle.cp_dense(gb, gc, hl.nbas).ravel(), want) < 1e-13
+
+
+def test_powr_recurse_on_identity_hamiltonian():
+    """H = c I: every step is exactly representable, so the vector keeps its
+    direction (the sign of c - E) with unit norm."""
+    nb = [3, 4, 3, 2]
+    hl = H.build_hoplist(nb, [(1.5, {})])
+    rng = np.random.default_rng(8)
+    F = rng.normal(size=(3, sum(nb)))
+    fc = rng.uniform(0.5, 1.5, 3)
+    b, c = oracle.powr_recurse(F, fc, nb, hl, 1, 4.0, 10)
+    v0 = oracle.cp_dense(F, fc, nb)
+    v1 = oracle.cp_dense(b, c, nb)
+    assert rel(v1, -v0 / np.linalg.norm(v0)) < 1e-8
+
+
+def test_powr_recurse_moves_toward_ground_state():
+    hl = H.coupled_oscillators(3, 5)
+    ex = np.linalg.eigvalsh(H.dense_hamiltonian(hl))
+    rng = np.random.default_rng(2)
+    F = rng.uniform(-0.5, 0.5, size=(4, int(hl.nbas.sum())))
+    fc = np.ones(4)
+    rq0 = oracle.rayleigh_quotient(F, fc, hl.nbas, hl)
+    b, c = oracle.powr_recurse(F, fc, hl.nbas, hl, 40, ex[-1] + 1.0, 20)
+    rq = oracle.rayleigh_quotient(b, c, hl.nbas, hl)
+    assert abs(oracle.cp_dot(b, c, b, c, hl.nbas) - 1) < 1e-12
+    assert rq < rq0 and rq - ex[0] < 0.25 * (rq0 - ex[0])
+
+
+def test_gramortho_exact_projection():
+    """Q_0 = x (rank 1), Q_1 = x + y (rank 2), x and y orthogonal products:
+    Q_1 - <Q_1, Q_0> Q_0 = y is representable at rank 2, so GRAMORTHO
+    returns y / |y|."""
+    nb = [3, 4, 3]
+    rng = np.random.default_rng(1)
+    x = [rng.normal(size=n) for n in nb]
+    y = [rng.normal(size=n) for n in nb]
+    y[0] = y[0] - x[0] * (y[0] @ x[0]) / (x[0] @ x[0])  # orthogonal in mode 0
+    base = np.array([np.concatenate(x), np.concatenate(x), np.concatenate(y)])
+    coef = np.array([1.0, 1.0, 0.7])
+    b, c = oracle.gramortho(base, coef, nb, 0, 2, 30, ranks=[1, 2])
+    yd = oracle.cp_dense(base[2:], coef[2:], nb)
+    got = oracle.cp_dense(b[1:], c[1:], nb)
+    assert rel(got, yd / np.linalg.norm(yd)) < 1e-8
+    xd = oracle.cp_dense(base[:1], coef[:1], nb)
+    assert rel(oracle.cp_dense(b[:1], c[:1], nb), xd / np.linalg.norm(xd)) < 1e-13
+
+
+def test_pgramortho_keeps_leading_vectors():
+    hl = H.coupled_oscillators(3, 5)
+    nb = hl.nbas
+    Q, qc = start_block(nb, 3, 4, 9)
+    b0, c0 = oracle.gramortho(Q, qc, nb, 3, 4, 10)
+    b1, c1 = oracle.gramortho(b0, c0, nb, 3, 4, 10, k=2)
+    np.testing.assert_array_equal(b1[:6], b0[:6])
+    np.testing.assert_array_equal(c1[:6], c0[:6])
+    D = dense_block(b1, c1, nb, [3] * 4)
+    np.testing.assert_allclose(np.einsum("ij,ij->i", D, D), 1.0, atol=1e-12)
