@@ -14,6 +14,7 @@
 #include "als.cuh"
 #include "common.cuh"
 #include "context.cuh"
+#include "intertwine.cuh"
 
 namespace mlcp {
 
@@ -298,6 +299,8 @@ std::vector<AlsShape> als_candidates(int nvec, int rGmax, int rFmax, int npmax, 
 
 }  // namespace
 
+bool autotune_on() { return autotune_enabled(); }
+
 int als_run_shape(Context* ctx, const AlsJob& job, cudaStream_t st, const AlsShape* forced);
 
 // Runs one batched reduction; everything is enqueued on `st`.  The launch
@@ -406,6 +409,7 @@ int autotune_report(char* buf, int len) {
     }
     out += "\n";
   }
+  gs_tune_report(out);
   if (buf && len > 0) {
     strncpy(buf, out.c_str(), (size_t)len - 1);
     buf[len - 1] = 0;

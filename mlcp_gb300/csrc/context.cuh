@@ -47,6 +47,9 @@ struct Context {
 // Context of the current device (created on first use).
 Context* get_context(int* status);
 
+// Launch-shape searches on (mlcp_gb300_set_autotune, MLCP_GB300_AUTOTUNE).
+bool autotune_on();
+
 // Ensure the workspace holds at least `bytes`; returns its base pointer.
 // The previous contents are not preserved.
 int ensure_workspace(Context* ctx, size_t bytes, void** out);

@@ -400,6 +400,16 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
   const int* d_off = cb.meta + (ndof + 1);
   const int* d_offp = cb.meta + 2 * (ndof + 1);
   const int* d_rank = ranks ? cb.meta + 3 * (ndof + 1) : nullptr;
+  // The Gram-Schmidt cluster size: measured once per block shape (on a
+  // scratch copy of the block, in qn, before anything is captured)
+  int gs_cl = 0;
+  if (nals > 0 && autotune_on()) {
+    GsParams g{};
+    g.D = ndof; g.R = R; g.nbloc = B; g.nD = Ly.nD; g.nDp = Ly.nDp; g.npmax = Ly.npmax; g.nals = nals;
+    g.nbas = d_nbas; g.off = d_off; g.offp = d_offp; g.base = cb.q; g.coef = cb.qc;
+    g.work = cb.gsw; g.status = cb.status + B; g.rank_v = d_rank;
+    if ((rc = gs_tuned_cluster(g, ctx->device, cb.qn, cb.qnc, st, &gs_cl))) return rc;
+  }
   // The device part of the cycle: status reset, POW_ALS, Gram-Schmidt,
   // PRODHV_ALS, Rayleigh-Ritz and the vector updates.  Every input it reads
   // (block, weights, shifts, ranks, operator table) sits in device buffers
@@ -423,7 +433,7 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
       GsParams g{};
       g.D = ndof; g.R = R; g.nbloc = B; g.nD = Ly.nD; g.nDp = Ly.nDp; g.npmax = Ly.npmax; g.nals = nals;
       g.nbas = d_nbas; g.off = d_off; g.offp = d_offp; g.base = cb.q; g.coef = cb.qc;
-      g.work = cb.gsw; g.status = cb.status + B; g.rank_v = d_rank;
+      g.work = cb.gsw; g.status = cb.status + B; g.rank_v = d_rank; g.cl = gs_cl;
       if (int r = gs_launch(g, st)) return r;
     }
     if (update) {
@@ -461,7 +471,8 @@ int intertwine_cycle(Context* ctx, double* base, double* coef, const int* nbas, 
                                         (unsigned long long)(uintptr_t)tab.alpha, (unsigned long long)ndof,
                                         (unsigned long long)R, (unsigned long long)B, (unsigned long long)T,
                                         (unsigned long long)npow, (unsigned long long)nals,
-                                        (unsigned long long)update, (unsigned long long)(ishift + 8),
+                                        (unsigned long long)update,
+                                        (unsigned long long)(ishift + 8) | ((unsigned long long)gs_cl << 8),
                                         (unsigned long long)(ranks != nullptr), (unsigned long long)Ly.nD,
                                         (unsigned long long)Ly.nDp,
                                         ((unsigned long long)tab.utot << 40) | ((unsigned long long)tab.umax << 20) |

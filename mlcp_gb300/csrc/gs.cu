@@ -32,6 +32,11 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
 
 #include "common.cuh"
 #include "dword.cuh"
@@ -653,9 +658,10 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
 }
 
 // CTAs per cluster: 16 (the non-portable maximum) unless the block is
-// smaller; MLCP_GB300_GS_CLUSTER fixes a smaller size (measurements).
-int gs_cluster_size(int nbloc) {
-  int cl = 16;
+// smaller or the caller asks for `pref` (the measured choice of
+// gs_tuned_cluster); MLCP_GB300_GS_CLUSTER fixes a size (measurements).
+int gs_cluster_size(int nbloc, int pref) {
+  int cl = pref > 0 ? std::max(2, std::min(16, pref)) : 16;
   if (const char* e = getenv("MLCP_GB300_GS_CLUSTER")) cl = std::max(2, std::min(16, atoi(e)));
   return nbloc > cl ? cl : (nbloc > 1 ? nbloc - 1 : 1);
 }
@@ -666,16 +672,19 @@ namespace {
 // per 16 SMs); the scratch is sized for it.
 constexpr int kMaxGroups = 9;
 
-int gs_nkmax(int nbloc, int ngrp) {
-  const int nc = gs_cluster_size(nbloc) * ngrp;
+// Cluster sizes the search tries (each clamped to the block).
+constexpr int kClusterCandidates[] = {16, 12, 8};
+
+int gs_nkmax(int nbloc, int ngrp, int cl) {
+  const int nc = gs_cluster_size(nbloc, cl) * ngrp;
   return std::max(1, (nbloc - 1 + nc - 1) / nc);
 }
 
 // Global scratch entries (dw) of one CTA with every movable group there.
-size_t gs_cta_work(int nbloc, int R, int nD, int D, int npm, int ngrp) {
+size_t gs_cta_work(int nbloc, int R, int nD, int D, int npm, int ngrp, int cl) {
   GsArrays a;
   size_t gw = 0;
-  gs_carve(GsDims{R, D, nD, npm, gs_nkmax(nbloc, ngrp), kGroupAll}, &a, nullptr, nullptr, &gw);
+  gs_carve(GsDims{R, D, nD, npm, gs_nkmax(nbloc, ngrp, cl), kGroupAll}, &a, nullptr, nullptr, &gw);
   return gw;
 }
 
@@ -685,8 +694,8 @@ bool gs_fit(const GsParams& p, int ngrp, int smem_max, int* gmask, size_t* smem)
   static const int masks[4] = {0, kGroupQ, kGroupQ | kGroupP, kGroupAll};
   for (int q = 0; q < 4; ++q) {
     GsArrays a;
-    const size_t b = gs_carve(GsDims{p.R, p.D, p.nD, p.npmax, gs_nkmax(p.nbloc, ngrp), masks[q]}, &a, nullptr,
-                              nullptr, nullptr);
+    const size_t b = gs_carve(GsDims{p.R, p.D, p.nD, p.npmax, gs_nkmax(p.nbloc, ngrp, p.cl), masks[q]}, &a,
+                              nullptr, nullptr, nullptr);
     if (b <= (size_t)smem_max) {
       *gmask = masks[q];
       *smem = b;
@@ -701,10 +710,17 @@ bool gs_fit(const GsParams& p, int ngrp, int smem_max, int* gmask, size_t* smem)
 size_t gs_work_doubles(int nbloc, int R, int nD, int D, int npm) {
   // the per-CTA scratch of the largest grid (one cluster owns the most per
   // CTA, so size the scratch for every CTA of kMaxGroups clusters at the
-  // one-cluster share), then the cluster partials and the arrival counter
-  const size_t per = gs_cta_work(nbloc, R, nD, D, npm, 1);
-  return (size_t)gs_cluster_size(nbloc) * kMaxGroups * per + (size_t)2 * kMaxGroups * R * npm + 2;
+  // one-cluster share), for every cluster size the search may pick, then
+  // the cluster partials and the arrival counter
+  size_t most = 0;
+  for (int c : kClusterCandidates) {
+    const int cl = gs_cluster_size(nbloc, c);
+    most = std::max(most, (size_t)cl * kMaxGroups * gs_cta_work(nbloc, R, nD, D, npm, 1, c));
+  }
+  return most + (size_t)2 * kMaxGroups * R * npm + 2;
 }
+
+namespace {
 
 // Clusters for a block: one when everything fits in shared memory (small
 // blocks are bound by the latency of each mode step, and a grid-wide step
@@ -715,15 +731,17 @@ int gs_groups(const GsParams& p, int num_sms, int smem_max) {
   int gmask = 0;
   size_t smem = 0;
   if (gs_fit(p, 1, smem_max, &gmask, &smem) && gmask == 0) return 1;
-  const int cl = gs_cluster_size(p.nbloc);
+  const int cl = gs_cluster_size(p.nbloc, p.cl);
   int g = std::min(kMaxGroups, num_sms / cl);
   g = std::min(g, (p.nbloc - 1 + cl - 1) / cl);
   return std::max(1, g);
 }
 
+}  // namespace
+
 int gs_launch(const GsParams& prm, cudaStream_t st) {
   GsParams p = prm;
-  const int cl = gs_cluster_size(p.nbloc);
+  const int cl = gs_cluster_size(p.nbloc, p.cl);
   int dev = 0, smem_max = 0, nsm = 0;
   MLCP_CUDA_TRY(cudaGetDevice(&dev));
   MLCP_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -732,8 +750,8 @@ int gs_launch(const GsParams& prm, cudaStream_t st) {
   int ngrp = env ? std::max(1, std::min(kMaxGroups, atoi(env))) : gs_groups(p, nsm, smem_max);
   if (ngrp * cl > nsm) ngrp = std::max(1, nsm / cl);
   p.ngrp = ngrp;
-  p.nkmax = gs_nkmax(p.nbloc, ngrp);
-  p.work_stride = (long long)gs_cta_work(p.nbloc, p.R, p.nD, p.D, p.npmax, ngrp);
+  p.nkmax = gs_nkmax(p.nbloc, ngrp, p.cl);
+  p.work_stride = (long long)gs_cta_work(p.nbloc, p.R, p.nD, p.D, p.npmax, ngrp, p.cl);
   size_t smem = 0;
   int gmask = 0;
   if (!gs_fit(p, ngrp, smem_max, &gmask, &smem)) {
@@ -767,6 +785,115 @@ int gs_launch(const GsParams& prm, cudaStream_t st) {
   cfg.numAttrs = ngrp > 1 ? 2 : 1;
   MLCP_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, p));
   return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// Cluster-size search
+// ---------------------------------------------------------------------------
+// A larger cluster spreads the earlier vectors over more CTAs but pays a
+// longer gather and cluster barrier at every mode step; which wins depends on
+// the block (measured on the 40-vector rank-16 block: 16 CTAs 27.7 ms per
+// cycle, 12 CTAs 28.7, 8 CTAs 31.2).  The first cycle of a block shape runs
+// one Gram-Schmidt sweep (nals = 1) with each candidate size on a scratch
+// copy of the block, times it with CUDA events on the cycle's stream and
+// caches the fastest for the process, per device and shape.  Off with
+// mlcp_gb300_set_autotune(0) / MLCP_GB300_AUTOTUNE=0 or a fixed
+// MLCP_GB300_GS_CLUSTER (then the 16-CTA rule applies).
+
+namespace {
+
+struct GsTuneKey {
+  int device, nbloc, R, D, nD, npmax, ragged;
+  bool operator<(const GsTuneKey& o) const {
+    return std::tie(device, nbloc, R, D, nD, npmax, ragged) <
+           std::tie(o.device, o.nbloc, o.R, o.D, o.nD, o.npmax, o.ragged);
+  }
+};
+
+struct GsTuneEntry {
+  int cl = 0;
+  std::vector<std::pair<int, float>> trials;  // (cluster size, ms of one sweep)
+};
+
+std::mutex g_gs_tune_mu;
+std::map<GsTuneKey, GsTuneEntry> g_gs_tune;
+
+}  // namespace
+
+int gs_tuned_cluster(const GsParams& p, int device, double* scratch_base, double* scratch_coef, cudaStream_t st,
+                     int* cl_out) {
+  *cl_out = 0;
+  if (getenv("MLCP_GB300_GS_CLUSTER") || p.nals <= 0) return kOk;
+  const GsTuneKey key{device, p.nbloc, p.R, p.D, p.nD, p.npmax, p.rank_v != nullptr};
+  {
+    std::lock_guard<std::mutex> lk(g_gs_tune_mu);
+    auto it = g_gs_tune.find(key);
+    if (it != g_gs_tune.end()) {
+      *cl_out = it->second.cl;
+      return kOk;
+    }
+  }
+  std::vector<int> cand;
+  for (int c : kClusterCandidates) {
+    const int cl = gs_cluster_size(p.nbloc, c);
+    if (std::find(cand.begin(), cand.end(), cl) == cand.end()) cand.push_back(cl);
+  }
+  GsTuneEntry entry;
+  if (cand.size() > 1) {
+    const size_t nvals = (size_t)p.nbloc * p.R * p.nD, ncoef = (size_t)p.nbloc * p.R;
+    cudaEvent_t e0, e1;
+    MLCP_CUDA_TRY(cudaEventCreate(&e0));
+    MLCP_CUDA_TRY(cudaEventCreate(&e1));
+    int rc = kOk;
+    float best = 0.f;
+    for (int cl : cand) {
+      MLCP_CUDA_TRY(cudaMemcpyAsync(scratch_base, p.base, sizeof(double) * nvals, cudaMemcpyDeviceToDevice, st));
+      MLCP_CUDA_TRY(cudaMemcpyAsync(scratch_coef, p.coef, sizeof(double) * ncoef, cudaMemcpyDeviceToDevice, st));
+      GsParams t = p;
+      t.base = scratch_base;
+      t.coef = scratch_coef;
+      t.nals = 1;
+      t.cl = cl;
+      MLCP_CUDA_TRY(cudaEventRecord(e0, st));
+      if ((rc = gs_launch(t, st))) break;
+      MLCP_CUDA_TRY(cudaEventRecord(e1, st));
+      MLCP_CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      MLCP_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+      entry.trials.push_back({cl, ms});
+      if (entry.trials.size() == 1 || ms < best) {
+        best = ms;
+        entry.cl = cl;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+  } else {
+    entry.cl = cand.empty() ? 0 : cand[0];
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_gs_tune_mu);
+    g_gs_tune[key] = entry;
+  }
+  *cl_out = entry.cl;
+  return kOk;
+}
+
+void gs_tune_report(std::string& out) {
+  std::lock_guard<std::mutex> lk(g_gs_tune_mu);
+  char line[160];
+  for (const auto& kv : g_gs_tune) {
+    const GsTuneKey& k = kv.first;
+    snprintf(line, sizeof(line), "gs nbloc=%d R=%d ndof=%d nD=%d%s: cluster %d;", k.nbloc, k.R, k.D, k.nD,
+             k.ragged ? " ragged" : "", kv.second.cl);
+    out += line;
+    for (const auto& t : kv.second.trials) {
+      snprintf(line, sizeof(line), " %d=%.3fms", t.first, t.second);
+      out += line;
+    }
+    out += "\n";
+  }
 }
 
 }  // namespace mlcp

@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "dword.cuh"
 
 namespace mlcp {
@@ -77,6 +79,7 @@ struct GsParams {
   double* work;   // per-CTA scratch for the arrays that do not fit in shared memory (gs_work_doubles)
   int* status;
   const int* rank_v;  // [nbloc] ranks <= R (terms beyond carry zero weight), or null: all R
+  int cl;             // CTAs per cluster asked for (0: the 16-CTA rule; see gs_tuned_cluster)
   // set by gs_launch
   int nkmax;             // earlier vectors owned by one CTA, at most
   int gmask;             // array groups placed in global scratch
@@ -86,6 +89,14 @@ struct GsParams {
   unsigned* xctr;        // [0] arrivals of the cluster leaders, [1] abort word; zeroed before the launch (ngrp > 1)
 };
 int gs_launch(const GsParams& p, cudaStream_t st);
+// The measured cluster size for p's block shape (cached per process, device
+// and shape; the first call times one sweep per candidate size on a scratch
+// copy of the block, scratch_base/scratch_coef of the block's size).  *cl
+// receives 0 (the rule) when the search is off or the size is fixed.
+int gs_tuned_cluster(const GsParams& p, int device, double* scratch_base, double* scratch_coef, cudaStream_t st,
+                     int* cl);
+// Appends one line per tuned block shape to out.
+void gs_tune_report(std::string& out);
 // Doubles of GsParams::work needed for a block of nbloc vectors (npm: the
 // largest 4-padded basis size).
 size_t gs_work_doubles(int nbloc, int R, int nD, int D, int npm);

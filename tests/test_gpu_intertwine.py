@@ -354,3 +354,32 @@ def test_gram_schmidt_over_several_clusters(case, groups, cuda_device, monkeypat
         compare_blocks(gb, gc, res[1][0], res[1][1], hl.nbas, rk, nbloc, tol=1e-9)
     finally:
         L.mlcp_gb300_set_cycle_graph(1)
+
+
+@pytest.mark.gpu
+def test_gram_schmidt_cluster_search(cuda_device):
+    """The first cycle of a block shape times one Gram-Schmidt sweep for each
+    candidate cluster size (16, 12 and 8 CTAs) on a scratch copy of the block
+    and keeps the fastest; the autotune report lists the trials.  The cycle
+    with the search off (the 16-CTA rule) agrees with it to 1e-9 (the cluster
+    size only changes the order of the partial sums)."""
+    from mlcp_gb300 import _lib
+    L = _lib.load()
+    hl = H.henon_heiles(D=4, n=6, lam=0.111803)
+    rk, nbloc = 5, 20
+    Q, qc = start_block(hl.nbas, rk, nbloc, seed=21)
+    eig0 = np.arange(nbloc, dtype=float)
+    tb, tc, te = IT.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, eig0, 2, 3, True, 1, 30.0)
+    lines = [ln for ln in _lib.autotune_report().splitlines() if ln.startswith(f"gs nbloc={nbloc} R={rk} ")]
+    assert len(lines) == 1, _lib.autotune_report()
+    chosen = int(lines[0].split("cluster ")[1].split(";")[0])
+    trials = dict((int(a), float(b[:-2])) for a, b in (t.split("=") for t in lines[0].split(";")[1].split()))
+    assert sorted(trials) == [8, 12, 16] and chosen in trials
+    assert trials[chosen] == min(trials.values())
+    L.mlcp_gb300_set_autotune(0)
+    try:
+        rb, rc, re_ = IT.intertwine(Q, qc, hl.nbas, rk, nbloc, hl, eig0, 2, 3, True, 1, 30.0)
+    finally:
+        L.mlcp_gb300_set_autotune(1)
+    np.testing.assert_allclose(te, re_, rtol=1e-9)
+    compare_blocks(tb, tc, rb, rc, hl.nbas, rk, nbloc, tol=1e-9)
