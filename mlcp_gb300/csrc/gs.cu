@@ -749,39 +749,52 @@ int gs_launch(const GsParams& prm, cudaStream_t st) {
   const char* env = getenv("MLCP_GB300_GS_GROUPS");  // a fixed cluster count (tests)
   int ngrp = env ? std::max(1, std::min(kMaxGroups, atoi(env))) : gs_groups(p, nsm, smem_max);
   if (ngrp * cl > nsm) ngrp = std::max(1, nsm / cl);
-  p.ngrp = ngrp;
-  p.nkmax = gs_nkmax(p.nbloc, ngrp, p.cl);
-  p.work_stride = (long long)gs_cta_work(p.nbloc, p.R, p.nD, p.D, p.npmax, ngrp, p.cl);
+  void (*kern)(GsParams) = nullptr;
   size_t smem = 0;
-  int gmask = 0;
-  if (!gs_fit(p, ngrp, smem_max, &gmask, &smem)) {
-    set_error("intertwinecpp_: Gram-Schmidt needs more shared memory than %d bytes (rank %d)", smem_max, p.R);
-    return kTooLarge;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[2];
+  for (int pass = 0;; ++pass) {
+    p.ngrp = ngrp;
+    p.nkmax = gs_nkmax(p.nbloc, ngrp, p.cl);
+    p.work_stride = (long long)gs_cta_work(p.nbloc, p.R, p.nD, p.D, p.npmax, ngrp, p.cl);
+    int gmask = 0;
+    if (!gs_fit(p, ngrp, smem_max, &gmask, &smem)) {
+      set_error("intertwinecpp_: Gram-Schmidt needs more shared memory than %d bytes (rank %d)", smem_max, p.R);
+      return kTooLarge;
+    }
+    p.gmask = gmask;
+    kern = p.gmask == 0 ? gs_kernel<true> : gs_kernel<false>;
+    MLCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (cl > 8) MLCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cfg = {};
+    cfg.gridDim = dim3(cl * ngrp);
+    cfg.blockDim = dim3(kGsThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    // several clusters wait on one another each step: all of them must be
+    // resident together, which a cooperative launch guarantees (or refuses)
+    attr[1].id = cudaLaunchAttributeCooperative;
+    attr[1].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (ngrp == 1) break;
+    // no more clusters than the GPU holds at once at this size and shared
+    // memory (the GPCs bound how many clusters of 8-16 CTAs fit); with fewer
+    // clusters each CTA owns more earlier vectors, so the layout is redone
+    int maxc = 0;
+    MLCP_CUDA_TRY(cudaOccupancyMaxActiveClusters(&maxc, (const void*)kern, &cfg));
+    if (maxc >= ngrp || pass >= 3) break;
+    ngrp = std::max(1, maxc);
   }
-  p.gmask = gmask;
   // the cluster partials and the arrival counter follow the per-CTA scratch
   dw* after = reinterpret_cast<dw*>(p.work) + (size_t)cl * ngrp * p.work_stride;
   p.xpart = after;
   p.xctr = reinterpret_cast<unsigned*>(after + (size_t)2 * kMaxGroups * p.R * p.npmax);
   if (ngrp > 1) MLCP_CUDA_TRY(cudaMemsetAsync(p.xctr, 0, 2 * sizeof(unsigned), st));  // arrivals, abort word
-  void (*kern)(GsParams) = p.gmask == 0 ? gs_kernel<true> : gs_kernel<false>;
-  MLCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (cl > 8) MLCP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(cl * ngrp);
-  cfg.blockDim = dim3(kGsThreads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = st;
-  cudaLaunchAttribute attr[2];
-  attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = cl;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  // several clusters wait on one another each step: all of them must be
-  // resident together, which a cooperative launch guarantees (or refuses)
-  attr[1].id = cudaLaunchAttributeCooperative;
-  attr[1].val.cooperative = 1;
-  cfg.attrs = attr;
   cfg.numAttrs = ngrp > 1 ? 2 : 1;
   MLCP_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, p));
   return kOk;
@@ -844,7 +857,6 @@ int gs_tuned_cluster(const GsParams& p, int device, double* scratch_base, double
     cudaEvent_t e0, e1;
     MLCP_CUDA_TRY(cudaEventCreate(&e0));
     MLCP_CUDA_TRY(cudaEventCreate(&e1));
-    int rc = kOk;
     float best = 0.f;
     for (int cl : cand) {
       MLCP_CUDA_TRY(cudaMemcpyAsync(scratch_base, p.base, sizeof(double) * nvals, cudaMemcpyDeviceToDevice, st));
@@ -855,7 +867,10 @@ int gs_tuned_cluster(const GsParams& p, int device, double* scratch_base, double
       t.nals = 1;
       t.cl = cl;
       MLCP_CUDA_TRY(cudaEventRecord(e0, st));
-      if ((rc = gs_launch(t, st))) break;
+      if (gs_launch(t, st) != kOk) {  // a size this GPU cannot launch for the block: no candidate
+        cudaGetLastError();
+        continue;
+      }
       MLCP_CUDA_TRY(cudaEventRecord(e1, st));
       MLCP_CUDA_TRY(cudaEventSynchronize(e1));
       float ms = 0.f;
@@ -868,7 +883,6 @@ int gs_tuned_cluster(const GsParams& p, int device, double* scratch_base, double
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    if (rc) return rc;
   } else {
     entry.cl = cand.empty() ? 0 : cand[0];
   }
