@@ -640,6 +640,7 @@ def run_gpu(args):
         if not args.no_fp64 and ws == 1:
             cyc_ms = line["power_cycle"]["gpu_ms_per_cycle"] if "power_cycle" in line else None
             line["fp64_gpu_baseline"] = fp64_gpu_baseline(batch, gcoef, gbase, e2e_value, cyc_ms)
+        line["autotune"] = _lib.autotune_report().strip().splitlines()  # with the legs' Gram-Schmidt shapes
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
