@@ -272,8 +272,11 @@ MLCP_API int mlcp_ws_apply(int nvec, int ndof, int n, int rank, const long long 
  * device-resident reduction of a batch shape times one sweep for every
  * feasible (cluster size, tile-ring depth) pair on the caller's data, F
  * restored after each, and caches the fastest per device and shape; the call
- * synchronises its stream while it tunes.  The report lists each cached
- * choice with its trial times; returns the report's length. */
+ * synchronises its stream while it tunes.  The same switch covers the power
+ * cycle's Gram-Schmidt: the first cycle of a block shape times one sweep with
+ * clusters of 16, 12 and 8 CTAs on a scratch copy of the block and keeps the
+ * fastest.  The report lists each cached choice with its trial times (lines
+ * "als ..." and "gs ..."); returns the report's length. */
 MLCP_API void mlcp_gb300_set_autotune(int enable);
 MLCP_API int mlcp_gb300_autotune_report(char *buf, int len);
 
