@@ -433,6 +433,15 @@ def run_cycle_bench(steps: int, cpu: bool):
         t0 = time.perf_counter()
         oracle.pals_cycle(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh)
         out["pals_cpu_ms_per_cycle"] = 1e3 * (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        pb, pc = oracle.pals_pow3(Q, qc, hl.nbas, CYC_R, CYC_B, hl, CYC_NPOW, 1, esh)
+        t1 = time.perf_counter()
+        pb, pc = oracle.pals_ortho2(pb, pc, hl.nbas, CYC_R, CYC_B, CYC_NALS)
+        t2 = time.perf_counter()
+        oracle.pals_diagonalize(pb, pc, hl.nbas, CYC_R, CYC_B, hl, CYC_NALS)
+        t3 = time.perf_counter()
+        out["pals_cpu_stage_ms"] = {"ALS_POW3": 1e3 * (t1 - t0), "ALS_ORTHO_2": 1e3 * (t2 - t1),
+                                    "Diagonalize": 1e3 * (t3 - t2)}
         out["cpu_threads"] = os.cpu_count()
         t0 = time.perf_counter()
         oracle.qhq_diag(gb, gc, hl.nbas, CYC_R, CYC_B, hl)
