@@ -648,6 +648,8 @@ def pals_sumlcvec2(base, coef, nbas, rk, nbloc, U, nitn, ranks=None, nthreads=0)
 def pals_diagonalize(base, coef, nbas, rk, nbloc, hl, nitn, ranks=None, nthreads=0):
     """Diagonalize with intertwining (src/BlockUtils.f90:184-225); returns
     (base, coef, eigenvalues, U with U[:, i] = eigenvector i)."""
+    if nitn < 1:
+        raise ValueError("Diagonalize with intertwining needs nitn >= 1 (PRODHV_ALS2 returns no H Q_i otherwise)")
     base, coef, rv = _block(base, coef, nbloc, rk, ranks)
     nb = np.ascontiguousarray(nbas, dtype=np.int32)
     eig = np.zeros(nbloc)
@@ -661,6 +663,8 @@ def pals_diagonalize(base, coef, nbas, rk, nbloc, hl, nitn, ranks=None, nthreads
 def pals_cycle(base, coef, nbas, rk, nbloc, hl, eigv, npow, nals, update=True, ishift=1, Eshift=0.0, nconv=0,
                ranks=None, nthreads=0):
     """One cycle of the Fortran host's CPU solver; returns (base, coef, eigv)."""
+    if update and nals < 1:
+        raise ValueError("the cycle's diagonalisation needs nals >= 1 (PRODHV_ALS2 returns no H Q_i otherwise)")
     base, coef, rv = _block(base, coef, nbloc, rk, ranks)
     eig = np.ascontiguousarray(eigv, dtype=np.float64).copy()
     nb = np.ascontiguousarray(nbas, dtype=np.int32)

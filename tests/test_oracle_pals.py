@@ -286,3 +286,22 @@ def test_pgramortho_keeps_leading_vectors():
     np.testing.assert_array_equal(c1[:6], c0[:6])
     D = dense_block(b1, c1, nb, [3] * 4)
     np.testing.assert_allclose(np.einsum("ij,ij->i", D, D), 1.0, atol=1e-12)
+
+
+def test_pals_edge_cases():
+    hl = H.coupled_oscillators(3, 4)
+    nb = hl.nbas
+    Q, qc = start_block(nb, 3, 1, 4)
+    # one vector: the Gram-Schmidt only normalises, the Rayleigh-Ritz value is <Q|H Q>_ALS / <Q|Q>
+    b, c, e = oracle.pals_cycle(Q, qc, nb, 3, 1, hl, np.zeros(1), 2, 3, True, 1, 20.0)
+    assert e.shape == (1,) and np.isfinite(e[0])
+    assert abs(oracle.cp_dot(b, c, b, c, nb) - 1) < 1e-12
+    # zero sweeps leave the vectors alone
+    b0, c0 = oracle.pals_pow3(Q, qc, nb, 3, 1, hl, 0)
+    np.testing.assert_array_equal(b0, Q)
+    b0, c0 = oracle.pals_sumlcvec2(Q, qc, nb, 3, 1, np.eye(1), 0)
+    np.testing.assert_array_equal(c0, qc)
+    with pytest.raises(ValueError):
+        oracle.pals_ortho2(Q, qc, nb, 3, 1, 2, ranks=[2])
+    with pytest.raises(ValueError):
+        oracle.pals_diagonalize(Q, qc, nb, 3, 1, hl, 0)
