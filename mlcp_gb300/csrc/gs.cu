@@ -41,6 +41,7 @@
 #include "common.cuh"
 #include "dword.cuh"
 #include "dwsolve.cuh"
+#include "fastdiv.cuh"
 #include "intertwine.cuh"
 
 namespace cg = cooperative_groups;
@@ -70,6 +71,7 @@ struct GsArrays {
   float *gi, *rred;
   dwsolve::ColScratch cs;
   int *nb, *off, *flags;
+  FastDiv* fd;  // divisors of the step's index splits: R, R*R, RRp, then R*n_d per mode
 };
 
 // Entries of R*R rounded up to whole warps.
@@ -127,6 +129,7 @@ __host__ __device__ inline size_t gs_carve(const GsDims& m, GsArrays* a, unsigne
   a->nb = (int*)take_s(sizeof(int) * (m.D + 1));
   a->off = (int*)take_s(sizeof(int) * (m.D + 1));
   a->flags = (int*)take_s(sizeof(int) * 4);
+  a->fd = (FastDiv*)take_s(sizeof(FastDiv) * (m.D + 3));
   if (gwork) *gwork = go;
   return so;
 }
@@ -274,10 +277,12 @@ __device__ void step_products(const Gs& c, int j, int nk, bool pre, int t0, dw q
   const dw pen = c.a.misc[0];
   for (int e = c.tid - t0; e < total; e += kGsThreads - t0) {
     if (e < npsn) {  // whole warps: npsn is a multiple of 32
-      const int kl = e / RRp, ee = e - kl * RRp;
+      int kl, ee;
+      c.a.fd[2].divmod((unsigned)e, &kl, &ee);
       dw contrib = dw_make(0.f);
       if (ee < RR) {
-        const int r = ee / R, i = ee - r * R;
+        int r, i;
+        c.a.fd[0].divmod((unsigned)ee, &r, &i);
         const dw* Pk = c.a.P + (size_t)kl * D * RR + ee;
         const dw pj = Pk[(size_t)j * RR], w = dw_mul(c.a.qc[(size_t)kl * R + r], dw_mul(c.a.fcs[i], qinv));
         dw prod;
@@ -299,9 +304,13 @@ __device__ void step_products(const Gs& c, int j, int nk, bool pre, int t0, dw q
       for (int d = 0; d < D; ++d)
         if (d != j) prod = dw_mul(prod, c.a.g[(size_t)d * RR + ee]);
       c.a.Gp[ee] = prod;
-      c.a.BB[ee] = mask_bb(c, ee % R, ee / R, (ee % R == ee / R) ? dw_add(prod, pen) : prod);
+      int i2, i;
+      c.a.fd[0].divmod((unsigned)ee, &i2, &i);
+      c.a.BB[ee] = mask_bb(c, i, i2, (i == i2) ? dw_add(prod, pen) : prod);
     } else {
-      const int ee = e - ngp, r = ee % R, m = ee / R;
+      const int ee = e - ngp;
+      int m, r;
+      c.a.fd[0].divmod((unsigned)ee, &m, &r);
       c.a.wf[ee] = dw_mul(dw_mul(c.a.fcs[r], qinv), c.a.fb[(size_t)r * c.nD + offj + m]);
     }
   }
@@ -317,8 +326,12 @@ __device__ void step_products(const Gs& c, int j, int nk, bool pre, int t0, dw q
 __device__ void step_dots(const Gs& c, int j, int nk, int w0) {
   const int R = c.R, RR = c.RR, nj = c.a.nb[j], offj = c.a.off[j], Rn = R * nj, half = (R + 1) / 2;
   const int total = (nk + 1) * 2 * Rn, w = c.tid - w0, nw = kGsThreads - w0;
+  const FastDiv fdrn = c.a.fd[3 + j];
   for (int e = w; e < total; e += nw) {
-    const int sh = e / Rn, em = e - sh * Rn, s = sh >> 1, i = em % R, m = em / R;
+    int sh, em, m, i;
+    fdrn.divmod((unsigned)e, &sh, &em);
+    c.a.fd[0].divmod((unsigned)em, &m, &i);
+    const int s = sh >> 1;
     const int r0 = (sh & 1) ? half : 0, r1 = (sh & 1) ? R : half;
     dw_acc acc = acc_zero();
     if (s == 0) {
@@ -456,7 +469,8 @@ __device__ void step_solve(const Gs& c, int j, const float* inv, bool gj_ok) {
 __device__ void step_preproducts(const Gs& c, int j, int jn, int nk, int t0, int nt) {
   const int RR = c.RR, D = c.D;
   for (int e = t0; e < (nk + 1) * RR; e += nt) {
-    const int kl = e / RR, ee = e - kl * RR;
+    int kl, ee;
+    c.a.fd[1].divmod((unsigned)e, &kl, &ee);
     const bool own = kl < nk;
     const dw* src = own ? c.a.P + (size_t)kl * D * RR + ee : c.a.g + ee;
     dw prod = dw_make(1.f);
@@ -479,10 +493,13 @@ __device__ dw step_update(const Gs& c, int j, int jn, int nk, bool pre) {
   dw qpart = dw_make(0.f);
   for (int e = c.tid; e < total; e += kGsThreads) {
     if (e < Rn) {
-      const int i = e % R, m = e / R;
+      int m, i;
+      c.a.fd[0].divmod((unsigned)e, &m, &i);
       c.a.fb[(size_t)i * c.nD + offj + m] = c.a.X[e];
     } else if (e < Rn + RR) {
-      const int ee = e - Rn, i = ee % R, i2 = ee / R;
+      const int ee = e - Rn;
+      int i2, i;
+      c.a.fd[0].divmod((unsigned)ee, &i2, &i);
       if (i > i2) continue;
       const int et = i2 + i * R;
       // prod_{d != j} G_d: Gp, or with `pre` pGp = prod_{d not in {j, jn}} G_d times G_jn
@@ -504,7 +521,9 @@ __device__ dw step_update(const Gs& c, int j, int jn, int nk, bool pre) {
         c.a.BB[et] = c.a.BB[ee];
       }
     } else {
-      const int ee = e - Rn - RR, kl = ee / RR, e2 = ee - kl * RR, r = e2 / R, i = e2 - r * R;
+      int kl, e2, r, i;
+      c.a.fd[1].divmod((unsigned)(e - Rn - RR), &kl, &e2);
+      c.a.fd[0].divmod((unsigned)e2, &r, &i);
       const dw* x = c.a.qf + ((size_t)kl * R + r) * c.nD + offj;
       const dw pre_k = pre ? c.a.ppsn[(size_t)kl * RR + e2] : dw_make(1.f);
       dw_acc acc = acc_zero();
@@ -550,6 +569,8 @@ __global__ void __launch_bounds__(kGsThreads, 1) gs_kernel(GsParams p) {
     c.a.nb[d] = d < c.D ? p.nbas[d] : 0;
     c.a.off[d] = p.off[d];
   }
+  for (int q = c.tid; q < c.D + 3; q += kGsThreads)
+    c.a.fd[q] = FastDiv((unsigned)(q == 0 ? c.R : q == 1 ? c.RR : q == 2 ? c.RRp : c.R * p.nbas[q - 3]));
   if (c.tid == 0) c.a.flags[1] = 0;
   __syncthreads();
 
