@@ -469,13 +469,14 @@ def run_cycle_bench(steps: int, cpu: bool):
 
 # Learned warm start inside a power iteration: a 6-mode quartic force field
 # of 8 functions per mode, 24 vectors of rank 30, (H - 30000) F reduced back
-# to rank 30 each cycle; cycles 1-5 train, 6-8 are judged.
+# to rank 30 each cycle; cycles 1-5 train, 6-8 are tested.
 WS_D, WS_N, WS_RANK, WS_NVEC, WS_SHIFT = 6, 8, 30, 24, 30000.0
 
 
 def run_warm_start_bench(dev):
     """Accept rate and sweeps saved by the MLP's proposals against the
-    reference's random start (the judge), and the on-GPU training time."""
+    reference's random start (the yardstick of the acceptance test), and the
+    on-GPU training time."""
     from mlcp_gb300 import hoplist as H
     from mlcp_gb300.warmstart import WarmStart, power_steps
     ws = WarmStart(ndof=WS_D, n=WS_N, rank=WS_RANK, seed=1, device=dev)
@@ -483,7 +484,7 @@ def run_warm_start_bench(dev):
     t0 = time.perf_counter()
     losses, stats, t_train = power_steps(ws, hl, nvec=WS_NVEC, shift=WS_SHIFT)
     return {"workload": f"synthetic QFF D={WS_D} n={WS_N}: {WS_NVEC} vectors, (H - {WS_SHIFT:g}) F of rank "
-                        f"{WS_RANK} x {hl.nterms} reduced to rank {WS_RANK}; cycles 1-5 train, 6-8 judged",
+                        f"{WS_RANK} x {hl.nterms} reduced to rank {WS_RANK}; cycles 1-5 train, 6-8 tested",
             "network": "3 layers, width 256, BF16 weights, FP32 accumulation (tcgen05)",
             "train_seconds": t_train, "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
             "accept_rate": float(np.mean([s["accept_rate"] for s in stats])),

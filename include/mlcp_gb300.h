@@ -201,7 +201,7 @@ MLCP_API int mlcp_als_batched_host(int nvec, int ndof, const int *nbas, const in
  * (d_coef/d_base in the reference layout: rF F terms, then rG target terms;
  * the F terms are overwritten).  For callers that cannot allocate device
  * memory at call time (a host whose device memory another allocator or pool
- * owns up front, a latency-critical loop that must stay out of the driver's
+ * owns up front, a latency-critical loop that must stay out of the CUDA
  * allocator): all scratch comes from a fixed 32 MiB array inside the library,
  * held by every GPU that loads it.  The first call on a device looks up that
  * array's address and must come before any stream capture.  Calls share the

@@ -15,7 +15,7 @@ proposes the starting factors instead, from the unreduced vector itself:
 * training pairs: (unreduced vector, converged reduction) from reductions
   the solver has already run (``collect``: ``mlcp_ws_targets`` matches each
   slot's input term with the reduction term it turned into);
-* the judge: both starts run the same fixed number of sweeps, and the
+* the acceptance test: both starts run the same fixed number of sweeps, and the
   proposal is accepted, vector by vector, when its relative residual
   ||F - G|| / ||G|| is no larger than the random start's; otherwise the
   random start's result is kept (the fallback).
@@ -111,7 +111,7 @@ class WarmStart:
                                    self.net.out_p, torch_stream()))
         self.net.check_status()
 
-    # -- the judged reduction --
+    # -- the reduction with the acceptance test --
     def reduce(self, batch, fixed_sweeps: int, max_sweeps: int, seed: int = 0):
         """Reduce a device copy of the batch from the proposal and from the
         random start for fixed_sweeps each; keep, per vector, the better
@@ -192,9 +192,9 @@ def power_steps(ws: WarmStart, hl, nvec: int, shift: float, ncycle: int = 8, tra
     unreduced vectors of power steps, workloads.power_batch).  Cycles
     1..train_cycles are the solver's own reductions -- each started from the
     vector's previous iterate (a random start in cycle 1), train_sweeps sweeps
-    -- and their pairs train the MLP; later cycles are judged reductions
+    -- and their pairs train the MLP; later cycles are tested reductions
     (WarmStart.reduce) whose result feeds the next cycle.  Returns
-    (training losses, per judged cycle stats, seconds spent training)."""
+    (training losses, per tested cycle stats, seconds spent training)."""
     import time
 
     import torch

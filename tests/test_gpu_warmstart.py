@@ -5,7 +5,7 @@ to rank 30 for a block of 24 vectors.  Cycles 1-5 are the solver's own
 reductions (each from the vector's previous iterate, 20 sweeps) and their
 (unreduced vector, reduction) pairs train the MLP (600 full-batch Adam
 steps); from cycle 6 on the MLP proposes the starts and the reference's
-random start (GetRandomCPvec) runs beside it as the fallback and the judge.
+random start (GetRandomCPvec) runs beside it as the fallback and the yardstick.
 
 Checks: training lowers the loss at least fivefold; over cycles 6-8 the
 proposal, after the same 3 fixed sweeps as the random start, is accepted

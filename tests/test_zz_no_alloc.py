@@ -3,7 +3,7 @@ allocating one (mlcp_als_batched), through the C ABI.
 
 Some callers cannot allocate device memory when they reduce a vector: hosts
 whose device memory is owned up front by another allocator or memory pool,
-and latency-critical loops that must stay out of the driver's allocator.
+and latency-critical loops that must stay out of the CUDA allocator.
 mlcp_als_noalloc serves them from a fixed scratch array inside the library.
 
 Checks: two calls in a row on different inputs match the allocating entry
