@@ -5,7 +5,7 @@ The reference implements the power-iteration hot path as CUDA C++
 src/modvecvec.cu, src/cpvector.cu, src/hoplist.cu, src/matrix.cu,
 src/linalg.cu, src/utils.cu).  Its shipped build is double precision
 (Makefile:17 ``USEDOUBLES = yes`` -> ``-DUSE_DOUBLES=1``): this is the plain
-FP64 GPU form that parity and speed are judged against.  This recipe builds
+FP64 GPU form that parity and speed are measured against.  This recipe builds
 that library, unchanged apart from one fix, so that the tests and the
 benchmark can run it beside ``libmlcp_gb300``.
 
