@@ -442,6 +442,10 @@ def run_cycle_bench(steps: int, cpu: bool):
         t3 = time.perf_counter()
         out["pals_cpu_stage_ms"] = {"ALS_POW3": 1e3 * (t1 - t0), "ALS_ORTHO_2": 1e3 * (t2 - t1),
                                     "Diagonalize": 1e3 * (t3 - t2)}
+        # the same solver at lowmem 3 (ALS_ORTHO_3, PRODHV_ALS3, ALS_SUMLCVEC_3: no stored PS)
+        t0 = time.perf_counter()
+        oracle.pals_cycle(Q, qc, hl.nbas, CYC_R, CYC_B, hl, eig0, CYC_NPOW, CYC_NALS, True, 1, esh, lowmem=3)
+        out["pals_lowmem3_cpu_ms_per_cycle"] = 1e3 * (time.perf_counter() - t0)
         out["cpu_threads"] = os.cpu_count()
         t0 = time.perf_counter()
         oracle.qhq_diag(gb, gc, hl.nbas, CYC_R, CYC_B, hl)

@@ -92,16 +92,19 @@ def lib() -> ctypes.CDLL:
                                             ctypes.POINTER(_D), ctypes.POINTER(_D), _I, _I, ctypes.c_int,
                                             ctypes.c_int, ctypes.c_int]
         c_i, c_d = ctypes.c_int, ctypes.c_double
-        for name in ("orc_pals_pow3", "orc_pals_ortho2", "orc_pals_prodhv2", "orc_pals_sumlcvec2",
-                     "orc_pals_diagonalize", "orc_pals_cycle"):
+        for name in ("orc_pals_pow3", "orc_pals_ortho2", "orc_pals_ortho3", "orc_pals_prodhv2", "orc_pals_prodhv3",
+                     "orc_pals_sumlcvec2", "orc_pals_sumlcvec3", "orc_pals_diagonalize", "orc_pals_cycle"):
             getattr(L, name).restype = c_i
         L.orc_pals_pow3.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, _I, _I, _D, _D, c_i, c_i, c_i, c_d, c_i]
-        L.orc_pals_ortho2.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, c_i]
-        L.orc_pals_prodhv2.argtypes = [_D, _D, _D, _D, _I, c_i, c_i, _I, _I, _D, _D, c_i, c_i, c_d, c_i]
-        L.orc_pals_sumlcvec2.argtypes = [_D, _D, _I, c_i, c_i, _I, _D, c_i, c_i]
-        L.orc_pals_diagonalize.argtypes = [_D, _D, _I, c_i, c_i, _I, _I, _I, _D, _D, c_i, c_i, _D, _D, c_i]
-        L.orc_pals_cycle.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, _I, _I, _D, _D, c_i, c_i, c_i, c_i, c_i, c_d,
-                                     _D, c_i]
+        for name in ("orc_pals_ortho2", "orc_pals_ortho3"):
+            getattr(L, name).argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, c_i]
+        for name in ("orc_pals_prodhv2", "orc_pals_prodhv3"):
+            getattr(L, name).argtypes = [_D, _D, _D, _D, _I, c_i, c_i, _I, _I, _D, _D, c_i, c_i, c_d, c_i]
+        for name in ("orc_pals_sumlcvec2", "orc_pals_sumlcvec3"):
+            getattr(L, name).argtypes = [_D, _D, _I, c_i, c_i, _I, _D, c_i, c_i]
+        L.orc_pals_diagonalize.argtypes = [_D, _D, _I, c_i, c_i, _I, _I, _I, _D, _D, c_i, c_i, c_i, _D, _D, c_i]
+        L.orc_pals_cycle.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, _I, _I, _D, _D, c_i, c_i, c_i, c_i, c_i, c_i,
+                                     c_d, _D, c_i]
         L.orc_prodhv.argtypes = [_D, _D, _I, c_i, c_i, _I, _I, _D, _D, c_i, c_i, c_d, _D, _D]
         L.orc_powr_recurse.restype = c_i
         L.orc_powr_recurse.argtypes = [_D, _D, _I, c_i, c_i, _I, _I, _D, _D, c_i, c_i, c_d, c_i]
@@ -614,38 +617,43 @@ def pals_pow3(base, coef, nbas, rk, nbloc, hl, npow, ishift=1, Eshift=0.0, nconv
     return base, coef
 
 
-def pals_ortho2(base, coef, nbas, rk, nbloc, nitn, ranks=None, nthreads=0):
-    """ALS_ORTHO_2 (src/ALSUtils.f90:156-377)."""
+def pals_ortho2(base, coef, nbas, rk, nbloc, nitn, ranks=None, nthreads=0, lowmem=4):
+    """ALS_ORTHO_2 (src/ALSUtils.f90:156-377); ALS_ORTHO_3 (:381-528) with lowmem 3."""
     base, coef, rv = _block(base, coef, nbloc, rk, ranks)
     nb = np.ascontiguousarray(nbas, dtype=np.int32)
-    _check(lib().orc_pals_ortho2(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), nitn, nthreads),
-           "ALS_ORTHO_2")
+    fn = lib().orc_pals_ortho3 if lowmem == 3 else lib().orc_pals_ortho2
+    _check(fn(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), nitn, nthreads),
+           "ALS_ORTHO_3" if lowmem == 3 else "ALS_ORTHO_2")
     return base, coef
 
 
-def pals_prodhv2(base, coef, nbas, hl, nitn, ishift=0, Eshift=0.0):
-    """PRODHV_ALS2 (src/ALSPow.f90:664-780): ALS fit of (H - Eshift) F, F's rank."""
+def pals_prodhv2(base, coef, nbas, hl, nitn, ishift=0, Eshift=0.0, lowmem=4):
+    """PRODHV_ALS2 (src/ALSPow.f90:664-780): ALS fit of (H - Eshift) F, F's
+    rank; PRODHV_ALS3 (:784-865) with lowmem 3."""
     fb = np.ascontiguousarray(base, dtype=np.float64)
     fc = np.ascontiguousarray(coef, dtype=np.float64)
     ob, oc = np.zeros_like(fb), np.zeros_like(fc)
     nb = np.ascontiguousarray(nbas, dtype=np.int32)
-    _check(lib().orc_pals_prodhv2(_dp(fb), _dp(fc), _dp(ob), _dp(oc), _ip(nb), len(nb), fc.size, _ip(hl.opid),
-                                  _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, ishift, float(Eshift), nitn),
-           "PRODHV_ALS2")
+    fn = lib().orc_pals_prodhv3 if lowmem == 3 else lib().orc_pals_prodhv2
+    _check(fn(_dp(fb), _dp(fc), _dp(ob), _dp(oc), _ip(nb), len(nb), fc.size, _ip(hl.opid), _ip(hl.mptr),
+              _dp(hl.coef), _dp(hl.mat), hl.nterms, ishift, float(Eshift), nitn),
+           "PRODHV_ALS3" if lowmem == 3 else "PRODHV_ALS2")
     return ob, oc
 
 
-def pals_sumlcvec2(base, coef, nbas, rk, nbloc, U, nitn, ranks=None, nthreads=0):
-    """UpdateVecs2 with ALS_SUMLCVEC_2: vector i <- fit of sum_l U[l, i] Q_l."""
+def pals_sumlcvec2(base, coef, nbas, rk, nbloc, U, nitn, ranks=None, nthreads=0, lowmem=4):
+    """UpdateVecs2 with ALS_SUMLCVEC_2 (ALS_SUMLCVEC_3 with lowmem 3):
+    vector i <- fit of sum_l U[l, i] Q_l."""
     base, coef, rv = _block(base, coef, nbloc, rk, ranks)
     nb = np.ascontiguousarray(nbas, dtype=np.int32)
     Ucm = np.ascontiguousarray(np.asarray(U, dtype=np.float64).T)
-    _check(lib().orc_pals_sumlcvec2(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), _dp(Ucm), nitn,
-                                    nthreads), "ALS_SUMLCVEC_2")
+    fn = lib().orc_pals_sumlcvec3 if lowmem == 3 else lib().orc_pals_sumlcvec2
+    _check(fn(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), _dp(Ucm), nitn, nthreads),
+           "ALS_SUMLCVEC_3" if lowmem == 3 else "ALS_SUMLCVEC_2")
     return base, coef
 
 
-def pals_diagonalize(base, coef, nbas, rk, nbloc, hl, nitn, ranks=None, nthreads=0):
+def pals_diagonalize(base, coef, nbas, rk, nbloc, hl, nitn, ranks=None, nthreads=0, lowmem=4):
     """Diagonalize with intertwining (src/BlockUtils.f90:184-225); returns
     (base, coef, eigenvalues, U with U[:, i] = eigenvector i)."""
     if nitn < 1:
@@ -655,22 +663,25 @@ def pals_diagonalize(base, coef, nbas, rk, nbloc, hl, nitn, ranks=None, nthreads
     eig = np.zeros(nbloc)
     U = np.zeros(nbloc * nbloc)
     _check(lib().orc_pals_diagonalize(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), _ip(hl.opid),
-                                      _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, nitn, _dp(eig), _dp(U),
-                                      nthreads), "Diagonalize")
+                                      _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, nitn, lowmem, _dp(eig),
+                                      _dp(U), nthreads), "Diagonalize")
     return base, coef, eig, U.reshape(nbloc, nbloc).T.copy()
 
 
 def pals_cycle(base, coef, nbas, rk, nbloc, hl, eigv, npow, nals, update=True, ishift=1, Eshift=0.0, nconv=0,
-               ranks=None, nthreads=0):
-    """One cycle of the Fortran host's CPU solver; returns (base, coef, eigv)."""
+               ranks=None, nthreads=0, lowmem=4):
+    """One cycle of the Fortran host's CPU solver (lowmem 4: the _2 forms;
+    lowmem 3: the _3 forms); returns (base, coef, eigv)."""
+    if lowmem not in (3, 4):
+        raise ValueError("lowmem 3 or 4 (ALS_POW3 with the _3 or the _2 forms) are restated")
     if update and nals < 1:
         raise ValueError("the cycle's diagonalisation needs nals >= 1 (PRODHV_ALS2 returns no H Q_i otherwise)")
     base, coef, rv = _block(base, coef, nbloc, rk, ranks)
     eig = np.ascontiguousarray(eigv, dtype=np.float64).copy()
     nb = np.ascontiguousarray(nbas, dtype=np.int32)
     _check(lib().orc_pals_cycle(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), nconv, _ip(hl.opid),
-                                _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, npow, nals, int(bool(update)),
-                                ishift, float(Eshift), _dp(eig), nthreads), "pals cycle")
+                                _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, npow, nals, lowmem,
+                                int(bool(update)), ishift, float(Eshift), _dp(eig), nthreads), "pals cycle")
     return base, coef, eig
 
 

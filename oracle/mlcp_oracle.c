@@ -1143,15 +1143,15 @@ static int rows_to_mode(double *coef, double *base, int rF, int nD, int gst, con
   return bad;
 }
 
-/* BuildbjkDirectX (src/ALSPow.f90:1154-1310) with recalcB = F: for mode k,
- *   BB(i,l)  = prod_{m != k} <F_l^m, Fo_i^m>,
+/* BuildbjkDirectX (src/ALSPow.f90:1154-1310): for mode k,
+ *   BB(i,l)  = prod_{m != k} <F_l^m, Fo_i^m>   (recalcB: <F_l^m, F_i^m>),
  *   bjk(l,:) = sum_t sum_i co_i [prod_{m != k} <F_l^m, h_{t,m} Fo_i^m>] h_{t,k} Fo_i^k
  *              - E sum_i co_i BB(i,l) Fo_i^k            (ishift != 0),
  * negated at k = 0 when ishift < 0.  The other modes are visited in the
  * order k+1, ..., D-1, 0, ..., k-1; T holds one applied factor. */
 static void buildbjk_direct(const hoplist *H, const double *focoef, const double *fobase, const double *fbase, int rF,
                             const int *nbas, const int *off, int ndof, int k, int ishift, double Eshift, double *BB,
-                            double *bjk, double *T) {
+                            double *bjk, double *T, int recalcB) {
   const int nD = off[ndof], n = nbas[k];
   for (int e = 0; e < rF * n; ++e) bjk[e] = 0.0;
   for (int t = 0; t < H->T; ++t)
@@ -1187,6 +1187,18 @@ static void buildbjk_direct(const hoplist *H, const double *focoef, const double
   }
   if (k == 0 && ishift < 0)
     for (int e = 0; e < rF * n; ++e) bjk[e] = -bjk[e];
+  if (recalcB) {  /* upper triangle, then mirrored */
+    for (int i = 0; i < rF; ++i) {
+      for (int l = i; l < rF; ++l) BB[i + (size_t)l * rF] = 1.0;
+      for (int m = 1; m < ndof; ++m) {
+        const int mm = (k + m) % ndof;
+        const double *x = fbase + (size_t)i * nD + off[mm];
+        for (int l = i; l < rF; ++l) BB[i + (size_t)l * rF] *= dot_n(fbase + (size_t)l * nD + off[mm], x, nbas[mm]);
+      }
+    }
+    for (int i = 1; i < rF; ++i)
+      for (int l = 0; l < i; ++l) BB[i + (size_t)l * rF] = BB[l + (size_t)i * rF];
+  }
 }
 
 /* ALS_POW3 (src/ALSPow.f90:569-660): nitn in-place sweeps of F <- ALS fit of
@@ -1202,7 +1214,7 @@ static int pals_pow3(const hoplist *H, double *coef, double *base, int rF, const
   for (int itn = 0; itn < nitn; ++itn)
     for (int k = 0; k < ndof; ++k) {
       const int n = nbas[k];
-      buildbjk_direct(H, coef, base, base, rF, nbas, off, ndof, k, ishift, Eshift, w->BB, w->bjk, w->T);
+      buildbjk_direct(H, coef, base, base, rF, nbas, off, ndof, k, ishift, Eshift, w->BB, w->bjk, w->T, 0);
       for (int i = 0; i < rF; ++i) w->BB[i + (size_t)i * rF] += valpen;
       lu_solve(w->BB, w->bjk, rF, n, w->ipiv);
       if (rows_to_mode(coef, base, rF, nD, off[k], w->bjk, n)) return 1;
@@ -1481,6 +1493,163 @@ static int pals_sumlcvec2(double *fcoef, double *fbase, int rF, const double *qc
   return 0;
 }
 
+/* PRODHV_ALS3 (src/ALSPow.f90:784-865): the least-memory form of
+ * PRODHV_ALS2.  Every mode step rebuilds BB = <F,F> and bjk from Fo and H
+ * directly (BuildbjkDirectX with recalcB), then adds 1e-10 max c_Fo, solves
+ * by LU and moves the row norms into the weights.  Returns 1 on a NaN. */
+static int pals_prodhv3(const hoplist *H, const double *focoef, const double *fobase, double *coef, double *base,
+                        int rF, const int *nbas, const int *off, int ndof, int ishift, double Eshift, int nitn,
+                        pals_ws *w) {
+  if (nitn == 0) return 0;
+  const int nD = off[ndof];
+  memcpy(coef, focoef, sizeof(double) * rF);
+  memcpy(base, fobase, sizeof(double) * (size_t)rF * nD);
+  const double valpen = maxval(coef, rF) * 1.0e-10;
+  for (int itn = 0; itn < nitn; ++itn)
+    for (int k = 0; k < ndof; ++k) {
+      const int n = nbas[k];
+      buildbjk_direct(H, focoef, fobase, base, rF, nbas, off, ndof, k, ishift, Eshift, w->BB, w->bjk, w->T, 1);
+      for (int i = 0; i < rF; ++i) w->BB[i + (size_t)i * rF] += valpen;
+      lu_solve(w->BB, w->bjk, rF, n, w->ipiv);
+      if (rows_to_mode(coef, base, rF, nD, off[k], w->bjk, n)) return 1;
+    }
+  return 0;
+}
+
+/* ALS_ORTHO_3 (src/ALSUtils.f90:381-528): ALS_ORTHO_2 without the stored
+ * PS.  At every mode step k of vector v, for each l <= v the block
+ * P_l(j,i) = prod_{m != k} <Q_l,j^m, Q_v,i^m> is rebuilt (CONSTPSTOT_OMP),
+ * with l < v also the mode-k block (CONSTPSk_OMP) for the coefficient
+ * coefs_l = -<Q_l, Q_v>; bjk accumulates l by l.  BB is the Q_v block plus
+ * 1e-10 max c_v (taken once per vector); after the solve the Q_v block is
+ * multiplied by the new mode-k Gram (UpdateBB) and the weights scaled to
+ * unit norm with it.  The blocks are built OpenMP-parallel over l, then
+ * summed in the reference's order.  Returns 1 on a NaN weight. */
+static int pals_ortho3(double *coef, double *base, const int *ranks, const int *toff, int nbloc, const int *nbas,
+                       const int *off, int ndof, int nitn, int nthreads) {
+  if (nitn == 0) return 0;
+  const int nD = off[ndof];
+  int nmax = 0, rmax = 0;
+  for (int d = 0; d < ndof; ++d) nmax = nbas[d] > nmax ? nbas[d] : nmax;
+  for (int v = 0; v < nbloc; ++v) rmax = ranks[v] > rmax ? ranks[v] : rmax;
+  const int rtot = toff[nbloc - 1] + ranks[nbloc - 1];
+  double *coefs = (double *)malloc(sizeof(double) * nbloc);
+  double *P = (double *)malloc(sizeof(double) * (size_t)rtot * rmax);   /* block l at rows toff[l].. */
+  double *Pk = (double *)malloc(sizeof(double) * (size_t)rtot * rmax);
+  double *BB = (double *)malloc(sizeof(double) * rmax * rmax);
+  double *BBmem = (double *)malloc(sizeof(double) * rmax * rmax);
+  double *bjk = (double *)malloc(sizeof(double) * (size_t)rmax * nmax);
+  int *ipiv = (int *)malloc(sizeof(int) * rmax);
+  int bad = 0;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#endif
+  (void)nthreads;
+  normcoef(coef, base, ranks[0], nbas, off, ndof);
+  for (int iv = 1; iv < nbloc && !bad; ++iv) {
+    double *fc = coef + toff[iv], *fb = base + (size_t)toff[iv] * nD;
+    const int rF = ranks[iv], rG = toff[iv] + rF, s = toff[iv];
+    const double valpen = maxval(fc, rF) * 1.0e-10;
+    for (int itn = 0; itn < nitn && !bad; ++itn)
+      for (int k = 0; k < ndof; ++k) {
+        const int n = nbas[k], gik = off[k];
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+        for (int l = 0; l <= iv; ++l) {
+          const double *gb = base + (size_t)toff[l] * nD;
+          for (int j = 0; j < ranks[l]; ++j)
+            for (int i = 0; i < rF; ++i)
+              P[toff[l] + j + (size_t)i * rG] = prodnd(fb + (size_t)i * nD, gb + (size_t)j * nD, nbas, ndof, k);
+          if (l < iv) const_psk(fb, rF, gb, ranks[l], nD, gik, n, Pk + toff[l], rG);
+        }
+        for (int e = 0; e < rF * n; ++e) bjk[e] = 0.0;
+        for (int l = 0; l <= iv; ++l) {
+          double c = 1.0;
+          if (l < iv) {
+            c = 0.0;
+            for (int j = 0; j < ranks[l]; ++j)
+              for (int i = 0; i < rF; ++i)
+                c = c - P[toff[l] + j + (size_t)i * rG] * Pk[toff[l] + j + (size_t)i * rG] * coef[toff[l] + j] * fc[i];
+          }
+          coefs[l] = c;
+          for (int j = 0; j < ranks[l]; ++j) {
+            const double gtmp = coefs[l] * coef[toff[l] + j];
+            const double *q = base + (size_t)(toff[l] + j) * nD + gik;
+            for (int i = 0; i < rF; ++i) {
+              const double g2 = gtmp * P[toff[l] + j + (size_t)i * rG];
+              for (int ir = 0; ir < n; ++ir) bjk[i + (size_t)ir * rF] += g2 * q[ir];
+            }
+          }
+        }
+        for (int i = 0; i < rF; ++i)
+          for (int j = 0; j < rF; ++j) BBmem[j + (size_t)i * rF] = P[s + j + (size_t)i * rG];
+        memcpy(BB, BBmem, sizeof(double) * rF * rF);
+        for (int i = 0; i < rF; ++i) BB[i + (size_t)i * rF] += valpen;
+        lu_solve(BB, bjk, rF, n, ipiv);
+        if (rows_to_mode(fc, fb, rF, nD, gik, bjk, n)) { bad = 1; break; }
+        update_bb(fb, rF, nD, gik, n, BBmem, 0);
+        double rn = 0.0;
+        for (int i = 0; i < rF; ++i) {
+          rn = rn + BBmem[i + (size_t)i * rF] * (fc[i] * fc[i]);
+          for (int j = 0; j < i; ++j) rn = rn + 2 * BBmem[j + (size_t)i * rF] * fc[i] * fc[j];
+        }
+        rn = 1 / sqrt(fabs(rn));
+        for (int i = 0; i < rF; ++i) fc[i] = rn * fc[i];
+      }
+  }
+  free(coefs); free(P); free(Pk); free(BB); free(BBmem); free(bjk); free(ipiv);
+  return bad;
+}
+
+/* ALS_SUMLCVEC_3 (src/ALSUtils.f90:895-1045): ALS_SUMLCVEC_2 without the
+ * stored PS.  bjk is built term by term of every Q_l: the products over the
+ * modes other than k (visited k+1, ..., D-1, 0, ..., k-1) of <F_i, Q_l,j>,
+ * times w_l c_l,j Q_l,j^k; BB = <F,F> is kept by UpdateBB as in the _2 form,
+ * and the weights are scaled to unit norm at the end.  Returns 1 on a NaN. */
+static int pals_sumlcvec3(double *fcoef, double *fbase, int rF, const double *qcoef, const double *qbase,
+                          const int *ranks, const int *toff, int nbloc, const double *w, const int *nbas,
+                          const int *off, int ndof, int nitn, pals_ws *ws) {
+  if (nitn == 0) return 0;
+  const int nD = off[ndof];
+  double *BBmem = ws->BBmem, *BB = ws->BB, *bjk = ws->bjk, *PSr = ws->psk;
+  const double valpen = maxval(fcoef, rF) * 1.0e-10;
+  const_bb(fbase, rF, nbas, ndof, nD, -1, BBmem);
+  for (int itn = 0; itn < nitn; ++itn)
+    for (int k = 0; k < ndof; ++k) {
+      const int n = nbas[k], gik = off[k];
+      for (int e = 0; e < rF * n; ++e) bjk[e] = 0.0;
+      for (int l = 0; l < nbloc; ++l)
+        for (int j = 0; j < ranks[l]; ++j) {
+          const double *q = qbase + (size_t)(toff[l] + j) * nD;
+          for (int i = 0; i < rF; ++i) PSr[i] = 1.0;
+          for (int m = 1; m < ndof; ++m) {
+            const int mm = (k + m) % ndof;
+            for (int i = 0; i < rF; ++i) PSr[i] = PSr[i] * dot_n(fbase + (size_t)i * nD + off[mm], q + off[mm], nbas[mm]);
+          }
+          const double gtmp = w[l] * qcoef[toff[l] + j];
+          for (int i = 0; i < rF; ++i) {
+            const double g2 = gtmp * PSr[i];
+            for (int ir = 0; ir < n; ++ir) bjk[i + (size_t)ir * rF] += g2 * q[gik + ir];
+          }
+        }
+      update_bb(fbase, rF, nD, gik, n, BBmem, 1);
+      memcpy(BB, BBmem, sizeof(double) * rF * rF);
+      for (int i = 0; i < rF; ++i) BB[i + (size_t)i * rF] += valpen;
+      lu_solve(BB, bjk, rF, n, ws->ipiv);
+      if (rows_to_mode(fcoef, fbase, rF, nD, gik, bjk, n)) return 1;
+      update_bb(fbase, rF, nD, gik, n, BBmem, 0);
+    }
+  double rn = 0.0;
+  for (int i = 0; i < rF; ++i) {
+    rn = rn + BBmem[i + (size_t)i * rF] * (fcoef[i] * fcoef[i]);
+    for (int j = 0; j < i; ++j) rn = rn + 2 * BBmem[i + (size_t)j * rF] * fcoef[i] * fcoef[j];
+  }
+  rn = 1 / sqrt(fabs(rn));
+  for (int i = 0; i < rF; ++i) fcoef[i] = rn * fcoef[i];
+  return 0;
+}
+
 static int *rank_offsets(const int *ranks, int nbloc) {
   int *toff = (int *)malloc(sizeof(int) * (nbloc + 1));
   toff[0] = 0;
@@ -1518,20 +1687,42 @@ int orc_pals_ortho2(double *base, double *coef, const int *nbas, int ndof, int n
   return bad;
 }
 
-int orc_pals_prodhv2(const double *fobase, const double *focoef, double *base, double *coef, const int *nbas,
-                     int ndof, int rF, const int *opid, const int *mptr, const double *Hcoef, const double *mat,
-                     int T, int ishift, double Eshift, int nitn) {
+int orc_pals_ortho3(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nitn,
+                    int nthreads) {
+  int *off = make_offsets(nbas, ndof), *toff = rank_offsets(ranks, nbloc);
+  const int bad = pals_ortho3(coef, base, ranks, toff, nbloc, nbas, off, ndof, nitn, nthreads);
+  free(off); free(toff);
+  return bad;
+}
+
+static int prodhv_any(const double *fobase, const double *focoef, double *base, double *coef, const int *nbas,
+                      int ndof, int rF, const int *opid, const int *mptr, const double *Hcoef, const double *mat,
+                      int T, int ishift, double Eshift, int nitn, int lowmem) {
   int *off = make_offsets(nbas, ndof);
   hoplist H = {T, ndof, opid, mptr, Hcoef, mat};
   pals_ws w = pals_ws_alloc(rF, rF * T + rF, max_nbas(nbas, ndof));
-  const int bad = pals_prodhv2(&H, focoef, fobase, coef, base, rF, nbas, off, ndof, ishift, Eshift, nitn, &w);
+  const int bad = lowmem == 3
+                      ? pals_prodhv3(&H, focoef, fobase, coef, base, rF, nbas, off, ndof, ishift, Eshift, nitn, &w)
+                      : pals_prodhv2(&H, focoef, fobase, coef, base, rF, nbas, off, ndof, ishift, Eshift, nitn, &w);
   pals_ws_free(&w);
   free(off);
   return bad;
 }
 
-int orc_pals_sumlcvec2(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
-                       const double *U, int nitn, int nthreads) {
+int orc_pals_prodhv2(const double *fobase, const double *focoef, double *base, double *coef, const int *nbas,
+                     int ndof, int rF, const int *opid, const int *mptr, const double *Hcoef, const double *mat,
+                     int T, int ishift, double Eshift, int nitn) {
+  return prodhv_any(fobase, focoef, base, coef, nbas, ndof, rF, opid, mptr, Hcoef, mat, T, ishift, Eshift, nitn, 4);
+}
+
+int orc_pals_prodhv3(const double *fobase, const double *focoef, double *base, double *coef, const int *nbas,
+                     int ndof, int rF, const int *opid, const int *mptr, const double *Hcoef, const double *mat,
+                     int T, int ishift, double Eshift, int nitn) {
+  return prodhv_any(fobase, focoef, base, coef, nbas, ndof, rF, opid, mptr, Hcoef, mat, T, ishift, Eshift, nitn, 3);
+}
+
+static int update_vecs2(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
+                        const double *U, int nitn, int nthreads, int lowmem) {
   int *off = make_offsets(nbas, ndof), *toff = rank_offsets(ranks, nbloc);
   const int nD = off[ndof], nmax = max_nbas(nbas, ndof), rtot = toff[nbloc];
   double *qb = (double *)malloc(sizeof(double) * (size_t)rtot * nD);
@@ -1545,13 +1736,25 @@ int orc_pals_sumlcvec2(double *base, double *coef, const int *nbas, int ndof, in
 #endif
   for (int v = 0; v < nbloc; ++v) {
     pals_ws w = pals_ws_alloc(ranks[v], rtot, nmax);
-    bad += pals_sumlcvec2(coef + toff[v], base + (size_t)toff[v] * nD, ranks[v], qc, qb, ranks, toff, nbloc,
-                          U + (size_t)v * nbloc, nbas, off, ndof, nitn, &w);
+    bad += lowmem == 3 ? pals_sumlcvec3(coef + toff[v], base + (size_t)toff[v] * nD, ranks[v], qc, qb, ranks, toff,
+                                        nbloc, U + (size_t)v * nbloc, nbas, off, ndof, nitn, &w)
+                       : pals_sumlcvec2(coef + toff[v], base + (size_t)toff[v] * nD, ranks[v], qc, qb, ranks, toff,
+                                        nbloc, U + (size_t)v * nbloc, nbas, off, ndof, nitn, &w);
     pals_ws_free(&w);
   }
   (void)nthreads;
   free(qb); free(qc); free(off); free(toff);
   return bad;
+}
+
+int orc_pals_sumlcvec2(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
+                       const double *U, int nitn, int nthreads) {
+  return update_vecs2(base, coef, nbas, ndof, nbloc, ranks, U, nitn, nthreads, 4);
+}
+
+int orc_pals_sumlcvec3(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
+                       const double *U, int nitn, int nthreads) {
+  return update_vecs2(base, coef, nbas, ndof, nbloc, ranks, U, nitn, nthreads, 3);
 }
 
 /* Diagonalize with intertwining (src/BlockUtils.f90:184-225): GetQHQ3
@@ -1566,7 +1769,7 @@ int orc_pals_sumlcvec2(double *base, double *coef, const int *nbas, int ndof, in
  * Returns the number of NaN events, or -1 on a failed eigensolve. */
 int orc_pals_diagonalize(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
                          const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int nitn,
-                         double *eigv, double *Uout, int nthreads) {
+                         int lowmem, double *eigv, double *Uout, int nthreads) {
   if (nitn < 1) return -1;
   int *off = make_offsets(nbas, ndof), *toff = rank_offsets(ranks, nbloc);
   const int nD = off[ndof], nmax = max_nbas(nbas, ndof);
@@ -1584,8 +1787,11 @@ int orc_pals_diagonalize(double *base, double *coef, const int *nbas, int ndof, 
     pals_ws w = pals_ws_alloc(rF, rF * T, nmax);
     double *hc = (double *)malloc(sizeof(double) * rF);
     double *hb = (double *)malloc(sizeof(double) * (size_t)rF * nD);
-    bad += pals_prodhv2(&H, coef + toff[i], base + (size_t)toff[i] * nD, hc, hb, rF, nbas, off, ndof, 0, 0.0, nitn,
-                        &w);
+    bad += lowmem == 3
+               ? pals_prodhv3(&H, coef + toff[i], base + (size_t)toff[i] * nD, hc, hb, rF, nbas, off, ndof, 0, 0.0,
+                              nitn, &w)
+               : pals_prodhv2(&H, coef + toff[i], base + (size_t)toff[i] * nD, hc, hb, rF, nbas, off, ndof, 0, 0.0,
+                              nitn, &w);
     for (int j = i; j < nbloc; ++j)
       QHQ[i + (size_t)j * nbloc] =
           prodvv_ab(coef + toff[j], base + (size_t)toff[j] * nD, ranks[j], hc, hb, rF, nbas, ndof, nD);
@@ -1614,7 +1820,7 @@ int orc_pals_diagonalize(double *base, double *coef, const int *nbas, int ndof, 
     bad = -1;
   } else {
     if (Uout) memcpy(Uout, U, sizeof(double) * (size_t)nbloc * nbloc);
-    bad += orc_pals_sumlcvec2(base, coef, nbas, ndof, nbloc, ranks, U, nitn, nthreads);
+    bad += update_vecs2(base, coef, nbas, ndof, nbloc, ranks, U, nitn, nthreads, lowmem);
   }
   free(QHQ); free(S); free(U); free(off); free(toff);
   return bad;
@@ -1629,15 +1835,17 @@ int orc_pals_diagonalize(double *base, double *coef, const int *nbas, int ndof, 
  * aborts on one), or -1 on a failed eigensolve. */
 int orc_pals_cycle(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
                    const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
-                   int nals, int update, int ishift, double Eshift, double *eigv, int nthreads) {
+                   int nals, int lowmem, int update, int ishift, double Eshift, double *eigv, int nthreads) {
+  if (lowmem != 3 && lowmem != 4) return -2;
   int bad = orc_pals_pow3(base, coef, nbas, ndof, nbloc, ranks, nconv, opid, mptr, Hcoef, mat, T, npow, ishift,
                           Eshift, nthreads);
   if (bad) return bad;
-  bad = orc_pals_ortho2(base, coef, nbas, ndof, nbloc, ranks, nals, nthreads);
+  bad = lowmem == 3 ? orc_pals_ortho3(base, coef, nbas, ndof, nbloc, ranks, nals, nthreads)
+                    : orc_pals_ortho2(base, coef, nbas, ndof, nbloc, ranks, nals, nthreads);
   if (bad) return bad;
   if (update)
-    bad = orc_pals_diagonalize(base, coef, nbas, ndof, nbloc, ranks, opid, mptr, Hcoef, mat, T, nals, eigv, NULL,
-                               nthreads);
+    bad = orc_pals_diagonalize(base, coef, nbas, ndof, nbloc, ranks, opid, mptr, Hcoef, mat, T, nals, lowmem, eigv,
+                               NULL, nthreads);
   return bad;
 }
 

@@ -124,8 +124,9 @@ int orc_reduc_als_batched(int nvec, const double *const *gcoef, const double *co
                           double *const *fcoef, double *const *fbase, const int *rF, const int *nbas, int ndof,
                           int nitn, int nthreads);
 
-/* The Fortran host's CPU power cycle, solver pals at lowmem 4
- * (src/Solver.f90:508-538).  A block holds nbloc vectors; vector v has
+/* The Fortran host's CPU power cycle, solver pals at lowmem 4 (the _2
+ * forms of the Gram-Schmidt, H-application and updates) or lowmem 3 (the
+ * least-memory _3 forms) (src/Solver.f90:508-538).  A block holds nbloc vectors; vector v has
  * ranks[v] terms, stored after the terms of vectors 0..v-1 (ragged blocks
  * are allowed, as in ALS_ORTHO_2's ranks table).  Each call returns the
  * number of NaN weights met (the reference aborts on one); the
@@ -134,28 +135,38 @@ int orc_reduc_als_batched(int nvec, const double *const *gcoef, const double *co
 int orc_pals_pow3(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
                   const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
                   int ishift, double Eshift, int nthreads);
-/* ALS_ORTHO_2 (src/ALSUtils.f90:156-377). */
+/* ALS_ORTHO_2 (src/ALSUtils.f90:156-377) and ALS_ORTHO_3 (:381-528). */
 int orc_pals_ortho2(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nitn,
+                    int nthreads);
+int orc_pals_ortho3(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nitn,
                     int nthreads);
 /* PRODHV_ALS2 (src/ALSPow.f90:664-780): (base, coef) <- ALS fit of
  * (H - Eshift) Fo, rF terms, starting from Fo. */
 int orc_pals_prodhv2(const double *fobase, const double *focoef, double *base, double *coef, const int *nbas,
                      int ndof, int rF, const int *opid, const int *mptr, const double *Hcoef, const double *mat,
                      int T, int ishift, double Eshift, int nitn);
+/* PRODHV_ALS3 (src/ALSPow.f90:784-865), the same fit without PS. */
+int orc_pals_prodhv3(const double *fobase, const double *focoef, double *base, double *coef, const int *nbas,
+                     int ndof, int rF, const int *opid, const int *mptr, const double *Hcoef, const double *mat,
+                     int T, int ishift, double Eshift, int nitn);
 /* UpdateVecs2 (src/BlockUtils.f90:479-516) with ALS_SUMLCVEC_2
  * (src/ALSUtils.f90:731-891): vector v <- fit of sum_l U[v*nbloc + l] Q_l. */
 int orc_pals_sumlcvec2(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
+                       const double *U, int nitn, int nthreads);
+/* The same with ALS_SUMLCVEC_3 (src/ALSUtils.f90:895-1045). */
+int orc_pals_sumlcvec3(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
                        const double *U, int nitn, int nthreads);
 /* Diagonalize with intertwining (src/BlockUtils.f90:184-225): GetQHQ3,
  * GetOverlaps, SolveGenEigval (upper triangles), UpdateVecs2.  U (optional)
  * receives the eigenvectors, column-major. */
 int orc_pals_diagonalize(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
                          const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int nitn,
-                         double *eigv, double *U, int nthreads);
-/* One cycle: ALS_POW3, ALS_ORTHO_2 and, with update, the diagonalisation. */
+                         int lowmem, double *eigv, double *U, int nthreads);
+/* One cycle: ALS_POW3, ALS_ORTHO_2 (_3) and, with update, the
+ * diagonalisation; lowmem 3 or 4 (else -2). */
 int orc_pals_cycle(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
                    const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
-                   int nals, int update, int ishift, double Eshift, double *eigv, int nthreads);
+                   int nals, int lowmem, int update, int ishift, double Eshift, double *eigv, int nthreads);
 
 /* PRODHV (src/MODHVECML.f90:50-110): the explicit (H - Eshift) F, rF T
  * terms (plus rF with a shift) into gbase/gcoef. */

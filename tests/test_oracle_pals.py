@@ -305,3 +305,73 @@ def test_pals_edge_cases():
         oracle.pals_ortho2(Q, qc, nb, 3, 1, 2, ranks=[2])
     with pytest.raises(ValueError):
         oracle.pals_diagonalize(Q, qc, nb, 3, 1, hl, 0)
+
+
+# --- lowmem 3: the least-memory _3 forms are the same fits as the _2 forms ---
+
+def test_ortho3_matches_ortho2():
+    hl = H.henon_heiles(D=4, n=5, lam=0.111803)
+    nb, rk, nbloc = hl.nbas, 4, 5
+    Q, qc = start_block(nb, rk, nbloc, 13)
+    Q, qc = oracle.pals_pow3(Q, qc, nb, rk, nbloc, hl, 2, 1, 9.0)
+    a = oracle.pals_ortho2(Q, qc, nb, rk, nbloc, 4)
+    b = oracle.pals_ortho2(Q, qc, nb, rk, nbloc, 4, lowmem=3)
+    assert rel(dense_block(*b, nb, [rk] * nbloc), dense_block(*a, nb, [rk] * nbloc)) < 1e-10
+
+
+def test_ortho3_ragged_matches_ortho2():
+    hl = H.coupled_oscillators(3, 5)
+    nb, ranks = hl.nbas, [2, 6, 3, 5]
+    rng = np.random.default_rng(17)
+    Q = rng.uniform(-0.5, 0.5, size=(sum(ranks), int(nb.sum())))
+    qc = rng.uniform(0.5, 1.0, sum(ranks))
+    a = oracle.pals_ortho2(Q, qc, nb, 0, len(ranks), 5, ranks=ranks)
+    b = oracle.pals_ortho2(Q, qc, nb, 0, len(ranks), 5, ranks=ranks, lowmem=3)
+    assert rel(dense_block(*b, nb, ranks), dense_block(*a, nb, ranks)) < 1e-10
+
+
+@pytest.mark.parametrize("ishift,E", [(0, 0.0), (1, 6.0), (-1, 6.0)])
+def test_prodhv3_matches_prodhv2(ishift, E):
+    """The same fit, except the sign with ishift < 0.  PRODHV_ALS2 changes
+    the sign of PS and bjk at the first mode (UpdateXPS, DowndateXPS), so
+    its targets are (H - E) F at the first mode and (E - H) F at the
+    others; BuildbjkDirectX, which PRODHV_ALS3 calls, changes the sign of
+    bjk at the first mode only: (E - H) F there, (H - E) F at the others.
+    A fit takes the sign of its last mode step's target, so after a sweep
+    PRODHV_ALS2 holds (E - H) F, as ishift < 0 asks, and PRODHV_ALS3
+    (H - E) F.  The cycles call both with ishift = 0."""
+    hl = H.random_hoplist([4, 5, 3, 4], 4, seed=3, coupling=2)
+    rng = np.random.default_rng(5)
+    F = rng.normal(size=(3, int(hl.nbas.sum())))
+    fc = rng.uniform(0.5, 1.5, 3)
+    a = oracle.pals_prodhv2(F, fc, hl.nbas, hl, 3, ishift, E)
+    b = oracle.pals_prodhv2(F, fc, hl.nbas, hl, 3, ishift, E, lowmem=3)
+    sign = -1 if ishift < 0 else 1
+    assert rel(oracle.cp_dense(*b, hl.nbas), sign * oracle.cp_dense(*a, hl.nbas)) < 1e-10
+    if ishift < 0:
+        want = (E * np.eye(int(np.prod(hl.nbas))) - H.dense_hamiltonian(hl)) @ oracle.cp_dense(F, fc, hl.nbas).ravel()
+        got = oracle.cp_dense(*a, hl.nbas).ravel()
+        assert got @ want > 0.99 * np.linalg.norm(got) * np.linalg.norm(want)
+
+
+def test_sumlcvec3_matches_sumlcvec2():
+    hl = H.henon_heiles(D=4, n=5, lam=0.111803)
+    nb, rk, nbloc = hl.nbas, 4, 4
+    Q, qc = start_block(nb, rk, nbloc, 19)
+    Q, qc = oracle.pals_ortho2(Q, qc, nb, rk, nbloc, 3)
+    U = np.linalg.qr(np.random.default_rng(8).normal(size=(nbloc, nbloc)))[0]
+    a = oracle.pals_sumlcvec2(Q, qc, nb, rk, nbloc, U, 4)
+    b = oracle.pals_sumlcvec2(Q, qc, nb, rk, nbloc, U, 4, lowmem=3)
+    assert rel(dense_block(*b, nb, [rk] * nbloc), dense_block(*a, nb, [rk] * nbloc)) < 1e-10
+
+
+def test_pals_cycle_lowmem3_matches_lowmem4():
+    hl = H.coupled_oscillators(3, 6)
+    nb, rk, nbloc = hl.nbas, 5, 4
+    Q, qc = start_block(nb, rk, nbloc, 23)
+    a = oracle.pals_cycle(Q, qc, nb, rk, nbloc, hl, np.zeros(nbloc), 3, 4, True, 1, 25.0)
+    b = oracle.pals_cycle(Q, qc, nb, rk, nbloc, hl, np.zeros(nbloc), 3, 4, True, 1, 25.0, lowmem=3)
+    np.testing.assert_allclose(b[2], a[2], rtol=1e-10)
+    assert rel(dense_block(b[0], b[1], nb, [rk] * nbloc), dense_block(a[0], a[1], nb, [rk] * nbloc)) < 1e-9
+    with pytest.raises(ValueError):
+        oracle.pals_cycle(Q, qc, nb, rk, nbloc, hl, np.zeros(nbloc), 3, 4, lowmem=2)
