@@ -204,7 +204,8 @@ MLCP_API int mlcp_als_batched_host(int nvec, int ndof, const int *nbas, const in
  * owns up front, a latency-critical loop that must stay out of the CUDA
  * allocator): all scratch comes from a fixed 32 MiB array inside the library,
  * held by every GPU that loads it.  The first call on a device looks up that
- * array's address and must come before any stream capture.  Calls share the
+ * array's address.  A call copies a few metadata words from the caller's stack
+ * (a pageable copy), so calls are not for stream capture.  Calls share the
  * array: calls whose work overlaps on the GPU race.  Sizes whose scratch
  * exceeds the array return an error; arguments are checked even when
  * nals = 0.  Enqueued on stream (NULL: the legacy default stream).  d_status

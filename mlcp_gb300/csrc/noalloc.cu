@@ -12,8 +12,8 @@
 //  * Scratch lives in g_noalloc_scratch (kNoAllocScratchBytes = 32 MiB).  Every
 //    GPU that loads this library holds the array until the process exits.
 //  * The first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress (with that device current).  Make that first call
-//    before any stream capture begins.
+//    cudaGetSymbolAddress (with that device current).  Calls are not for
+//    stream capture: the metadata below is a pageable copy from the stack.
 //  * All calls share the array and it keeps the previous call's contents.
 //    Every scratch region is fully written before it is read.  Calls whose
 //    work overlaps on the GPU (two streams, or two host threads) race on the
