@@ -96,6 +96,8 @@ def lib() -> ctypes.CDLL:
                      "orc_pals_sumlcvec2", "orc_pals_sumlcvec3", "orc_pals_diagonalize", "orc_pals_cycle"):
             getattr(L, name).restype = c_i
         L.orc_pals_pow3.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, _I, _I, _D, _D, c_i, c_i, c_i, c_d, c_i]
+        L.orc_pals_pow.restype = c_i
+        L.orc_pals_pow.argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, _I, _I, _D, _D, c_i, c_i, c_i, c_d, c_i, c_i]
         for name in ("orc_pals_ortho2", "orc_pals_ortho3"):
             getattr(L, name).argtypes = [_D, _D, _I, c_i, c_i, _I, c_i, c_i]
         for name in ("orc_pals_prodhv2", "orc_pals_prodhv3"):
@@ -607,6 +609,20 @@ def _check(rc: int, what: str) -> None:
         raise FloatingPointError(f"{what}: {'eigensolve failed' if rc < 0 else 'NaN weight'}")
 
 
+def pals_pow(base, coef, nbas, rk, nbloc, hl, npow, ishift=1, Eshift=0.0, nconv=0, ranks=None, nthreads=0,
+             lowmem=4):
+    """ALS_POW_alg (src/ALSPow.f90:83-112) on vectors nconv..nbloc-1: lowmem 0
+    ALS_POW0, 1 ALS_POW1, 2 ALS_POW2, 3 and 4 ALS_POW3."""
+    if lowmem not in (0, 1, 2, 3, 4):
+        raise ValueError("lowmem must be 0-4")
+    base, coef, rv = _block(base, coef, nbloc, rk, ranks)
+    nb = np.ascontiguousarray(nbas, dtype=np.int32)
+    _check(lib().orc_pals_pow(_dp(base), _dp(coef), _ip(nb), len(nb), nbloc, _ip(rv), nconv, _ip(hl.opid),
+                              _ip(hl.mptr), _dp(hl.coef), _dp(hl.mat), hl.nterms, npow, ishift, float(Eshift), lowmem,
+                              nthreads), f"ALS_POW (lowmem {lowmem})")
+    return base, coef
+
+
 def pals_pow3(base, coef, nbas, rk, nbloc, hl, npow, ishift=1, Eshift=0.0, nconv=0, ranks=None, nthreads=0):
     """ALS_POW3 (src/ALSPow.f90:569-660) on vectors nconv..nbloc-1."""
     base, coef, rv = _block(base, coef, nbloc, rk, ranks)
@@ -670,10 +686,11 @@ def pals_diagonalize(base, coef, nbas, rk, nbloc, hl, nitn, ranks=None, nthreads
 
 def pals_cycle(base, coef, nbas, rk, nbloc, hl, eigv, npow, nals, update=True, ishift=1, Eshift=0.0, nconv=0,
                ranks=None, nthreads=0, lowmem=4):
-    """One cycle of the Fortran host's CPU solver (lowmem 4: the _2 forms;
-    lowmem 3: the _3 forms); returns (base, coef, eigv)."""
-    if lowmem not in (3, 4):
-        raise ValueError("lowmem 3 or 4 (ALS_POW3 with the _3 or the _2 forms) are restated")
+    """One cycle of the Fortran host's CPU solver: ALS_POW_alg, ALS_ORTHO_alg
+    and the diagonalisation at lowmem 0-4 (the _3 forms at lowmem 3, the _2
+    forms otherwise); returns (base, coef, eigv)."""
+    if lowmem not in (0, 1, 2, 3, 4):
+        raise ValueError("lowmem must be 0-4")
     if update and nals < 1:
         raise ValueError("the cycle's diagonalisation needs nals >= 1 (PRODHV_ALS2 returns no H Q_i otherwise)")
     base, coef, rv = _block(base, coef, nbloc, rk, ranks)

@@ -1836,9 +1836,9 @@ int orc_pals_diagonalize(double *base, double *coef, const int *nbas, int ndof, 
 int orc_pals_cycle(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
                    const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
                    int nals, int lowmem, int update, int ishift, double Eshift, double *eigv, int nthreads) {
-  if (lowmem != 3 && lowmem != 4) return -2;
-  int bad = orc_pals_pow3(base, coef, nbas, ndof, nbloc, ranks, nconv, opid, mptr, Hcoef, mat, T, npow, ishift,
-                          Eshift, nthreads);
+  if (lowmem < 0 || lowmem > 4) return -2;
+  int bad = orc_pals_pow(base, coef, nbas, ndof, nbloc, ranks, nconv, opid, mptr, Hcoef, mat, T, npow, ishift, Eshift,
+                         lowmem, nthreads);
   if (bad) return bad;
   bad = lowmem == 3 ? orc_pals_ortho3(base, coef, nbas, ndof, nbloc, ranks, nals, nthreads)
                     : orc_pals_ortho2(base, coef, nbas, ndof, nbloc, ranks, nals, nthreads);
@@ -1956,5 +1956,236 @@ int orc_gramortho(double *base, double *coef, const int *nbas, int ndof, int nbl
     if (!bad) normcoef(qc, qb, ranks[i], nbas, off, ndof);
   }
   free(w); free(vc); free(vb); free(off); free(toff);
+  return bad;
+}
+
+/* ------------------------------------------------------------------ */
+/* ALS_POW0 / ALS_POW1 / ALS_POW2: the power step at lowmem 0, 1, 2     */
+/* ------------------------------------------------------------------ */
+
+/* PRODHV1 (src/ALSPow.f90:869-935): the mode-k factors and the weights of
+ * the explicit G = (H - E)F rewritten from the current F (term t rF + i:
+ * c_i, h_{t,k} F_i^k; shift rows: |E| c_i, F_i^k).  VecScalarMult changes
+ * the sign of the shift rows' first-mode factors when E < 0, at every call;
+ * at k = 0 the shift rows (ishift > 0) or the H rows (ishift < 0) change
+ * sign in the first mode, as PRODHV does. */
+static void prodhv1(const hoplist *H, const double *fc, const double *fb, int rF, const int *nbas, const int *off,
+                    int ndof, int k, int ishift, double E, double *gc, double *gb) {
+  const int nD = off[ndof], rFH = rF * H->T, n = nbas[k], n0 = nbas[0];
+  int ik = 0;
+  for (int t = 0; t < H->T; ++t)
+    for (int i = 0; i < rF; ++i, ++ik) {
+      gc[ik] = fc[i];
+      hv_base_prod(H, t, k, fb + (size_t)i * nD + off[k], gb + (size_t)ik * nD + off[k], n);
+    }
+  if (ishift == 0) return;
+  for (int i = 0; i < rF; ++i) {
+    memcpy(gb + (size_t)(rFH + i) * nD + off[k], fb + (size_t)i * nD + off[k], sizeof(double) * n);
+    gc[rFH + i] = fabs(E) * fc[i];
+    if (E < 0.0)
+      for (int q = 0; q < n0; ++q) gb[(size_t)(rFH + i) * nD + q] = -gb[(size_t)(rFH + i) * nD + q];
+  }
+  if (k == 0) {
+    const int s0 = ishift > 0 ? rFH : 0, s1 = ishift > 0 ? rFH + rF : rFH;
+    for (int r = s0; r < s1; ++r)
+      for (int q = 0; q < n0; ++q) gb[(size_t)r * nD + q] = -gb[(size_t)r * nD + q];
+  }
+}
+
+/* bjk(i, ir) = sum_j c_G,j G_j^k(ir) PS(j, i), rows ir, then terms j. */
+static void bjk_from_ps(const double *gc, const double *gb, int rG, int nD, int gst, int n, const double *PS, int rF,
+                        double *bjk) {
+  for (int e = 0; e < rF * n; ++e) bjk[e] = 0.0;
+  for (int ir = 0; ir < n; ++ir)
+    for (int j = 0; j < rG; ++j) {
+      const double gtmp = gc[j] * gb[(size_t)j * nD + gst + ir];
+      for (int i = 0; i < rF; ++i) bjk[i + (size_t)ir * rF] += gtmp * PS[j + (size_t)i * rG];
+    }
+}
+
+/* ALS_POW0 (src/ALSPow.f90:146-290): the explicit G = PRODHV(F) and one
+ * Gram (F, F) and one overlap (G, F) per mode; each mode step multiplies the
+ * other modes' matrices (modes k+1, k+2, ... cyclically), adds 1e-15 max c_G
+ * (the weights of the first G), solves, normalises the weights after the last
+ * mode, then rewrites G's mode k from the new F (PRODHV1) and that mode's
+ * two matrices (not after the very last step).  Returns 1 on a NaN. */
+static int pals_pow0(const hoplist *H, double *coef, double *base, int rF, const int *nbas, const int *off, int ndof,
+                     int nitn, int ishift, double Eshift) {
+  if (nitn == 0) return 0;
+  const int nD = off[ndof], rG = rF * H->T + (ishift != 0 ? rF : 0), nmax = max_nbas(nbas, ndof);
+  double *gc = (double *)malloc(sizeof(double) * rG);
+  double *gb = (double *)malloc(sizeof(double) * (size_t)rG * nD);
+  double *BB = (double *)malloc(sizeof(double) * (size_t)rF * rF * ndof);
+  double *PS = (double *)malloc(sizeof(double) * (size_t)rG * rF * ndof);
+  double *bjk = (double *)malloc(sizeof(double) * (size_t)rF * nmax);
+  int *ipiv = (int *)malloc(sizeof(int) * rF);
+  const size_t sb = (size_t)rF * rF, sp = (size_t)rG * rF;
+  prodhv_explicit(H, coef, base, rF, nbas, off, ndof, ishift, Eshift, gc, gb);
+  const double valpen = maxval(gc, rG) * 1.0e-15;
+  for (int d = 1; d < ndof; ++d) {
+    for (size_t e = 0; e < sb; ++e) BB[d * sb + e] = 1.0;
+    update_bb(base, rF, nD, off[d], nbas[d], BB + d * sb, 0);
+    for (size_t e = 0; e < sp; ++e) PS[d * sp + e] = 1.0;
+    update_ps(base, rF, gb, rG, nD, off[d], nbas[d], PS + d * sp, 0);
+  }
+  int bad = 0;
+  for (int itn = 0; itn < nitn && !bad; ++itn)
+    for (int k = 0; k < ndof; ++k) {
+      const int n = nbas[k];
+      double *Bk = BB + k * sb, *Pk = PS + k * sp;
+      const int k1 = (k + 1) % ndof;
+      memcpy(Bk, BB + k1 * sb, sizeof(double) * sb);
+      memcpy(Pk, PS + k1 * sp, sizeof(double) * sp);
+      for (int l = 2; l < ndof; ++l) {
+        const int kp = (k + l) % ndof;
+        for (size_t e = 0; e < sb; ++e) Bk[e] = Bk[e] * BB[kp * sb + e];
+        for (size_t e = 0; e < sp; ++e) Pk[e] = Pk[e] * PS[kp * sp + e];
+      }
+      for (int i = 0; i < rF; ++i) Bk[i + (size_t)i * rF] += valpen;
+      bjk_from_ps(gc, gb, rG, nD, off[k], n, Pk, rF, bjk);
+      lu_solve(Bk, bjk, rF, n, ipiv);
+      if (rows_to_mode(coef, base, rF, nD, off[k], bjk, n)) { bad = 1; break; }
+      if (k == ndof - 1) {
+        const double s = 1 / sqrt(fabs(prodvv_aa(coef, base, rF, nbas, ndof, nD)));
+        for (int i = 0; i < rF; ++i) coef[i] = coef[i] * s;
+      }
+      if (itn < nitn - 1 || k < ndof - 1) {
+        prodhv1(H, coef, base, rF, nbas, off, ndof, k, ishift, Eshift, gc, gb);
+        for (size_t e = 0; e < sb; ++e) Bk[e] = 1.0;
+        update_bb(base, rF, nD, off[k], n, Bk, 0);
+        for (size_t e = 0; e < sp; ++e) Pk[e] = 1.0;
+        update_ps(base, rF, gb, rG, nD, off[k], n, Pk, 0);
+      }
+    }
+  free(gc); free(gb); free(BB); free(PS); free(bjk); free(ipiv);
+  return bad;
+}
+
+/* ALS_POW1 (src/ALSPow.f90:294-440): the explicit G = PRODHV(F); with more
+ * than three modes BB and PS are kept by dividing mode k out before its step
+ * and multiplying the new one back after it, otherwise rebuilt at every step;
+ * penalty 1e-15 max c_G (the first G); after each step G's mode k is
+ * rewritten from the new F (PRODHV1).  Returns 1 on a NaN. */
+static int pals_pow1(const hoplist *H, double *coef, double *base, int rF, const int *nbas, const int *off, int ndof,
+                     int nitn, int ishift, double Eshift) {
+  if (nitn == 0) return 0;
+  const int nD = off[ndof], rG = rF * H->T + (ishift != 0 ? rF : 0), nmax = max_nbas(nbas, ndof);
+  const int update = ndof > 3;
+  double *gc = (double *)malloc(sizeof(double) * rG);
+  double *gb = (double *)malloc(sizeof(double) * (size_t)rG * nD);
+  double *BB = (double *)malloc(sizeof(double) * rF * rF);
+  double *BBmem = (double *)malloc(sizeof(double) * rF * rF);
+  double *PS = (double *)malloc(sizeof(double) * (size_t)rG * rF);
+  double *bjk = (double *)malloc(sizeof(double) * (size_t)rF * nmax);
+  int *ipiv = (int *)malloc(sizeof(int) * rF);
+  prodhv_explicit(H, coef, base, rF, nbas, off, ndof, ishift, Eshift, gc, gb);
+  const double valpen = maxval(gc, rG) * 1.0e-15;
+  if (update) {
+    const_bb(base, rF, nbas, ndof, nD, 0, BBmem);
+    const_ps(base, rF, gb, rG, nbas, ndof, nD, 0, PS);
+  }
+  int kp = -1, bad = 0;
+  for (int itn = 0; itn < nitn && !bad; ++itn)
+    for (int k = 0; k < ndof; ++k) {
+      const int n = nbas[k];
+      if (update) {
+        if (kp >= 0) {
+          update_bb(base, rF, nD, off[k], n, BBmem, 1);
+          update_ps(base, rF, gb, rG, nD, off[k], n, PS, 1);
+        }
+        memcpy(BB, BBmem, sizeof(double) * rF * rF);
+      } else {
+        const_bb(base, rF, nbas, ndof, nD, k, BB);
+        const_ps(base, rF, gb, rG, nbas, ndof, nD, k, PS);
+      }
+      for (int i = 0; i < rF; ++i) BB[i + (size_t)i * rF] += valpen;
+      bjk_from_ps(gc, gb, rG, nD, off[k], n, PS, rF, bjk);
+      lu_solve(BB, bjk, rF, n, ipiv);
+      bad = rows_to_mode(coef, base, rF, nD, off[k], bjk, n);
+      if (k == ndof - 1) {
+        const double s = 1 / sqrt(fabs(prodvv_aa(coef, base, rF, nbas, ndof, nD)));
+        for (int i = 0; i < rF; ++i) coef[i] = coef[i] * s;
+      }
+      prodhv1(H, coef, base, rF, nbas, off, ndof, k, ishift, Eshift, gc, gb);
+      if (bad) break;
+      if (update && (itn < nitn - 1 || k < ndof - 1)) {
+        update_bb(base, rF, nD, off[k], n, BBmem, 0);
+        update_ps(base, rF, gb, rG, nD, off[k], n, PS, 0);
+      }
+      kp = k;
+    }
+  free(gc); free(gb); free(BB); free(BBmem); free(PS); free(bjk); free(ipiv);
+  return bad;
+}
+
+/* ALS_POW2 (src/ALSPow.f90:444-565): PRODHV_ALS2's update and downdate of
+ * BB and PS (UpdateXPS / DowndateXPS with Fold = F), in place, penalty
+ * 1e-10 max c_F, the weights normalised after the last mode.  Returns 1 on
+ * a NaN. */
+static int pals_pow2(const hoplist *H, double *coef, double *base, int rF, const int *nbas, const int *off, int ndof,
+                     int nitn, int ishift, double Eshift, pals_ws *w) {
+  if (nitn == 0) return 0;
+  const int nD = off[ndof];
+  const int rG = rF * H->T + (ishift != 0 ? rF : 0);
+  const double valpen = maxval(coef, rF) * 1.0e-10;
+  const_bb(base, rF, nbas, ndof, nD, 0, w->BBmem);
+  for (size_t e = 0; e < (size_t)rG * rF; ++e) w->PS[e] = 1.0;
+  for (int k = 0; k < ndof; ++k)
+    xps_step(H, coef, base, base, rF, nbas, off, ndof, k, ishift, Eshift, w->PS, NULL, w->T, 0);
+  int kp = -1;
+  for (int itn = 0; itn < nitn; ++itn)
+    for (int k = 0; k < ndof; ++k) {
+      const int n = nbas[k];
+      if (kp >= 0) update_bb(base, rF, nD, off[k], n, w->BBmem, 1);
+      memcpy(w->BB, w->BBmem, sizeof(double) * rF * rF);
+      for (int i = 0; i < rF; ++i) w->BB[i + (size_t)i * rF] += valpen;
+      xps_step(H, coef, base, base, rF, nbas, off, ndof, k, ishift, Eshift, w->PS, w->bjk, w->T, 1);
+      lu_solve(w->BB, w->bjk, rF, n, w->ipiv);
+      if (rows_to_mode(coef, base, rF, nD, off[k], w->bjk, n)) return 1;
+      if (k == ndof - 1) {
+        const double s = 1 / sqrt(fabs(prodvv_aa(coef, base, rF, nbas, ndof, nD)));
+        for (int i = 0; i < rF; ++i) coef[i] = coef[i] * s;
+      }
+      if (itn < nitn - 1 || k < ndof - 1) {
+        update_bb(base, rF, nD, off[k], n, w->BBmem, 0);
+        xps_step(H, coef, base, base, rF, nbas, off, ndof, k, ishift, Eshift, w->PS, NULL, w->T, 0);
+      }
+      kp = k;
+    }
+  return 0;
+}
+
+/* ALS_POW_alg (src/ALSPow.f90:83-112) on vectors nconv..nbloc-1, OpenMP over
+ * vectors: lowmem 0 ALS_POW0, 1 ALS_POW1, 2 ALS_POW2, 3 and 4 ALS_POW3. */
+int orc_pals_pow(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
+                 const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow, int ishift,
+                 double Eshift, int lowmem, int nthreads) {
+  if (lowmem < 0 || lowmem > 4) return -2;
+  if (lowmem >= 3)
+    return orc_pals_pow3(base, coef, nbas, ndof, nbloc, ranks, nconv, opid, mptr, Hcoef, mat, T, npow, ishift,
+                         Eshift, nthreads);
+  int *off = make_offsets(nbas, ndof), *toff = rank_offsets(ranks, nbloc);
+  const int nD = off[ndof], nmax = max_nbas(nbas, ndof);
+  hoplist H = {T, ndof, opid, mptr, Hcoef, mat};
+  int bad = 0;
+#ifdef _OPENMP
+  if (nthreads < 1) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : bad)
+#endif
+  for (int v = nconv < 0 ? 0 : nconv; v < nbloc; ++v) {
+    double *c = coef + toff[v], *b = base + (size_t)toff[v] * nD;
+    const int r = ranks[v];
+    if (lowmem == 0) {
+      bad += pals_pow0(&H, c, b, r, nbas, off, ndof, npow, ishift, Eshift);
+    } else if (lowmem == 1) {
+      bad += pals_pow1(&H, c, b, r, nbas, off, ndof, npow, ishift, Eshift);
+    } else {
+      pals_ws w = pals_ws_alloc(r, r * T + r, nmax);
+      bad += pals_pow2(&H, c, b, r, nbas, off, ndof, npow, ishift, Eshift, &w);
+      pals_ws_free(&w);
+    }
+  }
+  (void)nthreads;
+  free(off); free(toff);
   return bad;
 }

@@ -135,6 +135,11 @@ int orc_reduc_als_batched(int nvec, const double *const *gcoef, const double *co
 int orc_pals_pow3(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
                   const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
                   int ishift, double Eshift, int nthreads);
+/* ALS_POW_alg (src/ALSPow.f90:83-112): lowmem 0 ALS_POW0, 1 ALS_POW1,
+ * 2 ALS_POW2, 3 and 4 ALS_POW3; -2 for another lowmem. */
+int orc_pals_pow(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
+                 const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow, int ishift,
+                 double Eshift, int lowmem, int nthreads);
 /* ALS_ORTHO_2 (src/ALSUtils.f90:156-377) and ALS_ORTHO_3 (:381-528). */
 int orc_pals_ortho2(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nitn,
                     int nthreads);
@@ -162,8 +167,9 @@ int orc_pals_sumlcvec3(double *base, double *coef, const int *nbas, int ndof, in
 int orc_pals_diagonalize(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks,
                          const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int nitn,
                          int lowmem, double *eigv, double *U, int nthreads);
-/* One cycle: ALS_POW3, ALS_ORTHO_2 (_3) and, with update, the
- * diagonalisation; lowmem 3 or 4 (else -2). */
+/* One cycle: ALS_POW_alg, ALS_ORTHO_alg and, with update, the
+ * diagonalisation, for lowmem 0-4 (else -2): the _3 forms at lowmem 3, the
+ * _2 forms otherwise (the dispatchers' choice). */
 int orc_pals_cycle(double *base, double *coef, const int *nbas, int ndof, int nbloc, const int *ranks, int nconv,
                    const int *opid, const int *mptr, const double *Hcoef, const double *mat, int T, int npow,
                    int nals, int lowmem, int update, int ishift, double Eshift, double *eigv, int nthreads);

@@ -374,4 +374,34 @@ def test_pals_cycle_lowmem3_matches_lowmem4():
     np.testing.assert_allclose(b[2], a[2], rtol=1e-10)
     assert rel(dense_block(b[0], b[1], nb, [rk] * nbloc), dense_block(a[0], a[1], nb, [rk] * nbloc)) < 1e-9
     with pytest.raises(ValueError):
-        oracle.pals_cycle(Q, qc, nb, rk, nbloc, hl, np.zeros(nbloc), 3, 4, lowmem=2)
+        oracle.pals_cycle(Q, qc, nb, rk, nbloc, hl, np.zeros(nbloc), 3, 4, lowmem=5)
+
+
+# --- lowmem 0-2: the other power steps of ALS_POW_alg ---
+
+@pytest.mark.parametrize("D", [3, 4])
+@pytest.mark.parametrize("ishift,esh", [(1, 9.0), (0, 0.0)])
+def test_pow_variants(D, ishift, esh):
+    """ALS_POW2 keeps BB and PS by update and downdate (UpdateXPS), ALS_POW3
+    rebuilds them: the same fit to rounding.  ALS_POW0 (per-mode matrices)
+    and ALS_POW1 (update and downdate, or rebuilt for three modes or fewer)
+    fit the explicit G with the penalty 1e-15 max c_G instead of 1e-10 max
+    c_F: the same as each other to rounding, within 1e-7 of ALS_POW3."""
+    hl = H.henon_heiles(D=D, n=5, lam=0.111803)
+    nb, rk, nbloc = hl.nbas, 4, 3
+    Q, qc = start_block(nb, rk, nbloc, 1)
+    res = {lm: dense_block(*oracle.pals_pow(Q, qc, nb, rk, nbloc, hl, 3, ishift, esh, lowmem=lm), nb, [rk] * nbloc)
+           for lm in (0, 1, 2, 3)}
+    assert rel(res[2], res[3]) < 1e-12
+    assert rel(res[0], res[1]) < 1e-12
+    assert rel(res[1], res[3]) < 1e-7
+
+
+def test_pals_cycle_every_lowmem():
+    hl = H.coupled_oscillators(3, 6)
+    nb, rk, nbloc = hl.nbas, 5, 4
+    Q, qc = start_block(nb, rk, nbloc, 23)
+    e = {lm: oracle.pals_cycle(Q, qc, nb, rk, nbloc, hl, np.zeros(nbloc), 3, 4, True, 1, 25.0, lowmem=lm)[2]
+         for lm in range(5)}
+    for lm in (0, 1, 2, 3):
+        np.testing.assert_allclose(e[lm], e[4], rtol=1e-7)
